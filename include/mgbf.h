@@ -1,0 +1,197 @@
+/*
+ * libmgbf -- GB300-native multigrid beta filter (MGBF) filtering pipeline.
+ *
+ * C-ABI drop-in for the filtering path of the reference's Fortran modules.
+ * Every entry point below names the reference interface it replaces
+ * (paths inside the reference project):
+ *
+ *   mg_entrymod.f90:36   mg_initialize            -> mgbf_create / mgbf_create_from_namelist
+ *   mg_parameter.f90:179 init_mg_parameter        -> mgbf_config_read_namelist
+ *   mg_filtering.f90:67  filtering_procedure      -> mgbf_filtering_procedure
+ *   mg_entrymod.f90:222  mg_finalize              -> mgbf_destroy
+ *
+ * The field is operated on in place, in the reference's layout
+ * VALL(km_all, 1-hx:im+hx, 1-hy:jm+hy) (mg_intstate.f90:157; level index
+ * fastest), over the whole filter grid im = nxPE*im_filt, jm = nyPE*jm_filt
+ * held by one GPU, or in a compact (km_all, im, jm) layout without halos.
+ * The caller owns the field; the handle owns setup tables and scratch.
+ *
+ * Errors are returned as negative codes (the reference calls `stop`).
+ * No entry point exits the process.  Calls on distinct handles are
+ * thread-safe; one handle is used by one host thread at a time.
+ */
+#ifndef MGBF_H
+#define MGBF_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGBF_ABI_VERSION 1
+#define MGBF_MAX_GEN 16
+
+/* ---- status codes ---------------------------------------------------- */
+#define MGBF_OK 0
+#define MGBF_ERR_ARG (-1)          /* null pointer, bad enum, bad size          */
+#define MGBF_ERR_CONFIG (-2)       /* inconsistent configuration                */
+#define MGBF_ERR_REACH (-3)        /* filter reach exceeds halo (getlinesum stop) */
+#define MGBF_ERR_DIVISIBILITY (-4) /* grid not divisible by 2^(gm-1), too small  */
+#define MGBF_ERR_UNSUPPORTED (-5)  /* mgbf_proc outside the supported set        */
+#define MGBF_ERR_CUDA (-6)         /* CUDA runtime error                         */
+#define MGBF_ERR_NAMELIST (-7)     /* namelist syntax / unknown field            */
+#define MGBF_ERR_IO (-8)           /* file cannot be read                        */
+#define MGBF_ERR_TIMEOUT (-9)      /* bounded device wait ran out                */
+#define MGBF_ERR_NOMEM (-10)       /* allocation failed                          */
+
+/* ---- storage types and memory spaces ---------------------------------- */
+#define MGBF_F64 0   /* double storage, double arithmetic                    */
+#define MGBF_F32 1   /* float storage, float arithmetic                      */
+#define MGBF_BF16 2  /* bfloat16 storage, float arithmetic                   */
+
+#define MGBF_MEM_DEVICE 0
+#define MGBF_MEM_HOST 1
+
+#define MGBF_LAYOUT_HALO 0     /* VALL(km_all, 1-hx:im+hx, 1-hy:jm+hy)       */
+#define MGBF_LAYOUT_COMPACT 1  /* (km_all, im, jm)                            */
+
+/*
+ * Configuration: the fields of namelist &PARAMETERS_MGBETA
+ * (mg_parameter.f90:190-208) with the same names and meaning, plus a few
+ * extensions at the end.  mgbf_config_init() sets the defaults below.
+ */
+typedef struct mgbf_config {
+    double mg_ampl01, mg_ampl02, mg_ampl03;
+    double mg_weig1, mg_weig2, mg_weig3, mg_weig4, mg_weig5;
+    int hx, hy, hz, p;
+    int mgbf_line, mgbf_proc, n_ens;
+    int lm_a, lm, km2, km3;
+    int l_loc, l_loc_vertical, l_filt_g1, l_lin_vertical, l_lin_horizontal;
+    int l_quad_horizontal, l_new_map, l_vertical_filter;
+    int ldelta, lquart, lhelm;
+    int gm_max;
+    int nm0, mm0, nxPE, nyPE, im_filt, jm_filt;
+    /* ---- extensions (0 keeps reference behaviour) ---- */
+    int gm_uncapped;                 /* 1: gm = gm_max, not min(gm_max, def_maxgen(nxPE,nyPE)) */
+    int n_weig_ext;                  /* >0: use weig_ext[0..n-1] as a_1..a_n (gens beyond n reuse the last) */
+    double weig_ext[MGBF_MAX_GEN];
+    double helm_b[MGBF_MAX_GEN];     /* Helmholtz b per generation (reference: 0) */
+    int layout;                      /* MGBF_LAYOUT_HALO (reference) or MGBF_LAYOUT_COMPACT */
+} mgbf_config;
+
+/* Derived sizes of a created handle. */
+typedef struct mgbf_dims {
+    int im, jm;            /* generation-1 filter grid                       */
+    int km_all;            /* leading dimension of the field                 */
+    int km, km3_all;
+    int gm;                /* generations actually used                      */
+    int hx, hy, hz;
+    int reach_h, reach_z;  /* filter reach (<= halo)                          */
+    int layout;
+    size_t field_elems;    /* elements of one field in the handle's layout   */
+    int hbeta_kernel;      /* 1: moment kernel, 0: direct-sum kernel          */
+} mgbf_dims;
+
+typedef struct mgbf_handle mgbf_handle;
+
+/* Defaults of the reference's namelist fields (the shipped RUN/mgbf.nml
+ * values for the booleans; sizes zero so they must be given). */
+int mgbf_config_init(mgbf_config* cfg);
+
+/* Parse &PARAMETERS_MGBETA from a namelist file (replaces the read in
+ * init_mg_parameter, mg_parameter.f90:210-212).  Unknown fields are an error.
+ * Extension fields may appear in the same group.  The optional errbuf gets a
+ * one-line message. */
+int mgbf_config_read_namelist(const char* path, mgbf_config* cfg, char* errbuf, size_t errlen);
+
+/* Validate a configuration and build a handle: FP64 setup of the filter
+ * tables (def_mg_weights, mg_intstate.f90:296-433; def_offset_coef,
+ * mg_interpolate.f90:61-86) and device scratch for the coarse generations.
+ * Replaces mg_initialize (mg_entrymod.f90:36) for the filtering path.
+ * Uses the current CUDA device. */
+int mgbf_create(const mgbf_config* cfg, mgbf_handle** out);
+
+/* mgbf_config_read_namelist + mgbf_create. */
+int mgbf_create_from_namelist(const char* path, mgbf_handle** out);
+
+/* Sizes derived at creation. */
+int mgbf_get_dims(const mgbf_handle* h, mgbf_dims* dims);
+
+/*
+ * filtering_procedure(mg_filt) (mg_filtering.f90:67-120) on the field in
+ * place.  Supported: 1 = filtering_rad2_bckg (mg_filtering.f90:560-680),
+ * 6 = filtering_rad2_ens (mg_filtering.f90:1000-1147).  2,3,4,5,7,8 return
+ * MGBF_ERR_UNSUPPORTED; any other value is a no-op returning MGBF_OK, as the
+ * reference's select has no default case.
+ *   vall:   field pointer (device or host, per mem), laid out per the
+ *           handle's layout, element type per dtype.
+ *   stream: cudaStream_t (NULL = legacy default stream).  Device calls are
+ *           asynchronous on the stream; host calls return after the result
+ *           is back in vall.
+ */
+int mgbf_filtering_procedure(mgbf_handle* h, int mg_filt, void* vall, int dtype, int mem,
+                             void* stream);
+
+/* Adjoint of filtering_procedure(mg_filt), run through the explicit
+ * transposed chain (no reference counterpart: the reference's adjoint test
+ * is an empty stub, RBETA_TEST.f90:64-69).  The operator is self-adjoint,
+ * so the result equals the forward up to rounding. */
+int mgbf_filtering_procedure_adjoint(mgbf_handle* h, int mg_filt, void* vall, int dtype, int mem,
+                                     void* stream);
+
+/*
+ * Gradients for y = L(a) x (no reference counterpart):
+ *   gx = L^T gy, and ga[g] = sum over points of u_g * v_g with
+ *   u_g = B_g R_g Bz^T x, v_g = B_g R_g Bz^T gy, for g = 1..gm.
+ * x, gy, gx: fields in the handle's layout (gx may alias gy).  ga: host
+ * array of gm doubles.  Coarse generations are recomputed from x.
+ * Returns after ga is on the host.
+ */
+int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, const void* gy,
+                                 void* gx, double* ga, int dtype, int mem, void* stream);
+
+/* Replace the per-generation weights a_1..a_n (n <= gm) without rebuilding. */
+int mgbf_set_weights(mgbf_handle* h, const double* a, int n);
+
+/* Release the handle (replaces mg_finalize / deallocate_mg_intstate). */
+int mgbf_destroy(mgbf_handle* h);
+
+/* Static description of a status code. */
+const char* mgbf_strerror(int code);
+
+/* Message of the most recent failure on the calling thread. */
+const char* mgbf_last_error(void);
+
+/* ------------------------------------------------------------------------
+ * Batched ensemble extension (no single reference counterpart: the
+ * reference needs one run per variable group because one lm and one
+ * mg_ampl02 serve every variable, mg_parameter.f90:293-294,
+ * mg_intstate.f90:383-390).  A batch is a list of variable groups on one
+ * horizontal grid; each group is a compact (nk, im, jm) field of nk =
+ * members * levels columns with its own horizontal reach, vertical filter
+ * and levels.  All groups are filtered by one call.
+ */
+typedef struct mgbf_group_desc {
+    int nk;               /* leading dimension of this group's field           */
+    int lm;               /* levels per vertical column (1: 2D, no z filter)   */
+    int nzcol;            /* z columns at offsets (c-1)*lm; 0 = no z filter     */
+    int hx, hy, hz, p;
+    double mg_ampl01, mg_ampl02;
+} mgbf_group_desc;
+
+typedef struct mgbf_batch mgbf_batch;
+
+/* im, jm: generation-1 grid; gm generations; weights a_1..a_gm; lquart as in
+ * the namelist; l_filt_g1 as in filtering_rad2_ens. */
+int mgbf_batch_create(int im, int jm, int gm, const double* weights, int lquart, int l_filt_g1,
+                      const mgbf_group_desc* groups, int ngroups, mgbf_batch** out);
+/* fields[g]: device pointer to group g's compact field; filtered in place.
+ * adjoint != 0 runs the transposed chain. */
+int mgbf_batch_apply(mgbf_batch* b, void* const* fields, int dtype, int adjoint, void* stream);
+int mgbf_batch_destroy(mgbf_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MGBF_H */

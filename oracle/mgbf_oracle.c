@@ -1,0 +1,800 @@
+/*
+ * FP64 CPU oracle for the MGBF filtering pipeline -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Restates, on one global filter grid, the reference's CPU algorithm for
+ * filtering_procedure(1) and filtering_procedure(6).  Every routine below
+ * names the reference routine (file:line, paths inside the reference project)
+ * whose loops it follows.  The MPI halo exchange of the reference collapses
+ * into the global-edge mirror/fold that mg_bocos applies at physical
+ * boundaries; interior rank boundaries disappear because one array holds the
+ * whole grid.  See mgbf_oracle.h for the parity status (unpinned).
+ *
+ * Only tests/, the smoke check and the benchmark's CPU-baseline leg use this.
+ */
+#include "mgbf_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------ arrays */
+
+typedef struct {
+    double* d;
+    int nk, ilo, ihi, jlo, jhi;
+} arr3;
+
+static inline size_t a3i(const arr3* a, int k, int i, int j) {
+    return (size_t)k + (size_t)a->nk * ((size_t)(i - a->ilo) +
+                                        (size_t)(a->ihi - a->ilo + 1) * (size_t)(j - a->jlo));
+}
+#define A3(a, k, i, j) ((a).d[a3i(&(a), (k), (i), (j))])
+
+static arr3 a3_alloc(int nk, int ilo, int ihi, int jlo, int jhi) {
+    arr3 a;
+    a.nk = nk; a.ilo = ilo; a.ihi = ihi; a.jlo = jlo; a.jhi = jhi;
+    size_t n = (size_t)nk * (size_t)(ihi - ilo + 1) * (size_t)(jhi - jlo + 1);
+    a.d = (double*)calloc(n ? n : 1, sizeof(double));
+    return a;
+}
+static void a3_free(arr3* a) { free(a->d); a->d = NULL; }
+
+/* Zero k-range [k0,k1) of every cell. */
+static void a3_zero(arr3 a, int k0, int k1) {
+    for (int j = a.jlo; j <= a.jhi; ++j)
+        for (int i = a.ilo; i <= a.ihi; ++i)
+            for (int k = k0; k < k1; ++k) A3(a, k, i, j) = 0.0;
+}
+static void a3_copy(arr3 dst, arr3 src, int k0, int k1) {
+    for (int j = dst.jlo; j <= dst.jhi; ++j)
+        for (int i = dst.ilo; i <= dst.ihi; ++i)
+            for (int k = k0; k < k1; ++k) A3(dst, k, i, j) = A3(src, k, i, j);
+}
+
+static inline double ipow(double x, int p) {
+    /* Fortran real**integer; p >= 0 */
+    double r = 1.0;
+    for (int t = 0; t < p; ++t) r *= x;
+    return r;
+}
+
+/* ------------------------------------------------------------------ setup */
+
+typedef struct {
+    double rmom2_1, rmom2_2;
+    double exx1;          /* el*rmom2_1 for the vertical filter          */
+    double exx2, eyy2;    /* el*rmom2_2 for the horizontal filter        */
+    double eyx2;          /* off-diagonal (zero: no anisotropy)          */
+    double ss1, ss2;      /* inverse line sums                           */
+    int reach1, reach2;
+} setup_t;
+
+static const double EPS = 1.e-12;
+
+/* mg_parameter.f90:567-572 (rmom2), mg_intstate.f90:360-431 (pasp, cholaspect,
+ * getlinesum), jp_pbfil.f90:74-107 (cholaspect1/2), 149-218 (getlinesum1/2). */
+static int setup(const orc_cfg* c, setup_t* s) {
+    double pee2 = 2.0 * c->p;
+    s->rmom2_1 = 1.0 / sqrt(pee2 + 3.0);
+    s->rmom2_2 = 1.0 / sqrt(pee2 + 4.0);
+    /* cholaspect1: el = 1/sqrt(pasp1) */
+    double el1 = 1.0 / sqrt(c->ampl01);
+    /* cholaspect2 on diag(pasp02,pasp02): inv -> diag(1/pasp02); Cholesky ->
+     * diag(sqrt(1/pasp02)), zero off-diagonal. */
+    double el2 = sqrt(1.0 / c->ampl02);
+    s->exx1 = el1 * s->rmom2_1;
+    s->exx2 = el2 * s->rmom2_2;
+    s->eyy2 = el2 * s->rmom2_2;
+    s->eyx2 = 0.0;
+
+    /* getlinesum1 (jp_pbfil.f90:149-180) with hx := hz */
+    {
+        double x = 1.0 / s->exx1;
+        int gxl = (int)ceil(-x + EPS), gxm = (int)floor(x - EPS);
+        if (c->l_vertical_filter && (gxl < -c->hz || gxm > c->hz)) return ORC_ERR_REACH;
+        double sum = 0.0;
+        for (int gx = gxl; gx <= gxm; ++gx) {
+            double xx = gx;
+            double rr = (xx * s->exx1) * (xx * s->exx1);
+            sum += ipow(1.0 - rr, c->p);
+        }
+        s->ss1 = 1.0 / sum;
+        s->reach1 = gxm;
+    }
+    /* getlinesum2 (jp_pbfil.f90:182-218) */
+    {
+        double sum = 0.0;
+        double exx = s->exx2, eyy = s->eyy2, eyx = s->eyx2;
+        double y = 1.0 / eyy;
+        int gyl = (int)ceil(-y + EPS), gym = (int)floor(y - EPS);
+        if (gyl < -c->hy || gym > c->hy) return ORC_ERR_REACH;
+        int reach = 0;
+        for (int gy = gyl; gy <= gym; ++gy) {
+            double yy = gy, xc = -yy * eyx;
+            double rrx = (yy * eyy) * (yy * eyy);
+            double x = sqrt(1.0 - rrx);
+            int gxl = (int)ceil((xc - x) / exx + EPS), gxm = (int)floor((xc + x) / exx - EPS);
+            if (gxl < -c->hx || gxm > c->hx) return ORC_ERR_REACH;
+            if (gxm > reach) reach = gxm;
+            for (int gx = gxl; gx <= gxm; ++gx) {
+                double xx = gx;
+                double rr = rrx + (xx * exx - xc) * (xx * exx - xc);
+                sum += ipow(1.0 - rr, c->p);
+            }
+        }
+        s->ss2 = 1.0 / sum;
+        s->reach2 = reach > gym ? reach : gym;
+    }
+    return ORC_OK;
+}
+
+int orc_setup_values(const orc_cfg* c, double out[8]) {
+    setup_t s;
+    int rc = setup(c, &s);
+    if (rc) return rc;
+    out[0] = s.rmom2_1; out[1] = s.rmom2_2; out[2] = s.exx1; out[3] = s.exx2;
+    out[4] = s.ss1; out[5] = s.ss2; out[6] = s.reach1; out[7] = s.reach2;
+    return ORC_OK;
+}
+
+/* --------------------------------------------------- horizontal beta filter */
+
+/* vrbeta2 (jp_pbfil.f90:888-928): gather over the extended domain, output on
+ * the interior, halo of the result zeroed; then a = b.  k-range [k0,k1). */
+static void vrbeta2(const setup_t* S, int p, arr3 a, arr3 b, int Lx, int Mx, int Ly, int My,
+                    int k0, int k1, double* tb) {
+    a3_zero(b, k0, k1);
+    double exx = S->exx2, eyy = S->eyy2, eyx = S->eyx2, s = S->ss2;
+    for (int iy = Ly; iy <= My; ++iy)
+        for (int ix = Lx; ix <= Mx; ++ix) {
+            for (int k = k0; k < k1; ++k) tb[k] = 0.0;
+            double y = 1.0 / eyy;
+            int gyl = (int)ceil(-y + EPS), gym = (int)floor(y - EPS);
+            for (int gy = gyl; gy <= gym; ++gy) {
+                int jy = iy + gy;
+                double yy = gy, xc = -yy * eyx;
+                double rrx = (yy * eyy) * (yy * eyy);
+                double x = sqrt(1.0 - rrx);
+                int gxl = (int)ceil((xc - x) / exx + EPS), gxm = (int)floor((xc + x) / exx - EPS);
+                for (int gx = gxl; gx <= gxm; ++gx) {
+                    int jx = ix + gx;
+                    double xx = gx;
+                    double rr = rrx + (xx * exx - xc) * (xx * exx - xc);
+                    double frow = s * ipow(1.0 - rr, p);
+                    const double* src = &A3(a, 0, jx, jy);
+                    for (int k = k0; k < k1; ++k) tb[k] += frow * src[k];
+                }
+            }
+            double* dst = &A3(b, 0, ix, iy);
+            for (int k = k0; k < k1; ++k) dst[k] = tb[k];
+        }
+    a3_copy(a, b, k0, k1);
+}
+
+/* vrbeta2t (jp_pbfil.f90:1011-1050): scatter from the interior into the
+ * extended domain (b starts at zero); then a = b. */
+static void vrbeta2t(const setup_t* S, int p, arr3 a, arr3 b, int Lx, int Mx, int Ly, int My,
+                     int k0, int k1) {
+    a3_zero(b, k0, k1);
+    double exx = S->exx2, eyy = S->eyy2, eyx = S->eyx2, s = S->ss2;
+    for (int iy = Ly; iy <= My; ++iy)
+        for (int ix = Lx; ix <= Mx; ++ix) {
+            const double* ta = &A3(a, 0, ix, iy);
+            double y = 1.0 / eyy;
+            int gyl = (int)ceil(-y + EPS), gym = (int)floor(y - EPS);
+            for (int gy = gyl; gy <= gym; ++gy) {
+                int jy = iy + gy;
+                double yy = gy, xc = -yy * eyx;
+                double rrx = (yy * eyy) * (yy * eyy);
+                double x = sqrt(1.0 - rrx);
+                int gxl = (int)ceil((xc - x) / exx + EPS), gxm = (int)floor((xc + x) / exx - EPS);
+                for (int gx = gxl; gx <= gxm; ++gx) {
+                    int jx = ix + gx;
+                    double xx = gx;
+                    double rr = rrx + (xx * exx - xc) * (xx * exx - xc);
+                    double frow = s * ipow(1.0 - rr, p);
+                    double* dst = &A3(b, 0, jx, jy);
+                    for (int k = k0; k < k1; ++k) dst[k] += frow * ta[k];
+                }
+            }
+        }
+    a3_copy(a, b, k0, k1);
+}
+
+/* ------------------------------------------------------ halo fill and fold */
+
+/* boco_2d semantics at physical edges (mg_bocos.f90:225-377): y first on the
+ * interior columns, then x on all rows including the y-halo rows;
+ * half-sample mirror W(1-t) = W(t), W(M+t) = W(M+1-t). */
+static void fill_h(arr3 W, int imax, int jmax, int nbx, int nby, int k0, int k1) {
+    for (int j = 1; j <= nby; ++j)
+        for (int i = 1; i <= imax; ++i)
+            for (int k = k0; k < k1; ++k) {
+                A3(W, k, i, -nby + j) = A3(W, k, i, nby + 1 - j);
+            }
+    for (int j = 1; j <= nby; ++j)
+        for (int i = 1; i <= imax; ++i)
+            for (int k = k0; k < k1; ++k) {
+                A3(W, k, i, jmax + j) = A3(W, k, i, jmax + 1 - j);
+            }
+    for (int j = 1 - nby; j <= jmax + nby; ++j)
+        for (int i = 1; i <= nbx; ++i)
+            for (int k = k0; k < k1; ++k) {
+                A3(W, k, -nbx + i, j) = A3(W, k, nbx + 1 - i, j);
+            }
+    for (int j = 1 - nby; j <= jmax + nby; ++j)
+        for (int i = 1; i <= nbx; ++i)
+            for (int k = k0; k < k1; ++k) {
+                A3(W, k, imax + i, j) = A3(W, k, imax + 1 - i, j);
+            }
+}
+
+/* bocoT_2d semantics at physical edges (mg_bocos.f90:929-1061): x first on
+ * all rows, then y on the interior columns; halo values are left in place. */
+static void fold_h(arr3 W, int imax, int jmax, int nbx, int nby, int k0, int k1) {
+    for (int j = 1 - nby; j <= jmax + nby; ++j)
+        for (int i = 1; i <= nbx; ++i)
+            for (int k = k0; k < k1; ++k) A3(W, k, i, j) += A3(W, k, 1 - i, j);
+    for (int j = 1 - nby; j <= jmax + nby; ++j)
+        for (int i = 1; i <= nbx; ++i)
+            for (int k = k0; k < k1; ++k)
+                A3(W, k, imax - nbx + i, j) += A3(W, k, imax + 1 + nbx - i, j);
+    for (int j = 1; j <= nby; ++j)
+        for (int i = 1; i <= imax; ++i)
+            for (int k = k0; k < k1; ++k) A3(W, k, i, j) += A3(W, k, i, 1 - j);
+    for (int j = 1; j <= nby; ++j)
+        for (int i = 1; i <= imax; ++i)
+            for (int k = k0; k < k1; ++k)
+                A3(W, k, i, jmax - nby + j) += A3(W, k, i, jmax + 1 + nby - j);
+}
+
+/* ------------------------------------------------ restriction/prolongation */
+
+/* def_offset_coef (mg_interpolate.f90:61-86) */
+static const double PC[4] = {-9.0 / 128.0, 111.0 / 128.0, 29.0 / 128.0, -3.0 / 128.0};
+static const double QC[4] = {-3.0 / 128.0, 29.0 / 128.0, 111.0 / 128.0, -9.0 / 128.0};
+static const double AC[3] = {5.0 / 32.0, 30.0 / 32.0, -3.0 / 32.0};
+static const double BC[3] = {-3.0 / 32.0, 30.0 / 32.0, 5.0 / 32.0};
+
+/* adjoint (mg_generations.f90:1117-1187): P^T as a separable scatter from
+ * F(1:im,1:jm) into W(-1:imL+2,-1:jmL+2); aux is (nk, 1:im, -1:jmL+2). */
+static void adjoint4(arr3 F, arr3 W, arr3 aux, int im, int jm, int k0, int k1) {
+    int imL = im / 2, jmL = jm / 2;
+    a3_zero(aux, k0, k1);
+    for (int j = jm; j >= 2; j -= 2) {
+        int jL = j / 2;
+        for (int i = im; i >= 1; --i)
+            for (int k = k0; k < k1; ++k) {
+                double f = A3(F, k, i, j);
+                A3(aux, k, i, jL + 2) += PC[3] * f;
+                A3(aux, k, i, jL + 1) += PC[2] * f;
+                A3(aux, k, i, jL) += PC[1] * f;
+                A3(aux, k, i, jL - 1) += PC[0] * f;
+            }
+    }
+    for (int j = jm - 1; j >= 1; j -= 2) {
+        int jL = j / 2;
+        for (int i = im; i >= 1; --i)
+            for (int k = k0; k < k1; ++k) {
+                double f = A3(F, k, i, j);
+                A3(aux, k, i, jL + 2) += QC[3] * f;
+                A3(aux, k, i, jL + 1) += QC[2] * f;
+                A3(aux, k, i, jL) += QC[1] * f;
+                A3(aux, k, i, jL - 1) += QC[0] * f;
+            }
+    }
+    a3_zero(W, k0, k1);
+    for (int jL = jmL + 2; jL >= -1; --jL) {
+        for (int i = im - 1; i >= 1; i -= 2) {
+            int iL = i / 2;
+            for (int k = k0; k < k1; ++k) {
+                double w = A3(aux, k, i, jL);
+                A3(W, k, iL + 2, jL) += QC[3] * w;
+                A3(W, k, iL + 1, jL) += QC[2] * w;
+                A3(W, k, iL, jL) += QC[1] * w;
+                A3(W, k, iL - 1, jL) += QC[0] * w;
+            }
+        }
+        for (int i = im; i >= 2; i -= 2) {
+            int iL = i / 2;
+            for (int k = k0; k < k1; ++k) {
+                double w = A3(aux, k, i, jL);
+                A3(W, k, iL + 2, jL) += PC[3] * w;
+                A3(W, k, iL + 1, jL) += PC[2] * w;
+                A3(W, k, iL, jL) += PC[1] * w;
+                A3(W, k, iL - 1, jL) += PC[0] * w;
+            }
+        }
+    }
+}
+
+/* direct1 (mg_generations.f90:1190-1250): P as a separable gather from
+ * W(-1:imL+2,-1:jmL+2) to F(1:im,1:jm); aux is (nk, 1:im, -1:jmL+2). */
+static void direct4(arr3 W, arr3 F, arr3 aux, int im, int jm, int k0, int k1) {
+    int jmL = jm / 2;
+    for (int jL = -1; jL <= jmL + 2; ++jL) {
+        for (int i = 1; i <= im - 1; i += 2) {
+            int iL = i / 2;
+            for (int k = k0; k < k1; ++k)
+                A3(aux, k, i, jL) = QC[0] * A3(W, k, iL - 1, jL) + QC[1] * A3(W, k, iL, jL) +
+                                    QC[2] * A3(W, k, iL + 1, jL) + QC[3] * A3(W, k, iL + 2, jL);
+        }
+        for (int i = 2; i <= im; i += 2) {
+            int iL = i / 2;
+            for (int k = k0; k < k1; ++k)
+                A3(aux, k, i, jL) = PC[0] * A3(W, k, iL - 1, jL) + PC[1] * A3(W, k, iL, jL) +
+                                    PC[2] * A3(W, k, iL + 1, jL) + PC[3] * A3(W, k, iL + 2, jL);
+        }
+    }
+    for (int j = 1; j <= jm - 1; j += 2) {
+        int jL = j / 2;
+        for (int i = 1; i <= im; ++i)
+            for (int k = k0; k < k1; ++k)
+                A3(F, k, i, j) = QC[0] * A3(aux, k, i, jL - 1) + QC[1] * A3(aux, k, i, jL) +
+                                 QC[2] * A3(aux, k, i, jL + 1) + QC[3] * A3(aux, k, i, jL + 2);
+    }
+    for (int j = 2; j <= jm; j += 2) {
+        int jL = j / 2;
+        for (int i = 1; i <= im; ++i)
+            for (int k = k0; k < k1; ++k)
+                A3(F, k, i, j) = PC[0] * A3(aux, k, i, jL - 1) + PC[1] * A3(aux, k, i, jL) +
+                                 PC[2] * A3(aux, k, i, jL + 1) + PC[3] * A3(aux, k, i, jL + 2);
+    }
+}
+
+/* adjoint2 (mg_generations.f90:1253-1316): quadratic P^T into
+ * W(0:imL+1,0:jmL+1); aux is (nk, 1:im, 0:jmL+1). */
+static void adjoint3(arr3 F, arr3 W, arr3 aux, int im, int jm, int k0, int k1) {
+    int jmL = jm / 2;
+    a3_zero(aux, k0, k1);
+    for (int j = jm; j >= 2; j -= 2) {
+        int jL = j / 2;
+        for (int i = im; i >= 1; --i)
+            for (int k = k0; k < k1; ++k) {
+                double f = A3(F, k, i, j);
+                A3(aux, k, i, jL + 1) += BC[2] * f;
+                A3(aux, k, i, jL) += BC[1] * f;
+                A3(aux, k, i, jL - 1) += BC[0] * f;
+            }
+    }
+    for (int j = jm - 1; j >= 1; j -= 2) {
+        int jL = (j + 1) / 2;
+        for (int i = im; i >= 1; --i)
+            for (int k = k0; k < k1; ++k) {
+                double f = A3(F, k, i, j);
+                A3(aux, k, i, jL + 1) += AC[2] * f;
+                A3(aux, k, i, jL) += AC[1] * f;
+                A3(aux, k, i, jL - 1) += AC[0] * f;
+            }
+    }
+    a3_zero(W, k0, k1);
+    for (int jL = jmL + 1; jL >= 0; --jL) {
+        for (int i = im - 1; i >= 1; i -= 2) {
+            int iL = (i + 1) / 2;
+            for (int k = k0; k < k1; ++k) {
+                double w = A3(aux, k, i, jL);
+                A3(W, k, iL + 1, jL) += AC[2] * w;
+                A3(W, k, iL, jL) += AC[1] * w;
+                A3(W, k, iL - 1, jL) += AC[0] * w;
+            }
+        }
+        for (int i = im; i >= 2; i -= 2) {
+            int iL = i / 2;
+            for (int k = k0; k < k1; ++k) {
+                double w = A3(aux, k, i, jL);
+                A3(W, k, iL + 1, jL) += BC[2] * w;
+                A3(W, k, iL, jL) += BC[1] * w;
+                A3(W, k, iL - 1, jL) += BC[0] * w;
+            }
+        }
+    }
+}
+
+/* direct2 (mg_generations.f90:1319-1374): quadratic P. */
+static void direct3(arr3 W, arr3 F, arr3 aux, int im, int jm, int k0, int k1) {
+    int jmL = jm / 2;
+    for (int jL = 0; jL <= jmL + 1; ++jL) {
+        for (int i = 1; i <= im - 1; i += 2) {
+            int iL = (i + 1) / 2;
+            for (int k = k0; k < k1; ++k)
+                A3(aux, k, i, jL) = AC[0] * A3(W, k, iL - 1, jL) + AC[1] * A3(W, k, iL, jL) +
+                                    AC[2] * A3(W, k, iL + 1, jL);
+        }
+        for (int i = 2; i <= im; i += 2) {
+            int iL = i / 2;
+            for (int k = k0; k < k1; ++k)
+                A3(aux, k, i, jL) = BC[0] * A3(W, k, iL - 1, jL) + BC[1] * A3(W, k, iL, jL) +
+                                    BC[2] * A3(W, k, iL + 1, jL);
+        }
+    }
+    for (int j = 1; j <= jm - 1; j += 2) {
+        int jL = (j + 1) / 2;
+        for (int i = 1; i <= im; ++i)
+            for (int k = k0; k < k1; ++k)
+                A3(F, k, i, j) = AC[0] * A3(aux, k, i, jL - 1) + AC[1] * A3(aux, k, i, jL) +
+                                 AC[2] * A3(aux, k, i, jL + 1);
+    }
+    for (int j = 2; j <= jm; j += 2) {
+        int jL = j / 2;
+        for (int i = 1; i <= im; ++i)
+            for (int k = k0; k < k1; ++k)
+                A3(F, k, i, j) = BC[0] * A3(aux, k, i, jL - 1) + BC[1] * A3(aux, k, i, jL) +
+                                 BC[2] * A3(aux, k, i, jL + 1);
+    }
+}
+
+/* ------------------------------------------------------------- vertical */
+
+/* sup_vrbeta1_bck / sup_vrbeta1_ens (mg_filtering.f90:2154-2202, 2042-2091)
+ * with vrbeta1 (jp_pbfil.f90:856-885): per (i,j), gather nz columns of lm
+ * levels at offsets (k-1)*lm, whole-sample mirror by hz, filter, write back.
+ * adj != 0 gives sup_vrbeta1T_* (mg_filtering.f90:2205-2262, 2094-2151) with
+ * vrbeta1t (jp_pbfil.f90:981-1009) and the edge fold. */
+static void vfilter(const orc_cfg* c, const setup_t* S, arr3 V, int adj) {
+    const int lm = c->lm, hz = c->hz, nz = c->nzcol, p = c->p;
+    const int ext = lm + 2 * hz;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(c->nthreads > 0 ? c->nthreads : omp_get_max_threads())
+#endif
+    for (int j = 1; j <= c->J; ++j) {
+        double* W = (double*)malloc(sizeof(double) * (size_t)nz * ext);
+        double* B = (double*)malloc(sizeof(double) * (size_t)nz * ext);
+#define WZ(arr, k, L) arr[(size_t)(k) + (size_t)nz * (size_t)((L) + hz - 1)]
+        for (int i = 1; i <= c->I; ++i) {
+            for (int k = 0; k < nz; ++k)
+                for (int L = 1; L <= lm; ++L) WZ(W, k, L) = A3(V, k * lm + L - 1, i, j);
+            for (int L = 1; L <= hz; ++L)
+                for (int k = 0; k < nz; ++k) {
+                    WZ(W, k, 1 - L) = WZ(W, k, 1 + L);
+                    WZ(W, k, lm + L) = WZ(W, k, lm - L);
+                }
+            for (size_t t = 0; t < (size_t)nz * ext; ++t) B[t] = 0.0;
+            double exx = S->exx1, s = S->ss1;
+            double x = 1.0 / exx;
+            int gxl = (int)ceil(-x + EPS), gxm = (int)floor(x - EPS);
+            if (!adj) {
+                for (int ix = 1; ix <= lm; ++ix) {
+                    for (int gx = gxl; gx <= gxm; ++gx) {
+                        int jx = ix + gx;
+                        double xx = gx, rr = (xx * exx) * (xx * exx);
+                        double frow = s * ipow(1.0 - rr, p);
+                        for (int k = 0; k < nz; ++k) WZ(B, k, ix) += frow * WZ(W, k, jx);
+                    }
+                }
+            } else {
+                for (int ix = 1; ix <= lm; ++ix) {
+                    for (int gx = gxl; gx <= gxm; ++gx) {
+                        int jx = ix + gx;
+                        double xx = gx, rr = (xx * exx) * (xx * exx);
+                        double frow = s * ipow(1.0 - rr, p);
+                        for (int k = 0; k < nz; ++k) WZ(B, k, jx) += frow * WZ(W, k, ix);
+                    }
+                }
+                for (int L = 1; L <= hz; ++L)
+                    for (int k = 0; k < nz; ++k) {
+                        WZ(B, k, 1 + L) += WZ(B, k, 1 - L);
+                        WZ(B, k, lm - L) += WZ(B, k, lm + L);
+                    }
+            }
+            for (int k = 0; k < nz; ++k)
+                for (int L = 1; L <= lm; ++L) A3(V, k * lm + L - 1, i, j) = WZ(B, k, L);
+        }
+#undef WZ
+        free(W);
+        free(B);
+    }
+}
+
+/* ------------------------------------------------------------- pipeline */
+
+typedef struct {
+    int I, J;
+    arr3 H;     /* (nk, 1-hx:I+hx, 1-hy:J+hy) */
+    arr3 tmp;   /* same shape, scratch for filters */
+    arr3 INT;   /* coarse transfer (nk, -1:I/2+2, -1:J/2+2) */
+    arr3 aux;   /* (nk, 1:I, -1:J/2+2) */
+} gen_t;
+
+static int check_cfg(const orc_cfg* c) {
+    if (!c || c->I <= 0 || c->J <= 0 || c->nk <= 0 || c->gm < 1 || c->gm > ORC_MAX_GEN) return ORC_ERR_ARG;
+    if (c->hx < 0 || c->hy < 0 || c->hz < 0 || c->p < 0) return ORC_ERR_ARG;
+    if (c->proc != 1 && c->proc != 6) return ORC_ERR_ARG;
+    int d = 1 << (c->gm - 1);
+    if (c->I % d || c->J % d) return ORC_ERR_DIV;
+    if (c->gm > 1 && (c->I / d < 2 || c->J / d < 2)) return ORC_ERR_DIV;
+    if (c->hx > c->I / d || c->hy > c->J / d) return ORC_ERR_DIV;
+    if (c->l_vertical_filter) {
+        if (c->lm < 1 || c->nzcol < 0 || (size_t)c->nzcol * c->lm > (size_t)c->nk) return ORC_ERR_ARG;
+        if (c->nzcol > 0 && c->hz >= c->lm) return ORC_ERR_ARG;
+    }
+    return ORC_OK;
+}
+
+static void gens_alloc(const orc_cfg* c, gen_t* G) {
+    for (int g = 0; g < c->gm; ++g) {
+        int I = c->I >> g, J = c->J >> g;
+        G[g].I = I; G[g].J = J;
+        G[g].H = g ? a3_alloc(c->nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy) : (arr3){0};
+        G[g].tmp = a3_alloc(c->nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy);
+        G[g].INT = a3_alloc(c->nk, -1, I / 2 + 2, -1, J / 2 + 2);
+        G[g].aux = a3_alloc(c->nk, 1, I, -1, J / 2 + 2);
+    }
+}
+static void gens_free(const orc_cfg* c, gen_t* G) {
+    for (int g = 0; g < c->gm; ++g) {
+        if (g) a3_free(&G[g].H);
+        a3_free(&G[g].tmp); a3_free(&G[g].INT); a3_free(&G[g].aux);
+    }
+}
+
+/* Restriction g -> g+1 (upsending, mg_generations.f90:158-207 and 382-432;
+ * lquart: upsending2*, 270-319, 497-547): adjoint + fold with halo 2 (1),
+ * then the coarse interior becomes generation g+1 (upsend_all). */
+static void restrict_gen(const orc_cfg* c, arr3 fine, gen_t* Gf, arr3 coarse, int k0, int k1) {
+    int I = Gf->I, J = Gf->J, IL = I / 2, JL = J / 2;
+    if (!c->lquart) {
+        adjoint4(fine, Gf->INT, Gf->aux, I, J, k0, k1);
+        fold_h(Gf->INT, IL, JL, 2, 2, k0, k1);
+        for (int j = 1; j <= JL; ++j)
+            for (int i = 1; i <= IL; ++i)
+                for (int k = k0; k < k1; ++k) A3(coarse, k, i, j) = A3(Gf->INT, k, i, j);
+    } else {
+        arr3 W = Gf->INT; /* view (0:IL+1, 0:JL+1) inside the (-1:IL+2) buffer */
+        W.ilo = 0; W.ihi = IL + 1; W.jlo = 0; W.jhi = JL + 1;
+        arr3 aux = Gf->aux; aux.jlo = 0; aux.jhi = JL + 1;
+        adjoint3(fine, W, aux, I, J, k0, k1);
+        fold_h(W, IL, JL, 1, 1, k0, k1);
+        for (int j = 1; j <= JL; ++j)
+            for (int i = 1; i <= IL; ++i)
+                for (int k = k0; k < k1; ++k) A3(coarse, k, i, j) = A3(W, k, i, j);
+    }
+}
+
+/* Prolongation and add g+1 -> g (downsending, mg_generations.f90:210-267,
+ * 435-494; lquart: downsending2*): coarse interior copied into the transfer
+ * array, halo 2 (1) filled, direct1 (direct2), result added to fine. */
+static void prolong_add(const orc_cfg* c, arr3 coarse, gen_t* Gf, arr3 fine, int k0, int k1) {
+    int I = Gf->I, J = Gf->J, IL = I / 2, JL = J / 2;
+    arr3 W = Gf->INT, aux = Gf->aux;
+    int nb = 2;
+    if (c->lquart) { W.ilo = 0; W.ihi = IL + 1; W.jlo = 0; W.jhi = JL + 1; aux.jlo = 0; aux.jhi = JL + 1; nb = 1; }
+    for (int j = 1; j <= JL; ++j)
+        for (int i = 1; i <= IL; ++i)
+            for (int k = k0; k < k1; ++k) A3(W, k, i, j) = A3(coarse, k, i, j);
+    fill_h(W, IL, JL, nb, nb, k0, k1);
+    /* H_PROX / V_PROX live in tmp's interior */
+    arr3 F = Gf->tmp;
+    arr3 Fi = F; /* interior-only view for direct: reuse the full array */
+    if (!c->lquart) direct4(W, Fi, aux, I, J, k0, k1);
+    else direct3(W, Fi, aux, I, J, k0, k1);
+    for (int j = 1; j <= J; ++j)
+        for (int i = 1; i <= I; ++i)
+            for (int k = k0; k < k1; ++k) A3(fine, k, i, j) += A3(F, k, i, j);
+}
+
+/* weighting / weighting_helm / weighting_ens (mg_generations.f90:901-1052). */
+static void weight_gen(const orc_cfg* c, arr3 V, int I, int J, double a, double b, int k0, int k1) {
+    if (!c->lhelm || b == 0.0) {
+        if (c->lhelm) {
+            /* a*V - 0*(Laplacian): the Laplacian reads halo cells left by the
+             * fold; they are finite, so the product is exactly zero. */
+        }
+        for (int j = 1; j <= J; ++j)
+            for (int i = 1; i <= I; ++i)
+                for (int k = k0; k < k1; ++k) A3(V, k, i, j) *= a;
+        return;
+    }
+    /* b != 0 is an extension (the reference fixes b = 0); the reference
+     * would read stale fold halos, so fill a 1-wide mirror halo first. */
+    fill_h(V, I, J, 1, 1, k0, k1);
+    size_t n = (size_t)(k1 - k0) * I * J;
+    double* out = (double*)malloc(sizeof(double) * (n ? n : 1));
+    size_t t = 0;
+    for (int j = 1; j <= J; ++j)
+        for (int i = 1; i <= I; ++i)
+            for (int k = k0; k < k1; ++k) {
+                double v = A3(V, k, i, j);
+                double lap = A3(V, k, i + 1, j) - 2 * v + A3(V, k, i - 1, j) + A3(V, k, i, j + 1) -
+                             2 * v + A3(V, k, i, j - 1);
+                out[t++] = a * v - b * lap;
+            }
+    t = 0;
+    for (int j = 1; j <= J; ++j)
+        for (int i = 1; i <= I; ++i)
+            for (int k = k0; k < k1; ++k) A3(V, k, i, j) = out[t++];
+    free(out);
+}
+
+static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G, int k0, int k1) {
+    const int gm = c->gm, hx = c->hx, hy = c->hy;
+    const int filt1 = (c->proc == 1) || c->l_filt_g1;
+    double* tb = (double*)malloc(sizeof(double) * (size_t)c->nk);
+    /* up: V -> H_2 -> ... -> H_gm */
+    for (int g = 0; g + 1 < gm; ++g) {
+        arr3 fine = g ? G[g].H : V;
+        restrict_gen(c, fine, &G[g], G[g + 1].H, k0, k1);
+    }
+    /* adjoint filter on all generations, fold, weight, fill, filter */
+    for (int g = 0; g < gm; ++g) {
+        arr3 U = g ? G[g].H : V;
+        int I = G[g].I, J = G[g].J;
+        if (g == 0 && !filt1) continue;
+        vrbeta2t(S, c->p, U, G[g].tmp, 1, I, 1, J, k0, k1);
+        fold_h(U, I, J, hx, hy, k0, k1);
+        weight_gen(c, U, I, J, c->a[g], c->b[g], k0, k1);
+        fill_h(U, I, J, hx, hy, k0, k1);
+        vrbeta2(S, c->p, U, G[g].tmp, 1, I, 1, J, k0, k1, tb);
+    }
+    /* down: H_gm -> ... -> H_2 -> V */
+    for (int g = gm - 1; g >= 1; --g) {
+        arr3 fine = (g - 1) ? G[g - 1].H : V;
+        prolong_add(c, G[g].H, &G[g - 1], fine, k0, k1);
+    }
+    free(tb);
+}
+
+int orc_filtering_procedure(const orc_cfg* c, double* Vd) {
+    int rc = check_cfg(c);
+    if (rc) return rc;
+    setup_t S;
+    rc = setup(c, &S);
+    if (rc) return rc;
+    arr3 V = {Vd, c->nk, 1 - c->hx, c->I + c->hx, 1 - c->hy, c->J + c->hy};
+    if (c->l_vertical_filter && c->nzcol > 0) vfilter(c, &S, V, 1);
+    gen_t G[ORC_MAX_GEN];
+    memset(G, 0, sizeof(G));
+    gens_alloc(c, G);
+    int nth = 1;
+#ifdef _OPENMP
+    nth = c->nthreads > 0 ? c->nthreads : omp_get_max_threads();
+    if (nth > c->nk) nth = c->nk;
+#pragma omp parallel num_threads(nth)
+    {
+        int t = omp_get_thread_num(), nt = omp_get_num_threads();
+        int k0 = (int)((long long)c->nk * t / nt), k1 = (int)((long long)c->nk * (t + 1) / nt);
+        if (k1 > k0) horizontal_pipeline(c, &S, V, G, k0, k1);
+    }
+#else
+    (void)nth;
+    horizontal_pipeline(c, &S, V, G, 0, c->nk);
+#endif
+    gens_free(c, G);
+    if (c->l_vertical_filter && c->nzcol > 0) vfilter(c, &S, V, 0);
+    return ORC_OK;
+}
+
+static double* to_halo(const orc_cfg* c, const double* x) {
+    size_t ni = (size_t)c->I + 2 * c->hx, nj = (size_t)c->J + 2 * c->hy;
+    double* V = (double*)calloc((size_t)c->nk * ni * nj, sizeof(double));
+    if (!V) return NULL;
+    arr3 a = {V, c->nk, 1 - c->hx, c->I + c->hx, 1 - c->hy, c->J + c->hy};
+    for (int j = 1; j <= c->J; ++j)
+        for (int i = 1; i <= c->I; ++i)
+            memcpy(&A3(a, 0, i, j), x + (size_t)c->nk * ((size_t)(i - 1) + (size_t)c->I * (j - 1)),
+                   sizeof(double) * c->nk);
+    return V;
+}
+static void from_halo(const orc_cfg* c, const double* V, double* y) {
+    arr3 a = {(double*)V, c->nk, 1 - c->hx, c->I + c->hx, 1 - c->hy, c->J + c->hy};
+    for (int j = 1; j <= c->J; ++j)
+        for (int i = 1; i <= c->I; ++i)
+            memcpy(y + (size_t)c->nk * ((size_t)(i - 1) + (size_t)c->I * (j - 1)), &A3(a, 0, i, j),
+                   sizeof(double) * c->nk);
+}
+
+int orc_filter_compact(const orc_cfg* c, const double* x, double* y) {
+    int rc = check_cfg(c);
+    if (rc) return rc;
+    double* V = to_halo(c, x);
+    if (!V) return ORC_ERR_ARG;
+    rc = orc_filtering_procedure(c, V);
+    if (!rc) from_halo(c, V, y);
+    free(V);
+    return rc;
+}
+
+/* u_g = B_g R_g Bz^T x for every generation, written into G[g] (gen 0 into V). */
+static void half_chain(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G) {
+    if (c->l_vertical_filter && c->nzcol > 0) vfilter(c, S, V, 1);
+    const int filt1 = (c->proc == 1) || c->l_filt_g1;
+    for (int g = 0; g + 1 < c->gm; ++g)
+        restrict_gen(c, g ? G[g].H : V, &G[g], G[g + 1].H, 0, c->nk);
+    for (int g = 0; g < c->gm; ++g) {
+        if (g == 0 && !filt1) continue;
+        arr3 U = g ? G[g].H : V;
+        vrbeta2t(S, c->p, U, G[g].tmp, 1, G[g].I, 1, G[g].J, 0, c->nk);
+        fold_h(U, G[g].I, G[g].J, c->hx, c->hy, 0, c->nk);
+    }
+}
+
+int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double* ga) {
+    int rc = check_cfg(c);
+    if (rc) return rc;
+    setup_t S;
+    rc = setup(c, &S);
+    if (rc) return rc;
+    double* Vx = to_halo(c, x);
+    double* Vy = to_halo(c, gy);
+    gen_t Gx[ORC_MAX_GEN], Gy[ORC_MAX_GEN];
+    memset(Gx, 0, sizeof(Gx)); memset(Gy, 0, sizeof(Gy));
+    gens_alloc(c, Gx); gens_alloc(c, Gy);
+    arr3 ax = {Vx, c->nk, 1 - c->hx, c->I + c->hx, 1 - c->hy, c->J + c->hy};
+    arr3 ay = {Vy, c->nk, 1 - c->hx, c->I + c->hx, 1 - c->hy, c->J + c->hy};
+    half_chain(c, &S, ax, Gx);
+    half_chain(c, &S, ay, Gy);
+    const int filt1 = (c->proc == 1) || c->l_filt_g1;
+    for (int g = 0; g < c->gm; ++g) {
+        double s = 0.0;
+        if (g == 0 && !filt1) { ga[g] = 0.0; continue; }
+        arr3 U = g ? Gx[g].H : ax, W = g ? Gy[g].H : ay;
+        for (int j = 1; j <= Gx[g].J; ++j)
+            for (int i = 1; i <= Gx[g].I; ++i)
+                for (int k = 0; k < c->nk; ++k) s += A3(U, k, i, j) * A3(W, k, i, j);
+        ga[g] = s;
+    }
+    gens_free(c, Gx); gens_free(c, Gy);
+    free(Vx); free(Vy);
+    return ORC_OK;
+}
+
+int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y) {
+    int rc = check_cfg(c);
+    if (rc) return rc;
+    setup_t S;
+    rc = setup(c, &S);
+    if (rc) return rc;
+    if (gen < 1 || gen > c->gm) return ORC_ERR_ARG;
+    int I = c->I >> (gen - 1), J = c->J >> (gen - 1), nk = c->nk;
+    if (which == 0 || which == 1) {
+        orc_cfg cc = *c; cc.I = I; cc.J = J;
+        double* V = to_halo(&cc, x);
+        arr3 a = {V, nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy};
+        vfilter(&cc, &S, a, which == 1);
+        from_halo(&cc, V, y);
+        free(V);
+        return ORC_OK;
+    }
+    if (which == 2 || which == 3) {
+        orc_cfg cc = *c; cc.I = I; cc.J = J;
+        double* V = to_halo(&cc, x);
+        arr3 a = {V, nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy};
+        arr3 t = a3_alloc(nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy);
+        double* tb = (double*)malloc(sizeof(double) * nk);
+        if (which == 2) {
+            fill_h(a, I, J, c->hx, c->hy, 0, nk);
+            vrbeta2(&S, c->p, a, t, 1, I, 1, J, 0, nk, tb);
+        } else {
+            vrbeta2t(&S, c->p, a, t, 1, I, 1, J, 0, nk);
+            fold_h(a, I, J, c->hx, c->hy, 0, nk);
+        }
+        from_halo(&cc, V, y);
+        free(tb); a3_free(&t); free(V);
+        return ORC_OK;
+    }
+    if (which == 4 || which == 5) {
+        if (gen >= c->gm) return ORC_ERR_ARG;
+        gen_t Gf;
+        memset(&Gf, 0, sizeof(Gf));
+        Gf.I = I; Gf.J = J;
+        Gf.tmp = a3_alloc(nk, 1, I, 1, J);
+        Gf.INT = a3_alloc(nk, -1, I / 2 + 2, -1, J / 2 + 2);
+        Gf.aux = a3_alloc(nk, 1, I, -1, J / 2 + 2);
+        arr3 fine = a3_alloc(nk, 1, I, 1, J);
+        arr3 coarse = a3_alloc(nk, 1, I / 2, 1, J / 2);
+        if (which == 4) {
+            memcpy(fine.d, x, sizeof(double) * (size_t)nk * I * J);
+            restrict_gen(c, fine, &Gf, coarse, 0, nk);
+            memcpy(y, coarse.d, sizeof(double) * (size_t)nk * (I / 2) * (J / 2));
+        } else {
+            memcpy(coarse.d, x, sizeof(double) * (size_t)nk * (I / 2) * (J / 2));
+            prolong_add(c, coarse, &Gf, fine, 0, nk); /* fine starts at zero */
+            memcpy(y, fine.d, sizeof(double) * (size_t)nk * I * J);
+        }
+        a3_free(&Gf.tmp); a3_free(&Gf.INT); a3_free(&Gf.aux); a3_free(&fine); a3_free(&coarse);
+        return ORC_OK;
+    }
+    return ORC_ERR_ARG;
+}

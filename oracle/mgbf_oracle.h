@@ -1,0 +1,84 @@
+/*
+ * FP64 CPU oracle for the MGBF filtering pipeline (test infrastructure only).
+ *
+ * This is a plain-C restatement of the reference's CPU algorithm for
+ * filtering_procedure(1) (filtering_rad2_bckg) and filtering_procedure(6)
+ * (filtering_rad2_ens), evaluated on the whole filter grid as one domain.
+ * It exists to check the CUDA library; only tests, the smoke check and the
+ * CPU-baseline leg of the benchmark call it.  Nothing in the shipped library
+ * links or executes it.
+ *
+ * Parity status: unpinned.  The reference is Fortran 90 + MPI and no Fortran
+ * compiler or MPI exists on the machines this project is built and tested on,
+ * and the reference ships no tests, golden vectors or known-answer data for
+ * this path.  The restatement is pinned only by its own invariants (adjoint
+ * pairs, unit row sums, self-adjointness, symmetry) and by agreement with an
+ * independent literal emulation of the reference's MPI tiling
+ * (oracle/virtual_ranks.py).
+ *
+ * Storage follows the reference's VALL(km_all, 1-hx:im+hx, 1-hy:jm+hy)
+ * (src.mgbf/mg_intstate.f90:157): level index fastest, then i, then j, FP64.
+ */
+#ifndef MGBF_ORACLE_H
+#define MGBF_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_MAX_GEN 16
+
+typedef struct orc_cfg {
+    int I, J;            /* generation-1 filter grid (im00 x jm00)            */
+    int nk;              /* leading dimension of VALL (km_all)                */
+    int hx, hy, hz;      /* halo widths (filter reach limits)                 */
+    int p;               /* beta-function exponent (integer, as in reference) */
+    double ampl01;       /* mg_ampl01: vertical aspect                        */
+    double ampl02;       /* mg_ampl02: horizontal aspect                      */
+    int gm;              /* number of generations                             */
+    double a[ORC_MAX_GEN];  /* per-generation weights a_g (a[0] = gen 1)      */
+    double b[ORC_MAX_GEN];  /* Helmholtz Laplacian coefficients (reference: 0) */
+    int lhelm;           /* use weighting_helm form                           */
+    int proc;            /* 1 (rad2_bckg) or 6 (rad2_ens)                     */
+    int l_vertical_filter;
+    int l_filt_g1;       /* proc 6 only                                       */
+    int lquart;          /* quadratic (3-point) interpolation                 */
+    int lm;              /* levels per vertical column                        */
+    int nzcol;           /* number of z columns at offsets (k-1)*lm           */
+    int nthreads;        /* OpenMP threads (<=0: runtime default)             */
+} orc_cfg;
+
+/* Error codes (negative), mirroring the library's. */
+#define ORC_OK 0
+#define ORC_ERR_ARG (-1)
+#define ORC_ERR_REACH (-3)
+#define ORC_ERR_DIV (-4)
+
+/* Apply the whole filtering procedure in place on V, laid out as
+ * (nk, 1-hx:I+hx, 1-hy:J+hy).  Halo contents on entry are ignored except
+ * where the reference would read them. */
+int orc_filtering_procedure(const orc_cfg* c, double* V);
+
+/* Same, on a compact (nk, I, J) array (x -> y; x == y allowed). */
+int orc_filter_compact(const orc_cfg* c, const double* x, double* y);
+
+/* Per-generation weight gradients: ga[g] = sum u_g * v_g with
+ * u_g = B_g R_g Bz^T x and v_g = B_g R_g Bz^T gy (compact arrays). */
+int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double* ga);
+
+/* Stage-level entry points on compact arrays, for adjoint-pair tests.
+ * which: 0 = z forward Bz, 1 = z adjoint Bz^T,
+ *        2 = horizontal forward (fill + vrbeta2), 3 = horizontal adjoint
+ *            (vrbeta2t + fold), on a generation-g grid (g given by gen),
+ *        4 = restriction R (g -> g+1; x is gen g, y is gen g+1),
+ *        5 = prolongation P (g+1 -> g; x is gen g+1, y is gen g). */
+int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y);
+
+/* Setup values (for tests): rmom2_1, rmom2_2, exx (1D), exx (2D), ss1, ss2,
+ * vertical reach, horizontal reach.  Returns error if a reach exceeds a halo. */
+int orc_setup_values(const orc_cfg* c, double out[8]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

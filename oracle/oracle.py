@@ -1,0 +1,169 @@
+"""ctypes wrapper around the FP64 C oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module.  It restates the reference's CPU algorithm for
+filtering_procedure(1|6); it is the checker, never the thing measured or
+shipped.  Parity with the reference itself is unpinned (see mgbf_oracle.h).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import build as _build
+
+MAX_GEN = 16
+
+
+class _Cfg(ctypes.Structure):
+    _fields_ = [
+        ("I", ctypes.c_int), ("J", ctypes.c_int), ("nk", ctypes.c_int),
+        ("hx", ctypes.c_int), ("hy", ctypes.c_int), ("hz", ctypes.c_int),
+        ("p", ctypes.c_int),
+        ("ampl01", ctypes.c_double), ("ampl02", ctypes.c_double),
+        ("gm", ctypes.c_int),
+        ("a", ctypes.c_double * MAX_GEN), ("b", ctypes.c_double * MAX_GEN),
+        ("lhelm", ctypes.c_int), ("proc", ctypes.c_int),
+        ("l_vertical_filter", ctypes.c_int), ("l_filt_g1", ctypes.c_int),
+        ("lquart", ctypes.c_int), ("lm", ctypes.c_int), ("nzcol", ctypes.c_int),
+        ("nthreads", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        lib = ctypes.CDLL(path)
+        dp = ctypes.POINTER(ctypes.c_double)
+        cp = ctypes.POINTER(_Cfg)
+        lib.orc_filtering_procedure.argtypes = [cp, dp]
+        lib.orc_filter_compact.argtypes = [cp, dp, dp]
+        lib.orc_weight_grads.argtypes = [cp, dp, dp, dp]
+        lib.orc_stage.argtypes = [cp, ctypes.c_int, ctypes.c_int, dp, dp]
+        lib.orc_setup_values.argtypes = [cp, dp]
+        for f in (lib.orc_filtering_procedure, lib.orc_filter_compact, lib.orc_weight_grads,
+                  lib.orc_stage, lib.orc_setup_values):
+            f.restype = ctypes.c_int
+        _lib = lib
+    return _lib
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+@dataclass
+class OracleConfig:
+    """Global-grid form of the reference's parameters (mg_parameter.f90)."""
+    I: int
+    J: int
+    nk: int
+    hx: int
+    hy: int
+    hz: int
+    p: int
+    ampl01: float
+    ampl02: float
+    gm: int
+    weights: List[float]
+    proc: int = 1
+    lm: int = 1
+    nzcol: int = 0
+    l_vertical_filter: bool = True
+    l_filt_g1: bool = True
+    lquart: bool = False
+    lhelm: bool = False
+    helm_b: Optional[List[float]] = None
+    nthreads: int = 0
+
+    def to_c(self) -> _Cfg:
+        c = _Cfg()
+        c.I, c.J, c.nk = self.I, self.J, self.nk
+        c.hx, c.hy, c.hz, c.p = self.hx, self.hy, self.hz, self.p
+        c.ampl01, c.ampl02 = float(self.ampl01), float(self.ampl02)
+        c.gm = self.gm
+        for g in range(self.gm):
+            c.a[g] = float(self.weights[g])
+            c.b[g] = float(self.helm_b[g]) if self.helm_b else 0.0
+        c.lhelm = int(self.lhelm)
+        c.proc = self.proc
+        c.l_vertical_filter = int(self.l_vertical_filter)
+        c.l_filt_g1 = int(self.l_filt_g1)
+        c.lquart = int(self.lquart)
+        c.lm = self.lm
+        c.nzcol = self.nzcol
+        c.nthreads = self.nthreads
+        return c
+
+    def gen_shape(self, g: int):
+        return (self.J >> (g - 1), self.I >> (g - 1), self.nk)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        raise OracleError(f"{what} failed with code {rc}")
+
+
+def filter_compact(cfg: OracleConfig, x: np.ndarray) -> np.ndarray:
+    """y = L x on a compact array shaped (J, I, nk) (C order == Fortran (nk,I,J))."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    assert x.shape == (cfg.J, cfg.I, cfg.nk), x.shape
+    y = np.empty_like(x)
+    c = cfg.to_c()
+    _check(_load().orc_filter_compact(ctypes.byref(c), _ptr(x), _ptr(y)), "orc_filter_compact")
+    return y
+
+
+def filtering_procedure(cfg: OracleConfig, vall: np.ndarray) -> None:
+    """In place on VALL laid out (J+2hy, I+2hx, nk) in C order."""
+    assert vall.dtype == np.float64 and vall.flags.c_contiguous
+    assert vall.shape == (cfg.J + 2 * cfg.hy, cfg.I + 2 * cfg.hx, cfg.nk)
+    c = cfg.to_c()
+    _check(_load().orc_filtering_procedure(ctypes.byref(c), _ptr(vall)), "orc_filtering_procedure")
+
+
+def weight_grads(cfg: OracleConfig, x: np.ndarray, gy: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    gy = np.ascontiguousarray(gy, dtype=np.float64)
+    ga = np.zeros(cfg.gm, dtype=np.float64)
+    c = cfg.to_c()
+    _check(_load().orc_weight_grads(ctypes.byref(c), _ptr(x), _ptr(gy), _ptr(ga)), "orc_weight_grads")
+    return ga
+
+
+STAGE_Z_FWD, STAGE_Z_ADJ, STAGE_H_FWD, STAGE_H_ADJ, STAGE_RESTRICT, STAGE_PROLONG = range(6)
+
+
+def stage(cfg: OracleConfig, which: int, gen: int, x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    J, I, nk = cfg.gen_shape(gen)
+    if which == STAGE_RESTRICT:
+        out_shape = (J // 2, I // 2, nk)
+    elif which == STAGE_PROLONG:
+        out_shape = (J, I, nk)
+    else:
+        out_shape = (J, I, nk)
+    y = np.zeros(out_shape, dtype=np.float64)
+    c = cfg.to_c()
+    _check(_load().orc_stage(ctypes.byref(c), which, gen, _ptr(x), _ptr(y)), f"orc_stage({which})")
+    return y
+
+
+def setup_values(cfg: OracleConfig) -> dict:
+    out = np.zeros(8, dtype=np.float64)
+    c = cfg.to_c()
+    _check(_load().orc_setup_values(ctypes.byref(c), _ptr(out)), "orc_setup_values")
+    keys = ["rmom2_1", "rmom2_2", "exx1", "exx2", "ss1", "ss2", "reach_z", "reach_h"]
+    return dict(zip(keys, out.tolist()))

@@ -1,0 +1,938 @@
+// C-ABI of libmgbf: configuration, namelist, handles, and the host-side
+// orchestration of the filtering pipeline on one GPU.
+//
+// Pipeline of filtering_procedure(1|6) (mg_filtering.f90:560-680,
+// 1000-1147) over the whole filter grid, with every generation one global
+// array (the reference's MPI tiles and my_hgen ranks collapse):
+//   1. x1 = Bz^T x                       sup_vrbeta1T_*       (k_zfilter, adjoint band)
+//   2. H_{g+1} = R H_g                    upsending*           (k_restrict)
+//   3. per generation u = B(a_g B u)      rbetaT, bocoT_2d, weighting*, boco_2d, rbeta
+//                                          (moment or direct radial kernel, twice;
+//                                           B^T == B for the half-sample mirror)
+//   4. H_{g-1} += P H_g, x1 += P H_2      downsending*         (k_prolong)
+//   5. y = Bz x1                          sup_vrbeta1_*        (k_zfilter, forward band)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/mgbf.h"
+#include "mgbf_kernels.cuh"
+#include "mgbf_setup.hpp"
+
+using namespace mgbf;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(MGBF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CU(call)                                         \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+#define LK(call)                                                           \
+    do {                                                                   \
+        int r_ = (call);                                                   \
+        if (r_ != 0) return fail(MGBF_ERR_CUDA, std::string(#call) + ": " + \
+                                 cudaGetErrorString((cudaError_t)r_));     \
+    } while (0)
+
+size_t elem_size(DType t) { return t == DType::F64 ? 8 : (t == DType::F32 ? 4 : 2); }
+size_t acc_size(DType t) { return t == DType::F64 ? 8 : 4; }
+
+// ------------------------------------------------------------- device memory
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) {
+        o.p = nullptr;
+        o.bytes = 0;
+    }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p;
+            bytes = o.bytes;
+            o.p = nullptr;
+            o.bytes = 0;
+        }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    int ensure(size_t n) {
+        if (bytes >= n && p) return 0;
+        release();
+        if (n == 0) return 0;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return cuda_fail(e, "cudaMalloc");
+        }
+        bytes = n;
+        return 0;
+    }
+};
+
+template <typename V>
+int upload(DevBuf& b, const std::vector<V>& v) {
+    int rc = b.ensure(v.size() * sizeof(V));
+    if (rc) return rc;
+    if (!v.empty()) CU(cudaMemcpy(b.p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+int upload_acc(DevBuf& b, const std::vector<double>& v, DType t) {
+    if (t == DType::F64) return upload(b, v);
+    std::vector<float> f(v.begin(), v.end());
+    return upload(b, f);
+}
+
+// ---------------------------------------------------------------- the plan
+
+// Tables converted to one accumulation type (float or double).
+struct AccTables {
+    bool ready = false;
+    DevBuf zfwd, zadj, hw;
+    std::vector<std::unique_ptr<DevBuf>> rwx, rwy, pwx, pwy;  // per generation
+};
+
+struct Group {
+    int nk = 0, lm = 1, nzcol = 0, hx = 0, hy = 0, hz = 0, p = 2;
+    double ampl01 = 1, ampl02 = 1;
+    HStencil hs;
+    ZStencil zs;
+    int HXP = 0;  // x padding of internal generation buffers
+    DevBuf mrow;  // int table, shared by all types
+    AccTables tab[2];  // [0] float, [1] double
+    // internal buffers per storage type and generation: A, B, C
+    struct Set {
+        std::vector<std::unique_ptr<DevBuf>> A, B, C;
+    } bufs[3];
+};
+
+struct Plan {
+    int I = 0, J = 0, gm = 1;
+    double a[MGBF_MAX_GEN] = {0};
+    bool lquart = false;
+    std::vector<Interp1D> ix, iy;  // per generation g (fine size I_g), g = 0..gm-2
+    DevBuf pix[MGBF_MAX_GEN], piy[MGBF_MAX_GEN];  // prolongation index tables
+    std::vector<Group> groups;
+    DevBuf dot;  // one double per generation
+    int device = 0;
+};
+
+int gen_I(const Plan& P, int g) { return P.I >> g; }
+int gen_J(const Plan& P, int g) { return P.J >> g; }
+
+// Device copies are made at first use, so that creating a handle (setup and
+// validation) needs no GPU.
+int ensure_tables(Plan& P, Group& G, DType t) {
+    const int ai = t == DType::F64 ? 1 : 0;
+    AccTables& T = G.tab[ai];
+    if (T.ready) return 0;
+    int rc;
+    for (int g = 0; g + 1 < P.gm; ++g) {
+        if (!P.pix[g].p && (rc = upload(P.pix[g], P.ix[g].pidx))) return rc;
+        if (!P.piy[g].p && (rc = upload(P.piy[g], P.iy[g].pidx))) return rc;
+    }
+    if (!P.dot.p && (rc = P.dot.ensure(sizeof(double) * MGBF_MAX_GEN))) return rc;
+    if (!G.zs.fwd.empty()) {
+        if ((rc = upload_acc(T.zfwd, G.zs.fwd, t))) return rc;
+        if ((rc = upload_acc(T.zadj, G.zs.adj, t))) return rc;
+    }
+    if ((rc = upload_acc(T.hw, G.hs.w, t))) return rc;
+    if (!G.mrow.p && (rc = upload(G.mrow, G.hs.mrow))) return rc;
+    const int ng = P.gm - 1;
+    T.rwx.clear(); T.rwy.clear(); T.pwx.clear(); T.pwy.clear();
+    for (int g = 0; g < ng; ++g) {
+        T.rwx.emplace_back(new DevBuf); T.rwy.emplace_back(new DevBuf);
+        T.pwx.emplace_back(new DevBuf); T.pwy.emplace_back(new DevBuf);
+        if ((rc = upload_acc(*T.rwx[g], P.ix[g].rw, t))) return rc;
+        if ((rc = upload_acc(*T.rwy[g], P.iy[g].rw, t))) return rc;
+        if ((rc = upload_acc(*T.pwx[g], P.ix[g].pw, t))) return rc;
+        if ((rc = upload_acc(*T.pwy[g], P.iy[g].pw, t))) return rc;
+    }
+    T.ready = true;
+    return 0;
+}
+
+size_t gen_elems(const Plan& P, const Group& G, int g) {
+    return (size_t)G.nk * (size_t)(gen_I(P, g) + 2 * G.HXP) * (size_t)gen_J(P, g);
+}
+
+View gen_view(const Plan& P, const Group& G, void* base, DType t, int g) {
+    View v;
+    v.si = G.nk;
+    v.sj = (long long)G.nk * (gen_I(P, g) + 2 * G.HXP);
+    v.p = static_cast<char*>(base) + elem_size(t) * (size_t)G.nk * G.HXP;
+    return v;
+}
+
+int ensure_bufs(Plan& P, Group& G, DType t, bool needC) {
+    auto& S = G.bufs[(int)t];
+    auto grow = [&](std::vector<std::unique_ptr<DevBuf>>& v) -> int {
+        if ((int)v.size() < P.gm) v.resize(P.gm);
+        for (int g = 0; g < P.gm; ++g) {
+            if (!v[g]) v[g].reset(new DevBuf);
+            int rc = v[g]->ensure(gen_elems(P, G, g) * elem_size(t));
+            if (rc) return rc;
+        }
+        return 0;
+    };
+    int rc;
+    if ((rc = grow(S.A))) return rc;
+    if ((rc = grow(S.B))) return rc;
+    if (needC && (rc = grow(S.C))) return rc;
+    return 0;
+}
+
+// ------------------------------------------------------------ kernel calls
+
+struct Exec {
+    Plan& P;
+    Group& G;
+    DType t;
+    void* stream;
+    int ai() const { return t == DType::F64 ? 1 : 0; }
+    View A(int g) { return gen_view(P, G, G.bufs[(int)t].A[g]->p, t, g); }
+    View B(int g) { return gen_view(P, G, G.bufs[(int)t].B[g]->p, t, g); }
+    View C(int g) { return gen_view(P, G, G.bufs[(int)t].C[g]->p, t, g); }
+
+    int zstage(View in, View out, bool adjoint, int nzcol, int mirror) {
+        if (nzcol <= 0 || G.zs.fwd.empty()) {
+            LK(launch_copy(t, in, out, G.nk, P.I, P.J, mirror, stream));
+            return 0;
+        }
+        ZArgs a;
+        a.in = in; a.out = out; a.nk = G.nk; a.I = P.I; a.J = P.J;
+        a.lm = G.lm; a.nzk = nzcol * G.lm; a.mz = G.zs.mz;
+        a.band = adjoint ? G.tab[ai()].zadj.p : G.tab[ai()].zfwd.p;
+        a.mirror_hx = mirror;
+        LK(launch_zfilter(t, a, stream));
+        return 0;
+    }
+    int restrict_(int g, View fine, View coarse) {
+        RestrictArgs a;
+        a.fine = fine; a.coarse = coarse; a.nk = G.nk; a.If = gen_I(P, g); a.Jf = gen_J(P, g);
+        a.wx = G.tab[ai()].rwx[g]->p; a.wy = G.tab[ai()].rwy[g]->p;
+        a.mirror_hx = G.hs.R;
+        LK(launch_restrict(t, a, stream));
+        return 0;
+    }
+    int prolong(int g, View coarse, View base, View out) {  // coarse gen g+1 -> fine gen g
+        ProlongArgs a;
+        a.coarse = coarse; a.base = base; a.out = out; a.nk = G.nk;
+        a.If = gen_I(P, g); a.Jf = gen_J(P, g); a.ntap = P.ix[g].ntap;
+        a.ix = static_cast<const int*>(P.pix[g].p); a.iy = static_cast<const int*>(P.piy[g].p);
+        a.wxp = G.tab[ai()].pwx[g]->p; a.wyp = G.tab[ai()].pwy[g]->p;
+        a.has_base = 1;
+        LK(launch_prolong(t, a, stream));
+        return 0;
+    }
+    int hpass(int g, View in, View out, double scale, int mirror) {
+        const int I = gen_I(P, g), J = gen_J(P, g);
+        if (G.hs.canonical && hmom_available(t, G.hs.R, G.hs.p)) {
+            HMomArgs a;
+            a.in = in; a.out = out; a.nk = G.nk; a.I = I; a.J = J;
+            a.mirror_hx = mirror; a.scale = scale;
+            const int tx = hmom_tx_for((int)acc_size(t), G.hs.R);
+            const long long w0 = (long long)((G.nk + 31) / 32) * ((I + tx - 1) / tx);
+            const long long target = 152LL * 24;
+            long long nz = (target + w0 - 1) / w0;
+            int rows = (int)((J + nz - 1) / nz);
+            rows = std::max(rows, std::min(J, 4 * G.hs.R));
+            a.rows = rows;
+            LK(launch_hmom(t, G.hs.R, G.hs.p, a, G.hs.mom, stream));
+            return 0;
+        }
+        HDirectArgs a;
+        a.in = in; a.out = out; a.nk = G.nk; a.I = I; a.J = J; a.R = G.hs.R;
+        a.mrow = static_cast<const int*>(G.mrow.p);
+        a.w = G.tab[ai()].hw.p; a.mirror_hx = mirror; a.scale = scale;
+        LK(launch_hdirect(t, a, stream));
+        return 0;
+    }
+
+    // Steps 1-2 and the first radial pass: leaves B_g R_g Bz^T x in `dst(g)`
+    // (with mirror halo when mirror_out) and R_g Bz^T x in A(g).
+    template <typename DstF>
+    int half_chain(View x, int nzcol, bool filt1, DstF dst, bool mirror_out, const double* scales) {
+        int rc;
+        if ((rc = zstage(x, A(0), true, nzcol, G.hs.R))) return rc;
+        for (int g = 0; g + 1 < P.gm; ++g)
+            if ((rc = restrict_(g, A(g), A(g + 1)))) return rc;
+        for (int g = 0; g < P.gm; ++g) {
+            if (g == 0 && !filt1) continue;
+            if ((rc = hpass(g, A(g), dst(g), scales ? scales[g] : 1.0, mirror_out ? G.hs.R : 0))) return rc;
+        }
+        return 0;
+    }
+
+    // Steps 3b-5: src(g) holds B_g R_g Bz^T x (mirrored), already multiplied
+    // by a_g unless scales are given; finishes into y.
+    template <typename SrcF>
+    int second_half(SrcF src, View y, int nzcol, bool filt1, const double* scales) {
+        int rc;
+        for (int g = 0; g < P.gm; ++g) {
+            if (g == 0 && !filt1) continue;
+            if ((rc = hpass(g, src(g), A(g), scales ? scales[g] : 1.0, 0))) return rc;
+        }
+        const bool z = nzcol > 0 && !G.zs.fwd.empty();
+        for (int g = P.gm - 1; g >= 1; --g) {
+            if (g == 1 && !z) {
+                if ((rc = prolong(0, A(1), A(0), y))) return rc;
+            } else {
+                if ((rc = prolong(g - 1, A(g), A(g - 1), A(g - 1)))) return rc;
+            }
+        }
+        if (z) return zstage(A(0), y, false, nzcol, 0);
+        if (P.gm == 1) return zstage(A(0), y, false, 0, 0);
+        return 0;
+    }
+
+    int forward(View x, View y, int nzcol, bool filt1) {
+        int rc;
+        auto Bf = [&](int g) { return B(g); };
+        if ((rc = half_chain(x, nzcol, filt1, Bf, true, P.a))) return rc;
+        return second_half(Bf, y, nzcol, filt1, nullptr);
+    }
+};
+
+// --------------------------------------------------------------- handles
+
+}  // namespace
+
+struct mgbf_handle {
+    mgbf_config cfg;
+    Plan plan;
+    int nzcol_proc1 = 0, nzcol_proc6 = 0;
+    size_t field_elems = 0;
+    DevBuf stage[3], stage2[3], stage3[3];
+};
+
+struct mgbf_batch {
+    Plan plan;
+    bool filt1 = true;
+};
+
+namespace {
+
+// ------------------------------------------------------------ config logic
+
+int def_maxgen(int nxm, int nym) {  // mg_parameter.f90:578-611
+    int npx = nxm, gx = 1;
+    do { npx = (npx + 1) / 2; ++gx; } while (npx != 1 && gx < 64);
+    int npy = nym, gy = 1;
+    do { npy = (npy + 1) / 2; ++gy; } while (npy != 1 && gy < 64);
+    return std::min(gx, gy);
+}
+
+void gen_weights(const mgbf_config& c, int gm, double* a) {
+    if (c.n_weig_ext > 0) {
+        for (int g = 0; g < gm; ++g) a[g] = c.weig_ext[std::min(g, c.n_weig_ext - 1)];
+        return;
+    }
+    // a_diff_f = mg_weig1; a_diff_h by my_hgen: 2,3,4 -> weig2..4, else weig5
+    // (mg_intstate.f90:333-351)
+    for (int g = 0; g < gm; ++g) {
+        const int gen = g + 1;
+        a[g] = gen == 1 ? c.mg_weig1
+             : gen == 2 ? c.mg_weig2
+             : gen == 3 ? c.mg_weig3
+             : gen == 4 ? c.mg_weig4
+             : c.mg_weig5;
+    }
+}
+
+int build_interps(Plan& P) {
+    std::string err;
+    P.ix.assign(std::max(P.gm - 1, 0), Interp1D());
+    P.iy.assign(std::max(P.gm - 1, 0), Interp1D());
+    for (int g = 0; g + 1 < P.gm; ++g) {
+        int rc = build_interp(gen_I(P, g), P.lquart, P.ix[g], err);
+        if (!rc) rc = build_interp(gen_J(P, g), P.lquart, P.iy[g], err);
+        if (rc) return fail(rc, err);
+    }
+    return 0;
+}
+
+int build_group(Plan& P, Group& G, bool zneeded) {
+    std::string err;
+    int rc = build_hstencil(G.p, G.ampl02, G.hx, G.hy, G.hs, err);
+    if (rc) return fail(rc, err);
+    rc = build_zstencil(G.p, G.ampl01, G.hz, G.lm, zneeded, G.zs, err);
+    if (rc) return fail(rc, err);
+    const int IG = gen_I(P, P.gm - 1), JG = gen_J(P, P.gm - 1);
+    if (G.hs.R > IG || G.hs.R > JG)
+        return fail(MGBF_ERR_DIVISIBILITY, "horizontal reach " + std::to_string(G.hs.R) +
+                                               " exceeds the coarsest generation " +
+                                               std::to_string(IG) + "x" + std::to_string(JG));
+    G.HXP = G.hs.R + 8;
+    return 0;
+}
+
+int validate_grid(int I, int J, int gm) {
+    if (I <= 0 || J <= 0) return fail(MGBF_ERR_CONFIG, "filter grid must be positive (nxPE*im_filt, nyPE*jm_filt)");
+    if (gm < 1 || gm > MGBF_MAX_GEN) return fail(MGBF_ERR_CONFIG, "gm must be in 1.." + std::to_string(MGBF_MAX_GEN));
+    const int d = 1 << (gm - 1);
+    if (I % d || J % d)
+        return fail(MGBF_ERR_DIVISIBILITY, "filter grid " + std::to_string(I) + "x" + std::to_string(J) +
+                                               " not divisible by 2^(gm-1)=" + std::to_string(d));
+    return 0;
+}
+
+int view_of_field(const mgbf_handle* h, void* p, View& v) {
+    const Plan& P = h->plan;
+    const int nk = h->plan.groups[0].nk;
+    v.si = nk;
+    if (h->cfg.layout == MGBF_LAYOUT_HALO) {
+        const int hx = h->cfg.hx, hy = h->cfg.hy;
+        v.sj = (long long)nk * (P.I + 2 * hx);
+        v.p = p;
+        return (int)((size_t)nk * (hx + (size_t)(P.I + 2 * hx) * hy));  // offset in elements
+    }
+    v.sj = (long long)nk * P.I;
+    v.p = p;
+    return 0;
+}
+
+View field_view(const mgbf_handle* h, void* p, DType t) {
+    View v;
+    int off = view_of_field(h, p, v);
+    v.p = static_cast<char*>(p) + elem_size(t) * (size_t)off;
+    return v;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) {
+            cudaSetDevice(dev);
+        } else {
+            prev = -1;
+            cudaGetLastError();
+        }
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+bool valid_dtype(int d) { return d == MGBF_F64 || d == MGBF_F32 || d == MGBF_BF16; }
+
+// ------------------------------------------------------------- namelist
+
+std::string lower(std::string s) {
+    for (auto& ch : s) ch = (char)std::tolower((unsigned char)ch);
+    return s;
+}
+
+struct Field {
+    enum Kind { INT, DBL, BOOL, DBLARR } kind;
+    void* ptr;
+    int n;
+};
+
+std::map<std::string, Field> field_table(mgbf_config* c) {
+    std::map<std::string, Field> m;
+    auto D = [&](const char* n, double* p) { m[n] = {Field::DBL, p, 1}; };
+    auto I = [&](const char* n, int* p) { m[n] = {Field::INT, p, 1}; };
+    auto B = [&](const char* n, int* p) { m[n] = {Field::BOOL, p, 1}; };
+    D("mg_ampl01", &c->mg_ampl01); D("mg_ampl02", &c->mg_ampl02); D("mg_ampl03", &c->mg_ampl03);
+    D("mg_weig1", &c->mg_weig1); D("mg_weig2", &c->mg_weig2); D("mg_weig3", &c->mg_weig3);
+    D("mg_weig4", &c->mg_weig4); D("mg_weig5", &c->mg_weig5);
+    I("hx", &c->hx); I("hy", &c->hy); I("hz", &c->hz); I("p", &c->p);
+    B("mgbf_line", &c->mgbf_line); I("mgbf_proc", &c->mgbf_proc); I("n_ens", &c->n_ens);
+    I("lm_a", &c->lm_a); I("lm", &c->lm); I("km2", &c->km2); I("km3", &c->km3);
+    B("l_loc", &c->l_loc); B("l_loc_vertical", &c->l_loc_vertical); B("l_filt_g1", &c->l_filt_g1);
+    B("l_lin_vertical", &c->l_lin_vertical); B("l_lin_horizontal", &c->l_lin_horizontal);
+    B("l_quad_horizontal", &c->l_quad_horizontal); B("l_new_map", &c->l_new_map);
+    B("l_vertical_filter", &c->l_vertical_filter);
+    B("ldelta", &c->ldelta); B("lquart", &c->lquart); B("lhelm", &c->lhelm);
+    I("gm_max", &c->gm_max);
+    I("nm0", &c->nm0); I("mm0", &c->mm0); I("nxpe", &c->nxPE); I("nype", &c->nyPE);
+    I("im_filt", &c->im_filt); I("jm_filt", &c->jm_filt);
+    // extensions
+    B("gm_uncapped", &c->gm_uncapped); I("n_weig_ext", &c->n_weig_ext);
+    m["weig_ext"] = {Field::DBLARR, c->weig_ext, MGBF_MAX_GEN};
+    m["helm_b"] = {Field::DBLARR, c->helm_b, MGBF_MAX_GEN};
+    I("layout", &c->layout);
+    return m;
+}
+
+bool parse_int(const std::string& s, int& v) {
+    if (s.empty()) return false;
+    char* end = nullptr;
+    long x = std::strtol(s.c_str(), &end, 10);
+    if (*end) return false;
+    v = (int)x;
+    return true;
+}
+bool parse_dbl(std::string s, double& v) {
+    for (auto& ch : s)
+        if (ch == 'd' || ch == 'D') ch = 'e';
+    if (s.empty()) return false;
+    char* end = nullptr;
+    v = std::strtod(s.c_str(), &end);
+    return *end == 0;
+}
+bool parse_bool(const std::string& s0, int& v) {
+    std::string s = lower(s0);
+    if (s == ".true." || s == "t" || s == ".t." || s == "true") { v = 1; return true; }
+    if (s == ".false." || s == "f" || s == ".f." || s == "false") { v = 0; return true; }
+    return false;
+}
+
+int parse_namelist_text(const std::string& text, mgbf_config* c, std::string& err) {
+    // strip comments
+    std::string clean;
+    {
+        std::istringstream in(text);
+        std::string line;
+        while (std::getline(in, line)) {
+            size_t b = line.find('!');
+            if (b != std::string::npos) line.resize(b);
+            clean += line + "\n";
+        }
+    }
+    std::string low = lower(clean);
+    size_t start = low.find("&parameters_mgbeta");
+    if (start == std::string::npos) {
+        err = "group &PARAMETERS_MGBETA not found";
+        return MGBF_ERR_NAMELIST;
+    }
+    size_t body = start + std::strlen("&parameters_mgbeta");
+    size_t stop = low.find('/', body);
+    size_t stop2 = low.find("&end", body);
+    if (stop2 != std::string::npos && (stop == std::string::npos || stop2 < stop)) stop = stop2;
+    if (stop == std::string::npos) {
+        err = "group &PARAMETERS_MGBETA is not terminated by '/'";
+        return MGBF_ERR_NAMELIST;
+    }
+    std::string s = clean.substr(body, stop - body);
+    std::string spaced;
+    for (char ch : s) {
+        if (ch == '=') spaced += " = ";
+        else if (ch == ',' || ch == '\n' || ch == '\r' || ch == '\t' || ch == ';') spaced += ' ';
+        else spaced += ch;
+    }
+    std::vector<std::string> tok;
+    {
+        std::istringstream in(spaced);
+        std::string t;
+        while (in >> t) tok.push_back(t);
+    }
+    auto fields = field_table(c);
+    size_t i = 0;
+    while (i < tok.size()) {
+        if (i + 1 >= tok.size() || tok[i + 1] != "=") {
+            err = "expected 'name =' at '" + tok[i] + "'";
+            return MGBF_ERR_NAMELIST;
+        }
+        std::string name = lower(tok[i]);
+        i += 2;
+        std::vector<std::string> vals;
+        while (i < tok.size() && !(i + 1 < tok.size() && tok[i + 1] == "=")) vals.push_back(tok[i++]);
+        auto it = fields.find(name);
+        if (it == fields.end()) {
+            err = "unknown namelist item '" + name + "'";
+            return MGBF_ERR_NAMELIST;
+        }
+        Field& f = it->second;
+        if (vals.empty()) {
+            err = "no value for '" + name + "'";
+            return MGBF_ERR_NAMELIST;
+        }
+        if ((int)vals.size() > f.n) {
+            err = "too many values for '" + name + "'";
+            return MGBF_ERR_NAMELIST;
+        }
+        for (size_t q = 0; q < vals.size(); ++q) {
+            const std::string& v = vals[q];
+            bool ok = false;
+            switch (f.kind) {
+                case Field::INT: ok = parse_int(v, *static_cast<int*>(f.ptr)); break;
+                case Field::DBL: ok = parse_dbl(v, *static_cast<double*>(f.ptr)); break;
+                case Field::BOOL: ok = parse_bool(v, *static_cast<int*>(f.ptr)); break;
+                case Field::DBLARR: ok = parse_dbl(v, static_cast<double*>(f.ptr)[q]); break;
+            }
+            if (!ok) {
+                err = "bad value '" + v + "' for '" + name + "'" +
+                      (f.kind == Field::INT ? " (integer expected)" : "");
+                return MGBF_ERR_NAMELIST;
+            }
+        }
+        if (name == "weig_ext") c->n_weig_ext = (int)vals.size();
+    }
+    return MGBF_OK;
+}
+
+}  // namespace
+
+// ===================================================================== ABI
+
+extern "C" {
+
+const char* mgbf_strerror(int code) {
+    switch (code) {
+        case MGBF_OK: return "ok";
+        case MGBF_ERR_ARG: return "invalid argument";
+        case MGBF_ERR_CONFIG: return "inconsistent configuration";
+        case MGBF_ERR_REACH: return "filter reach exceeds halo";
+        case MGBF_ERR_DIVISIBILITY: return "grid not divisible by 2^(gm-1) or too small";
+        case MGBF_ERR_UNSUPPORTED: return "unsupported filtering procedure or option";
+        case MGBF_ERR_CUDA: return "CUDA error";
+        case MGBF_ERR_NAMELIST: return "namelist error";
+        case MGBF_ERR_IO: return "file cannot be read";
+        case MGBF_ERR_TIMEOUT: return "device wait timed out";
+        case MGBF_ERR_NOMEM: return "out of memory";
+        default: return "unknown error";
+    }
+}
+
+const char* mgbf_last_error(void) { return g_last_error.c_str(); }
+
+int mgbf_config_init(mgbf_config* c) {
+    if (!c) return fail(MGBF_ERR_ARG, "null config");
+    std::memset(c, 0, sizeof(*c));
+    c->mg_ampl01 = 1.0; c->mg_ampl02 = 1.0; c->mg_ampl03 = 1.0;
+    c->mg_weig1 = 1.0; c->mg_weig2 = 1.0; c->mg_weig3 = 1.0; c->mg_weig4 = 1.0; c->mg_weig5 = 1.0;
+    c->hx = 6; c->hy = 6; c->hz = 3; c->p = 2;
+    c->mgbf_proc = 1; c->n_ens = 1;
+    c->lm_a = 1; c->lm = 1; c->km2 = 0; c->km3 = 1;
+    c->l_filt_g1 = 1; c->l_new_map = 1; c->l_vertical_filter = 1;
+    c->gm_max = 4;
+    c->nxPE = 1; c->nyPE = 1;
+    c->layout = MGBF_LAYOUT_HALO;
+    return MGBF_OK;
+}
+
+int mgbf_config_read_namelist(const char* path, mgbf_config* cfg, char* errbuf, size_t errlen) {
+    if (!path || !cfg) return fail(MGBF_ERR_ARG, "null argument");
+    std::ifstream in(path);
+    std::string err;
+    int rc;
+    if (!in) {
+        err = std::string("cannot open namelist file '") + path + "'";
+        rc = MGBF_ERR_IO;
+    } else {
+        std::stringstream ss;
+        ss << in.rdbuf();
+        rc = parse_namelist_text(ss.str(), cfg, err);
+    }
+    if (rc) {
+        if (errbuf && errlen) std::snprintf(errbuf, errlen, "%s", err.c_str());
+        return fail(rc, err);
+    }
+    return MGBF_OK;
+}
+
+int mgbf_create(const mgbf_config* cfg, mgbf_handle** out) {
+    if (!cfg || !out) return fail(MGBF_ERR_ARG, "null argument");
+    *out = nullptr;
+    const mgbf_config& c = *cfg;
+    if (c.nxPE <= 0 || c.nyPE <= 0 || c.im_filt <= 0 || c.jm_filt <= 0)
+        return fail(MGBF_ERR_CONFIG, "nxPE, nyPE, im_filt, jm_filt must be positive");
+    if (c.n_ens <= 0 || c.lm <= 0 || c.km2 < 0 || c.km3 < 0 || c.km2 + c.km3 <= 0)
+        return fail(MGBF_ERR_CONFIG, "n_ens, lm must be positive and km2+km3 > 0");
+    if (c.p < 0 || c.p > 8) return fail(MGBF_ERR_CONFIG, "p must be an integer in 0..8");
+    if (c.hx < 0 || c.hy < 0 || c.hz < 0) return fail(MGBF_ERR_CONFIG, "halo widths must be >= 0");
+    if (c.gm_max < 1) return fail(MGBF_ERR_CONFIG, "gm_max must be >= 1");
+    if (c.layout != MGBF_LAYOUT_HALO && c.layout != MGBF_LAYOUT_COMPACT)
+        return fail(MGBF_ERR_CONFIG, "unknown layout");
+    // init_mg_parameter: analysis-grid divisibility checks (mg_parameter.f90:447-455)
+    if (c.nm0 % c.nxPE) return fail(MGBF_ERR_CONFIG, "nm0 is not divisible by nxm");
+    if (c.mm0 % c.nyPE) return fail(MGBF_ERR_CONFIG, "mm0 is not divisible by nym");
+    for (int g = 0; g < MGBF_MAX_GEN; ++g)
+        if (c.helm_b[g] != 0.0)
+            return fail(MGBF_ERR_UNSUPPORTED, "helm_b != 0 is not supported on the GPU path (the reference fixes b = 0)");
+    std::string err;
+    int rc = check_other_reaches(c.p, c.mg_ampl02, c.mg_ampl03, c.hx, c.hy, c.hz, err);
+    if (rc) return fail(rc, err);
+
+    std::unique_ptr<mgbf_handle> h(new mgbf_handle);
+    h->cfg = c;
+    Plan& P = h->plan;
+    if (cudaGetDevice(&P.device) != cudaSuccess) {
+        P.device = 0;
+        cudaGetLastError();
+    }
+    P.I = c.nxPE * c.im_filt;
+    P.J = c.nyPE * c.jm_filt;
+    P.gm = c.gm_uncapped ? c.gm_max : std::min(c.gm_max, def_maxgen(c.nxPE, c.nyPE));
+    if ((rc = validate_grid(P.I, P.J, P.gm))) return rc;
+    P.lquart = c.lquart != 0;
+    gen_weights(c, P.gm, P.a);
+    const int km = c.km2 + c.lm * c.km3;
+    const int km_all = km * c.n_ens;
+    h->nzcol_proc1 = c.km3;
+    h->nzcol_proc6 = c.km3 * c.n_ens;
+    const bool zneeded = c.l_vertical_filter && c.km3 > 0 && c.lm > 1;
+    P.groups.resize(1);
+    Group& G = P.groups[0];
+    G.nk = km_all; G.lm = c.lm; G.nzcol = c.km3 * c.n_ens;
+    G.hx = c.hx; G.hy = c.hy; G.hz = c.hz; G.p = c.p;
+    G.ampl01 = c.mg_ampl01; G.ampl02 = c.mg_ampl02;
+    if ((rc = build_group(P, G, zneeded))) return rc;
+    if ((rc = build_interps(P))) return rc;
+    h->field_elems = c.layout == MGBF_LAYOUT_HALO
+                         ? (size_t)km_all * (P.I + 2 * c.hx) * (size_t)(P.J + 2 * c.hy)
+                         : (size_t)km_all * P.I * (size_t)P.J;
+    *out = h.release();
+    return MGBF_OK;
+}
+
+int mgbf_create_from_namelist(const char* path, mgbf_handle** out) {
+    mgbf_config c;
+    mgbf_config_init(&c);
+    int rc = mgbf_config_read_namelist(path, &c, nullptr, 0);
+    if (rc) return rc;
+    return mgbf_create(&c, out);
+}
+
+int mgbf_get_dims(const mgbf_handle* h, mgbf_dims* d) {
+    if (!h || !d) return fail(MGBF_ERR_ARG, "null argument");
+    const Plan& P = h->plan;
+    const Group& G = P.groups[0];
+    std::memset(d, 0, sizeof(*d));
+    d->im = P.I; d->jm = P.J; d->km_all = G.nk;
+    d->km = h->cfg.km2 + h->cfg.lm * h->cfg.km3;
+    d->km3_all = h->cfg.km3 * h->cfg.n_ens;
+    d->gm = P.gm; d->hx = h->cfg.hx; d->hy = h->cfg.hy; d->hz = h->cfg.hz;
+    d->reach_h = G.hs.R; d->reach_z = G.zs.mz; d->layout = h->cfg.layout;
+    d->field_elems = h->field_elems;
+    d->hbeta_kernel = (G.hs.canonical && hmom_available(DType::F32, G.hs.R, G.hs.p)) ? 1 : 0;
+    return MGBF_OK;
+}
+
+int mgbf_set_weights(mgbf_handle* h, const double* a, int n) {
+    if (!h || !a || n < 1 || n > h->plan.gm) return fail(MGBF_ERR_ARG, "bad weights");
+    for (int g = 0; g < n; ++g) h->plan.a[g] = a[g];
+    return MGBF_OK;
+}
+
+static int check_proc(mgbf_handle* h, int mg_filt, bool& noop) {
+    noop = false;
+    if (mg_filt == 1 || mg_filt == 6) {
+        if (mg_filt == 1 && h->cfg.n_ens != 1)
+            return fail(MGBF_ERR_CONFIG, "filtering_rad2_bckg (proc 1) needs n_ens = 1: its arrays are dimensioned km, not km_all");
+        if (mg_filt == 6 && h->cfg.l_vertical_filter && h->cfg.km2 > 0 && h->cfg.km3 > 0)
+            return fail(MGBF_ERR_CONFIG, "filtering_rad2_ens (proc 6) with the vertical filter needs km2 = 0: sup_vrbeta1_ens views VALL with leading dimension km3_all*lm");
+        return MGBF_OK;
+    }
+    if (mg_filt >= 2 && mg_filt <= 8)
+        return fail(MGBF_ERR_UNSUPPORTED, "filtering procedure " + std::to_string(mg_filt) + " is not implemented (supported: 1, 6)");
+    noop = true;  // no case default in the reference's select
+    return MGBF_OK;
+}
+
+static int run_proc(mgbf_handle* h, int mg_filt, const void* xin, void* yout, DType t, void* stream) {
+    Plan& P = h->plan;
+    Group& G = P.groups[0];
+    int rc;
+    if ((rc = ensure_tables(P, G, t))) return rc;
+    if ((rc = ensure_bufs(P, G, t, false))) return rc;
+    const int nzcol = (h->cfg.l_vertical_filter && h->cfg.lm > 1) ? (mg_filt == 1 ? h->nzcol_proc1 : h->nzcol_proc6) : 0;
+    const bool filt1 = mg_filt == 1 || h->cfg.l_filt_g1;
+    Exec ex{P, G, t, stream};
+    View x = field_view(h, const_cast<void*>(xin), t);
+    View y = field_view(h, yout, t);
+    if ((rc = ex.forward(x, y, nzcol, filt1))) return rc;
+    if (h->cfg.layout == MGBF_LAYOUT_HALO && filt1)
+        LK(launch_zero_halo(t, y, G.nk, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
+    return 0;
+}
+
+static int with_field(mgbf_handle* h, int mg_filt, void* vall, int dtype, int mem, void* stream) {
+    if (!h || !vall) return fail(MGBF_ERR_ARG, "null argument");
+    if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");
+    if (mem != MGBF_MEM_DEVICE && mem != MGBF_MEM_HOST) return fail(MGBF_ERR_ARG, "bad memory space");
+    bool noop;
+    int rc = check_proc(h, mg_filt, noop);
+    if (rc || noop) return rc;
+    DeviceGuard dg(h->plan.device);
+    const DType t = (DType)dtype;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (mem == MGBF_MEM_DEVICE) return run_proc(h, mg_filt, vall, vall, t, stream);
+    const size_t bytes = h->field_elems * elem_size(t);
+    DevBuf& st = h->stage[(int)t];
+    if ((rc = st.ensure(bytes))) return rc;
+    CU(cudaMemcpyAsync(st.p, vall, bytes, cudaMemcpyHostToDevice, s));
+    if ((rc = run_proc(h, mg_filt, st.p, st.p, t, stream))) return rc;
+    CU(cudaMemcpyAsync(vall, st.p, bytes, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    return 0;
+}
+
+int mgbf_filtering_procedure(mgbf_handle* h, int mg_filt, void* vall, int dtype, int mem, void* stream) {
+    return with_field(h, mg_filt, vall, dtype, mem, stream);
+}
+
+int mgbf_filtering_procedure_adjoint(mgbf_handle* h, int mg_filt, void* vall, int dtype, int mem,
+                                     void* stream) {
+    // L^T = (Bz M Bz^T)^T = Bz M^T Bz^T with M = sum_g P_g B_g a_g B_g^T R_g;
+    // transposing each stage in reverse order reproduces the same launch
+    // sequence (Bz^T first, restriction = P^T, B^T = B, a_g, B, P, Bz).
+    return with_field(h, mg_filt, vall, dtype, mem, stream);
+}
+
+int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, const void* gy, void* gx,
+                                 double* ga, int dtype, int mem, void* stream) {
+    if (!h || !x || !gy || !gx || !ga) return fail(MGBF_ERR_ARG, "null argument");
+    if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");
+    if (mem != MGBF_MEM_DEVICE && mem != MGBF_MEM_HOST) return fail(MGBF_ERR_ARG, "bad memory space");
+    bool noop;
+    int rc = check_proc(h, mg_filt, noop);
+    if (rc) return rc;
+    if (noop) return fail(MGBF_ERR_UNSUPPORTED, "no filtering procedure " + std::to_string(mg_filt));
+    DeviceGuard dg(h->plan.device);
+    const DType t = (DType)dtype;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Plan& P = h->plan;
+    Group& G = P.groups[0];
+    if ((rc = ensure_tables(P, G, t))) return rc;
+    if ((rc = ensure_bufs(P, G, t, true))) return rc;
+    const void *dx = x, *dgy = gy;
+    void* dgx = gx;
+    const size_t bytes = h->field_elems * elem_size(t);
+    if (mem == MGBF_MEM_HOST) {
+        if ((rc = h->stage[(int)t].ensure(bytes)) || (rc = h->stage2[(int)t].ensure(bytes))) return rc;
+        CU(cudaMemcpyAsync(h->stage[(int)t].p, x, bytes, cudaMemcpyHostToDevice, s));
+        CU(cudaMemcpyAsync(h->stage2[(int)t].p, gy, bytes, cudaMemcpyHostToDevice, s));
+        dx = h->stage[(int)t].p;
+        dgy = h->stage2[(int)t].p;
+        dgx = h->stage2[(int)t].p;
+    }
+    const int nzcol = (h->cfg.l_vertical_filter && h->cfg.lm > 1) ? (mg_filt == 1 ? h->nzcol_proc1 : h->nzcol_proc6) : 0;
+    const bool filt1 = mg_filt == 1 || h->cfg.l_filt_g1;
+    Exec ex{P, G, t, stream};
+    View vx = field_view(h, const_cast<void*>(dx), t);
+    View vg = field_view(h, const_cast<void*>(dgy), t);
+    View vo = field_view(h, dgx, t);
+    // u_g = B_g R_g Bz^T x  -> C(g)
+    auto Cf = [&](int g) { return ex.C(g); };
+    if ((rc = ex.half_chain(vx, nzcol, filt1, Cf, false, nullptr))) return rc;
+    // v_g = B_g R_g Bz^T gy -> B(g) (mirrored for the second pass)
+    auto Bf = [&](int g) { return ex.B(g); };
+    if ((rc = ex.half_chain(vg, nzcol, filt1, Bf, true, nullptr))) return rc;
+    CU(cudaMemsetAsync(P.dot.p, 0, sizeof(double) * MGBF_MAX_GEN, s));
+    double* dots = static_cast<double*>(P.dot.p);
+    for (int g = 0; g < P.gm; ++g) {
+        if (g == 0 && !filt1) continue;
+        DotArgs da;
+        da.a = ex.B(g); da.b = ex.C(g); da.nk = G.nk; da.I = gen_I(P, g); da.J = gen_J(P, g);
+        da.out = dots + g;
+        LK(launch_dot(t, da, stream));
+    }
+    // gx = L gy = Bz sum_g P_g B_g (a_g v_g)
+    if ((rc = ex.second_half(Bf, vo, nzcol, filt1, P.a))) return rc;
+    if (h->cfg.layout == MGBF_LAYOUT_HALO && filt1)
+        LK(launch_zero_halo(t, vo, G.nk, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
+    CU(cudaMemcpyAsync(ga, P.dot.p, sizeof(double) * P.gm, cudaMemcpyDeviceToHost, s));
+    if (mem == MGBF_MEM_HOST)
+        CU(cudaMemcpyAsync(gx, h->stage2[(int)t].p, bytes, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    return 0;
+}
+
+int mgbf_destroy(mgbf_handle* h) {
+    if (!h) return MGBF_OK;
+    DeviceGuard dg(h->plan.device);
+    delete h;
+    return MGBF_OK;
+}
+
+// ------------------------------------------------------------ batched API
+
+int mgbf_batch_create(int im, int jm, int gm, const double* weights, int lquart, int l_filt_g1,
+                      const mgbf_group_desc* groups, int ngroups, mgbf_batch** out) {
+    if (!out || !groups || ngroups <= 0 || !weights) return fail(MGBF_ERR_ARG, "null argument");
+    *out = nullptr;
+    int rc = validate_grid(im, jm, gm);
+    if (rc) return rc;
+    std::unique_ptr<mgbf_batch> b(new mgbf_batch);
+    Plan& P = b->plan;
+    if (cudaGetDevice(&P.device) != cudaSuccess) {
+        P.device = 0;
+        cudaGetLastError();
+    }
+    P.I = im; P.J = jm; P.gm = gm; P.lquart = lquart != 0;
+    for (int g = 0; g < gm; ++g) P.a[g] = weights[g];
+    b->filt1 = l_filt_g1 != 0;
+    P.groups.resize(ngroups);
+    for (int q = 0; q < ngroups; ++q) {
+        const mgbf_group_desc& d = groups[q];
+        Group& G = P.groups[q];
+        if (d.nk <= 0 || d.lm <= 0 || d.nzcol < 0 || (long long)d.nzcol * d.lm > d.nk)
+            return fail(MGBF_ERR_CONFIG, "group " + std::to_string(q) + ": bad nk/lm/nzcol");
+        G.nk = d.nk; G.lm = d.lm; G.nzcol = d.nzcol; G.hx = d.hx; G.hy = d.hy; G.hz = d.hz; G.p = d.p;
+        G.ampl01 = d.mg_ampl01; G.ampl02 = d.mg_ampl02;
+        const bool zneeded = d.nzcol > 0 && d.lm > 1;
+        if ((rc = build_group(P, G, zneeded))) return rc;
+    }
+    if ((rc = build_interps(P))) return rc;
+    *out = b.release();
+    return MGBF_OK;
+}
+
+int mgbf_batch_apply(mgbf_batch* b, void* const* fields, int dtype, int adjoint, void* stream) {
+    (void)adjoint;  // the transposed chain issues the same launches (see mgbf_filtering_procedure_adjoint)
+    if (!b || !fields) return fail(MGBF_ERR_ARG, "null argument");
+    if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");
+    DeviceGuard dg(b->plan.device);
+    const DType t = (DType)dtype;
+    Plan& P = b->plan;
+    int rc;
+    for (auto& G : P.groups) {
+        if ((rc = ensure_tables(P, G, t))) return rc;
+        if ((rc = ensure_bufs(P, G, t, false))) return rc;
+    }
+    for (size_t q = 0; q < P.groups.size(); ++q) {
+        Group& G = P.groups[q];
+        if (!fields[q]) return fail(MGBF_ERR_ARG, "null field pointer");
+        View v;
+        v.p = fields[q]; v.si = G.nk; v.sj = (long long)G.nk * P.I;
+        Exec ex{P, G, t, stream};
+        const int nzcol = (G.lm > 1) ? G.nzcol : 0;
+        if ((rc = ex.forward(v, v, nzcol, b->filt1))) return rc;
+    }
+    return MGBF_OK;
+}
+
+int mgbf_batch_destroy(mgbf_batch* b) {
+    if (!b) return MGBF_OK;
+    DeviceGuard dg(b->plan.device);
+    delete b;
+    return MGBF_OK;
+}
+
+}  // extern "C"

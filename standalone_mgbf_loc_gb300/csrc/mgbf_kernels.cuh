@@ -1,0 +1,109 @@
+// Internal interface between the host orchestration (mgbf_capi.cpp) and the
+// sm_103a kernels (mgbf_kernels.cu, mgbf_hbeta.cu).  Plain C++ types only.
+//
+// Field views: element (k, i, j) of a generation field lives at
+//   p + k + si*i + sj*j        (k, i, j 0-based; k stride is always 1)
+// Views produced for a horizontal filter carry an x halo of `hx` mirrored
+// columns on each side (columns -hx..-1 and I..I+hx-1 are readable).
+#pragma once
+#include <cstdint>
+
+namespace mgbf {
+
+enum class DType : int { F64 = 0, F32 = 1, BF16 = 2 };
+
+struct View {
+    void* p = nullptr;
+    long long si = 0, sj = 0;
+};
+
+// Maximum horizontal reach handled by the kernels and maximum power p of the
+// moment kernel.
+constexpr int kMaxReach = 32;
+constexpr int kMaxMomP = 4;
+constexpr int kMaxZBand = 2 * 32 + 1;
+
+struct ZArgs {
+    View in, out;
+    int nk, I, J;
+    int lm, nzk;        // levels per column, number of z-filtered leading entries (nzcol*lm)
+    int mz;             // half bandwidth
+    const void* band;   // lm x (2mz+1) weights (accumulation type), device
+    int mirror_hx;      // write a mirrored x halo of this width (0: none)
+};
+
+struct RestrictArgs {
+    View fine, coarse;
+    int nk, If, Jf;     // fine interior sizes; coarse = If/2, Jf/2
+    const void* wx;     // Ic x 8 weights for fine columns 2c-3 .. 2c+4
+    const void* wy;     // Jc x 8
+    int mirror_hx;      // x halo width to mirror into the coarse view
+};
+
+struct ProlongArgs {
+    View coarse, base, out;  // out = base + P(coarse); out may equal base
+    int nk, If, Jf;          // fine interior sizes
+    int ntap;                // 4 (cubic offset stencil) or 3 (quadratic)
+    const int* ix;           // If x ntap coarse column indices (reflected)
+    const void* wxp;         // If x ntap weights
+    const int* iy;           // Jf x ntap
+    const void* wyp;         // Jf x ntap
+    int has_base;
+};
+
+struct HDirectArgs {
+    View in, out;
+    int nk, I, J;
+    int R;                   // reach
+    const int* mrow;         // 2R+1 row half-widths (-1: empty row), device
+    const void* w;           // (2R+1)^2 weights, device
+    int mirror_hx;
+    double scale;            // multiplies every output (generation weight)
+};
+
+template <typename A>
+struct HMomCoefs {
+    A coef[(kMaxReach + 1) * (kMaxMomP + 1)];  // coef[gy*(P+1)+q], gy = 0..R
+    A upow[(kMaxReach + 1) * (kMaxMomP + 1)];  // upow[m*(P+1)+q] = (e^2 m^2)^q
+};
+
+struct HMomArgs {
+    View in, out;
+    int nk, I, J;
+    int rows;                // output rows per block (<= 0: all rows)
+    int mirror_hx;
+    double scale;            // multiplies every output (generation weight)
+};
+
+// Reaches with a compiled moment kernel (p = 2).
+#define MGBF_HMOM_REACHES(X) X(4) X(5) X(6) X(8) X(10) X(12) X(16) X(24)
+
+// Columns per thread of the moment kernel for reach R, chosen to keep the
+// ring of output rows and the input row segment in registers.
+constexpr int hmom_tx_for(int elem_bytes, int R) {
+    return elem_bytes == 8 ? (R <= 8 ? 2 : 1) : (R <= 12 ? 4 : 2);
+}
+
+struct DotArgs {
+    View a, b;
+    int nk, I, J;
+    double* out;             // device accumulator (one double)
+};
+
+// Launchers; return 0 or a cudaError_t value.
+int launch_zfilter(DType t, const ZArgs& a, void* stream);
+int launch_restrict(DType t, const RestrictArgs& a, void* stream);
+int launch_prolong(DType t, const ProlongArgs& a, void* stream);
+int launch_hdirect(DType t, const HDirectArgs& a, void* stream);
+int launch_mirror_x(DType t, View v, int nk, int I, int J, int hx, void* stream);
+int launch_copy(DType t, View in, View out, int nk, int I, int J, int mirror_hx, void* stream);
+int launch_zero_halo(DType t, View v, int nk, int I, int J, int hx, int hy, void* stream);
+int launch_dot(DType t, const DotArgs& a, void* stream);
+
+// Moment kernel: returns -1 if no instantiation matches (R, p); the caller
+// then uses the direct kernel.  coefs are in double; converted internally.
+bool hmom_available(DType t, int R, int p);
+int launch_hmom(DType t, int R, int p, const HMomArgs& a, const HMomCoefs<double>& c,
+                void* stream);
+
+}  // namespace mgbf

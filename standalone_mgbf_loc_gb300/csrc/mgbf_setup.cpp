@@ -1,0 +1,268 @@
+// FP64 setup of the filter tables; see mgbf_setup.hpp for the reference
+// routines restated here.
+#include "mgbf_setup.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+
+#include "../../include/mgbf.h"
+
+namespace mgbf {
+
+static double ipow(double x, int p) {
+    double r = 1.0;
+    for (int t = 0; t < p; ++t) r *= x;
+    return r;
+}
+
+static double binom(int n, int k) {
+    double r = 1.0;
+    for (int t = 1; t <= k; ++t) r = r * (n - k + t) / t;
+    return r;
+}
+
+int canonical_width(int R, int gy) {
+    const long lim = (long)R * R + R - (long)gy * gy;
+    int m = 0;
+    while ((long)(m + 1) * (m + 1) <= lim) ++m;
+    return m;
+}
+
+int build_hstencil(int p, double ampl02, int hx, int hy, HStencil& H, std::string& err) {
+    if (!(ampl02 > 0.0)) {
+        err = "mg_ampl02 must be positive";
+        return MGBF_ERR_CONFIG;
+    }
+    const double rmom2_2 = 1.0 / std::sqrt(2.0 * p + 4.0);
+    const double el = std::sqrt(1.0 / ampl02);  // cholaspect2 on diag(ampl02)
+    const double exx = el * rmom2_2, eyy = el * rmom2_2, eyx = 0.0;
+    H.p = p;
+    H.exx = exx;
+    H.eyy = eyy;
+    // getlinesum2 (jp_pbfil.f90:182-218)
+    const double y = 1.0 / eyy;
+    const int gyl = (int)std::ceil(-y + kEps), gym = (int)std::floor(y - kEps);
+    if (gyl < -hy || gym > hy) {
+        err = "getlinesum2: filter reach " + std::to_string(std::max(-gyl, gym)) +
+              " exceeds hy=" + std::to_string(hy);
+        return MGBF_ERR_REACH;
+    }
+    std::vector<int> gxl(gym - gyl + 1 > 0 ? gym - gyl + 1 : 0), gxm(gxl.size());
+    double sum = 0.0;
+    int R = std::max(-gyl, gym);
+    for (int gy = gyl; gy <= gym; ++gy) {
+        const double yy = gy, xc = -yy * eyx;
+        const double rrx = (yy * eyy) * (yy * eyy);
+        const double x = std::sqrt(1.0 - rrx);
+        const int lo = (int)std::ceil((xc - x) / exx + kEps), hi = (int)std::floor((xc + x) / exx - kEps);
+        if (lo < -hx || hi > hx) {
+            err = "getlinesum2: filter reach " + std::to_string(std::max(-lo, hi)) +
+                  " exceeds hx=" + std::to_string(hx);
+            return MGBF_ERR_REACH;
+        }
+        gxl[gy - gyl] = lo;
+        gxm[gy - gyl] = hi;
+        R = std::max(R, std::max(-lo, hi));
+        for (int gx = lo; gx <= hi; ++gx) {
+            const double xx = gx;
+            const double rr = rrx + (xx * exx - xc) * (xx * exx - xc);
+            sum += ipow(1.0 - rr, p);
+        }
+    }
+    if (!(sum > 0.0)) {
+        err = "getlinesum2: empty or degenerate stencil";
+        return MGBF_ERR_CONFIG;
+    }
+    if (R > kMaxReach) {
+        err = "horizontal reach " + std::to_string(R) + " exceeds the supported maximum " +
+              std::to_string(kMaxReach);
+        return MGBF_ERR_UNSUPPORTED;
+    }
+    const double s = 1.0 / sum;
+    H.s = s;
+    H.R = R;
+    const int W = 2 * R + 1;
+    H.mrow.assign(W, -1);
+    H.w.assign((size_t)W * W, 0.0);
+    bool symmetric = (gyl == -gym);
+    for (int gy = gyl; gy <= gym; ++gy) {
+        const int lo = gxl[gy - gyl], hi = gxm[gy - gyl];
+        if (lo != -hi) symmetric = false;
+        H.mrow[gy + R] = hi;
+        const double yy = gy, xc = -yy * eyx;
+        const double rrx = (yy * eyy) * (yy * eyy);
+        for (int gx = lo; gx <= hi; ++gx) {
+            const double xx = gx;
+            const double rr = rrx + (xx * exx - xc) * (xx * exx - xc);
+            H.w[(size_t)(gy + R) * W + (gx + R)] = s * ipow(1.0 - rr, p);  // frow
+        }
+    }
+    if (!symmetric) {
+        err = "radial support is not symmetric";
+        return MGBF_ERR_CONFIG;
+    }
+    bool canon = (gyl == -R && gym == R);
+    for (int gy = -R; gy <= R && canon; ++gy)
+        if (H.mrow[gy + R] != canonical_width(R, std::abs(gy))) canon = false;
+    H.canonical = canon && p <= kMaxMomP;
+    H.mom = HMomCoefs<double>{};
+    if (H.canonical) {
+        const int PQ = p + 1;
+        for (int gy = 0; gy <= R; ++gy) {
+            const double A = 1.0 - (gy * eyy) * (gy * eyy);
+            for (int q = 0; q <= p; ++q)
+                H.mom.coef[gy * PQ + q] = s * binom(p, q) * ((q & 1) ? -1.0 : 1.0) * ipow(A, p - q);
+        }
+        for (int m = 0; m <= R; ++m) {
+            const double u = (m * exx) * (m * exx);
+            for (int q = 0; q <= p; ++q) H.mom.upow[m * PQ + q] = ipow(u, q);
+        }
+    }
+    return MGBF_OK;
+}
+
+int build_zstencil(int p, double ampl01, int hz, int lm, bool need, ZStencil& Z, std::string& err) {
+    if (!(ampl01 > 0.0)) {
+        err = "mg_ampl01 must be positive";
+        return MGBF_ERR_CONFIG;
+    }
+    const double rmom2_1 = 1.0 / std::sqrt(2.0 * p + 3.0);
+    const double el = 1.0 / std::sqrt(ampl01);  // cholaspect1
+    const double exx = el * rmom2_1;
+    const double x = 1.0 / exx;
+    const int gxl = (int)std::ceil(-x + kEps), gxm = (int)std::floor(x - kEps);
+    // getlinesum1 (jp_pbfil.f90:149-180), called unconditionally in
+    // def_mg_weights (mg_intstate.f90:429)
+    if (gxl < -hz || gxm > hz) {
+        err = "getlinesum1: filter reach " + std::to_string(std::max(-gxl, gxm)) +
+              " exceeds hz=" + std::to_string(hz);
+        return MGBF_ERR_REACH;
+    }
+    double sum = 0.0;
+    for (int gx = gxl; gx <= gxm; ++gx) {
+        const double xx = gx;
+        sum += ipow(1.0 - (xx * exx) * (xx * exx), p);
+    }
+    const double s = 1.0 / sum;
+    const int mz = std::max(-gxl, gxm);
+    Z.lm = lm;
+    Z.mz = mz;
+    Z.exx = exx;
+    Z.s = s;
+    Z.wz.assign(2 * mz + 1, 0.0);
+    for (int gx = gxl; gx <= gxm; ++gx) {
+        const double xx = gx;
+        Z.wz[gx + mz] = s * ipow(1.0 - (xx * exx) * (xx * exx), p);  // frow of vrbeta1
+    }
+    if (!need) return MGBF_OK;
+    if (mz > lm - 1) {
+        err = "vertical reach " + std::to_string(mz) + " needs lm >= " + std::to_string(mz + 1);
+        return MGBF_ERR_CONFIG;
+    }
+    const int bw = 2 * mz + 1;
+    Z.fwd.assign((size_t)lm * bw, 0.0);
+    Z.adj.assign((size_t)lm * bw, 0.0);
+    // forward: W(1-L) = W(1+L), W(lm+L) = W(lm-L) (whole-sample mirror,
+    // mg_filtering.f90:2178-2181), then b(L) = sum_g w(g) W(L+g)
+    for (int L = 0; L < lm; ++L)
+        for (int g = gxl; g <= gxm; ++g) {
+            int q = L + g;
+            if (q < 0) q = -q;
+            if (q > lm - 1) q = 2 * (lm - 1) - q;
+            Z.fwd[(size_t)L * bw + (q - L) + mz] += Z.wz[g + mz];
+        }
+    for (int L = 0; L < lm; ++L)
+        for (int d = -mz; d <= mz; ++d) {
+            const int r = L + d;
+            if (r < 0 || r >= lm) continue;
+            Z.adj[(size_t)L * bw + d + mz] = Z.fwd[(size_t)r * bw + (-d) + mz];
+        }
+    return MGBF_OK;
+}
+
+int build_interp(int nf, bool quart, Interp1D& T, std::string& err) {
+    // def_offset_coef (mg_interpolate.f90:61-86)
+    static const double PC[4] = {-9.0 / 128.0, 111.0 / 128.0, 29.0 / 128.0, -3.0 / 128.0};
+    static const double QC[4] = {-3.0 / 128.0, 29.0 / 128.0, 111.0 / 128.0, -9.0 / 128.0};
+    static const double AC[3] = {5.0 / 32.0, 30.0 / 32.0, -3.0 / 32.0};
+    static const double BC[3] = {-3.0 / 32.0, 30.0 / 32.0, 5.0 / 32.0};
+    if (nf % 2) {
+        err = "generation size " + std::to_string(nf) + " is odd";
+        return MGBF_ERR_DIVISIBILITY;
+    }
+    const int nc = nf / 2;
+    const int nt = quart ? 3 : 4;
+    if (nc < (quart ? 1 : 2)) {
+        err = "coarse generation size " + std::to_string(nc) + " too small for the interpolation halo";
+        return MGBF_ERR_DIVISIBILITY;
+    }
+    T.nf = nf;
+    T.nc = nc;
+    T.ntap = nt;
+    T.pidx.assign((size_t)nf * nt, 0);
+    T.pw.assign((size_t)nf * nt, 0.0);
+    std::vector<double> P((size_t)nf * nc, 0.0);
+    for (int i = 1; i <= nf; ++i) {
+        int iL;
+        const double* cf;
+        if (!quart) {  // direct1 (mg_generations.f90:1190-1250)
+            iL = i / 2;
+            cf = (i % 2) ? QC : PC;
+        } else {  // direct2 (mg_generations.f90:1319-1374)
+            if (i % 2) { iL = (i + 1) / 2; cf = AC; }
+            else { iL = i / 2; cf = BC; }
+        }
+        for (int t = 0; t < nt; ++t) {
+            int c = iL - 1 + t;             // coarse index with halo 2 (1)
+            if (c < 1) c = 1 - c;           // boco_2d half-sample mirror
+            if (c > nc) c = 2 * nc + 1 - c;
+            T.pidx[(size_t)(i - 1) * nt + t] = c - 1;
+            T.pw[(size_t)(i - 1) * nt + t] = cf[t];
+            P[(size_t)(i - 1) * nc + (c - 1)] += cf[t];
+        }
+    }
+    T.rw.assign((size_t)nc * 8, 0.0);
+    for (int c = 0; c < nc; ++c)
+        for (int f = 0; f < nf; ++f) {
+            const double v = P[(size_t)f * nc + c];
+            if (v == 0.0) continue;
+            const int a = f - (2 * c - 3);
+            if (a < 0 || a >= 8) {
+                err = "restriction stencil wider than 8";
+                return MGBF_ERR_CONFIG;
+            }
+            T.rw[(size_t)c * 8 + a] = v;
+        }
+    return MGBF_OK;
+}
+
+int check_other_reaches(int p, double ampl02, double ampl03, int hx, int hy, int hz, std::string& err) {
+    // getlinesum(hx,1,im,paspx,ssx) / (hy,...,paspy,ssy): paspx = pasp02 is
+    // used without cholaspect (mg_intstate.f90:370-375,427-428).
+    const double rmom2_1 = 1.0 / std::sqrt(2.0 * p + 3.0);
+    {
+        const double exx = ampl02 * rmom2_1;
+        const double x = 1.0 / exx;
+        const int lo = (int)std::ceil(-x + kEps), hi = (int)std::floor(x - kEps);
+        if (lo < -hx || hi > hx || lo < -hy || hi > hy) {
+            err = "getlinesum1 on paspx/paspy: reach " + std::to_string(std::max(-lo, hi)) +
+                  " exceeds hx/hy";
+            return MGBF_ERR_REACH;
+        }
+    }
+    // getlinesum3 on pasp3 = diag(ampl03) after cholaspect3.
+    if (ampl03 > 0.0) {
+        const double rmom2_3 = 1.0 / std::sqrt(2.0 * p + 5.0);
+        const double e = std::sqrt(1.0 / ampl03) * rmom2_3;
+        const double z = 1.0 / e;
+        const int hi = (int)std::floor(z - kEps);
+        if (hi > hz || hi > hy || hi > hx) {
+            err = "getlinesum3 on pasp3: reach " + std::to_string(hi) + " exceeds hx/hy/hz";
+            return MGBF_ERR_REACH;
+        }
+    }
+    return MGBF_OK;
+}
+
+}  // namespace mgbf

@@ -1,0 +1,64 @@
+// FP64 host-side setup of the MGBF filter tables.
+//
+// Restates the reference's setup arithmetic (all FP64, as in the reference):
+//   rmom2_k            mg_parameter.f90:567-572
+//   cholaspect1/2      jp_pbfil.f90:74-107 (diagonal aspect tensors)
+//   getlinesum1/2      jp_pbfil.f90:149-218 (support and normalisation)
+//   vrbeta1/2 weights  jp_pbfil.f90:856-928 (frow = s*(1-rr)^p)
+//   def_offset_coef    mg_interpolate.f90:61-86
+// and turns them into the tables the kernels consume: banded z matrices
+// (with the whole-sample mirror and edge fold folded in), the radial
+// support table, dense radial weights, moment coefficients, and
+// restriction/prolongation index/weight rows with the half-sample mirror
+// folded in.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "mgbf_kernels.cuh"
+
+namespace mgbf {
+
+constexpr double kEps = 1.e-12;  // jp_pbfil.f90: eps in getlinesum / rbeta
+
+struct HStencil {
+    int p = 2;
+    double exx = 0, eyy = 0, s = 0;
+    int R = 0;                  // reach: max |gx|, |gy| in the support
+    std::vector<int> mrow;      // 2R+1 row half-widths (-1: empty row)
+    std::vector<double> w;      // (2R+1)^2 dense weights (zero outside)
+    bool canonical = false;     // support == disk of radius R + 1/2
+    HMomCoefs<double> mom{};    // moment coefficients (valid if canonical)
+};
+
+struct ZStencil {
+    int lm = 0, mz = 0;
+    double exx = 0, s = 0;
+    std::vector<double> wz;     // 2mz+1 tap weights
+    std::vector<double> fwd;    // lm x (2mz+1) band of Bz
+    std::vector<double> adj;    // lm x (2mz+1) band of Bz^T
+};
+
+struct Interp1D {
+    int nf = 0, nc = 0, ntap = 4;
+    std::vector<double> rw;     // nc x 8 restriction weights, fine f = 2c-3+a
+    std::vector<int> pidx;      // nf x ntap coarse indices (mirrored)
+    std::vector<double> pw;     // nf x ntap prolongation weights
+};
+
+// Returns 0 or an MGBF_ERR_* code with a message in err.
+int build_hstencil(int p, double ampl02, int hx, int hy, HStencil& out, std::string& err);
+int build_zstencil(int p, double ampl01, int hz, int lm, bool need_mirror, ZStencil& out,
+                   std::string& err);
+int build_interp(int nf, bool quart, Interp1D& out, std::string& err);
+
+// Reach checks def_mg_weights performs for the other filters of the
+// reference (getlinesum on paspx/paspy, mg_intstate.f90:427-428, which skip
+// cholaspect; getlinesum3 on pasp3, mg_intstate.f90:431).
+int check_other_reaches(int p, double ampl02, double ampl03, int hx, int hy, int hz,
+                        std::string& err);
+
+// Canonical row half-width of a disk of radius R + 1/2.
+int canonical_width(int R, int gy);
+
+}  // namespace mgbf

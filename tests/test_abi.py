@@ -1,0 +1,183 @@
+"""CPU tests of the C-ABI library: it loads, exports every symbol that
+include/mgbf.h declares, and its host-side logic (namelist, validation,
+error codes) works without a GPU.  No compute call is made here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig, MGBFError, _abi
+from tests.helpers import canonical, small_config
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "mgbf.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mgbf_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = header_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _abi.SIGNATURES, n
+
+
+def test_strerror_codes(lib):
+    for code in range(0, -11, -1):
+        assert lib.mgbf_strerror(code)
+    assert lib.mgbf_strerror(-99) == b"unknown error"
+
+
+NML = """
+&PARAMETERS_MGBETA
+! comment line
+  mg_ampl01=2.0, mg_ampl02=5.28125, mg_ampl03=1.,
+  mg_weig1=10.,mg_weig2=50.,mg_weig3=100.,mg_weig4=200.,mg_weig5=0.,
+  hx=6,hy=6,hz=3,p=2,
+  mgbf_line=.false., mgbf_proc=6, n_ens=20,
+  lm_a = 65, lm = 65,
+  km2=0,km3=6,
+  l_loc=.false.
+  l_filt_g1 =.true.,
+  l_vertical_filter=.true.,
+  ldelta=.true.,
+  lquart=.false., lhelm=.false.,
+  gm_max=4,
+  nm0 = 1440, mm0 = 960,
+  nxPE=20,nyPE=20,im_filt=64,jm_filt=32,
+/
+"""
+
+
+def write(tmp_path, text, name="mgbeta.nml"):
+    p = tmp_path / name
+    p.write_text(text)
+    return str(p)
+
+
+def test_namelist_parse(lib, tmp_path):
+    c = MGBFConfig.from_namelist(write(tmp_path, NML))
+    assert c.mgbf_proc == 6 and c.n_ens == 20 and c.lm == 65 and c.km3 == 6
+    assert c.mg_weig4 == 200.0 and c.mg_ampl02 == 5.28125
+    assert c.l_filt_g1 and c.l_vertical_filter and not c.lquart and c.ldelta
+    assert (c.nxPE, c.nyPE, c.im_filt, c.jm_filt) == (20, 20, 64, 32)
+
+
+def test_namelist_case_and_fortran_exponents(lib, tmp_path):
+    text = NML.replace("&PARAMETERS_MGBETA", "&parameters_mgbeta").replace("mg_ampl01=2.0", "MG_AMPL01=2.0D0")
+    c = MGBFConfig.from_namelist(write(tmp_path, text))
+    assert c.mg_ampl01 == 2.0
+
+
+def test_namelist_real_for_integer_p_is_rejected(lib, tmp_path):
+    # the shipped RUN/mgbf.nml says p=1.3 while p is an integer (mg_parameter.f90:110)
+    with pytest.raises(MGBFError) as e:
+        MGBFConfig.from_namelist(write(tmp_path, NML.replace("p=2", "p=1.3")))
+    assert e.value.code == _abi.MGBF_ERR_NAMELIST
+
+
+def test_namelist_unknown_item(lib, tmp_path):
+    with pytest.raises(MGBFError) as e:
+        MGBFConfig.from_namelist(write(tmp_path, NML.replace("hx=6", "hxx=6")))
+    assert e.value.code == _abi.MGBF_ERR_NAMELIST
+
+
+def test_namelist_missing_file(lib):
+    with pytest.raises(MGBFError) as e:
+        MGBFConfig.from_namelist("/nonexistent/mgbeta.nml")
+    assert e.value.code == _abi.MGBF_ERR_IO
+
+
+def test_namelist_extensions(lib, tmp_path):
+    text = NML.replace("gm_max=4,", "gm_max=6, gm_uncapped=.true., weig_ext=1.0,0.5,0.25, layout=1,")
+    c = MGBFConfig.from_namelist(write(tmp_path, text))
+    assert c.gm_uncapped and c.weig_ext == [1.0, 0.5, 0.25] and c.layout == 1
+
+
+def test_create_from_namelist_and_dims(lib, tmp_path):
+    op = MGBF.from_namelist(write(tmp_path, NML))
+    d = op.dims
+    assert (d.im, d.jm) == (1280, 640)
+    assert d.km_all == 20 * 65 * 6 and d.km3_all == 120
+    assert d.gm == 4  # min(gm_max, def_maxgen(20, 20) = 6)
+    assert d.reach_h == 6 and d.hbeta_kernel == 1
+    assert op.field_shape() == (640 + 12, 1280 + 12, 20 * 65 * 6)
+    op.close()
+
+
+def test_generation_cap_follows_rank_layout(lib):
+    c = small_config(nxPE=2, nyPE=2, im_filt=32, jm_filt=32, gm_max=4, hx=4, hy=4)
+    assert MGBF(c).dims.gm == 2  # def_maxgen(2,2) = 2
+    c.gm_uncapped = True
+    assert MGBF(c).dims.gm == 4
+
+
+@pytest.mark.parametrize("change,code", [
+    (dict(hx=3), _abi.MGBF_ERR_REACH),                       # getlinesum2 stop
+    (dict(hz=1), _abi.MGBF_ERR_REACH),                       # getlinesum1 stop
+    (dict(nxPE=1, im_filt=66, gm_uncapped=True), _abi.MGBF_ERR_DIVISIBILITY),  # 66 % 4
+    (dict(nm0=10), _abi.MGBF_ERR_CONFIG),                    # nm0 not divisible by nxm
+    (dict(mg_ampl03=100.0), _abi.MGBF_ERR_REACH),            # getlinesum3 on pasp3
+    (dict(helm_b=[0.1]), _abi.MGBF_ERR_UNSUPPORTED),
+    (dict(p=-1), _abi.MGBF_ERR_CONFIG),
+])
+def test_create_validation(lib, change, code):
+    with pytest.raises(MGBFError) as e:
+        MGBF(small_config(**change))
+    assert e.value.code == code
+
+
+def test_reach_larger_than_coarsest_generation(lib):
+    c = small_config(nxPE=1, nyPE=1, im_filt=16, jm_filt=16, gm_max=3, gm_uncapped=True,
+                     hx=6, hy=6, mg_ampl02=canonical(6))
+    with pytest.raises(MGBFError) as e:
+        MGBF(c)
+    assert e.value.code == _abi.MGBF_ERR_DIVISIBILITY
+
+
+def test_unsupported_and_unknown_procedures(lib):
+    op = MGBF(small_config())
+    x = np.zeros(op.field_shape())
+    for proc in (2, 3, 4, 5, 7, 8):
+        with pytest.raises(MGBFError) as e:
+            op.filtering_procedure(proc, x)
+        assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
+    # no case default in the reference's select: other values do nothing
+    x[...] = 1.0
+    op.filtering_procedure(0, x)
+    op.filtering_procedure(9, x)
+    assert (x == 1.0).all()
+
+
+def test_proc1_requires_single_member(lib):
+    op = MGBF(small_config(n_ens=2))
+    with pytest.raises(MGBFError) as e:
+        op.filtering_procedure(1, np.zeros(op.field_shape()))
+    assert e.value.code == _abi.MGBF_ERR_CONFIG
+
+
+def test_proc6_vertical_requires_km2_zero(lib):
+    op = MGBF(small_config(km2=1, n_ens=2))
+    with pytest.raises(MGBFError) as e:
+        op.filtering_procedure(6, np.zeros(op.field_shape()))
+    assert e.value.code == _abi.MGBF_ERR_CONFIG
+
+
+def test_shape_and_dtype_checks(lib):
+    op = MGBF(small_config())
+    with pytest.raises(MGBFError):
+        op.filtering_procedure(1, np.zeros((3, 3, 3)))
+    with pytest.raises(MGBFError):
+        op.filtering_procedure(1, np.zeros(op.field_shape(), dtype=np.int32))
+
+
+def test_null_arguments_rejected(lib):
+    assert lib.mgbf_filtering_procedure(None, 1, None, 0, 0, None) == _abi.MGBF_ERR_ARG
+    assert lib.mgbf_create(None, None) == _abi.MGBF_ERR_ARG
+    assert lib.mgbf_destroy(None) == _abi.MGBF_OK

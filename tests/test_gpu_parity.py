@@ -1,0 +1,206 @@
+"""GPU parity of libmgbf against the FP64 oracle, through the C-ABI.
+
+Tolerances (relative L2 against the FP64 oracle):
+  FP64 storage/arithmetic      1e-12
+  FP32 storage/arithmetic      1e-5
+  BF16 storage, FP32 arithmetic 2e-2  (2^-8 rounding at every stored stage)
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from standalone_mgbf_loc_gb300 import MGBF, MGBFBatch, GroupDesc, _abi
+from tests.helpers import canonical, canonical_z, oracle_cfg, rel_l2, small_config
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = {torch.float64: 1e-12, torch.float32: 1e-5, torch.bfloat16: 2e-2}
+
+
+def run_gpu(op, proc, x, dtype, cuda, adjoint=False):
+    t = torch.from_numpy(x).to(device=cuda, dtype=dtype).contiguous()
+    if adjoint:
+        op.filtering_procedure_adjoint(proc, t)
+    else:
+        op.filtering_procedure(proc, t)
+    torch.cuda.synchronize()
+    return t.double().cpu().numpy()
+
+
+def compact_input(op, seed=0):
+    return np.random.default_rng(seed).standard_normal(op.field_shape())
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("proc", [1, 6])
+@pytest.mark.parametrize("lquart", [False, True])
+def test_parity_moment_kernel(lib, cuda, dtype, proc, lquart):
+    c = small_config(lquart=lquart, n_ens=1 if proc == 1 else 2)
+    op = MGBF(c)
+    assert op.dims.hbeta_kernel == 1
+    x = compact_input(op)
+    y = run_gpu(op, proc, x, dtype, cuda)
+    ref = O.filter_compact(oracle_cfg(c, proc), x)
+    assert rel_l2(y, ref) < TOL[dtype]
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("ampl02", [2.0, 2.5, 1.3])
+def test_parity_direct_kernel(lib, cuda, dtype, ampl02):
+    c = small_config(mg_ampl02=ampl02)
+    op = MGBF(c)
+    assert op.dims.hbeta_kernel == 0
+    x = compact_input(op, 1)
+    y = run_gpu(op, 1, x, dtype, cuda)
+    ref = O.filter_compact(oracle_cfg(c, 1), x)
+    assert rel_l2(y, ref) < TOL[dtype]
+
+
+@pytest.mark.parametrize("p", [1, 3])
+def test_parity_other_powers(lib, cuda, p):
+    c = small_config(p=p, mg_ampl02=canonical(4, p), mg_ampl01=canonical_z(2, p), mg_ampl03=0.5)
+    op = MGBF(c)
+    x = compact_input(op, 2)
+    y = run_gpu(op, 1, x, torch.float64, cuda)
+    assert rel_l2(y, O.filter_compact(oracle_cfg(c, 1), x)) < 1e-12
+
+
+def test_proc6_without_generation1_filter(lib, cuda):
+    c = small_config(n_ens=3, l_filt_g1=False)
+    op = MGBF(c)
+    x = compact_input(op, 3)
+    y = run_gpu(op, 6, x, torch.float64, cuda)
+    assert rel_l2(y, O.filter_compact(oracle_cfg(c, 6), x)) < 1e-12
+
+
+def test_2d_variables_and_no_vertical_filter(lib, cuda):
+    c = small_config(km2=3, km3=2)
+    op = MGBF(c)
+    x = compact_input(op, 4)
+    y = run_gpu(op, 1, x, torch.float64, cuda)
+    assert rel_l2(y, O.filter_compact(oracle_cfg(c, 1), x)) < 1e-12
+    c2 = small_config(l_vertical_filter=False)
+    op2 = MGBF(c2)
+    y2 = run_gpu(op2, 1, x[..., :op2.dims.km_all], torch.float64, cuda)
+    assert rel_l2(y2, O.filter_compact(oracle_cfg(c2, 1), x[..., :op2.dims.km_all])) < 1e-12
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_halo_layout_in_place(lib, cuda, dtype):
+    """VALL(km_all, 1-hx:im+hx, 1-hy:jm+hy) in place; halos end up zero."""
+    c = small_config(layout=_abi.MGBF_LAYOUT_HALO)
+    op = MGBF(c)
+    v = np.random.default_rng(5).standard_normal(op.field_shape())
+    ref = v.copy()
+    O.filtering_procedure(oracle_cfg(c, 1), ref)
+    y = run_gpu(op, 1, v, dtype, cuda)
+    assert rel_l2(y, ref) < TOL[dtype]
+    hx, hy = c.hx, c.hy
+    inner = np.zeros(y.shape, bool)
+    inner[hy:-hy, hx:-hx, :] = True
+    assert np.abs(y[~inner]).max() == 0.0
+
+
+def test_host_memory_path(lib, cuda):
+    c = small_config()
+    op = MGBF(c)
+    x = compact_input(op, 6)
+    h64 = x.copy()
+    op.filtering_procedure(1, h64)
+    h32 = x.astype(np.float32)
+    op.filtering_procedure(1, h32)
+    ref = O.filter_compact(oracle_cfg(c, 1), x)
+    assert rel_l2(h64, ref) < 1e-12
+    assert rel_l2(h32, ref) < 1e-5
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-6)])
+@pytest.mark.parametrize("proc", [1, 6])
+def test_adjoint_dot_product(lib, cuda, dtype, tol, proc):
+    c = small_config(n_ens=1 if proc == 1 else 2)
+    op = MGBF(c)
+    rng = np.random.default_rng(7)
+    x, y = rng.standard_normal(op.field_shape()), rng.standard_normal(op.field_shape())
+    lx = run_gpu(op, proc, x, dtype, cuda)
+    lty = run_gpu(op, proc, y, dtype, cuda, adjoint=True)
+    a, b = (lx * y).sum(), (x * lty).sum()
+    assert abs(a - b) / max(abs(a), abs(b)) < tol
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-11), (torch.float32, 1e-4)])
+@pytest.mark.parametrize("proc", [1, 6])
+def test_weight_gradients(lib, cuda, dtype, tol, proc):
+    c = small_config(n_ens=1 if proc == 1 else 2)
+    op = MGBF(c)
+    rng = np.random.default_rng(8)
+    x, gy = rng.standard_normal(op.field_shape()), rng.standard_normal(op.field_shape())
+    tx = torch.from_numpy(x).to(cuda, dtype)
+    tg = torch.from_numpy(gy).to(cuda, dtype)
+    gx, ga = op.apply_with_weight_grads(proc, tx, tg)
+    oc = oracle_cfg(c, proc)
+    ga_ref = O.weight_grads(oc, x, gy)
+    gx_ref = O.filter_compact(oc, gy)
+    assert np.abs(ga - ga_ref).max() / np.abs(ga_ref).max() < tol
+    assert rel_l2(gx.double().cpu().numpy(), gx_ref) < max(tol, TOL[dtype])
+
+
+def test_autograd_function_finite_differences(lib, cuda):
+    from standalone_mgbf_loc_gb300.autograd import mgbf_apply
+    c = small_config()
+    op = MGBF(c)
+    rng = np.random.default_rng(9)
+    x = torch.from_numpy(rng.standard_normal(op.field_shape())).to(cuda).requires_grad_(True)
+    w = torch.tensor([1.0, 0.5, 0.25], dtype=torch.float64, device=cuda, requires_grad=True)
+    r = torch.from_numpy(rng.standard_normal(op.field_shape())).to(cuda)
+    loss = (mgbf_apply(op, x, w, 1) * r).sum()
+    loss.backward()
+    h = 1e-3
+    for g in range(3):
+        wp, wm = w.detach().clone(), w.detach().clone()
+        wp[g] += h
+        wm[g] -= h
+        fd = ((mgbf_apply(op, x.detach(), wp, 1) * r).sum() - (mgbf_apply(op, x.detach(), wm, 1) * r).sum()) / (2 * h)
+        assert float(w.grad[g]) == pytest.approx(float(fd), rel=1e-8, abs=1e-8)
+    d = torch.from_numpy(rng.standard_normal(op.field_shape())).to(cuda)
+    fd = ((mgbf_apply(op, x.detach() + h * d, w.detach(), 1) * r).sum()
+          - (mgbf_apply(op, x.detach() - h * d, w.detach(), 1) * r).sum()) / (2 * h)
+    assert float((x.grad * d).sum()) == pytest.approx(float(fd), rel=1e-8)
+
+
+def test_config1_impulse_and_noise(lib, cuda):
+    """256x256x32, 4 generations (8x8 ranks), h=6, hz=3, weights 1,.5,.25,.125."""
+    c = small_config(nxPE=8, nyPE=8, im_filt=32, jm_filt=32, lm=32, km3=1, gm_max=4, hx=6, hy=6, hz=3,
+                     mg_ampl02=canonical(6), mg_ampl01=canonical_z(3))
+    op = MGBF(c)
+    imp = np.zeros(op.field_shape())
+    imp[127, 127, 15] = 1.0  # Fortran (128,128,16)
+    noise = np.random.default_rng(0).standard_normal(op.field_shape())
+    oc = oracle_cfg(c, 1)
+    for x in (imp, noise):
+        ref = O.filter_compact(oc, x)
+        for dtype in (torch.float64, torch.float32):
+            assert rel_l2(run_gpu(op, 1, x, dtype, cuda), ref) < TOL[dtype]
+
+
+def test_batched_groups(lib, cuda):
+    """Groups with their own reach and levels in one call == per-group oracle runs."""
+    I = J = 64
+    gm = 3
+    w = [1.0, 0.5, 0.25]
+    groups = [
+        GroupDesc(nk=3 * 8, lm=8, nzcol=3, hx=4, hy=4, hz=2, p=2, mg_ampl01=canonical_z(2), mg_ampl02=canonical(4)),
+        GroupDesc(nk=2 * 6, lm=6, nzcol=2, hx=6, hy=6, hz=2, p=2, mg_ampl01=canonical_z(2), mg_ampl02=canonical(6)),
+        GroupDesc(nk=5, lm=1, nzcol=0, hx=5, hy=5, hz=2, p=2, mg_ampl01=canonical_z(2), mg_ampl02=canonical(5) * 0.9),
+    ]
+    b = MGBFBatch(I, J, gm, w, groups)
+    rng = np.random.default_rng(10)
+    xs = [rng.standard_normal((J, I, g.nk)) for g in groups]
+    ts = [torch.from_numpy(x).to(cuda, torch.float32).contiguous() for x in xs]
+    b.apply(ts)
+    torch.cuda.synchronize()
+    for g, x, t in zip(groups, xs, ts):
+        oc = O.OracleConfig(I=I, J=J, nk=g.nk, hx=g.hx, hy=g.hy, hz=g.hz, p=g.p, ampl01=g.mg_ampl01,
+                            ampl02=g.mg_ampl02, gm=gm, weights=w, proc=6, lm=g.lm, nzcol=g.nzcol,
+                            l_vertical_filter=g.nzcol > 0)
+        assert rel_l2(t.double().cpu().numpy(), O.filter_compact(oc, x)) < 1e-5
