@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 MGBF filtering path.
+
+Workload (one "step" = forward + adjoint of the whole batch): batched
+ensemble localization, 80 members x 4 variables on a 512x512 filter grid --
+three 3D variables with 64, 64 and 48 levels and one 2D variable -- with 5
+generations, p = 2, horizontal reaches {8, 10, 12, 16}, vertical reach 4,
+FP32 storage and arithmetic.  Inputs are seeded N(0,1) fields generated on
+the device (torch.Generator, seed 1000 + rank); one field set is 14.8 GB, far
+larger than L2, so no flush is needed between steps.
+
+Prints one JSON line (rank 0).  `--impl reference` times the CPU restatement
+of the reference's filtering_procedure (the oracle; the Fortran reference
+cannot be built on these machines) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = ("grid-pt applications/s fwd+adj (fraction of HBM roofline), "
+          "batched FP32 vs plain FP64, rel-L2")
+UNIT = "grid-pt applications/s"
+
+IM = JM = 512
+GM = 5
+HZ = 4
+P = 2
+# variable groups: (levels, horizontal reach)
+VARS = [(64, 8), (64, 10), (48, 12), (1, 16)]
+# generation weights normalised so that L maps a constant field to itself
+WEIGHTS = [4.0 ** (-g) / GM for g in range(GM)]
+WORKLOAD = ("batched ensemble localization: 80 members x {64,64,48,1} levels (3D,3D,3D,2D), "
+            "512x512, 5 generations, p=2, h={8,10,12,16}, hz=4, FP32, forward+adjoint")
+
+
+def ampl02(h: int) -> float:
+    """mg_ampl02 whose radial support has reach h (disk radius h+1/2)."""
+    return (h + 0.5) ** 2 / (2 * P + 4)
+
+
+def ampl01(hz: int) -> float:
+    return (hz + 0.5) ** 2 / (2 * P + 3)
+
+
+def groups(members: int):
+    from standalone_mgbf_loc_gb300 import GroupDesc
+    out = []
+    for lm, h in VARS:
+        out.append(GroupDesc(nk=members * lm, lm=lm, nzcol=members if lm > 1 else 0, hx=h, hy=h, hz=HZ, p=P,
+                             mg_ampl01=ampl01(HZ), mg_ampl02=ampl02(h)))
+    return out
+
+
+# ----------------------------------------------------------------- helpers
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names[1:], parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------ CPU (oracle)
+
+def oracle_member_cfg(group_index: int, nthreads: int):
+    from oracle import oracle as O
+    lm, h = VARS[group_index]
+    return O.OracleConfig(I=IM, J=JM, nk=lm, hx=h, hy=h, hz=HZ, p=P, ampl01=ampl01(HZ), ampl02=ampl02(h), gm=GM,
+                          weights=WEIGHTS, proc=6, lm=lm, nzcol=1 if lm > 1 else 0,
+                          l_vertical_filter=lm > 1, nthreads=nthreads)
+
+
+def cpu_step(x: np.ndarray, nthreads: int):
+    """One sample step on the host: forward + adjoint of one member of the
+    first variable (64 levels, reach 8) on the full 512x512 grid."""
+    from oracle import oracle as O
+    c = oracle_member_cfg(0, nthreads)
+    y = O.filter_compact(c, x)
+    z = O.filter_compact(c, y)  # the adjoint chain equals the forward chain
+    return y, z
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    x = np.random.default_rng(1000).standard_normal((JM, IM, VARS[0][0]))
+    pts = float(IM * JM * VARS[0][0])
+    for _ in range(args.warmup):
+        cpu_step(x, nthreads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_step(x, nthreads)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = 2 * pts / dt
+    sample = "one member of the 64-level variable (512x512x64, reach 8, 5 generations), forward+adjoint per step"
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic: seeded N(0,1) (numpy seed 1000)",
+        "config": {"workload": WORKLOAD, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference's filtering_procedure (FP64, OpenMP); the Fortran+MPI "
+                "reference has no compiler on these machines",
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    from __graft_entry__ import build
+    build()
+    from standalone_mgbf_loc_gb300 import MGBFBatch, _abi
+    members = args.members
+    gdesc = groups(members)
+    batch = MGBFBatch(IM, JM, GM, WEIGHTS, gdesc)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1000 + rank)
+    fields = [torch.randn((JM, IM, g.nk), generator=gen, device=dev, dtype=torch.float32) for g in gdesc]
+    pristine0 = fields[0][:, :, :VARS[0][0]].double().cpu().numpy() if rank == 0 else None
+    pts_op = float(sum(IM * JM * g.nk for g in gdesc))
+
+    def step():
+        batch.apply(fields, adjoint=False)
+        batch.apply(fields, adjoint=True)
+
+    # correctness sample: member 0 of the first variable after one forward
+    batch.apply(fields, adjoint=False)
+    torch.cuda.synchronize()
+    gpu_member0 = fields[0][:, :, :VARS[0][0]].double().cpu().numpy() if rank == 0 else None
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = ws * 2 * pts_op / (ms_step * 1e-3)
+
+    # stage timers: dominant-kernel launch durations (separate, untimed pass)
+    _abi.timers_enable(True)
+    nstep_t = 2
+    for _ in range(nstep_t):
+        step()
+    torch.cuda.synchronize()
+    stats = _abi.timers_read()
+    _abi.timers_enable(False)
+    launches_per_step = sum(v[0] for v in stats.values()) / nstep_t
+    hb = [stats[k] for k in ("hfiltT", "hfilt") if k in stats]
+    h_launch = sum(v[0] for v in hb)
+    h_ms = sum(v[1] for v in hb)
+    h_pts = sum(v[2] for v in hb)
+    peak, peak_kind = measured_peaks()
+    s = 4  # bytes per FP32 element
+    achieved = (2 * s * h_pts) / (h_ms * 1e-3) / 1e9 if h_ms > 0 else None
+    stage_ms = {k: round(v[1] / nstep_t, 3) for k, v in stats.items()}
+    # DRAM traffic of the radial kernel per grid point and pass, from the ncu
+    # capture summarised in profiles/ (None until measured).
+    traffic_per_pt = HMOM_DRAM_BYTES_PER_POINT
+    traffic = (traffic_per_pt * h_pts / h_launch) if (traffic_per_pt and h_launch) else None
+
+    # end to end: pinned host fields -> device, forward + adjoint, device -> host
+    host = [f.to("cpu").pin_memory() for f in fields]
+    outs = [torch.empty_like(h).pin_memory() for h in host]
+    h2d = sum(h.numel() * h.element_size() for h in host)
+    e2e_steps = max(1, min(args.steps, 5))
+    for _ in range(1):
+        for h, f in zip(host, fields):
+            f.copy_(h, non_blocking=True)
+        step()
+        for o, f in zip(outs, fields):
+            o.copy_(f, non_blocking=True)
+    torch.cuda.synchronize()
+    barrier()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    for _ in range(e2e_steps):
+        for h, f in zip(host, fields):
+            f.copy_(h, non_blocking=True)
+        step()
+        for o, f in zip(outs, fields):
+            o.copy_(f, non_blocking=True)
+    e3.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e2.elapsed_time(e3)
+    if dist is not None:
+        t = torch.tensor([ms_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    e2e_value = ws * 2 * pts_op / (ms_e2e / e2e_steps * 1e-3)
+    del host, outs
+
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras["fp64_plain"] = plain_forward(torch, dev, torch.float64)
+        extras["fp32_plain"] = plain_forward(torch, dev, torch.float32)
+
+    result = None
+    if rank == 0:
+        cpu = None
+        rel = None
+        if not args.no_extras:
+            nthreads = os.cpu_count() or 1
+            t0 = time.perf_counter()
+            y, _ = cpu_step(pristine0, nthreads)
+            dt = time.perf_counter() - t0
+            rel = float(np.linalg.norm(gpu_member0 - y) / np.linalg.norm(y))
+            cpu = {"value": 2 * IM * JM * VARS[0][0] / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+                   "sample": "one member of the 64-level variable (512x512x64, reach 8), forward+adjoint, "
+                             "FP64 CPU restatement with OpenMP"}
+        result = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded N(0,1) fields generated on the device (torch.Generator seed 1000+rank)",
+            "config": {"workload": WORKLOAD, "members_per_gpu": members, "grid": [IM, JM], "generations": GM,
+                       "points_per_op_per_gpu": pts_op, "l2": "no flush: one field set (14.8 GB) >> L2 (129 MB)",
+                       "parallelism": f"replicas x{ws} (independent members per GPU, no collective)"},
+            "roofline": {"bound": "hbm", "kernel": "k_hmom (radial beta, moment form)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "peak_source": peak_kind,
+                         "algorithmic_bytes": "2 x 4 B per grid point per launch (read + write, FP32)",
+                         "launches": h_launch / nstep_t, "avg_launch_ms": h_ms / h_launch if h_launch else None},
+            "stages_ms_per_step": stage_ms,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                    "steps": e2e_steps},
+            "gpu_launches": int(round(launches_per_step * args.steps)),
+            "clocks": clk.summary(),
+            "rel_l2_vs_oracle": rel,
+        }
+        result.update(extras)
+        print(json.dumps(result), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+# Measured DRAM bytes per grid point and pass of k_hmom (profiles/); None if
+# not yet measured.
+HMOM_DRAM_BYTES_PER_POINT = None
+
+
+def plain_forward(torch, dev, dtype):
+    """Plain unbatched forward of one 3D field, 768x768x64, 5 generations,
+    reach 12, vertical reach 4 (filtering_procedure(1))."""
+    from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig
+    cfg = MGBFConfig(nxPE=16, nyPE=16, im_filt=48, jm_filt=48, lm=64, km3=1, km2=0, n_ens=1, gm_max=5,
+                     hx=12, hy=12, hz=4, p=2, mg_ampl02=ampl02(12), mg_ampl01=ampl01(4),
+                     mg_weig1=1.0, mg_weig2=0.5, mg_weig3=0.25, mg_weig4=0.125, mg_weig5=0.0625, layout=1)
+    op = MGBF(cfg)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(7)
+    x = torch.randn(op.field_shape(), generator=gen, device=dev, dtype=dtype)
+    for _ in range(2):
+        op.filtering_procedure(1, x)
+    torch.cuda.synchronize()
+    n = 5
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(n):
+        op.filtering_procedure(1, x)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / n
+    pts = float(np.prod(op.field_shape()))
+    op.close()
+    return {"workload": "plain forward, one 3D field 768x768x64, 5 generations, h=12, hz=4",
+            "dtype": str(dtype).replace("torch.", ""), "ms": ms, "value": pts / (ms * 1e-3), "unit": UNIT}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--members", type=int, default=80)
+    ap.add_argument("--no-extras", action="store_true", help="skip the plain-forward and CPU-baseline legs")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -157,6 +157,28 @@ int mgbf_set_weights(mgbf_handle* h, const double* a, int n);
 /* Release the handle (replaces mg_finalize / deallocate_mg_intstate). */
 int mgbf_destroy(mgbf_handle* h);
 
+/* ------------------------------------------------------------------------
+ * Stage timers: the counterpart of the reference's mg_timers (btim/etim
+ * around every stage, mg_timers.f90:70-104; per-rank report,
+ * mg_timers.f90:106-199).  When enabled, every kernel launch of the
+ * library is bracketed by CUDA events on its stream and accumulated per
+ * stage under the reference's timer names: vfiltT, upsend, hfiltT (first
+ * radial pass, with the weighting), hfilt (second radial pass), dnsend,
+ * vfilt, plus copy, halo and wgrad.  Process-wide; not for concurrent use
+ * from several host threads.
+ */
+typedef struct mgbf_timer_stat {
+    char name[16];
+    long long count;       /* launches                                      */
+    double total_ms;       /* summed CUDA-event durations                    */
+    double points;         /* grid points processed (sum over launches)      */
+} mgbf_timer_stat;
+
+/* on != 0 enables and resets the timers; 0 disables them. */
+int mgbf_timers_enable(int on);
+/* Synchronises outstanding timer events and copies up to max stats. */
+int mgbf_timers_read(mgbf_timer_stat* out, int max, int* n);
+
 /* Static description of a status code. */
 const char* mgbf_strerror(int code);
 

@@ -68,6 +68,10 @@ class MgbfGroupDesc(ctypes.Structure):
     ]
 
 
+class MgbfTimerStat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 16), ("count", ctypes.c_longlong), ("total_ms", _D), ("points", _D)]
+
+
 # Every symbol include/mgbf.h declares, with its ctypes signature.
 _VP = ctypes.c_void_p
 _HP = ctypes.c_void_p
@@ -88,7 +92,21 @@ SIGNATURES = {
                                ctypes.POINTER(_HP)]),
     "mgbf_batch_apply": (_I, [_HP, ctypes.POINTER(_VP), _I, _I, _VP]),
     "mgbf_batch_destroy": (_I, [_HP]),
+    "mgbf_timers_enable": (_I, [_I]),
+    "mgbf_timers_read": (_I, [ctypes.POINTER(MgbfTimerStat), _I, ctypes.POINTER(_I)]),
 }
+
+
+def timers_enable(on: bool = True) -> None:
+    check(load().mgbf_timers_enable(int(on)), "mgbf_timers_enable")
+
+
+def timers_read() -> dict:
+    """{stage: (launches, total_ms, points)} accumulated since timers_enable()."""
+    arr = (MgbfTimerStat * 16)()
+    n = _I()
+    check(load().mgbf_timers_read(arr, 16, ctypes.byref(n)), "mgbf_timers_read")
+    return {arr[i].name.decode(): (arr[i].count, arr[i].total_ms, arr[i].points) for i in range(n.value)}
 
 _lib = None
 

@@ -116,6 +116,69 @@ int upload_acc(DevBuf& b, const std::vector<double>& v, DType t) {
     return upload(b, f);
 }
 
+// ------------------------------------------------------------ stage timers
+
+enum Stage { ST_VFILTT, ST_UPSEND, ST_HFILTT, ST_HFILT, ST_DNSEND, ST_VFILT, ST_COPY, ST_HALO, ST_WGRAD, ST_N };
+const char* kStageNames[ST_N] = {"vfiltT", "upsend", "hfiltT", "hfilt", "dnsend", "vfilt", "copy", "halo", "wgrad"};
+
+struct TimerEvent {
+    cudaEvent_t a, b;
+    int stage;
+    double points;
+};
+
+struct Timers {
+    bool on = false;
+    std::vector<TimerEvent> pending;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;
+    long long count[ST_N] = {0};
+    double ms[ST_N] = {0}, pts[ST_N] = {0};
+    void reset() {
+        flush();
+        for (int s = 0; s < ST_N; ++s) count[s] = 0, ms[s] = 0, pts[s] = 0;
+    }
+    void flush() {
+        for (auto& e : pending) {
+            float t = 0.f;
+            if (cudaEventSynchronize(e.b) == cudaSuccess && cudaEventElapsedTime(&t, e.a, e.b) == cudaSuccess) {
+                ms[e.stage] += t;
+                count[e.stage] += 1;
+                pts[e.stage] += e.points;
+            }
+            pool.emplace_back(e.a, e.b);
+        }
+        pending.clear();
+        cudaGetLastError();
+    }
+};
+Timers g_timers;
+
+// Brackets one launch with events when the timers are on.
+struct StageTimer {
+    TimerEvent ev{};
+    bool active = false;
+    void* stream;
+    StageTimer(int stage, void* s, double points) : stream(s) {
+        if (!g_timers.on) return;
+        if (!g_timers.pool.empty()) {
+            ev.a = g_timers.pool.back().first;
+            ev.b = g_timers.pool.back().second;
+            g_timers.pool.pop_back();
+        } else if (cudaEventCreate(&ev.a) != cudaSuccess || cudaEventCreate(&ev.b) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        ev.stage = stage;
+        ev.points = points;
+        active = cudaEventRecord(ev.a, static_cast<cudaStream_t>(stream)) == cudaSuccess;
+    }
+    ~StageTimer() {
+        if (!active) return;
+        cudaEventRecord(ev.b, static_cast<cudaStream_t>(stream));
+        g_timers.pending.push_back(ev);
+    }
+};
+
 // ---------------------------------------------------------------- the plan
 
 // Tables converted to one accumulation type (float or double).
@@ -227,11 +290,15 @@ struct Exec {
     View B(int g) { return gen_view(P, G, G.bufs[(int)t].B[g]->p, t, g); }
     View C(int g) { return gen_view(P, G, G.bufs[(int)t].C[g]->p, t, g); }
 
+    double pts(int g) const { return (double)G.nk * gen_I(P, g) * gen_J(P, g); }
+
     int zstage(View in, View out, bool adjoint, int nzcol, int mirror) {
         if (nzcol <= 0 || G.zs.fwd.empty()) {
+            StageTimer tm(ST_COPY, stream, pts(0));
             LK(launch_copy(t, in, out, G.nk, P.I, P.J, mirror, stream));
             return 0;
         }
+        StageTimer tm(adjoint ? ST_VFILTT : ST_VFILT, stream, pts(0));
         ZArgs a;
         a.in = in; a.out = out; a.nk = G.nk; a.I = P.I; a.J = P.J;
         a.lm = G.lm; a.nzk = nzcol * G.lm; a.mz = G.zs.mz;
@@ -245,6 +312,7 @@ struct Exec {
         a.fine = fine; a.coarse = coarse; a.nk = G.nk; a.If = gen_I(P, g); a.Jf = gen_J(P, g);
         a.wx = G.tab[ai()].rwx[g]->p; a.wy = G.tab[ai()].rwy[g]->p;
         a.mirror_hx = G.hs.R;
+        StageTimer tm(ST_UPSEND, stream, pts(g));
         LK(launch_restrict(t, a, stream));
         return 0;
     }
@@ -255,11 +323,13 @@ struct Exec {
         a.ix = static_cast<const int*>(P.pix[g].p); a.iy = static_cast<const int*>(P.piy[g].p);
         a.wxp = G.tab[ai()].pwx[g]->p; a.wyp = G.tab[ai()].pwy[g]->p;
         a.has_base = 1;
+        StageTimer tm(ST_DNSEND, stream, pts(g));
         LK(launch_prolong(t, a, stream));
         return 0;
     }
-    int hpass(int g, View in, View out, double scale, int mirror) {
+    int hpass(int g, View in, View out, double scale, int mirror, int stage) {
         const int I = gen_I(P, g), J = gen_J(P, g);
+        StageTimer tm(stage, stream, pts(g));
         if (G.hs.canonical && hmom_available(t, G.hs.R, G.hs.p)) {
             HMomArgs a;
             a.in = in; a.out = out; a.nk = G.nk; a.I = I; a.J = J;
@@ -292,7 +362,7 @@ struct Exec {
             if ((rc = restrict_(g, A(g), A(g + 1)))) return rc;
         for (int g = 0; g < P.gm; ++g) {
             if (g == 0 && !filt1) continue;
-            if ((rc = hpass(g, A(g), dst(g), scales ? scales[g] : 1.0, mirror_out ? G.hs.R : 0))) return rc;
+            if ((rc = hpass(g, A(g), dst(g), scales ? scales[g] : 1.0, mirror_out ? G.hs.R : 0, ST_HFILTT))) return rc;
         }
         return 0;
     }
@@ -304,7 +374,7 @@ struct Exec {
         int rc;
         for (int g = 0; g < P.gm; ++g) {
             if (g == 0 && !filt1) continue;
-            if ((rc = hpass(g, src(g), A(g), scales ? scales[g] : 1.0, 0))) return rc;
+            if ((rc = hpass(g, src(g), A(g), scales ? scales[g] : 1.0, 0, ST_HFILT))) return rc;
         }
         const bool z = nzcol > 0 && !G.zs.fwd.empty();
         for (int g = P.gm - 1; g >= 1; --g) {
@@ -767,8 +837,10 @@ static int run_proc(mgbf_handle* h, int mg_filt, const void* xin, void* yout, DT
     View x = field_view(h, const_cast<void*>(xin), t);
     View y = field_view(h, yout, t);
     if ((rc = ex.forward(x, y, nzcol, filt1))) return rc;
-    if (h->cfg.layout == MGBF_LAYOUT_HALO && filt1)
+    if (h->cfg.layout == MGBF_LAYOUT_HALO && filt1) {
+        StageTimer tm(ST_HALO, stream, 0.0);
         LK(launch_zero_halo(t, y, G.nk, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
+    }
     return 0;
 }
 
@@ -851,17 +923,43 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
         DotArgs da;
         da.a = ex.B(g); da.b = ex.C(g); da.nk = G.nk; da.I = gen_I(P, g); da.J = gen_J(P, g);
         da.out = dots + g;
+        StageTimer tm(ST_WGRAD, stream, ex.pts(g));
         LK(launch_dot(t, da, stream));
     }
     // gx = L gy = Bz sum_g P_g B_g (a_g v_g)
     if ((rc = ex.second_half(Bf, vo, nzcol, filt1, P.a))) return rc;
-    if (h->cfg.layout == MGBF_LAYOUT_HALO && filt1)
+    if (h->cfg.layout == MGBF_LAYOUT_HALO && filt1) {
+        StageTimer tm(ST_HALO, stream, 0.0);
         LK(launch_zero_halo(t, vo, G.nk, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
+    }
     CU(cudaMemcpyAsync(ga, P.dot.p, sizeof(double) * P.gm, cudaMemcpyDeviceToHost, s));
     if (mem == MGBF_MEM_HOST)
         CU(cudaMemcpyAsync(gx, h->stage2[(int)t].p, bytes, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
     return 0;
+}
+
+int mgbf_timers_enable(int on) {
+    g_timers.reset();
+    g_timers.on = on != 0;
+    return MGBF_OK;
+}
+
+int mgbf_timers_read(mgbf_timer_stat* out, int max, int* n) {
+    if (!out || max < 0) return fail(MGBF_ERR_ARG, "null argument");
+    g_timers.flush();
+    int k = 0;
+    for (int st = 0; st < ST_N && k < max; ++st) {
+        if (!g_timers.count[st]) continue;
+        std::memset(&out[k], 0, sizeof(out[k]));
+        std::snprintf(out[k].name, sizeof(out[k].name), "%s", kStageNames[st]);
+        out[k].count = g_timers.count[st];
+        out[k].total_ms = g_timers.ms[st];
+        out[k].points = g_timers.pts[st];
+        ++k;
+    }
+    if (n) *n = k;
+    return MGBF_OK;
 }
 
 int mgbf_destroy(mgbf_handle* h) {
