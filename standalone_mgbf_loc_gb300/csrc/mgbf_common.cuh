@@ -23,6 +23,61 @@ __device__ __forceinline__ void stv(float* p, float v) { *p = v; }
 __device__ __forceinline__ void stv(double* p, double v) { *p = v; }
 __device__ __forceinline__ void stv(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
 
+// Four consecutive level values (k, k+1, k+2, k+3; k % 4 == 0) as one
+// vector access: float4, two double2, or four bf16 in 8 bytes.
+template <typename T> struct V4;
+template <> struct V4<float> {
+    static __device__ __forceinline__ void ld(const float* p, float (&v)[4]) {
+        const float4 x = __ldg(reinterpret_cast<const float4*>(p));
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    }
+    static __device__ __forceinline__ void ldc(const float* p, float (&v)[4]) {
+        const float4 x = *reinterpret_cast<const float4*>(p);
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    }
+    static __device__ __forceinline__ void st(float* p, const float (&v)[4]) {
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+};
+template <> struct V4<double> {
+    static __device__ __forceinline__ void ld(const double* p, double (&v)[4]) {
+        const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+        const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    }
+    static __device__ __forceinline__ void ldc(const double* p, double (&v)[4]) {
+        const double2 a = *reinterpret_cast<const double2*>(p);
+        const double2 b = *(reinterpret_cast<const double2*>(p) + 1);
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    }
+    static __device__ __forceinline__ void st(double* p, const double (&v)[4]) {
+        reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+    }
+};
+template <> struct V4<__nv_bfloat16> {
+    static __device__ __forceinline__ void unpack(uint2 u, float (&v)[4]) {
+        v[0] = __uint_as_float(u.x << 16);
+        v[1] = __uint_as_float(u.x & 0xffff0000u);
+        v[2] = __uint_as_float(u.y << 16);
+        v[3] = __uint_as_float(u.y & 0xffff0000u);
+    }
+    static __device__ __forceinline__ void ld(const __nv_bfloat16* p, float (&v)[4]) {
+        unpack(__ldg(reinterpret_cast<const uint2*>(p)), v);
+    }
+    static __device__ __forceinline__ void ldc(const __nv_bfloat16* p, float (&v)[4]) {
+        unpack(*reinterpret_cast<const uint2*>(p), v);
+    }
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, const float (&v)[4]) {
+        const __nv_bfloat162 a = __floats2bfloat162_rn(v[0], v[1]);
+        const __nv_bfloat162 b = __floats2bfloat162_rn(v[2], v[3]);
+        uint2 u;
+        u.x = *reinterpret_cast<const unsigned*>(&a);
+        u.y = *reinterpret_cast<const unsigned*>(&b);
+        *reinterpret_cast<uint2*>(p) = u;
+    }
+};
+
 // Half-sample mirror of a 0-based index into [0, n): -1 -> 0, n -> n-1
 // (the reference's physical-boundary halo fill, mg_bocos.f90:225-377),
 // clamped so that rows only used for discarded outputs stay in range.

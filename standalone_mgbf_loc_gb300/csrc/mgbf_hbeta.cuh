@@ -41,7 +41,8 @@ __host__ __device__ constexpr int mcanon(int gy) {
 
 template <int R, int P, int TX, int U, typename T>
 __global__ void __launch_bounds__(128) k_hmom(HMomArgs a,
-                                                  const __grid_constant__ HMomCoefs<typename AccOf<T>::type> c) {
+                                              const __grid_constant__ HMomCoefs<typename AccOf<T>::type> c) {
+    static_assert(U == 2, "the row pipeline alternates two register buffers");
     using A = typename AccOf<T>::type;
     constexpr int NS = TX + 2 * R;  // input columns per row
     constexpr int NR = 2 * R + U;   // ring of output rows
@@ -55,49 +56,56 @@ __global__ void __launch_bounds__(128) k_hmom(HMomArgs a,
     const int je = min(jb + a.rows, a.J);
     const T* inb = static_cast<const T*>(a.in.p) + k + a.in.si * (long long)(i0 - R);
     T* outb = static_cast<T*>(a.out.p) + k;
-
     const A scale = static_cast<A>(a.scale);
+
     A acc[NR][TX];
 #pragma unroll
     for (int r = 0; r < NR; ++r)
 #pragma unroll
         for (int q = 0; q < TX; ++q) acc[r][q] = A(0);
 
-    for (int jin0 = jb - R; jin0 < je + R; jin0 += U) {
+    auto load_row = [&](int jin, A (&seg)[NS]) {
+        const T* rp = inb + a.in.sj * (long long)reflect_half(jin, a.J);
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int jr = reflect_half(jin0 + u, a.J);
-            const T* rp = inb + a.in.sj * (long long)jr;
-            A seg[NS];
+        for (int s = 0; s < NS; ++s) seg[s] = ldv(rp + a.in.si * (long long)s);
+    };
+    // moments of one input row, emitted into the ring rows u-gy+R and u+gy+R
+    auto row = [&](const A (&seg)[NS], const int u) {
 #pragma unroll
-            for (int s = 0; s < NS; ++s) seg[s] = ldv(rp + a.in.si * (long long)s);
+        for (int q = 0; q < TX; ++q) {
+            A t[PQ];
+            t[0] = seg[R + q];
 #pragma unroll
-            for (int q = 0; q < TX; ++q) {
-                A t[PQ];
-                t[0] = seg[R + q];
+            for (int e = 1; e < PQ; ++e) t[e] = A(0);
 #pragma unroll
-                for (int e = 1; e < PQ; ++e) t[e] = A(0);
+            for (int m = 0; m <= R; ++m) {
+                if (m > 0) {
+                    const A pr = seg[R + q + m] + seg[R + q - m];
+                    t[0] += pr;
 #pragma unroll
-                for (int m = 0; m <= R; ++m) {
-                    if (m > 0) {
-                        const A pr = seg[R + q + m] + seg[R + q - m];
-                        t[0] += pr;
+                    for (int e = 1; e < PQ; ++e) t[e] = fma(c.upow[m * PQ + e], pr, t[e]);
+                }
 #pragma unroll
-                        for (int e = 1; e < PQ; ++e) t[e] = fma(c.upow[m * PQ + e], pr, t[e]);
-                    }
+                for (int gy = 0; gy <= R; ++gy) {
+                    if (mcanon<R>(gy) == m) {
+                        A v = c.coef[gy * PQ] * t[0];
 #pragma unroll
-                    for (int gy = 0; gy <= R; ++gy) {
-                        if (mcanon<R>(gy) == m) {
-                            A v = c.coef[gy * PQ] * t[0];
-#pragma unroll
-                            for (int e = 1; e < PQ; ++e) v = fma(c.coef[gy * PQ + e], t[e], v);
-                            acc[R + u - gy][q] += v;
-                            if (gy) acc[R + u + gy][q] += v;
-                        }
+                        for (int e = 1; e < PQ; ++e) v = fma(c.coef[gy * PQ + e], t[e], v);
+                        acc[R + u - gy][q] += v;
+                        if (gy) acc[R + u + gy][q] += v;
                     }
                 }
             }
         }
+    };
+
+    A segA[NS], segB[NS];
+    load_row(jb - R, segA);
+    for (int jin0 = jb - R; jin0 < je + R; jin0 += U) {
+        load_row(jin0 + 1, segB);  // in flight while row jin0 is processed
+        row(segA, 0);
+        load_row(jin0 + 2, segA);
+        row(segB, 1);
         // rows jin0-R .. jin0-R+U-1 have received every contribution
 #pragma unroll
         for (int u = 0; u < U; ++u) {

@@ -11,6 +11,9 @@
 #include "mgbf_common.cuh"
 #include "mgbf_kernels.cuh"
 
+#include <algorithm>
+#include <cstdint>
+
 namespace mgbf {
 
 // ------------------------------------------------------------- z filter
@@ -18,37 +21,111 @@ namespace mgbf {
 // band is the FP64-built matrix of sup_vrbeta1_* / sup_vrbeta1T_*
 // (mg_filtering.f90:2042-2262) including the whole-sample mirror and, for
 // the adjoint, the edge fold; entries k >= nzk (2D variables) are copied.
-template <typename T>
-__global__ void __launch_bounds__(256) k_zfilter(ZArgs a) {
+// One lane per level k (coalesced), ZI consecutive columns i per thread; the
+// band row of the lane's level sits in registers (MZ = compile-time half
+// width; taps outside the column get weight 0 and a clamped address).
+template <typename T, int MZ, int ZI>
+__global__ void __launch_bounds__(128) k_zfilter(ZArgs a) {
     using A = typename AccOf<T>::type;
-    extern __shared__ unsigned char smem_raw[];
-    A* band = reinterpret_cast<A*>(smem_raw);
-    const int bw = 2 * a.mz + 1;
-    const int nb = a.lm * bw;
-    for (int t = threadIdx.x; t < nb; t += blockDim.x) band[t] = static_cast<const A*>(a.band)[t];
-    __syncthreads();
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)a.nk * a.I) return;
-    const int i = (int)(t / a.nk);
-    const int k = (int)(t - (long long)i * a.nk);
-    const int j = blockIdx.y;
-    const T* in = static_cast<const T*>(a.in.p) + a.in.sj * j + a.in.si * i;
-    A v;
-    if (k < a.nzk) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.nk) return;
+    const int i0 = blockIdx.y * ZI;
+    const int j = blockIdx.z;
+    const T* in = static_cast<const T*>(a.in.p) + a.in.sj * j;
+    T* out = static_cast<T*>(a.out.p) + a.out.sj * j + k;
+    const bool zc = k < a.nzk;
+    A w[2 * MZ + 1];
+    int off[2 * MZ + 1];
+    if (zc) {
         const int L = k % a.lm;
         const int c0 = k - L;
-        const A* b = band + L * bw + a.mz;
-        const int dlo = max(-a.mz, -L), dhi = min(a.mz, a.lm - 1 - L);
-        v = A(0);
-        for (int d = dlo; d <= dhi; ++d) v = fma(b[d], ldv(in + c0 + L + d), v);
-    } else {
-        v = ldv(in + k);
+        const A* b = static_cast<const A*>(a.band) + (size_t)L * (2 * a.mz + 1) + a.mz;
+#pragma unroll
+        for (int d = -MZ; d <= MZ; ++d) {
+            const bool ok = d >= -a.mz && d <= a.mz && L + d >= 0 && L + d < a.lm;
+            w[d + MZ] = ok ? b[d] : A(0);
+            off[d + MZ] = ok ? c0 + L + d : k;
+        }
     }
+#pragma unroll
+    for (int q = 0; q < ZI; ++q) {
+        const int i = i0 + q;
+        if (i >= a.I) break;
+        const T* row = in + a.in.si * i;
+        A v;
+        if (zc) {
+            v = A(0);
+#pragma unroll
+            for (int d = 0; d < 2 * MZ + 1; ++d) v = fma(w[d], ldv(row + off[d]), v);
+        } else {
+            v = ldv(row + k);
+        }
+        stv(out + a.out.si * i, v);
+        if (a.mirror_hx) {
+            if (i < a.mirror_hx) stv(out + a.out.si * (-1 - i), v);
+            if (i >= a.I - a.mirror_hx) stv(out + a.out.si * (2 * a.I - 1 - i), v);
+        }
+    }
+}
+
+// Vectorised z filter: each thread owns levels k..k+3 (k % 4 == 0) and ZI
+// columns; the band rows of its four levels sit in registers (levels past
+// nzk get the identity row, so 2D variables are copied by the same code);
+// the window k-4NB .. k+4NB+3 comes in 2NB+1 vector loads.  Needs
+// nk % 4 == 0 and 16-byte aligned views.
+template <typename T, int MZ, int ZI>
+__global__ void __launch_bounds__(128) k_zfilter4(ZArgs a) {
+    using A = typename AccOf<T>::type;
+    constexpr int NB = (MZ + 3) / 4;
+    constexpr int NWIN = 4 * (2 * NB + 1);
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (k >= a.nk) return;
+    const int i0 = blockIdx.y * ZI;
+    const int j = blockIdx.z;
+    A w[4][2 * MZ + 1];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int kq = k + q;
+        const bool zc = kq < a.nzk;
+        const int L = zc ? kq % a.lm : 0;
+        const A* b = static_cast<const A*>(a.band) + (size_t)L * (2 * a.mz + 1) + a.mz;
+#pragma unroll
+        for (int d = -MZ; d <= MZ; ++d) {
+            const bool ok = zc && d >= -a.mz && d <= a.mz && L + d >= 0 && L + d < a.lm;
+            w[q][d + MZ] = ok ? b[d] : ((!zc && d == 0) ? A(1) : A(0));
+        }
+    }
+    int voff[2 * NB + 1];
+#pragma unroll
+    for (int v = 0; v < 2 * NB + 1; ++v) voff[v] = min(max(k + 4 * (v - NB), 0), a.nk - 4);
+    const T* in = static_cast<const T*>(a.in.p) + a.in.sj * j;
     T* out = static_cast<T*>(a.out.p) + a.out.sj * j + k;
-    stv(out + a.out.si * i, v);
-    if (a.mirror_hx) {
-        if (i < a.mirror_hx) stv(out + a.out.si * (-1 - i), v);
-        if (i >= a.I - a.mirror_hx) stv(out + a.out.si * (2 * a.I - 1 - i), v);
+#pragma unroll
+    for (int c = 0; c < ZI; ++c) {
+        const int i = i0 + c;
+        if (i >= a.I) break;
+        const T* row = in + a.in.si * i;
+        A x[NWIN];
+#pragma unroll
+        for (int v = 0; v < 2 * NB + 1; ++v) {
+            A t[4];
+            V4<T>::ld(row + voff[v], t);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) x[4 * v + e] = t[e];
+        }
+        A y[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            A acc = A(0);
+#pragma unroll
+            for (int d = -MZ; d <= MZ; ++d) acc = fma(w[q][d + MZ], x[4 * NB + q + d], acc);
+            y[q] = acc;
+        }
+        V4<T>::st(out + a.out.si * i, y);
+        if (a.mirror_hx) {
+            if (i < a.mirror_hx) V4<T>::st(out + a.out.si * (-1 - i), y);
+            if (i >= a.I - a.mirror_hx) V4<T>::st(out + a.out.si * (2 * a.I - 1 - i), y);
+        }
     }
 }
 
@@ -56,73 +133,322 @@ __global__ void __launch_bounds__(256) k_zfilter(ZArgs a) {
 // coarse(c,d) = sum_b wy[d][b] sum_a wx[c][a] fine(2c-3+a, 2d-3+b): the
 // separable transpose of (P o fill2) (adjoint + bocoT_2d(...,2,2),
 // mg_generations.f90:1117-1187, mg_bocos.f90:929-1061) with the mirror
-// images already merged into the 8-wide weight rows.
+// images already merged into the 8-wide weight rows.  Each thread makes a
+// RC x RC block of coarse points from its (2RC+6)^2 fine footprint, loaded
+// once: every fine row is first reduced along x, then added into the coarse
+// rows it feeds.
+constexpr int RC = 4;
 template <typename T>
-__global__ void __launch_bounds__(256) k_restrict(RestrictArgs a) {
+__global__ void __launch_bounds__(128) k_restrict(RestrictArgs a) {
     using A = typename AccOf<T>::type;
-    const int Ic = a.If / 2;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)a.nk * Ic) return;
-    const int c = (int)(t / a.nk);
-    const int k = (int)(t - (long long)c * a.nk);
-    const int d = blockIdx.y;
-    const A* wx = static_cast<const A*>(a.wx) + c * 8;
-    const A* wy = static_cast<const A*>(a.wy) + d * 8;
-    const T* fine = static_cast<const T*>(a.fine.p) + k;
-    A acc = A(0);
+    constexpr int NF = 2 * RC + 6;
+    const int Ic = a.If / 2, Jc = a.Jf / 2;
+    int k = blockIdx.x * 32 + threadIdx.x;
+    const bool kv = k < a.nk;
+    if (!kv) k = a.nk - 1;
+    const int c0 = (blockIdx.y * blockDim.y + threadIdx.y) * RC;
+    if (c0 >= Ic) return;
+    const int d0 = blockIdx.z * RC;
+    A wx[RC][8], wy[RC][8];
 #pragma unroll
-    for (int b = 0; b < 8; ++b) {
-        const int fj = 2 * d - 3 + b;
-        if (fj < 0 || fj >= a.Jf) continue;
-        const T* row = fine + a.fine.sj * fj;
-        A r = A(0);
+    for (int c = 0; c < RC; ++c) {
+        const int cc = min(c0 + c, Ic - 1);
+        const int dd = min(d0 + c, Jc - 1);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            const int fi = 2 * c - 3 + q;
-            if (fi < 0 || fi >= a.If) continue;
-            r = fma(wx[q], ldv(row + a.fine.si * fi), r);
+            wx[c][q] = static_cast<const A*>(a.wx)[cc * 8 + q];
+            wy[c][q] = static_cast<const A*>(a.wy)[dd * 8 + q];
         }
-        acc = fma(wy[b], r, acc);
     }
-    T* out = static_cast<T*>(a.coarse.p) + a.coarse.sj * d + k;
-    stv(out + a.coarse.si * c, acc);
-    if (a.mirror_hx) {
-        if (c < a.mirror_hx) stv(out + a.coarse.si * (-1 - c), acc);
-        if (c >= Ic - a.mirror_hx) stv(out + a.coarse.si * (2 * Ic - 1 - c), acc);
+    int fcol[NF];
+#pragma unroll
+    for (int s = 0; s < NF; ++s) fcol[s] = min(max(2 * c0 - 3 + s, 0), a.If - 1);
+    const T* fine = static_cast<const T*>(a.fine.p) + k;
+    A acc[RC][RC];
+#pragma unroll
+    for (int r = 0; r < RC; ++r)
+#pragma unroll
+        for (int c = 0; c < RC; ++c) acc[r][c] = A(0);
+#pragma unroll
+    for (int rr = 0; rr < NF; ++rr) {
+        const int fj = min(max(2 * d0 - 3 + rr, 0), a.Jf - 1);
+        const T* row = fine + a.fine.sj * fj;
+        A seg[NF];
+#pragma unroll
+        for (int s = 0; s < NF; ++s) seg[s] = ldv(row + a.fine.si * fcol[s]);
+        A xr[RC];
+#pragma unroll
+        for (int c = 0; c < RC; ++c) {
+            A v = A(0);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v = fma(wx[c][q], seg[2 * c + q], v);
+            xr[c] = v;
+        }
+#pragma unroll
+        for (int r = 0; r < RC; ++r) {
+            const int b = rr - 2 * r;  // fine row 2(d0+r)-3+b
+            if (b >= 0 && b < 8) {
+#pragma unroll
+                for (int c = 0; c < RC; ++c) acc[r][c] = fma(wy[r][b], xr[c], acc[r][c]);
+            }
+        }
+    }
+    if (!kv) return;
+#pragma unroll
+    for (int r = 0; r < RC; ++r) {
+        const int d = d0 + r;
+        if (d >= Jc) break;
+        T* out = static_cast<T*>(a.coarse.p) + a.coarse.sj * d + k;
+#pragma unroll
+        for (int c = 0; c < RC; ++c) {
+            const int cc = c0 + c;
+            if (cc >= Ic) break;
+            const A v = acc[r][c];
+            stv(out + a.coarse.si * cc, v);
+            if (cc < a.mirror_hx) stv(out + a.coarse.si * (-1 - cc), v);
+            if (cc >= Ic - a.mirror_hx) stv(out + a.coarse.si * (2 * Ic - 1 - cc), v);
+        }
+    }
+}
+
+// Vectorised restriction: levels k..k+3 per thread, RV x RV coarse block.
+constexpr int RV = 2;
+template <typename T>
+__global__ void __launch_bounds__(128) k_restrict4(RestrictArgs a) {
+    using A = typename AccOf<T>::type;
+    constexpr int NF = 2 * RV + 6;
+    const int Ic = a.If / 2, Jc = a.Jf / 2;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (k >= a.nk) return;
+    const int c0 = blockIdx.y * RV;
+    const int d0 = blockIdx.z * RV;
+    A wx[RV][8], wy[RV][8];
+#pragma unroll
+    for (int c = 0; c < RV; ++c) {
+        const int cc = min(c0 + c, Ic - 1), dd = min(d0 + c, Jc - 1);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            wx[c][q] = static_cast<const A*>(a.wx)[cc * 8 + q];
+            wy[c][q] = static_cast<const A*>(a.wy)[dd * 8 + q];
+        }
+    }
+    int fcol[NF];
+#pragma unroll
+    for (int s = 0; s < NF; ++s) fcol[s] = min(max(2 * c0 - 3 + s, 0), a.If - 1);
+    const T* fine = static_cast<const T*>(a.fine.p) + k;
+    A acc[RV][RV][4];
+#pragma unroll
+    for (int r = 0; r < RV; ++r)
+#pragma unroll
+        for (int c = 0; c < RV; ++c)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[r][c][e] = A(0);
+#pragma unroll
+    for (int rr = 0; rr < NF; ++rr) {
+        const int fj = min(max(2 * d0 - 3 + rr, 0), a.Jf - 1);
+        const T* row = fine + a.fine.sj * fj;
+        A seg[NF][4];
+#pragma unroll
+        for (int s = 0; s < NF; ++s) V4<T>::ld(row + a.fine.si * fcol[s], seg[s]);
+#pragma unroll
+        for (int c = 0; c < RV; ++c) {
+            A xr[4] = {A(0), A(0), A(0), A(0)};
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) xr[e] = fma(wx[c][q], seg[2 * c + q][e], xr[e]);
+#pragma unroll
+            for (int r = 0; r < RV; ++r) {
+                const int b = rr - 2 * r;
+                if (b >= 0 && b < 8) {
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) acc[r][c][e] = fma(wy[r][b], xr[e], acc[r][c][e]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < RV; ++r) {
+        const int d = d0 + r;
+        if (d >= Jc) break;
+        T* out = static_cast<T*>(a.coarse.p) + a.coarse.sj * d + k;
+#pragma unroll
+        for (int c = 0; c < RV; ++c) {
+            const int cc = c0 + c;
+            if (cc >= Ic) break;
+            V4<T>::st(out + a.coarse.si * cc, acc[r][c]);
+            if (cc < a.mirror_hx) V4<T>::st(out + a.coarse.si * (-1 - cc), acc[r][c]);
+            if (cc >= Ic - a.mirror_hx) V4<T>::st(out + a.coarse.si * (2 * Ic - 1 - cc), acc[r][c]);
+        }
     }
 }
 
 // -------------------------------------------------------- prolongation
-// out(i,j) = base(i,j) + sum_b wy[j][b] sum_a wx[i][a] coarse(ix[i][a], iy[j][b]):
-// downsend + boco_2d(...,2,2) + direct1 + add (mg_generations.f90:210-267,
-// 1190-1250); x pass inside, y pass outside, as direct1 orders them.
-template <typename T>
-__global__ void __launch_bounds__(256) k_prolong(ProlongArgs a) {
+// out(i,j) = base(i,j) + (P o fill2) coarse: downsend + boco_2d(...,2,2) +
+// direct1 + add (mg_generations.f90:210-267, 1190-1250), or the quadratic
+// direct2 with fill1 (1319-1374).  Fine points come in pairs that read the
+// same NT coarse cells: with the 4-point offset stencil fine columns
+// (2m-1, 2m) (0-based) use coarse m-2..m+1 with weights p and q
+// (def_offset_coef, mg_interpolate.f90:76-79); with the quadratic stencil
+// (2m, 2m+1) use m-1..m+1 with a and b.  Coarse indices are mirrored
+// (half-sample) at the edges; the weights stay those of the fine parity, as
+// in direct1 after boco_2d.  Each thread makes PX column pairs x one row
+// pair; x pass inside, y pass outside, as direct1 orders them.
+template <int NT> struct PCoef;
+template <> struct PCoef<4> {
+    static __device__ __forceinline__ double c0(int t) {  // p_coef
+        return t == 0 ? -9.0 / 128.0 : t == 1 ? 111.0 / 128.0 : t == 2 ? 29.0 / 128.0 : -3.0 / 128.0;
+    }
+    static __device__ __forceinline__ double c1(int t) {  // q_coef
+        return t == 0 ? -3.0 / 128.0 : t == 1 ? 29.0 / 128.0 : t == 2 ? 111.0 / 128.0 : -9.0 / 128.0;
+    }
+};
+template <> struct PCoef<3> {
+    static __device__ __forceinline__ double c0(int t) {  // a_coef
+        return t == 0 ? 5.0 / 32.0 : t == 1 ? 30.0 / 32.0 : -3.0 / 32.0;
+    }
+    static __device__ __forceinline__ double c1(int t) {  // b_coef
+        return t == 0 ? -3.0 / 32.0 : t == 1 ? 30.0 / 32.0 : 5.0 / 32.0;
+    }
+};
+
+constexpr int PX = 4;
+template <typename T, int NT>
+__global__ void __launch_bounds__(128) k_prolong(ProlongArgs a) {
     using A = typename AccOf<T>::type;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)a.nk * a.If) return;
-    const int i = (int)(t / a.nk);
-    const int k = (int)(t - (long long)i * a.nk);
-    const int j = blockIdx.y;
-    const int nt = a.ntap;
-    const int* ixp = a.ix + i * nt;
-    const int* iyp = a.iy + j * nt;
-    const A* wxp = static_cast<const A*>(a.wxp) + i * nt;
-    const A* wyp = static_cast<const A*>(a.wyp) + j * nt;
+    constexpr int O = NT == 4 ? 1 : 0;       // fine column of pair m is 2m - O
+    constexpr int S = NT == 4 ? 2 : 1;       // first coarse tap of pair m is m - S
+    constexpr int NC = PX + NT - 1;          // coarse columns per thread
+    const int Ic = a.If / 2, Jc = a.Jf / 2;
+    const int npx = Ic + O, npy = Jc + O;    // pairs per direction
+    int k = blockIdx.x * 32 + threadIdx.x;
+    const bool kv = k < a.nk;
+    if (!kv) k = a.nk - 1;
+    const int m0 = (blockIdx.y * blockDim.y + threadIdx.y) * PX;
+    if (m0 >= npx) return;
+    const int n = blockIdx.z;  // row pair
+    int ccol[NC];
+#pragma unroll
+    for (int s = 0; s < NC; ++s) ccol[s] = reflect_half(m0 - S + s, Ic);
     const T* coarse = static_cast<const T*>(a.coarse.p) + k;
-    A acc = A(0);
-    for (int b = 0; b < nt; ++b) {
-        const T* row = coarse + a.coarse.sj * iyp[b];
-        A r = A(0);
-        for (int q = 0; q < nt; ++q) r = fma(wxp[q], ldv(row + a.coarse.si * ixp[q]), r);
-        acc = fma(wyp[b], r, acc);
+    A r0[2 * PX], r1[2 * PX];  // fine rows 2n-O and 2n+1-O
+#pragma unroll
+    for (int q = 0; q < 2 * PX; ++q) r0[q] = r1[q] = A(0);
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        const int cr = reflect_half(n - S + t, Jc);
+        const T* row = coarse + a.coarse.sj * cr;
+        A v[NC];
+#pragma unroll
+        for (int s = 0; s < NC; ++s) v[s] = ldv(row + a.coarse.si * ccol[s]);
+        const A wy0 = (A)PCoef<NT>::c0(t), wy1 = (A)PCoef<NT>::c1(t);
+#pragma unroll
+        for (int q = 0; q < PX; ++q) {
+            A x0 = A(0), x1 = A(0);
+#pragma unroll
+            for (int u = 0; u < NT; ++u) {
+                x0 = fma((A)PCoef<NT>::c0(u), v[q + u], x0);
+                x1 = fma((A)PCoef<NT>::c1(u), v[q + u], x1);
+            }
+            r0[2 * q] = fma(wy0, x0, r0[2 * q]);
+            r0[2 * q + 1] = fma(wy0, x1, r0[2 * q + 1]);
+            r1[2 * q] = fma(wy1, x0, r1[2 * q]);
+            r1[2 * q + 1] = fma(wy1, x1, r1[2 * q + 1]);
+        }
     }
+    if (!kv) return;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int fj = 2 * n - O + h;
+        if (fj < 0 || fj >= a.Jf) continue;
+        const T* base = static_cast<const T*>(a.base.p) + a.base.sj * fj + k;
+        T* out = static_cast<T*>(a.out.p) + a.out.sj * fj + k;
+#pragma unroll
+        for (int q = 0; q < 2 * PX; ++q) {
+            const int fi = 2 * m0 - O + q;
+            if (fi < 0 || fi >= a.If) continue;
+            A v = h ? r1[q] : r0[q];
+            if (a.has_base) v = ldc(base + a.base.si * fi) + v;
+            stv(out + a.out.si * fi, v);
+        }
+    }
+}
+
+// Vectorised prolongation: levels k..k+3 per thread, PV column pairs x one
+// row pair; the base values are fetched first so their latency overlaps
+// the coarse loads.
+constexpr int PV = 2;
+template <typename T, int NT>
+__global__ void __launch_bounds__(128) k_prolong4(ProlongArgs a) {
+    using A = typename AccOf<T>::type;
+    constexpr int O = NT == 4 ? 1 : 0;
+    constexpr int S = NT == 4 ? 2 : 1;
+    constexpr int NC = PV + NT - 1;
+    const int Ic = a.If / 2, Jc = a.Jf / 2;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (k >= a.nk) return;
+    const int m0 = blockIdx.y * PV;
+    const int n = blockIdx.z;
+    A b0[2 * PV][4], b1[2 * PV][4];
     if (a.has_base) {
-        const T* base = static_cast<const T*>(a.base.p) + a.base.sj * j + a.base.si * i + k;
-        acc = ldc(base) + acc;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int fj = min(max(2 * n - O + h, 0), a.Jf - 1);
+            const T* base = static_cast<const T*>(a.base.p) + a.base.sj * fj + k;
+#pragma unroll
+            for (int q = 0; q < 2 * PV; ++q) {
+                const int fi = min(max(2 * m0 - O + q, 0), a.If - 1);
+                if (h) V4<T>::ldc(base + a.base.si * fi, b1[q]);
+                else V4<T>::ldc(base + a.base.si * fi, b0[q]);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 2 * PV; ++q)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) b0[q][e] = b1[q][e] = A(0);
     }
-    T* out = static_cast<T*>(a.out.p) + a.out.sj * j + a.out.si * i + k;
-    stv(out, acc);
+    int ccol[NC];
+#pragma unroll
+    for (int s = 0; s < NC; ++s) ccol[s] = reflect_half(m0 - S + s, Ic);
+    const T* coarse = static_cast<const T*>(a.coarse.p) + k;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        const int cr = reflect_half(n - S + t, Jc);
+        const T* row = coarse + a.coarse.sj * cr;
+        A v[NC][4];
+#pragma unroll
+        for (int s = 0; s < NC; ++s) V4<T>::ld(row + a.coarse.si * ccol[s], v[s]);
+        const A wy0 = (A)PCoef<NT>::c0(t), wy1 = (A)PCoef<NT>::c1(t);
+#pragma unroll
+        for (int q = 0; q < PV; ++q) {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                A x0 = A(0), x1 = A(0);
+#pragma unroll
+                for (int u = 0; u < NT; ++u) {
+                    x0 = fma((A)PCoef<NT>::c0(u), v[q + u][e], x0);
+                    x1 = fma((A)PCoef<NT>::c1(u), v[q + u][e], x1);
+                }
+                b0[2 * q][e] = fma(wy0, x0, b0[2 * q][e]);
+                b0[2 * q + 1][e] = fma(wy0, x1, b0[2 * q + 1][e]);
+                b1[2 * q][e] = fma(wy1, x0, b1[2 * q][e]);
+                b1[2 * q + 1][e] = fma(wy1, x1, b1[2 * q + 1][e]);
+            }
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int fj = 2 * n - O + h;
+        if (fj < 0 || fj >= a.Jf) continue;
+        T* out = static_cast<T*>(a.out.p) + a.out.sj * fj + k;
+#pragma unroll
+        for (int q = 0; q < 2 * PV; ++q) {
+            const int fi = 2 * m0 - O + q;
+            if (fi < 0 || fi >= a.If) continue;
+            V4<T>::st(out + a.out.si * fi, h ? b1[q] : b0[q]);
+        }
+    }
 }
 
 // ------------------------------------------- direct-sum radial beta filter
@@ -266,34 +592,78 @@ static inline int last_err() {
     return e == cudaSuccess ? 0 : (int)e;
 }
 
-int launch_zfilter(DType t, const ZArgs& a, void* stream) {
-    const long long n = (long long)a.nk * a.I;
-    if (n == 0 || a.J == 0) return 0;
-    dim3 block(256), grid((unsigned)((n + 255) / 256), a.J);
-    const size_t sm = acc_size(t) * a.lm * (2 * a.mz + 1);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (sm > 48 * 1024) {
-        MGBF_DISPATCH(t, (cudaFuncSetAttribute(k_zfilter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)));
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+template <typename T, int MZ>
+static void zlaunch(const ZArgs& a, cudaStream_t s) {
+    constexpr int ZI = 4;
+    if constexpr (MZ <= 8) {  // the vector form keeps 4*(2MZ+1) weights in registers
+        const bool vec = a.nk % 4 == 0 && aligned16(a.in.p) && aligned16(a.out.p);
+        if (vec) {
+            const int nt = a.nk / 4;
+            dim3 block(128), grid((nt + 127) / 128, (a.I + ZI - 1) / ZI, a.J);
+            k_zfilter4<T, MZ, ZI><<<grid, block, 0, s>>>(a);
+            return;
+        }
     }
-    MGBF_DISPATCH(t, (k_zfilter<T><<<grid, block, sm, s>>>(a)));
+    dim3 block(128), grid((a.nk + 127) / 128, (a.I + ZI - 1) / ZI, a.J);
+    k_zfilter<T, MZ, ZI><<<grid, block, 0, s>>>(a);
+}
+
+int launch_zfilter(DType t, const ZArgs& a, void* stream) {
+    if (a.nk == 0 || a.I == 0 || a.J == 0) return 0;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int mz = a.mz;
+    if (mz > kMaxZReach) return (int)cudaErrorInvalidValue;
+    MGBF_DISPATCH(t, (mz <= 2 ? zlaunch<T, 2>(a, s)
+                      : mz <= 4 ? zlaunch<T, 4>(a, s)
+                      : mz <= 6 ? zlaunch<T, 6>(a, s)
+                      : mz <= 8 ? zlaunch<T, 8>(a, s)
+                      : zlaunch<T, kMaxZReach>(a, s)));
     return last_err();
 }
 
 int launch_restrict(DType t, const RestrictArgs& a, void* stream) {
-    const long long n = (long long)a.nk * (a.If / 2);
-    if (n == 0) return 0;
-    dim3 block(256), grid((unsigned)((n + 255) / 256), a.Jf / 2);
+    const int Ic = a.If / 2, Jc = a.Jf / 2;
+    if (a.nk == 0 || Ic == 0 || Jc == 0) return 0;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (a.nk % 4 == 0 && aligned16(a.fine.p) && aligned16(a.coarse.p)) {
+        const int nt = a.nk / 4;
+        dim3 block(std::min(128, ((nt + 31) / 32) * 32)), grid((nt + block.x - 1) / block.x, (Ic + RV - 1) / RV,
+                                                             (Jc + RV - 1) / RV);
+        MGBF_DISPATCH(t, (k_restrict4<T><<<grid, block, 0, s>>>(a)));
+        return last_err();
+    }
+    constexpr int NW = 4;
+    const int nstrip = (Ic + RC - 1) / RC;
+    dim3 block(32, NW), grid((a.nk + 31) / 32, (nstrip + NW - 1) / NW, (Jc + RC - 1) / RC);
     MGBF_DISPATCH(t, (k_restrict<T><<<grid, block, 0, s>>>(a)));
     return last_err();
 }
 
 int launch_prolong(DType t, const ProlongArgs& a, void* stream) {
-    const long long n = (long long)a.nk * a.If;
-    if (n == 0) return 0;
-    dim3 block(256), grid((unsigned)((n + 255) / 256), a.Jf);
+    if (a.nk == 0 || a.If == 0 || a.Jf == 0) return 0;
+    const int O = a.ntap == 4 ? 1 : 0;
+    const int npx = a.If / 2 + O, npy = a.Jf / 2 + O;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    MGBF_DISPATCH(t, (k_prolong<T><<<grid, block, 0, s>>>(a)));
+    if (a.nk % 4 == 0 && aligned16(a.coarse.p) && aligned16(a.out.p) && (!a.has_base || aligned16(a.base.p))) {
+        const int nt = a.nk / 4;
+        dim3 block(std::min(128, ((nt + 31) / 32) * 32)), grid((nt + block.x - 1) / block.x, (npx + PV - 1) / PV, npy);
+        if (a.ntap == 4) {
+            MGBF_DISPATCH(t, (k_prolong4<T, 4><<<grid, block, 0, s>>>(a)));
+        } else {
+            MGBF_DISPATCH(t, (k_prolong4<T, 3><<<grid, block, 0, s>>>(a)));
+        }
+        return last_err();
+    }
+    constexpr int NW = 4;
+    const int nstrip = (npx + PX - 1) / PX;
+    dim3 block(32, NW), grid((a.nk + 31) / 32, (nstrip + NW - 1) / NW, npy);
+    if (a.ntap == 4) {
+        MGBF_DISPATCH(t, (k_prolong<T, 4><<<grid, block, 0, s>>>(a)));
+    } else {
+        MGBF_DISPATCH(t, (k_prolong<T, 3><<<grid, block, 0, s>>>(a)));
+    }
     return last_err();
 }
 

@@ -21,7 +21,7 @@ struct View {
 // moment kernel.
 constexpr int kMaxReach = 32;
 constexpr int kMaxMomP = 4;
-constexpr int kMaxZBand = 2 * 32 + 1;
+constexpr int kMaxZReach = 16;  // vertical reach handled by the z kernel
 
 struct ZArgs {
     View in, out;

@@ -146,6 +146,11 @@ int build_zstencil(int p, double ampl01, int hz, int lm, bool need, ZStencil& Z,
     }
     const double s = 1.0 / sum;
     const int mz = std::max(-gxl, gxm);
+    if (need && mz > kMaxZReach) {
+        err = "vertical reach " + std::to_string(mz) + " exceeds the supported maximum " +
+              std::to_string(kMaxZReach);
+        return MGBF_ERR_UNSUPPORTED;
+    }
     Z.lm = lm;
     Z.mz = mz;
     Z.exx = exx;
