@@ -151,6 +151,11 @@ int mgbf_filtering_procedure_adjoint(mgbf_handle* h, int mg_filt, void* vall, in
 int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, const void* gy,
                                  void* gx, double* ga, int dtype, int mem, void* stream);
 
+/* Device-side status: MGBF_ERR_TIMEOUT if a bounded wait inside a kernel
+ * (a TMA-fed pipeline stage) ran out since the last check, else MGBF_OK.
+ * Synchronises with the device and clears the status. */
+int mgbf_status(mgbf_handle* h);
+
 /* Replace the per-generation weights a_1..a_n (n <= gm) without rebuilding. */
 int mgbf_set_weights(mgbf_handle* h, const double* a, int n);
 
@@ -212,6 +217,8 @@ int mgbf_batch_create(int im, int jm, int gm, const double* weights, int lquart,
  * adjoint != 0 runs the transposed chain. */
 int mgbf_batch_apply(mgbf_batch* b, void* const* fields, int dtype, int adjoint, void* stream);
 int mgbf_batch_destroy(mgbf_batch* b);
+/* As mgbf_status, for a batch. */
+int mgbf_batch_status(mgbf_batch* b);
 
 #ifdef __cplusplus
 }

@@ -92,6 +92,8 @@ SIGNATURES = {
                                ctypes.POINTER(_HP)]),
     "mgbf_batch_apply": (_I, [_HP, ctypes.POINTER(_VP), _I, _I, _VP]),
     "mgbf_batch_destroy": (_I, [_HP]),
+    "mgbf_status": (_I, [_HP]),
+    "mgbf_batch_status": (_I, [_HP]),
     "mgbf_timers_enable": (_I, [_I]),
     "mgbf_timers_read": (_I, [ctypes.POINTER(MgbfTimerStat), _I, ctypes.POINTER(_I)]),
 }

@@ -11,6 +11,7 @@
 //                                           B^T == B for the half-sample mirror)
 //   4. H_{g-1} += P H_g, x1 += P H_2      downsending*         (k_prolong)
 //   5. y = Bz x1                          sup_vrbeta1_*        (k_zfilter, forward band)
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -116,6 +117,47 @@ int upload_acc(DevBuf& b, const std::vector<double>& v, DType t) {
     return upload(b, f);
 }
 
+// ------------------------------------------------------------- tensor maps
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on libcuda); null when unavailable.
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return (EncodeTiledFn) nullptr;
+        }
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// 3D map of a padded generation buffer (levels, columns incl. x halo, rows)
+// with a box of 64 levels x cols x 1 row.  Returns false if the buffer does
+// not meet TMA's rules (16-byte aligned base and strides).
+bool make_tmap(CUtensorMap* m, void* base, DType t, int nk, int ncols, int nrows, int box_cols) {
+    if (t == DType::F64) return false;
+    const size_t es = t == DType::F32 ? 4 : 2;
+    if (((uintptr_t)base & 15u) || (nk * es) % 16) return false;
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)nk, (cuuint64_t)ncols, (cuuint64_t)nrows};
+    cuuint64_t strides[2] = {(cuuint64_t)nk * es, (cuuint64_t)nk * es * ncols};
+    cuuint32_t box[3] = {64, (cuuint32_t)box_cols, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(m, t == DType::F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims,
+                    strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 // ------------------------------------------------------------ stage timers
 
 enum Stage { ST_VFILTT, ST_UPSEND, ST_HFILTT, ST_HFILT, ST_DNSEND, ST_VFILT, ST_COPY, ST_HALO, ST_WGRAD, ST_N };
@@ -200,6 +242,10 @@ struct Group {
     struct Set {
         std::vector<std::unique_ptr<DevBuf>> A, B, C;
     } bufs[3];
+    // TMA maps of the A/B buffers: key = dtype*64 + gen*2 + (0: A, 1: B),
+    // each with the base address it was encoded for
+    std::map<int, std::pair<void*, std::unique_ptr<CUtensorMap>>> tmaps;
+    std::map<int, void*> tmap_failed;
 };
 
 struct Plan {
@@ -209,7 +255,8 @@ struct Plan {
     std::vector<Interp1D> ix, iy;  // per generation g (fine size I_g), g = 0..gm-2
     DevBuf pix[MGBF_MAX_GEN], piy[MGBF_MAX_GEN];  // prolongation index tables
     std::vector<Group> groups;
-    DevBuf dot;  // one double per generation
+    DevBuf dot;     // one double per generation
+    DevBuf status;  // device status word of bounded waits
     int device = 0;
 };
 
@@ -228,6 +275,10 @@ int ensure_tables(Plan& P, Group& G, DType t) {
         if (!P.piy[g].p && (rc = upload(P.piy[g], P.iy[g].pidx))) return rc;
     }
     if (!P.dot.p && (rc = P.dot.ensure(sizeof(double) * MGBF_MAX_GEN))) return rc;
+    if (!P.status.p) {
+        if ((rc = P.status.ensure(sizeof(int)))) return rc;
+        CU(cudaMemset(P.status.p, 0, sizeof(int)));
+    }
     if (!G.zs.fwd.empty()) {
         if ((rc = upload_acc(T.zfwd, G.zs.fwd, t))) return rc;
         if ((rc = upload_acc(T.zadj, G.zs.adj, t))) return rc;
@@ -327,13 +378,36 @@ struct Exec {
         LK(launch_prolong(t, a, stream));
         return 0;
     }
-    int hpass(int g, View in, View out, double scale, int mirror, int stage) {
+    // TMA map of generation buffer A (which = 0) or B (1), made at first use.
+    const CUtensorMap* tmap(int g, int which) {
+        if (which < 0 || t == DType::F64) return nullptr;
+        const int key = (int)t * 64 + g * 2 + which;
+        auto& v = G.bufs[(int)t];
+        void* base = which == 0 ? v.A[g]->p : v.B[g]->p;
+        auto it = G.tmaps.find(key);
+        if (it != G.tmaps.end() && it->second.first == base) return it->second.second.get();
+        auto f = G.tmap_failed.find(key);
+        if (f != G.tmap_failed.end() && f->second == base) return nullptr;
+        std::unique_ptr<CUtensorMap> m(new CUtensorMap);
+        if (!make_tmap(m.get(), base, t, G.nk, gen_I(P, g) + 2 * G.HXP, gen_J(P, g), hmom_tma_cols(G.hs.R))) {
+            G.tmap_failed[key] = base;
+            return nullptr;
+        }
+        auto& slot = G.tmaps[key];
+        slot.first = base;
+        slot.second = std::move(m);
+        return slot.second.get();
+    }
+
+    int hpass(int g, View in, View out, double scale, int mirror, int stage, int which_in) {
         const int I = gen_I(P, g), J = gen_J(P, g);
         StageTimer tm(stage, stream, pts(g));
         if (G.hs.canonical && hmom_available(t, G.hs.R, G.hs.p)) {
             HMomArgs a;
             a.in = in; a.out = out; a.nk = G.nk; a.I = I; a.J = J;
-            a.mirror_hx = mirror; a.scale = scale;
+            a.mirror_hx = mirror; a.scale = scale * G.hs.s; a.halo = G.HXP;
+            a.tmap = tmap(g, which_in);
+            a.status = static_cast<int*>(P.status.p);
             const int tx = hmom_tx_for((int)acc_size(t), G.hs.R);
             const long long w0 = (long long)((G.nk + 31) / 32) * ((I + tx - 1) / tx);
             const long long target = 152LL * 24;
@@ -362,19 +436,18 @@ struct Exec {
             if ((rc = restrict_(g, A(g), A(g + 1)))) return rc;
         for (int g = 0; g < P.gm; ++g) {
             if (g == 0 && !filt1) continue;
-            if ((rc = hpass(g, A(g), dst(g), scales ? scales[g] : 1.0, mirror_out ? G.hs.R : 0, ST_HFILTT))) return rc;
+            if ((rc = hpass(g, A(g), dst(g), scales ? scales[g] : 1.0, mirror_out ? G.hs.R : 0, ST_HFILTT, 0))) return rc;
         }
         return 0;
     }
 
-    // Steps 3b-5: src(g) holds B_g R_g Bz^T x (mirrored), already multiplied
+    // Steps 3b-5: B(g) holds B_g R_g Bz^T x (mirrored), already multiplied
     // by a_g unless scales are given; finishes into y.
-    template <typename SrcF>
-    int second_half(SrcF src, View y, int nzcol, bool filt1, const double* scales) {
+    int second_half(View y, int nzcol, bool filt1, const double* scales) {
         int rc;
         for (int g = 0; g < P.gm; ++g) {
             if (g == 0 && !filt1) continue;
-            if ((rc = hpass(g, src(g), A(g), scales ? scales[g] : 1.0, 0, ST_HFILT))) return rc;
+            if ((rc = hpass(g, B(g), A(g), scales ? scales[g] : 1.0, 0, ST_HFILT, 1))) return rc;
         }
         const bool z = nzcol > 0 && !G.zs.fwd.empty();
         for (int g = P.gm - 1; g >= 1; --g) {
@@ -393,7 +466,7 @@ struct Exec {
         int rc;
         auto Bf = [&](int g) { return B(g); };
         if ((rc = half_chain(x, nzcol, filt1, Bf, true, P.a))) return rc;
-        return second_half(Bf, y, nzcol, filt1, nullptr);
+        return second_half(y, nzcol, filt1, nullptr);
     }
 };
 
@@ -927,7 +1000,7 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
         LK(launch_dot(t, da, stream));
     }
     // gx = L gy = Bz sum_g P_g B_g (a_g v_g)
-    if ((rc = ex.second_half(Bf, vo, nzcol, filt1, P.a))) return rc;
+    if ((rc = ex.second_half(vo, nzcol, filt1, P.a))) return rc;
     if (h->cfg.layout == MGBF_LAYOUT_HALO && filt1) {
         StageTimer tm(ST_HALO, stream, 0.0);
         LK(launch_zero_halo(t, vo, G.nk, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
@@ -937,6 +1010,28 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
         CU(cudaMemcpyAsync(gx, h->stage2[(int)t].p, bytes, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
     return 0;
+}
+
+static int read_status(Plan& P) {
+    if (!P.status.p) return MGBF_OK;
+    DeviceGuard dg(P.device);
+    int v = 0;
+    CU(cudaMemcpy(&v, P.status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (v) {
+        CU(cudaMemset(P.status.p, 0, sizeof(int)));
+        return fail(MGBF_ERR_TIMEOUT, "a bounded device wait ran out in a radial-filter kernel");
+    }
+    return MGBF_OK;
+}
+
+int mgbf_status(mgbf_handle* h) {
+    if (!h) return fail(MGBF_ERR_ARG, "null handle");
+    return read_status(h->plan);
+}
+
+int mgbf_batch_status(mgbf_batch* b) {
+    if (!b) return fail(MGBF_ERR_ARG, "null handle");
+    return read_status(b->plan);
 }
 
 int mgbf_timers_enable(int on) {

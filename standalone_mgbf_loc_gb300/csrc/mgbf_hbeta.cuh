@@ -6,7 +6,9 @@
 // u = (e gx)^2:  w = s * sum_q C(p,q) (-1)^q A(gy)^(p-q) u^q,  A = 1 - (e gy)^2.
 // So the row sum  sum_{|gx|<=m(gy)} w a(i+gx)  equals
 //   sum_q c_q(gy) T_q^{m(gy)}(i),   T_q^m(i) = sum_{|gx|<=m} (e gx)^(2q) a(i+gx),
-// and T_q^m grows from T_q^{m-1} by (e m)^(2q) (a(i+m)+a(i-m)).  One pass over
+// and T_q^m grows from T_q^{m-1} by (e m)^(2q) (a(i+m)+a(i-m)).  With the
+// binomial factors and signs folded into the increments (T'_q) and s moved
+// to the store, the row sum is the Horner form ((T'_0 A + T'_1) A + ...) + T'_p.  One pass over
 // m = 0..R per input row yields every row width the disk needs; each width is
 // emitted (symmetrically for +gy and -gy) into a ring of output-row
 // accumulators as the kernel streams down the rows.  This is the same linear
@@ -27,7 +29,10 @@
 #include "mgbf_common.cuh"
 #include "mgbf_kernels.cuh"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
+
+#include <cstdint>
 
 namespace mgbf {
 
@@ -88,9 +93,10 @@ __global__ void __launch_bounds__(128) k_hmom(HMomArgs a,
 #pragma unroll
                 for (int gy = 0; gy <= R; ++gy) {
                     if (mcanon<R>(gy) == m) {
-                        A v = c.coef[gy * PQ] * t[0];
+                        const A Ay = c.coef[gy * PQ];  // A(gy) = 1 - (e gy)^2
+                        A v = t[0];
 #pragma unroll
-                        for (int e = 1; e < PQ; ++e) v = fma(c.coef[gy * PQ + e], t[e], v);
+                        for (int e = 1; e < PQ; ++e) v = fma(v, Ay, t[e]);
                         acc[R + u - gy][q] += v;
                         if (gy) acc[R + u + gy][q] += v;
                     }
@@ -135,6 +141,477 @@ __global__ void __launch_bounds__(128) k_hmom(HMomArgs a,
     }
 }
 
+// Shared-memory staged variant: the block's rows (32 levels x the block's
+// column range + 2R halo) are copied into a DS-deep ring of tiles by
+// cp.async (16-byte chunks, zero-filled outside the field), DS-1 rows ahead
+// of the row being filtered; lanes then read their row segment from shared
+// memory.  Needs nk * sizeof(T) to be a multiple of 16 (16-byte aligned
+// columns; chunks never straddle a column end).
+constexpr int kStages = 4;
+constexpr int kStageWarps = 4;
+
+__device__ __forceinline__ void cp_async16(unsigned saddr, const void* g, int bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(g), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <int R, int TX, typename T>
+constexpr size_t hmom_stage_bytes() {
+    return (size_t)kStages * (kStageWarps * TX + 2 * R) * 32 * sizeof(T);
+}
+
+template <int R, int P, int TX, typename T>
+__global__ void __launch_bounds__(128) k_hmom_st(HMomArgs a,
+                                                 const __grid_constant__ HMomCoefs<typename AccOf<T>::type> c) {
+    using A = typename AccOf<T>::type;
+    constexpr int U = 2;
+    constexpr int NS = TX + 2 * R;
+    constexpr int NR = 2 * R + U;
+    constexpr int PQ = P + 1;
+    constexpr int NC = kStageWarps * TX + 2 * R;   // tile columns
+    constexpr int CH = 32 * (int)sizeof(T) / 16;   // 16-byte chunks per column
+    constexpr int TILE = NC * 32;                  // elements per tile
+    constexpr int EPC = 16 / (int)sizeof(T);       // elements per chunk
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* tiles = reinterpret_cast<T*>(smem_raw);
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const int lane = threadIdx.x, warp = threadIdx.y, tid = warp * 32 + lane;
+    const int k0 = blockIdx.x * 32;
+    const int ib = blockIdx.y * (kStageWarps * TX);
+    const int jb = blockIdx.z * a.rows;
+    const int je = min(jb + a.rows, a.J);
+    const T* gin = static_cast<const T*>(a.in.p);
+    const int colmax = a.I + a.halo - 1;  // last readable column of the padded buffer
+
+    auto issue = [&](int jin, int st) {
+        const int jr = reflect_half(jin, a.J);
+        const T* rowp = gin + a.in.sj * (long long)jr + k0;
+        for (int q = tid; q < NC * CH; q += kStageWarps * 32) {
+            const int col = q / CH, ch = q - col * CH;
+            const int gcol = ib - R + col;
+            const bool ok = gcol <= colmax && k0 + ch * EPC < a.nk;
+            const T* src = ok ? rowp + a.in.si * (long long)gcol + ch * EPC : gin;
+            cp_async16(sbase + (unsigned)(((st * TILE + col * 32) * (int)sizeof(T)) + ch * 16), src, ok ? 16 : 0);
+        }
+        cp_async_commit();
+    };
+
+    const int i0 = ib + warp * TX;
+    const bool kv = k0 + lane < a.nk;
+    T* outb = static_cast<T*>(a.out.p) + k0 + lane;
+    const A scale = static_cast<A>(a.scale);
+    A acc[NR][TX];
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+#pragma unroll
+        for (int q = 0; q < TX; ++q) acc[r][q] = A(0);
+
+    auto row = [&](const int st, const int u) {
+        const T* tp = tiles + st * TILE + warp * TX * 32 + lane;
+        A seg[NS];
+#pragma unroll
+        for (int s2 = 0; s2 < NS; ++s2) seg[s2] = ldc(tp + s2 * 32);
+#pragma unroll
+        for (int q = 0; q < TX; ++q) {
+            A t[PQ];
+            t[0] = seg[R + q];
+#pragma unroll
+            for (int e = 1; e < PQ; ++e) t[e] = A(0);
+#pragma unroll
+            for (int m = 0; m <= R; ++m) {
+                if (m > 0) {
+                    const A pr = seg[R + q + m] + seg[R + q - m];
+                    t[0] += pr;
+#pragma unroll
+                    for (int e = 1; e < PQ; ++e) t[e] = fma(c.upow[m * PQ + e], pr, t[e]);
+                }
+#pragma unroll
+                for (int gy = 0; gy <= R; ++gy) {
+                    if (mcanon<R>(gy) == m) {
+                        const A Ay = c.coef[gy * PQ];
+                        A v = t[0];
+#pragma unroll
+                        for (int e = 1; e < PQ; ++e) v = fma(v, Ay, t[e]);
+                        acc[R + u - gy][q] += v;
+                        if (gy) acc[R + u + gy][q] += v;
+                    }
+                }
+            }
+        }
+    };
+
+    const int nrows = je - jb + 2 * R;  // input rows jb-R .. je+R-1
+#pragma unroll
+    for (int s2 = 0; s2 < kStages - 1; ++s2) issue(jb - R + s2, s2);
+    for (int r0 = 0; r0 < nrows; r0 += U) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int r = r0 + u;
+            cp_async_wait<kStages - 2>();
+            __syncthreads();
+            issue(jb - R + r + kStages - 1, (r + kStages - 1) % kStages);
+            row(r % kStages, u);
+        }
+        const int jin0 = jb - R + r0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int jo = jin0 - R + u;
+            if (kv && jo >= jb && jo < je) {
+                T* orow = outb + a.out.sj * (long long)jo;
+#pragma unroll
+                for (int q = 0; q < TX; ++q) {
+                    const int i = i0 + q;
+                    if (i < a.I) {
+                        const A v = acc[u][q] * scale;
+                        stv(orow + a.out.si * (long long)i, v);
+                        if (i < a.mirror_hx) stv(orow + a.out.si * (long long)(-1 - i), v);
+                        if (i >= a.I - a.mirror_hx) stv(orow + a.out.si * (long long)(2 * a.I - 1 - i), v);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < NR - U; ++r)
+#pragma unroll
+            for (int q = 0; q < TX; ++q) acc[r][q] = acc[r + U][q];
+#pragma unroll
+        for (int r = NR - U; r < NR; ++r)
+#pragma unroll
+            for (int q = 0; q < TX; ++q) acc[r][q] = A(0);
+    }
+    cp_async_wait<0>();
+}
+
+// Packed variant for FP32 arithmetic (FP32 or BF16 storage): each lane owns
+// two adjacent levels (k, k+1) as one float2, so every multiply-add of the
+// moment recurrences and of the Horner emission is one f32x2 instruction
+// (__ffma2_rn / __fadd2_rn); the block covers 64 levels.  Rows are staged
+// through shared memory as in k_hmom_st (DS-deep cp.async ring, 16-byte
+// chunks) and U = 4 rows share one ring shift.
+template <typename T> struct P2;
+template <> struct P2<float> {
+    static __device__ __forceinline__ float2 lds(const float* p) { return *reinterpret_cast<const float2*>(p); }
+    static __device__ __forceinline__ void st(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+};
+template <> struct P2<__nv_bfloat16> {
+    static __device__ __forceinline__ float2 lds(const __nv_bfloat16* p) {
+        const unsigned u = *reinterpret_cast<const unsigned*>(p);
+        return make_float2(__uint_as_float(u << 16), __uint_as_float(u & 0xffff0000u));
+    }
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, float2 v) {
+        *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(v.x, v.y);
+    }
+};
+
+struct HMomCoefs2 {
+    float2 coef[kMaxReach + 1];                  // (A(gy), A(gy))
+    float2 upow[(kMaxReach + 1) * (kMaxMomP + 1)];  // (c, c) of HMomCoefs::upow
+};
+
+template <int R, int TX, typename T>
+constexpr size_t hmom_p2_stage_bytes() {
+    return (size_t)kStages * (kStageWarps * TX + 2 * R) * 64 * sizeof(T);
+}
+
+template <int R, int P, int TX, typename T>
+__global__ void __launch_bounds__(128) k_hmom_p2(HMomArgs a, const __grid_constant__ HMomCoefs2 c) {
+    constexpr int U = kStages;                     // stage index == u
+    constexpr int NS = TX + 2 * R;
+    constexpr int NR = 2 * R + U;
+    constexpr int PQ = P + 1;
+    constexpr int NC = kStageWarps * TX + 2 * R;
+    constexpr int CB = 64 * (int)sizeof(T);        // bytes per tile column
+    constexpr int CH = CB / 16;
+    constexpr int TILE = NC * 64;
+    constexpr int EPC = 16 / (int)sizeof(T);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* tiles = reinterpret_cast<T*>(smem_raw);
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const int lane = threadIdx.x, warp = threadIdx.y, tid = warp * 32 + lane;
+    const int k0 = blockIdx.x * 64;
+    const int ib = blockIdx.y * (kStageWarps * TX);
+    const int jb = blockIdx.z * a.rows;
+    const int je = min(jb + a.rows, a.J);
+    const T* gin = static_cast<const T*>(a.in.p);
+    const int colmax = a.I + a.halo - 1;
+
+    auto issue = [&](int jin, int st) {
+        const int jr = reflect_half(jin, a.J);
+        const T* rowp = gin + a.in.sj * (long long)jr + k0;
+        for (int q = tid; q < NC * CH; q += kStageWarps * 32) {
+            const int col = q / CH, ch = q - col * CH;
+            const int gcol = ib - R + col;
+            const bool ok = gcol <= colmax && k0 + ch * EPC < a.nk;
+            const T* src = ok ? rowp + a.in.si * (long long)gcol + ch * EPC : gin;
+            cp_async16(sbase + (unsigned)(((st * TILE + col * 64) * (int)sizeof(T)) + ch * 16), src, ok ? 16 : 0);
+        }
+        cp_async_commit();
+    };
+
+    const int i0 = ib + warp * TX;
+    const int kl = k0 + 2 * lane;
+    const bool kv = kl < a.nk;                     // nk is even: both levels valid
+    T* outb = static_cast<T*>(a.out.p) + kl;
+    const float2 scale = make_float2((float)a.scale, (float)a.scale);
+    float2 acc[NR][TX];
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+#pragma unroll
+        for (int q = 0; q < TX; ++q) acc[r][q] = make_float2(0.f, 0.f);
+
+    auto row = [&](const int st, const int u) {
+        const T* tp = tiles + st * TILE + warp * TX * 64 + 2 * lane;
+        float2 seg[NS];
+#pragma unroll
+        for (int s2 = 0; s2 < NS; ++s2) seg[s2] = P2<T>::lds(tp + s2 * 64);
+#pragma unroll
+        for (int q = 0; q < TX; ++q) {
+            float2 t[PQ];
+            t[0] = seg[R + q];
+#pragma unroll
+            for (int e = 1; e < PQ; ++e) t[e] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int m = 0; m <= R; ++m) {
+                if (m > 0) {
+                    const float2 pr = __fadd2_rn(seg[R + q + m], seg[R + q - m]);
+                    t[0] = __fadd2_rn(t[0], pr);
+#pragma unroll
+                    for (int e = 1; e < PQ; ++e) t[e] = __ffma2_rn(c.upow[m * PQ + e], pr, t[e]);
+                }
+#pragma unroll
+                for (int gy = 0; gy <= R; ++gy) {
+                    if (mcanon<R>(gy) == m) {
+                        float2 v = t[0];
+#pragma unroll
+                        for (int e = 1; e < PQ; ++e) v = __ffma2_rn(v, c.coef[gy], t[e]);
+                        acc[R + u - gy][q] = __fadd2_rn(acc[R + u - gy][q], v);
+                        if (gy) acc[R + u + gy][q] = __fadd2_rn(acc[R + u + gy][q], v);
+                    }
+                }
+            }
+        }
+    };
+
+    const int nrows = je - jb + 2 * R;
+#pragma unroll
+    for (int s2 = 0; s2 < kStages - 1; ++s2) issue(jb - R + s2, s2);
+    for (int r0 = 0; r0 < nrows; r0 += U) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            cp_async_wait<kStages - 2>();
+            __syncthreads();
+            issue(jb - R + r0 + u + kStages - 1, (u + kStages - 1) % kStages);
+            row(u, u);
+        }
+        const int jin0 = jb - R + r0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int jo = jin0 - R + u;
+            if (kv && jo >= jb && jo < je) {
+                T* orow = outb + a.out.sj * (long long)jo;
+#pragma unroll
+                for (int q = 0; q < TX; ++q) {
+                    const int i = i0 + q;
+                    if (i < a.I) {
+                        const float2 v = __fmul2_rn(acc[u][q], scale);
+                        P2<T>::st(orow + a.out.si * (long long)i, v);
+                        if (i < a.mirror_hx) P2<T>::st(orow + a.out.si * (long long)(-1 - i), v);
+                        if (i >= a.I - a.mirror_hx) P2<T>::st(orow + a.out.si * (long long)(2 * a.I - 1 - i), v);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < NR - U; ++r)
+#pragma unroll
+            for (int q = 0; q < TX; ++q) acc[r][q] = acc[r + U][q];
+#pragma unroll
+        for (int r = NR - U; r < NR; ++r)
+#pragma unroll
+            for (int q = 0; q < TX; ++q) acc[r][q] = make_float2(0.f, 0.f);
+    }
+    cp_async_wait<0>();
+}
+
+// TMA variant of the packed kernel: one thread issues one
+// cp.async.bulk.tensor.3d per input row (box 64 levels x NC columns x 1 row
+// of the padded generation buffer; out-of-range levels and columns are
+// zero-filled by the copy engine) into a kStages-deep ring of tiles, each
+// guarded by an mbarrier with expect_tx.  Consumers wait on the barrier
+// parity with a bounded number of polls; if the bound runs out the block
+// records the failure in a.status and leaves through a block-uniform exit
+// after a bounded drain of its own copies.
+__device__ __forceinline__ void mbar_init(unsigned addr, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(addr), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned addr, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(addr), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned addr, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned addr, unsigned parity) {
+    constexpr int kMaxPolls = 1 << 20;
+    for (int it = 0; it < kMaxPolls; ++it)
+        if (mbar_try_wait(addr, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load_3d(unsigned dst, const void* tmap, int c0, int c1, int c2, unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
+        "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+
+template <int R, int P, int TX, typename T>
+__global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
+                                                  const __grid_constant__ HMomCoefs2 c) {
+    constexpr int U = kStages;
+    constexpr int NS = TX + 2 * R;
+    constexpr int NR = 2 * R + U;
+    constexpr int PQ = P + 1;
+    constexpr int NC = kStageWarps * TX + 2 * R;
+    constexpr int TILE = NC * 64;
+    constexpr unsigned TILE_BYTES = TILE * sizeof(T);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long bars[kStages];
+    T* tiles = reinterpret_cast<T*>(smem_raw);
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const unsigned bbase = (unsigned)__cvta_generic_to_shared(bars);
+    const int lane = threadIdx.x, warp = threadIdx.y, tid = warp * 32 + lane;
+    const int k0 = blockIdx.x * 64;
+    const int ib = blockIdx.y * (kStageWarps * TX);
+    const int jb = blockIdx.z * a.rows;
+    const int je = min(jb + a.rows, a.J);
+    const int nrows = je - jb + 2 * R;
+    const int nrp = ((nrows + U - 1) / U) * U;  // rows read by the unrolled loop
+    if (tid == 0) {
+#pragma unroll
+        for (int s2 = 0; s2 < kStages; ++s2) mbar_init(bbase + 8 * s2, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int r) {
+        if (tid == 0 && r < nrp) {
+            const int st = r % kStages;
+            const int jr = reflect_half(jb - R + r, a.J);
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            mbar_expect_tx(bbase + 8 * st, TILE_BYTES);
+            tma_load_3d(sbase + st * TILE_BYTES, &tmap, k0, ib - R + a.halo, jr, bbase + 8 * st);
+        }
+    };
+
+    const int i0 = ib + warp * TX;
+    const int kl = k0 + 2 * lane;
+    const bool kv = kl < a.nk;
+    T* outb = static_cast<T*>(a.out.p) + kl;
+    const float2 scale = make_float2((float)a.scale, (float)a.scale);
+    float2 acc[NR][TX];
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+#pragma unroll
+        for (int q = 0; q < TX; ++q) acc[r][q] = make_float2(0.f, 0.f);
+
+    auto row = [&](const int st, const int u) {
+        const T* tp = tiles + st * TILE + warp * TX * 64 + 2 * lane;
+        float2 seg[NS];
+#pragma unroll
+        for (int s2 = 0; s2 < NS; ++s2) seg[s2] = P2<T>::lds(tp + s2 * 64);
+#pragma unroll
+        for (int q = 0; q < TX; ++q) {
+            float2 t[PQ];
+            t[0] = seg[R + q];
+#pragma unroll
+            for (int e = 1; e < PQ; ++e) t[e] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int m = 0; m <= R; ++m) {
+                if (m > 0) {
+                    const float2 pr = __fadd2_rn(seg[R + q + m], seg[R + q - m]);
+                    t[0] = __fadd2_rn(t[0], pr);
+#pragma unroll
+                    for (int e = 1; e < PQ; ++e) t[e] = __ffma2_rn(c.upow[m * PQ + e], pr, t[e]);
+                }
+#pragma unroll
+                for (int gy = 0; gy <= R; ++gy) {
+                    if (mcanon<R>(gy) == m) {
+                        float2 v = t[0];
+#pragma unroll
+                        for (int e = 1; e < PQ; ++e) v = __ffma2_rn(v, c.coef[gy], t[e]);
+                        acc[R + u - gy][q] = __fadd2_rn(acc[R + u - gy][q], v);
+                        if (gy) acc[R + u + gy][q] = __fadd2_rn(acc[R + u + gy][q], v);
+                    }
+                }
+            }
+        }
+    };
+
+#pragma unroll
+    for (int s2 = 0; s2 < kStages - 1; ++s2) issue(s2);
+    bool failed = false;
+    int waited = 0;  // rows whose barrier has been waited
+    for (int r0 = 0; r0 < nrp && !failed; r0 += U) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int r = r0 + u;
+            const bool ok = mbar_wait_bounded(bbase + 8 * u, (unsigned)((r / kStages) & 1));
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            waited = r + 1;
+            issue(r + kStages - 1);
+            row(u, u);
+        }
+        if (failed) break;
+        const int jin0 = jb - R + r0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int jo = jin0 - R + u;
+            if (kv && jo >= jb && jo < je) {
+                T* orow = outb + a.out.sj * (long long)jo;
+#pragma unroll
+                for (int q = 0; q < TX; ++q) {
+                    const int i = i0 + q;
+                    if (i < a.I) {
+                        const float2 v = __fmul2_rn(acc[u][q], scale);
+                        P2<T>::st(orow + a.out.si * (long long)i, v);
+                        if (i < a.mirror_hx) P2<T>::st(orow + a.out.si * (long long)(-1 - i), v);
+                        if (i >= a.I - a.mirror_hx) P2<T>::st(orow + a.out.si * (long long)(2 * a.I - 1 - i), v);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < NR - U; ++r)
+#pragma unroll
+            for (int q = 0; q < TX; ++q) acc[r][q] = acc[r + U][q];
+#pragma unroll
+        for (int r = NR - U; r < NR; ++r)
+#pragma unroll
+            for (int q = 0; q < TX; ++q) acc[r][q] = make_float2(0.f, 0.f);
+    }
+    if (failed) {
+        // record, then drain this block's outstanding copies (bounded) before exit
+        if (tid == 0) {
+            atomicExch(a.status, 1);
+            const int issued = min(nrp, waited + kStages - 1);
+            for (int r = waited; r < issued; ++r) mbar_wait_bounded(bbase + 8 * (r % kStages), (unsigned)((r / kStages) & 1));
+        }
+        __syncthreads();
+    }
+}
+
+// Columns per thread of the packed kernels.
+constexpr int hmom_p2_tx(int R) { return hmom_tma_tx(R); }
+
 template <int R, int P, typename T>
 static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t s) {
     using A = typename AccOf<T>::type;
@@ -151,7 +628,44 @@ static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t
     HMomArgs b = a;
     b.rows = rows;
     dim3 block(32, NW), grid((a.nk + 31) / 32, (nstrip + NW - 1) / NW, (a.J + rows - 1) / rows);
-    k_hmom<R, P, TX, U, T><<<grid, block, 0, s>>>(b, c);
+    // columns must start on 16-byte boundaries and 16-byte chunks must not
+    // straddle the end of a column: nk * sizeof(T) % 16 == 0
+    const bool staged = (a.nk * (int)sizeof(T)) % 16 == 0 && (((uintptr_t)a.in.p) & 15u) == 0 && a.halo >= R;
+    if constexpr (sizeof(A) == 4) {
+        // packed pairs: nk even and 16-byte aligned columns
+        if (staged && a.nk % 2 == 0 && ((uintptr_t)a.out.p & 7u) == 0) {
+            constexpr int TX2 = hmom_p2_tx(R);
+            HMomCoefs2 c2;
+            for (int g = 0; g <= kMaxReach; ++g) c2.coef[g] = make_float2((float)cd.coef[g * (P + 1)], (float)cd.coef[g * (P + 1)]);
+            for (int t = 0; t < (kMaxReach + 1) * (kMaxMomP + 1); ++t)
+                c2.upow[t] = make_float2((float)cd.upow[t], (float)cd.upow[t]);
+            const int nstrip2 = (a.I + TX2 - 1) / TX2;
+            dim3 grid2((a.nk + 63) / 64, (nstrip2 + NW - 1) / NW, (a.J + rows - 1) / rows);
+            if (a.tmap && a.status) {
+                static_assert(hmom_tma_tx(R) == TX2, "tile shape");
+                constexpr size_t smt = (size_t)kStages * (kStageWarps * TX2 + 2 * R) * 64 * sizeof(T);
+                if (smt > 48 * 1024)
+                    cudaFuncSetAttribute(k_hmom_tma<R, P, TX2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+                k_hmom_tma<R, P, TX2, T><<<grid2, block, smt, s>>>(b, *static_cast<const CUtensorMap*>(a.tmap), c2);
+                cudaError_t e = cudaGetLastError();
+                return e == cudaSuccess ? 0 : (int)e;
+            }
+            constexpr size_t sm2 = hmom_p2_stage_bytes<R, TX2, T>();
+            if (sm2 > 48 * 1024)
+                cudaFuncSetAttribute(k_hmom_p2<R, P, TX2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+            k_hmom_p2<R, P, TX2, T><<<grid2, block, sm2, s>>>(b, c2);
+            cudaError_t e = cudaGetLastError();
+            return e == cudaSuccess ? 0 : (int)e;
+        }
+    }
+    if (staged) {
+        static_assert(NW == kStageWarps, "block shape");
+        constexpr size_t sm = hmom_stage_bytes<R, TX, T>();
+        if (sm > 48 * 1024) cudaFuncSetAttribute(k_hmom_st<R, P, TX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_hmom_st<R, P, TX, T><<<grid, block, sm, s>>>(b, c);
+    } else {
+        k_hmom<R, P, TX, U, T><<<grid, block, 0, s>>>(b, c);
+    }
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? 0 : (int)e;
 }

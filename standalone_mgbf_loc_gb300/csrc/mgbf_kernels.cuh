@@ -63,8 +63,8 @@ struct HDirectArgs {
 
 template <typename A>
 struct HMomCoefs {
-    A coef[(kMaxReach + 1) * (kMaxMomP + 1)];  // coef[gy*(P+1)+q], gy = 0..R
-    A upow[(kMaxReach + 1) * (kMaxMomP + 1)];  // upow[m*(P+1)+q] = (e^2 m^2)^q
+    A coef[(kMaxReach + 1) * (kMaxMomP + 1)];  // coef[gy*(P+1)] = A(gy) = 1 - (e gy)^2
+    A upow[(kMaxReach + 1) * (kMaxMomP + 1)];  // upow[m*(P+1)+q] = C(P,q) (-1)^q (e m)^(2q)
 };
 
 struct HMomArgs {
@@ -72,8 +72,16 @@ struct HMomArgs {
     int nk, I, J;
     int rows;                // output rows per block (<= 0: all rows)
     int mirror_hx;
-    double scale;            // multiplies every output (generation weight)
+    int halo;                // x padding of the input view (readable columns -halo..I+halo-1)
+    double scale;            // multiplies every output (normalisation s x generation weight)
+    const void* tmap;        // host copy of a 3D TMA tensor map of the input buffer, or null
+    int* status;             // device status word: set to 1 when a bounded wait runs out
 };
+
+// Tile columns of the TMA moment kernel for reach R (box = 64 levels x this
+// many columns x 1 row); the host encodes tensor maps with this box.
+constexpr int hmom_tma_tx(int R) { return R <= 12 ? 2 : 1; }
+constexpr int hmom_tma_cols(int R) { return 4 * hmom_tma_tx(R) + 2 * R; }
 
 // Reaches with a compiled moment kernel (p = 2).
 #define MGBF_HMOM_REACHES(X) X(4) X(5) X(6) X(8) X(10) X(12) X(16) X(24)

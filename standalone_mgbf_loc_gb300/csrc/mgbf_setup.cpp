@@ -108,15 +108,16 @@ int build_hstencil(int p, double ampl02, int hx, int hy, HStencil& H, std::strin
     H.canonical = canon && p <= kMaxMomP;
     H.mom = HMomCoefs<double>{};
     if (H.canonical) {
+        // Row gy of the disk: w = s (A - u)^p with A = 1 - (e gy)^2,
+        // u = (e gx)^2 = sum_q C(p,q) A^(p-q) (-u)^q: the kernel keeps
+        // T'_q = C(p,q) (-1)^q sum u^q a and evaluates Horner in A; s is
+        // applied at the store (HMomArgs::scale).
         const int PQ = p + 1;
-        for (int gy = 0; gy <= R; ++gy) {
-            const double A = 1.0 - (gy * eyy) * (gy * eyy);
-            for (int q = 0; q <= p; ++q)
-                H.mom.coef[gy * PQ + q] = s * binom(p, q) * ((q & 1) ? -1.0 : 1.0) * ipow(A, p - q);
-        }
+        for (int gy = 0; gy <= R; ++gy) H.mom.coef[gy * PQ] = 1.0 - (gy * eyy) * (gy * eyy);
         for (int m = 0; m <= R; ++m) {
             const double u = (m * exx) * (m * exx);
-            for (int q = 0; q <= p; ++q) H.mom.upow[m * PQ + q] = ipow(u, q);
+            for (int q = 0; q <= p; ++q)
+                H.mom.upow[m * PQ + q] = binom(p, q) * ((q & 1) ? -1.0 : 1.0) * ipow(u, q);
         }
     }
     return MGBF_OK;

@@ -217,6 +217,10 @@ class MGBF:
                    "apply_with_weight_grads")
         return gx, np.array(list(ga))
 
+    def status(self) -> None:
+        """Raise if a bounded device wait ran out since the last check."""
+        _abi.check(self._lib.mgbf_status(self._h), "mgbf_status")
+
     def set_weights(self, a: Sequence[float]) -> None:
         arr = (ctypes.c_double * len(a))(*[float(v) for v in a])
         _abi.check(self._lib.mgbf_set_weights(self._h, arr, len(a)), "set_weights")
@@ -301,6 +305,9 @@ class MGBFBatch:
         if len(dts) != 1:
             raise MGBFError(_abi.MGBF_ERR_ARG, "all groups must share a dtype")
         _abi.check(self._lib.mgbf_batch_apply(self._h, ptrs, dts.pop(), int(adjoint), stream), "mgbf_batch_apply")
+
+    def status(self) -> None:
+        _abi.check(self._lib.mgbf_batch_status(self._h), "mgbf_batch_status")
 
     def close(self):
         if getattr(self, "_h", None):

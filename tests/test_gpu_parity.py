@@ -25,6 +25,7 @@ def run_gpu(op, proc, x, dtype, cuda, adjoint=False):
     else:
         op.filtering_procedure(proc, t)
     torch.cuda.synchronize()
+    op.status()  # no bounded device wait ran out
     return t.double().cpu().numpy()
 
 
@@ -200,6 +201,7 @@ def test_batched_groups(lib, cuda):
     ts = [torch.from_numpy(x).to(cuda, torch.float32).contiguous() for x in xs]
     b.apply(ts)
     torch.cuda.synchronize()
+    b.status()
     for g, x, t in zip(groups, xs, ts):
         oc = O.OracleConfig(I=I, J=J, nk=g.nk, hx=g.hx, hy=g.hy, hz=g.hz, p=g.p, ampl01=g.mg_ampl01,
                             ampl02=g.mg_ampl02, gm=gm, weights=w, proc=6, lm=g.lm, nzcol=g.nzcol,
