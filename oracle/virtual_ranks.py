@@ -1,0 +1,312 @@
+"""Literal emulation of the reference's MPI-decomposed filtering -- TEST
+INFRASTRUCTURE ONLY.
+
+A second, independent restatement of filtering_procedure(1|6) that keeps the
+reference's structure: every rank (nx, my) owns an im x jm tile with halos;
+halos are filled and folded by emulated point-to-point exchange in the
+reference's order; restriction output of 2x2 finer tiles is assembled into the
+quadrants of one coarser tile (upsend_all) and scattered back (downsend_all).
+It exists to show that the global-grid oracle (mgbf_oracle.c), which
+collapses the tiling into one array, computes the same operator.  Only tests
+import it.
+
+Followed routines (reference paths):
+  boco_2d_g1/gh      mg_bocos.f90:89-784    (N/S rows first, then E/W columns
+                                             including the halo rows; mirror at
+                                             physical edges)
+  bocoT_2d_g1/gh     mg_bocos.f90:787-1422  (E/W first over all rows, then N/S)
+  upsend_all         mg_bocos.f90:2911-3492 (quadrants SW, SE, NW, NE)
+  downsend_all       mg_bocos.f90:3495-4041
+  adjoint/direct1    mg_generations.f90:1117-1250, adjoint2/direct2 1253-1374
+  upsending/downsending[_ens] mg_generations.f90:158-267, 382-494
+  vrbeta2/vrbeta2t   jp_pbfil.f90:888-928, 1011-1050
+  sup_vrbeta1[T]_*   mg_filtering.f90:2042-2262
+  filtering_rad2_bckg / _ens  mg_filtering.f90:560-680, 1000-1147
+Arrays are numpy (J_ext, I_ext, nk) per tile: Fortran element (k, i, j) with
+i in 1-h..im+h sits at [j-1+h, i-1+h, k-1].
+"""
+from __future__ import annotations
+
+import math
+from typing import Dict, List, Tuple
+
+import numpy as np
+
+EPS = 1e-12
+PC = np.array([-9.0, 111.0, 29.0, -3.0]) / 128.0
+QC = np.array([-3.0, 29.0, 111.0, -9.0]) / 128.0
+AC = np.array([5.0, 30.0, -3.0]) / 32.0
+BC = np.array([-3.0, 30.0, 5.0]) / 32.0
+
+
+def def_maxgen(nxm: int, nym: int) -> int:
+    def one(n):
+        g = 1
+        while True:
+            n = (n + 1) // 2
+            g += 1
+            if n == 1:
+                return g
+    return min(one(nxm), one(nym))
+
+
+def radial_stencil(p: int, ampl02: float):
+    """(gx, gy, w) of vrbeta2 with its normalisation (getlinesum2)."""
+    rmom2_2 = 1.0 / math.sqrt(2 * p + 4)
+    e = math.sqrt(1.0 / ampl02) * rmom2_2
+    out = []
+    y = 1.0 / e
+    for gy in range(math.ceil(-y + EPS), math.floor(y - EPS) + 1):
+        rrx = (gy * e) ** 2
+        x = math.sqrt(1.0 - rrx)
+        for gx in range(math.ceil(-x / e + EPS), math.floor(x / e - EPS) + 1):
+            out.append((gx, gy, (1.0 - (rrx + (gx * e) ** 2)) ** p))
+    s = 1.0 / sum(w for _, _, w in out)
+    return [(gx, gy, s * w) for gx, gy, w in out]
+
+
+def line_stencil(p: int, ampl01: float):
+    rmom2_1 = 1.0 / math.sqrt(2 * p + 3)
+    e = (1.0 / math.sqrt(ampl01)) * rmom2_1
+    x = 1.0 / e
+    g = list(range(math.ceil(-x + EPS), math.floor(x - EPS) + 1))
+    w = [(1.0 - (t * e) ** 2) ** p for t in g]
+    s = 1.0 / sum(w)
+    return [(t, s * v) for t, v in zip(g, w)]
+
+
+class Tile:
+    """One rank's array with halo h (same in x and y)."""
+
+    def __init__(self, nk, im, jm, h):
+        self.im, self.jm, self.h = im, jm, h
+        self.a = np.zeros((jm + 2 * h, im + 2 * h, nk))
+
+    def interior(self):
+        h = self.h
+        return self.a[h:h + self.jm, h:h + self.im, :]
+
+
+class Layout:
+    """Tiles of one generation: ntx x nty tiles of im x jm."""
+
+    def __init__(self, ntx, nty, nk, im, jm, h):
+        self.ntx, self.nty = ntx, nty
+        self.t = {(x, y): Tile(nk, im, jm, h) for x in range(ntx) for y in range(nty)}
+
+    def __getitem__(self, k):
+        return self.t[k]
+
+    def keys(self):
+        return self.t.keys()
+
+    # -------------------------------------------------------------- boco_2d
+    def fill(self, nb):
+        """boco_2d: N/S halo rows on interior columns, then E/W halo columns on
+        all rows (incl. halo rows); mirror at the physical edges."""
+        ny, nx = self.nty, self.ntx
+        snap = {k: v.a.copy() for k, v in self.t.items()}
+        for (x, y), T in self.t.items():
+            h, im, jm = T.h, T.im, T.jm
+            ci = slice(h, h + im)
+            for j in range(1, nb + 1):  # south halo row 1-j (j = 1..nb)
+                if y == 0:
+                    T.a[h - j, ci] = snap[(x, y)][h + j - 1, ci]
+                else:
+                    T.a[h - j, ci] = snap[(x, y - 1)][h + jm - j, ci]
+                if y == ny - 1:
+                    T.a[h + jm - 1 + j, ci] = snap[(x, y)][h + jm - j, ci]
+                else:
+                    T.a[h + jm - 1 + j, ci] = snap[(x, y + 1)][h + j - 1, ci]
+        snap = {k: v.a.copy() for k, v in self.t.items()}
+        for (x, y), T in self.t.items():
+            h, im, jm = T.h, T.im, T.jm
+            rj = slice(h - nb, h + jm + nb)
+            for i in range(1, nb + 1):
+                if x == 0:
+                    T.a[rj, h - i] = snap[(x, y)][rj, h + i - 1]
+                else:
+                    T.a[rj, h - i] = snap[(x - 1, y)][rj, h + im - i]
+                if x == nx - 1:
+                    T.a[rj, h + im - 1 + i] = snap[(x, y)][rj, h + im - i]
+                else:
+                    T.a[rj, h + im - 1 + i] = snap[(x + 1, y)][rj, h + i - 1]
+
+    # ------------------------------------------------------------- bocoT_2d
+    def fold(self, nb):
+        """bocoT_2d: E/W halo columns (all rows) added to the neighbour's (or
+        the mirrored own) interior, then N/S halo rows (interior columns)."""
+        ny, nx = self.nty, self.ntx
+        snap = {k: v.a.copy() for k, v in self.t.items()}
+        for (x, y), T in self.t.items():
+            h, im, jm = T.h, T.im, T.jm
+            rj = slice(h - nb, h + jm + nb)
+            for i in range(1, nb + 1):
+                # from west: own west halo (mirror) or the west neighbour's east halo
+                if x == 0:
+                    T.a[rj, h + i - 1] += snap[(x, y)][rj, h - i]
+                else:
+                    T.a[rj, h + i - 1] += snap[(x - 1, y)][rj, h + im - 1 + i]
+                if x == nx - 1:
+                    T.a[rj, h + im - i] += snap[(x, y)][rj, h + im - 1 + i]
+                else:
+                    T.a[rj, h + im - i] += snap[(x + 1, y)][rj, h - i]
+        snap = {k: v.a.copy() for k, v in self.t.items()}
+        for (x, y), T in self.t.items():
+            h, im, jm = T.h, T.im, T.jm
+            ci = slice(h, h + im)
+            for j in range(1, nb + 1):
+                if y == 0:
+                    T.a[h + j - 1, ci] += snap[(x, y)][h - j, ci]
+                else:
+                    T.a[h + j - 1, ci] += snap[(x, y - 1)][h + jm - 1 + j, ci]
+                if y == ny - 1:
+                    T.a[h + jm - j, ci] += snap[(x, y)][h + jm - 1 + j, ci]
+                else:
+                    T.a[h + jm - j, ci] += snap[(x, y + 1)][h - j, ci]
+
+
+def vrbeta2(T: Tile, st):
+    h, im, jm = T.h, T.im, T.jm
+    b = np.zeros_like(T.a)
+    for gx, gy, w in st:
+        b[h:h + jm, h:h + im] += w * T.a[h + gy:h + gy + jm, h + gx:h + gx + im]
+    T.a = b
+
+
+def vrbeta2t(T: Tile, st):
+    h, im, jm = T.h, T.im, T.jm
+    b = np.zeros_like(T.a)
+    src = T.a[h:h + jm, h:h + im]
+    for gx, gy, w in st:
+        b[h + gy:h + gy + jm, h + gx:h + gx + im] += w * src
+    T.a = b
+
+
+def adjoint(F: np.ndarray, quart: bool) -> np.ndarray:
+    """P^T of one tile interior F (jm, im, nk) into the coarse transfer
+    array with halo 2 (1 if quart): returns (jmL+2hb, imL+2hb, nk)."""
+    jm, im, nk = F.shape
+    hb = 1 if quart else 2
+    imL, jmL = im // 2, jm // 2
+    W = np.zeros((jmL + 2 * hb, imL + 2 * hb, nk))
+    P1 = prolong_matrix(im, quart)  # (im, imL+2hb): fine x coarse-with-halo
+    P2 = prolong_matrix(jm, quart)
+    # W = P2^T F P1 (y pass then x pass; same operator as the loops)
+    W += np.einsum("ja,jik,ib->abk", P2, F, P1)
+    return W
+
+
+def prolong_matrix(n: int, quart: bool) -> np.ndarray:
+    """direct1/direct2 coefficients: fine (n) from coarse with halo."""
+    hb = 1 if quart else 2
+    nL = n // 2
+    M = np.zeros((n, nL + 2 * hb))
+    for i in range(1, n + 1):
+        if not quart:
+            iL = i // 2
+            cf = QC if i % 2 else PC
+            for t in range(4):
+                M[i - 1, iL - 1 + t + hb - 1] += cf[t]
+        else:
+            if i % 2:
+                iL, cf = (i + 1) // 2, AC
+            else:
+                iL, cf = i // 2, BC
+            for t in range(3):
+                M[i - 1, iL - 1 + t + hb - 1] += cf[t]
+    return M
+
+
+def direct(W: np.ndarray, im: int, jm: int, quart: bool) -> np.ndarray:
+    P1 = prolong_matrix(im, quart)
+    P2 = prolong_matrix(jm, quart)
+    return np.einsum("ja,abk,ib->jik", P2, W, P1)
+
+
+def vfilter(V: np.ndarray, lm: int, nzcol: int, zst, adj: bool):
+    """sup_vrbeta1[T]_*: columns of lm levels at offsets (c-1)*lm."""
+    hz = max(abs(g) for g, _ in zst)
+    for c in range(nzcol):
+        col = V[..., c * lm:(c + 1) * lm]
+        W = np.zeros(col.shape[:2] + (lm + 2 * hz,))
+        W[..., hz:hz + lm] = col
+        for L in range(1, hz + 1):
+            W[..., hz - L] = W[..., hz + L]
+            W[..., hz + lm - 1 + L] = W[..., hz + lm - 1 - L]
+        B = np.zeros_like(W)
+        if not adj:
+            for g, w in zst:
+                B[..., hz:hz + lm] += w * W[..., hz + g:hz + g + lm]
+        else:
+            for g, w in zst:
+                B[..., hz + g:hz + g + lm] += w * W[..., hz:hz + lm]
+            for L in range(1, hz + 1):
+                B[..., hz + L] += B[..., hz - L]
+                B[..., hz + lm - 1 - L] += B[..., hz + lm - 1 + L]
+        V[..., c * lm:(c + 1) * lm] = B[..., hz:hz + lm]
+
+
+def filtering(x: np.ndarray, *, nxPE, nyPE, im, jm, hx, p, ampl01, ampl02, weights, gm, proc=1, lm=1,
+              nzcol=0, lquart=False, l_filt_g1=True) -> np.ndarray:
+    """Apply filtering_procedure(proc) to the global compact field x
+    (J, I, nk) through the emulated rank tiles; returns the global result."""
+    J, I, nk = x.shape
+    assert I == nxPE * im and J == nyPE * jm
+    h = hx
+    st = radial_stencil(p, ampl02)
+    filt1 = proc == 1 or l_filt_g1
+    hb = 1 if lquart else 2
+    V = x.copy()
+    if nzcol:
+        vfilter(V, lm, nzcol, line_stencil(p, ampl01), adj=True)
+    # generation layouts: gen g has (nxPE >> (g-1)) x (nyPE >> (g-1)) full tiles
+    gens: List[Layout] = []
+    for g in range(gm):
+        ntx, nty = nxPE >> g, nyPE >> g
+        assert ntx >= 1 and nty >= 1 and (ntx << g) == nxPE and (nty << g) == nyPE, "power-of-2 rank layout"
+        gens.append(Layout(ntx, nty, nk, im, jm, h))
+    for (tx, ty) in gens[0].keys():
+        gens[0][(tx, ty)].interior()[...] = V[ty * jm:(ty + 1) * jm, tx * im:(tx + 1) * im]
+    # upsending: adjoint, bocoT with halo 2 on the finer layout, upsend into quadrants
+    for g in range(gm - 1):
+        fine = gens[g]
+        tr = Layout(fine.ntx, fine.nty, nk, im // 2, jm // 2, hb)
+        for k in fine.keys():
+            tr[k].a = adjoint(fine[k].interior(), lquart)
+        tr.fold(hb)
+        coarse = gens[g + 1]
+        for (tx, ty) in fine.keys():
+            q = coarse[(tx // 2, ty // 2)]
+            ox, oy = (tx % 2) * (im // 2), (ty % 2) * (jm // 2)
+            q.interior()[oy:oy + jm // 2, ox:ox + im // 2] = tr[(tx, ty)].interior()
+    # filters at all generations
+    for g in range(gm):
+        if g == 0 and not filt1:
+            continue
+        L = gens[g]
+        for k in L.keys():
+            vrbeta2t(L[k], st)
+        L.fold(h)
+        for k in L.keys():
+            L[k].interior()[...] *= weights[g]
+        L.fill(h)
+        for k in L.keys():
+            vrbeta2(L[k], st)
+    # downsending: coarse quadrants to the finer tiles' transfer arrays, fill halo 2, direct, add
+    for g in range(gm - 1, 0, -1):
+        fine, coarse = gens[g - 1], gens[g]
+        tr = Layout(fine.ntx, fine.nty, nk, im // 2, jm // 2, hb)
+        for (tx, ty) in fine.keys():
+            q = coarse[(tx // 2, ty // 2)]
+            ox, oy = (tx % 2) * (im // 2), (ty % 2) * (jm // 2)
+            tr[(tx, ty)].interior()[...] = q.interior()[oy:oy + jm // 2, ox:ox + im // 2]
+        tr.fill(hb)
+        for k in fine.keys():
+            fine[k].interior()[...] += direct(tr[k].a, im, jm, lquart)
+    out = np.empty_like(V)
+    for (tx, ty) in gens[0].keys():
+        out[ty * jm:(ty + 1) * jm, tx * im:(tx + 1) * im] = gens[0][(tx, ty)].interior()
+    if nzcol:
+        vfilter(out, lm, nzcol, line_stencil(p, ampl01), adj=False)
+    return out
