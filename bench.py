@@ -235,11 +235,8 @@ def run_gpu(args):
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
-    ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    from standalone_mgbf_loc_gb300.sharding import max_over_ranks
+    ms = max_over_ranks(e0.elapsed_time(e1), dev)
     ms_step = ms / args.steps
     value = ws * 2 * pts_op / (ms_step * 1e-3)
 
@@ -288,11 +285,7 @@ def run_gpu(args):
             o.copy_(f, non_blocking=True)
     e3.record(stream)
     torch.cuda.synchronize()
-    ms_e2e = e2.elapsed_time(e3)
-    if dist is not None:
-        t = torch.tensor([ms_e2e], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    ms_e2e = max_over_ranks(e2.elapsed_time(e3), dev)
     e2e_value = ws * 2 * pts_op / (ms_e2e / e2e_steps * 1e-3)
     del host, outs
 
