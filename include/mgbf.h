@@ -169,7 +169,8 @@ int mgbf_destroy(mgbf_handle* h);
  * library is bracketed by CUDA events on its stream and accumulated per
  * stage under the reference's timer names: vfiltT, upsend, hfiltT (first
  * radial pass, with the weighting), hfilt (second radial pass), dnsend,
- * vfilt, plus copy, halo and wgrad.  Process-wide; not for concurrent use
+ * vfilt, dnsend+vfilt (the last prolongation fused with the vertical
+ * forward filter), plus copy, halo and wgrad.  Process-wide; not for concurrent use
  * from several host threads.
  */
 typedef struct mgbf_timer_stat {

@@ -160,8 +160,8 @@ bool make_tmap(CUtensorMap* m, void* base, DType t, int nk, int ncols, int nrows
 
 // ------------------------------------------------------------ stage timers
 
-enum Stage { ST_VFILTT, ST_UPSEND, ST_HFILTT, ST_HFILT, ST_DNSEND, ST_VFILT, ST_COPY, ST_HALO, ST_WGRAD, ST_N };
-const char* kStageNames[ST_N] = {"vfiltT", "upsend", "hfiltT", "hfilt", "dnsend", "vfilt", "copy", "halo", "wgrad"};
+enum Stage { ST_VFILTT, ST_UPSEND, ST_HFILTT, ST_HFILT, ST_DNSEND, ST_VFILT, ST_DNSEND_VFILT, ST_COPY, ST_HALO, ST_WGRAD, ST_N };
+const char* kStageNames[ST_N] = {"vfiltT", "upsend", "hfiltT", "hfilt", "dnsend", "vfilt", "dnsend+vfilt", "copy", "halo", "wgrad"};
 
 struct TimerEvent {
     cudaEvent_t a, b;
@@ -399,6 +399,23 @@ struct Exec {
         return slot.second.get();
     }
 
+    // y = Bz (base + P coarse) for the generation 2 -> 1 step; -1 if the
+    // fused kernel does not cover this shape.
+    int prolong_z(View coarse, View base, View y, int nzcol) {
+        ProlongZArgs z;
+        ProlongArgs& a = z.p;
+        a.coarse = coarse; a.base = base; a.out = y; a.nk = G.nk;
+        a.If = P.I; a.Jf = P.J; a.ntap = P.ix[0].ntap;
+        a.ix = static_cast<const int*>(P.pix[0].p); a.iy = static_cast<const int*>(P.piy[0].p);
+        a.wxp = G.tab[ai()].pwx[0]->p; a.wyp = G.tab[ai()].pwy[0]->p;
+        a.has_base = 1;
+        z.band = G.tab[ai()].zfwd.p; z.lm = G.lm; z.nzk = nzcol * G.lm; z.mz = G.zs.mz;
+        if (z.lm < 2 || z.lm > 256 || z.mz > 8) return -1;  // the fused kernel's limits
+        StageTimer tm(ST_DNSEND_VFILT, stream, pts(0));
+        LK(launch_prolong_z(t, z, stream));
+        return 0;
+    }
+
     int hpass(int g, View in, View out, double scale, int mirror, int stage, int which_in) {
         const int I = gen_I(P, g), J = gen_J(P, g);
         StageTimer tm(stage, stream, pts(g));
@@ -450,16 +467,15 @@ struct Exec {
             if ((rc = hpass(g, B(g), A(g), scales ? scales[g] : 1.0, 0, ST_HFILT, 1))) return rc;
         }
         const bool z = nzcol > 0 && !G.zs.fwd.empty();
-        for (int g = P.gm - 1; g >= 1; --g) {
-            if (g == 1 && !z) {
-                if ((rc = prolong(0, A(1), A(0), y))) return rc;
-            } else {
-                if ((rc = prolong(g - 1, A(g), A(g - 1), A(g - 1)))) return rc;
-            }
-        }
-        if (z) return zstage(A(0), y, false, nzcol, 0);
-        if (P.gm == 1) return zstage(A(0), y, false, 0, 0);
-        return 0;
+        for (int g = P.gm - 1; g >= 2; --g)
+            if ((rc = prolong(g - 1, A(g), A(g - 1), A(g - 1)))) return rc;
+        if (P.gm == 1) return zstage(A(0), y, false, z ? nzcol : 0, 0);
+        if (!z) return prolong(0, A(1), A(0), y);
+        // last prolongation and the vertical forward filter in one pass
+        int r = prolong_z(A(1), A(0), y, nzcol);
+        if (r != -1) return r;
+        if ((rc = prolong(0, A(1), A(0), A(0)))) return rc;
+        return zstage(A(0), y, false, nzcol, 0);
     }
 
     int forward(View x, View y, int nzcol, bool filt1) {

@@ -471,10 +471,17 @@ __device__ __forceinline__ void tma_load_3d(unsigned dst, const void* tmap, int 
         : "memory");
 }
 
+constexpr int kTmaStages = 8;  // rows in flight: kTmaStages - 2
+
+template <int R, int TX, typename T>
+constexpr size_t hmom_tma_stage_bytes() {
+    return (size_t)kTmaStages * (kStageWarps * TX + 2 * R) * 64 * sizeof(T);
+}
+
 template <int R, int P, int TX, typename T>
 __global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
                                                   const __grid_constant__ HMomCoefs2 c) {
-    constexpr int U = kStages;
+    constexpr int U = 4;                           // rows per ring shift
     constexpr int NS = TX + 2 * R;
     constexpr int NR = 2 * R + U;
     constexpr int PQ = P + 1;
@@ -482,7 +489,7 @@ __global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_const
     constexpr int TILE = NC * 64;
     constexpr unsigned TILE_BYTES = TILE * sizeof(T);
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) unsigned long long bars[kStages];
+    __shared__ __align__(8) unsigned long long bars[kTmaStages];
     T* tiles = reinterpret_cast<T*>(smem_raw);
     const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
     const unsigned bbase = (unsigned)__cvta_generic_to_shared(bars);
@@ -495,13 +502,13 @@ __global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_const
     const int nrp = ((nrows + U - 1) / U) * U;  // rows read by the unrolled loop
     if (tid == 0) {
 #pragma unroll
-        for (int s2 = 0; s2 < kStages; ++s2) mbar_init(bbase + 8 * s2, 1);
+        for (int s2 = 0; s2 < kTmaStages; ++s2) mbar_init(bbase + 8 * s2, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
     auto issue = [&](int r) {
         if (tid == 0 && r < nrp) {
-            const int st = r % kStages;
+            const int st = r % kTmaStages;
             const int jr = reflect_half(jb - R + r, a.J);
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_expect_tx(bbase + 8 * st, TILE_BYTES);
@@ -520,33 +527,52 @@ __global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_const
 #pragma unroll
         for (int q = 0; q < TX; ++q) acc[r][q] = make_float2(0.f, 0.f);
 
-    auto row = [&](const int st, const int u) {
-        const T* tp = tiles + st * TILE + warp * TX * 64 + 2 * lane;
-        float2 seg[NS];
+    // Two input rows (ring slots u and u+1) at once: their moment chains are
+    // independent, which doubles the work in flight per warp.
+    auto row2 = [&](const int st0, const int st1, const int u) {
+        const T* tp0 = tiles + st0 * TILE + warp * TX * 64 + 2 * lane;
+        const T* tp1 = tiles + st1 * TILE + warp * TX * 64 + 2 * lane;
+        float2 sa[NS], sb[NS];
 #pragma unroll
-        for (int s2 = 0; s2 < NS; ++s2) seg[s2] = P2<T>::lds(tp + s2 * 64);
+        for (int s2 = 0; s2 < NS; ++s2) {
+            sa[s2] = P2<T>::lds(tp0 + s2 * 64);
+            sb[s2] = P2<T>::lds(tp1 + s2 * 64);
+        }
 #pragma unroll
         for (int q = 0; q < TX; ++q) {
-            float2 t[PQ];
-            t[0] = seg[R + q];
+            float2 ta[PQ], tb[PQ];
+            ta[0] = sa[R + q];
+            tb[0] = sb[R + q];
 #pragma unroll
-            for (int e = 1; e < PQ; ++e) t[e] = make_float2(0.f, 0.f);
+            for (int e = 1; e < PQ; ++e) ta[e] = tb[e] = make_float2(0.f, 0.f);
 #pragma unroll
             for (int m = 0; m <= R; ++m) {
                 if (m > 0) {
-                    const float2 pr = __fadd2_rn(seg[R + q + m], seg[R + q - m]);
-                    t[0] = __fadd2_rn(t[0], pr);
+                    const float2 pa = __fadd2_rn(sa[R + q + m], sa[R + q - m]);
+                    const float2 pb = __fadd2_rn(sb[R + q + m], sb[R + q - m]);
+                    ta[0] = __fadd2_rn(ta[0], pa);
+                    tb[0] = __fadd2_rn(tb[0], pb);
 #pragma unroll
-                    for (int e = 1; e < PQ; ++e) t[e] = __ffma2_rn(c.upow[m * PQ + e], pr, t[e]);
+                    for (int e = 1; e < PQ; ++e) {
+                        ta[e] = __ffma2_rn(c.upow[m * PQ + e], pa, ta[e]);
+                        tb[e] = __ffma2_rn(c.upow[m * PQ + e], pb, tb[e]);
+                    }
                 }
 #pragma unroll
                 for (int gy = 0; gy <= R; ++gy) {
                     if (mcanon<R>(gy) == m) {
-                        float2 v = t[0];
+                        float2 va = ta[0], vb = tb[0];
 #pragma unroll
-                        for (int e = 1; e < PQ; ++e) v = __ffma2_rn(v, c.coef[gy], t[e]);
-                        acc[R + u - gy][q] = __fadd2_rn(acc[R + u - gy][q], v);
-                        if (gy) acc[R + u + gy][q] = __fadd2_rn(acc[R + u + gy][q], v);
+                        for (int e = 1; e < PQ; ++e) {
+                            va = __ffma2_rn(va, c.coef[gy], ta[e]);
+                            vb = __ffma2_rn(vb, c.coef[gy], tb[e]);
+                        }
+                        acc[R + u - gy][q] = __fadd2_rn(acc[R + u - gy][q], va);
+                        acc[R + u + 1 - gy][q] = __fadd2_rn(acc[R + u + 1 - gy][q], vb);
+                        if (gy) {
+                            acc[R + u + gy][q] = __fadd2_rn(acc[R + u + gy][q], va);
+                            acc[R + u + 1 + gy][q] = __fadd2_rn(acc[R + u + 1 + gy][q], vb);
+                        }
                     }
                 }
             }
@@ -554,21 +580,25 @@ __global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_const
     };
 
 #pragma unroll
-    for (int s2 = 0; s2 < kStages - 1; ++s2) issue(s2);
+    for (int s2 = 0; s2 < kTmaStages - 2; ++s2) issue(s2);
     bool failed = false;
     int waited = 0;  // rows whose barrier has been waited
     for (int r0 = 0; r0 < nrp && !failed; r0 += U) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
+        for (int u = 0; u < U; u += 2) {
             const int r = r0 + u;
-            const bool ok = mbar_wait_bounded(bbase + 8 * u, (unsigned)((r / kStages) & 1));
+            const int st0 = r % kTmaStages, st1 = (r + 1) % kTmaStages;
+            const unsigned par = (unsigned)((r / kTmaStages) & 1);  // r even: r, r+1 share a phase
+            const bool ok = mbar_wait_bounded(bbase + 8 * st0, par) && mbar_wait_bounded(bbase + 8 * st1, par);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
             }
-            waited = r + 1;
-            issue(r + kStages - 1);
-            row(u, u);
+            waited = r + 2;
+            // the previous pair's stages are free now
+            issue(r + kTmaStages - 2);
+            issue(r + kTmaStages - 1);
+            row2(st0, st1, u);
         }
         if (failed) break;
         const int jin0 = jb - R + r0;
@@ -602,8 +632,9 @@ __global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_const
         // record, then drain this block's outstanding copies (bounded) before exit
         if (tid == 0) {
             atomicExch(a.status, 1);
-            const int issued = min(nrp, waited + kStages - 1);
-            for (int r = waited; r < issued; ++r) mbar_wait_bounded(bbase + 8 * (r % kStages), (unsigned)((r / kStages) & 1));
+            const int issued = min(nrp, waited + kTmaStages - 2);
+            for (int r = waited; r < issued; ++r)
+                mbar_wait_bounded(bbase + 8 * (r % kTmaStages), (unsigned)((r / kTmaStages) & 1));
         }
         __syncthreads();
     }
@@ -643,16 +674,23 @@ static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t
             dim3 grid2((a.nk + 63) / 64, (nstrip2 + NW - 1) / NW, (a.J + rows - 1) / rows);
             if (a.tmap && a.status) {
                 static_assert(hmom_tma_tx(R) == TX2, "tile shape");
-                constexpr size_t smt = (size_t)kStages * (kStageWarps * TX2 + 2 * R) * 64 * sizeof(T);
-                if (smt > 48 * 1024)
-                    cudaFuncSetAttribute(k_hmom_tma<R, P, TX2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+                constexpr size_t smt = hmom_tma_stage_bytes<R, TX2, T>();
+                // opt in above the default 48 KB (dynamic + the static mbarriers)
+                if (smt + 1024 > 48 * 1024) {
+                    cudaError_t ea = cudaFuncSetAttribute(k_hmom_tma<R, P, TX2, T>,
+                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+                    if (ea != cudaSuccess) return (int)ea;
+                }
                 k_hmom_tma<R, P, TX2, T><<<grid2, block, smt, s>>>(b, *static_cast<const CUtensorMap*>(a.tmap), c2);
                 cudaError_t e = cudaGetLastError();
                 return e == cudaSuccess ? 0 : (int)e;
             }
             constexpr size_t sm2 = hmom_p2_stage_bytes<R, TX2, T>();
-            if (sm2 > 48 * 1024)
-                cudaFuncSetAttribute(k_hmom_p2<R, P, TX2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+            if (sm2 + 1024 > 48 * 1024) {
+                cudaError_t ea = cudaFuncSetAttribute(k_hmom_p2<R, P, TX2, T>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+                if (ea != cudaSuccess) return (int)ea;
+            }
             k_hmom_p2<R, P, TX2, T><<<grid2, block, sm2, s>>>(b, c2);
             cudaError_t e = cudaGetLastError();
             return e == cudaSuccess ? 0 : (int)e;
@@ -661,7 +699,10 @@ static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t
     if (staged) {
         static_assert(NW == kStageWarps, "block shape");
         constexpr size_t sm = hmom_stage_bytes<R, TX, T>();
-        if (sm > 48 * 1024) cudaFuncSetAttribute(k_hmom_st<R, P, TX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (sm + 1024 > 48 * 1024) {
+            cudaError_t ea = cudaFuncSetAttribute(k_hmom_st<R, P, TX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            if (ea != cudaSuccess) return (int)ea;
+        }
         k_hmom_st<R, P, TX, T><<<grid, block, sm, s>>>(b, c);
     } else {
         k_hmom<R, P, TX, U, T><<<grid, block, 0, s>>>(b, c);

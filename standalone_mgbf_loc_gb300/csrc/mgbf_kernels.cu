@@ -451,6 +451,105 @@ __global__ void __launch_bounds__(128) k_prolong4(ProlongArgs a) {
     }
 }
 
+// Fused prolongation + vertical forward filter.  A block owns KT = c*lm
+// consecutive levels (whole z columns, one lane per level) and a 2 x 2PZ
+// block of fine points (PZ column pairs x one row pair): each lane first
+// forms base + P(coarse) for its level at the 4PZ points into shared memory,
+// then applies its band row across the column from shared memory and
+// writes y.  Generation 1 is thereby never written back before the z filter.
+constexpr int PZ = 2;
+template <typename T, int NT, int MZ>
+__global__ void __launch_bounds__(256) k_prolong_z(ProlongZArgs z) {
+    using A = typename AccOf<T>::type;
+    constexpr int O = NT == 4 ? 1 : 0;
+    constexpr int S = NT == 4 ? 2 : 1;
+    constexpr int NC = PZ + NT - 1;
+    constexpr int NP = 4 * PZ;  // fine points per lane: rows h = 0,1 x columns q = 0..2PZ-1
+    extern __shared__ unsigned char smem_raw[];
+    A* buf = reinterpret_cast<A*>(smem_raw);  // [NP][KT]
+    const ProlongArgs& a = z.p;
+    const int KT = blockDim.x;
+    const int tid = threadIdx.x;
+    const int k = blockIdx.x * KT + tid;
+    const bool kv = k < a.nk;
+    const int kk = kv ? k : a.nk - 1;
+    const int Ic = a.If / 2, Jc = a.Jf / 2;
+    const int m0 = blockIdx.y * PZ;
+    const int n = blockIdx.z;
+    // prolongation (x pass inside, y pass outside, as direct1)
+    int ccol[NC];
+#pragma unroll
+    for (int s2 = 0; s2 < NC; ++s2) ccol[s2] = reflect_half(m0 - S + s2, Ic);
+    const T* coarse = static_cast<const T*>(a.coarse.p) + kk;
+    A r0[2 * PZ], r1[2 * PZ];
+#pragma unroll
+    for (int q = 0; q < 2 * PZ; ++q) r0[q] = r1[q] = A(0);
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        const T* row = coarse + a.coarse.sj * reflect_half(n - S + t, Jc);
+        A v[NC];
+#pragma unroll
+        for (int s2 = 0; s2 < NC; ++s2) v[s2] = ldv(row + a.coarse.si * ccol[s2]);
+        const A wy0 = (A)PCoef<NT>::c0(t), wy1 = (A)PCoef<NT>::c1(t);
+#pragma unroll
+        for (int q = 0; q < PZ; ++q) {
+            A x0 = A(0), x1 = A(0);
+#pragma unroll
+            for (int u = 0; u < NT; ++u) {
+                x0 = fma((A)PCoef<NT>::c0(u), v[q + u], x0);
+                x1 = fma((A)PCoef<NT>::c1(u), v[q + u], x1);
+            }
+            r0[2 * q] = fma(wy0, x0, r0[2 * q]);
+            r0[2 * q + 1] = fma(wy0, x1, r0[2 * q + 1]);
+            r1[2 * q] = fma(wy1, x0, r1[2 * q]);
+            r1[2 * q + 1] = fma(wy1, x1, r1[2 * q + 1]);
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int fj = min(max(2 * n - O + h, 0), a.Jf - 1);
+        const T* base = static_cast<const T*>(a.base.p) + a.base.sj * fj + kk;
+#pragma unroll
+        for (int q = 0; q < 2 * PZ; ++q) {
+            const int fi = min(max(2 * m0 - O + q, 0), a.If - 1);
+            const A v = ldc(base + a.base.si * fi) + (h ? r1[q] : r0[q]);
+            buf[(h * 2 * PZ + q) * KT + tid] = v;
+        }
+    }
+    __syncthreads();
+    if (!kv) return;
+    // vertical forward filter from shared memory
+    const bool zc = k < z.nzk;
+    A w[2 * MZ + 1];
+    int off[2 * MZ + 1];
+    {
+        const int L = zc ? k % z.lm : 0;
+        const A* b = static_cast<const A*>(z.band) + (size_t)L * (2 * z.mz + 1) + z.mz;
+#pragma unroll
+        for (int d = -MZ; d <= MZ; ++d) {
+            const bool ok = zc && d >= -z.mz && d <= z.mz && L + d >= 0 && L + d < z.lm;
+            w[d + MZ] = ok ? b[d] : ((!zc && d == 0) ? A(1) : A(0));
+            off[d + MZ] = ok ? tid + d : tid;
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int fj = 2 * n - O + h;
+        if (fj < 0 || fj >= a.Jf) continue;
+        T* out = static_cast<T*>(a.out.p) + a.out.sj * fj + k;
+#pragma unroll
+        for (int q = 0; q < 2 * PZ; ++q) {
+            const int fi = 2 * m0 - O + q;
+            if (fi < 0 || fi >= a.If) continue;
+            const A* col = buf + (h * 2 * PZ + q) * KT;
+            A acc = A(0);
+#pragma unroll
+            for (int d = 0; d < 2 * MZ + 1; ++d) acc = fma(w[d], col[off[d]], acc);
+            stv(out + a.out.si * fi, acc);
+        }
+    }
+}
+
 // ------------------------------------------- direct-sum radial beta filter
 // General support table (any aspect, any integer p): the gather form of
 // fill_h + vrbeta2 (jp_pbfil.f90:888-928).  Because the radial weights are
@@ -664,6 +763,27 @@ int launch_prolong(DType t, const ProlongArgs& a, void* stream) {
     } else {
         MGBF_DISPATCH(t, (k_prolong<T, 3><<<grid, block, 0, s>>>(a)));
     }
+    return last_err();
+}
+
+template <typename T, int MZ>
+static void pzlaunch(const ProlongZArgs& z, int KT, dim3 grid, cudaStream_t s) {
+    const size_t sm = sizeof(typename AccOf<T>::type) * 4 * PZ * KT;
+    if (z.p.ntap == 4) k_prolong_z<T, 4, MZ><<<grid, KT, sm, s>>>(z);
+    else k_prolong_z<T, 3, MZ><<<grid, KT, sm, s>>>(z);
+}
+
+int launch_prolong_z(DType t, const ProlongZArgs& z, void* stream) {
+    const ProlongArgs& a = z.p;
+    if (z.lm < 2 || z.lm > 256 || z.mz > 8 || !a.has_base) return -1;
+    const int KT = (256 / z.lm) * z.lm;
+    const int O = a.ntap == 4 ? 1 : 0;
+    const int npx = a.If / 2 + O, npy = a.Jf / 2 + O;
+    dim3 grid((a.nk + KT - 1) / KT, (npx + PZ - 1) / PZ, npy);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    MGBF_DISPATCH(t, (z.mz <= 2 ? pzlaunch<T, 2>(z, KT, grid, s)
+                      : z.mz <= 4 ? pzlaunch<T, 4>(z, KT, grid, s)
+                      : pzlaunch<T, 8>(z, KT, grid, s)));
     return last_err();
 }
 

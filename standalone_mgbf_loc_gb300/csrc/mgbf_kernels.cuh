@@ -51,6 +51,14 @@ struct ProlongArgs {
     int has_base;
 };
 
+// Fused last prolongation (generation 2 -> 1) and vertical forward filter:
+// y = Bz (base + P coarse).  Blocks cover whole z columns.
+struct ProlongZArgs {
+    ProlongArgs p;      // coarse = generation 2, base = generation 1, out = y
+    const void* band;   // lm x (2mz+1) forward band
+    int lm, nzk, mz;
+};
+
 struct HDirectArgs {
     View in, out;
     int nk, I, J;
@@ -102,6 +110,9 @@ struct DotArgs {
 int launch_zfilter(DType t, const ZArgs& a, void* stream);
 int launch_restrict(DType t, const RestrictArgs& a, void* stream);
 int launch_prolong(DType t, const ProlongArgs& a, void* stream);
+// Returns -1 when the shape is outside the fused kernel's limits (lm > 256 or
+// vertical reach > 8); the caller then runs prolongation and z filter apart.
+int launch_prolong_z(DType t, const ProlongZArgs& a, void* stream);
 int launch_hdirect(DType t, const HDirectArgs& a, void* stream);
 int launch_mirror_x(DType t, View v, int nk, int I, int J, int hx, void* stream);
 int launch_copy(DType t, View in, View out, int nk, int I, int J, int mirror_hx, void* stream);

@@ -17,7 +17,7 @@ CASES = {
 def case_config(name) -> MGBFConfig:
     kw, _, _, _ = CASES[name]
     d = dict(nxPE=4, nyPE=4, im_filt=8, jm_filt=8, gm_max=3, hx=4, hy=4, hz=1, p=2,
-             mg_ampl02=canonical(4), mg_ampl01=canonical_z(1), mg_ampl03=0.5,
+             mg_ampl02=canonical(4), mg_ampl01=canonical_z(1), mg_ampl03=0.3,
              mg_weig1=1.0, mg_weig2=0.5, mg_weig3=0.25, layout=1)
     d.update(kw)
     return MGBFConfig(**d)

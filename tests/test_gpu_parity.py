@@ -46,6 +46,19 @@ def test_parity_moment_kernel(lib, cuda, dtype, proc, lquart):
     assert rel_l2(y, ref) < TOL[dtype]
 
 
+@pytest.mark.parametrize("h", [5, 8, 10, 12, 16, 24])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32, torch.bfloat16])
+def test_parity_moment_kernel_reaches(lib, cuda, h, dtype):
+    """Every compiled reach (the larger ones use > 48 KB of shared memory)."""
+    c = small_config(nxPE=4, nyPE=4, im_filt=48 if h < 24 else 96, jm_filt=48 if h < 24 else 96, lm=8, km3=1,
+                     gm_max=3, hx=h, hy=h, hz=2, mg_ampl02=canonical(h), mg_ampl01=canonical_z(2))
+    op = MGBF(c)
+    assert op.dims.hbeta_kernel == 1 and op.dims.reach_h == h
+    x = compact_input(op, h)
+    y = run_gpu(op, 1, x, dtype, cuda)
+    assert rel_l2(y, O.filter_compact(oracle_cfg(c, 1), x)) < TOL[dtype]
+
+
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 @pytest.mark.parametrize("ampl02", [2.0, 2.5, 1.3])
 def test_parity_direct_kernel(lib, cuda, dtype, ampl02):
