@@ -221,6 +221,31 @@ int mgbf_batch_destroy(mgbf_batch* b);
 /* As mgbf_status, for a batch. */
 int mgbf_batch_status(mgbf_batch* b);
 
+/* ------------------------------------------------------------------------
+ * Allocation-free radial filtering (no counterpart in the reference).
+ *
+ * For callers that cannot allocate device memory -- work being captured
+ * into a CUDA graph, applications whose device memory is all handed out by
+ * their own pool, fixed memory budgets -- this computes
+ *     y = weight * B(B(x))
+ * on one compact FP32 field x (nk, im, jm) (level index fastest), where B is
+ * the radial beta filter with half-sample mirror boundaries: the
+ * generation-1 filtering of filtering_procedure with one generation and no
+ * vertical filter.  x and y are device pointers supplied by the caller (y may
+ * equal x).  Its two intermediate fields live in a static device array of
+ * 2 * MGBF_NOALLOC_MAX_ELEMS floats (64 MiB) that every GPU loading the
+ * library holds until exit; nk*(im+2*(reach+8))*jm must not exceed
+ * MGBF_NOALLOC_MAX_ELEMS, larger fields return MGBF_ERR_ARG.  The radial
+ * support must be the disk of radius reach+1/2 with p = 2 and a compiled
+ * reach (4,5,6,8,10,12,16,24), else MGBF_ERR_UNSUPPORTED.  The first call on
+ * a device looks up the array's device address and should come before any
+ * stream capture.  Calls share the array, so calls that overlap on the GPU
+ * race and must be ordered by the caller.  Asynchronous on `stream`.
+ */
+#define MGBF_NOALLOC_MAX_ELEMS ((size_t)8 << 20)
+int mgbf_radial_filter_noalloc(const float* x, float* y, int nk, int im, int jm, int p, double mg_ampl02,
+                               int hx, int hy, double weight, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

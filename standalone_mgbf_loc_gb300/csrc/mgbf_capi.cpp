@@ -34,10 +34,10 @@ using namespace mgbf;
 
 namespace {
 
-thread_local std::string g_last_error;
+thread_local char g_last_error[512];
 
 int fail(int code, const std::string& msg) {
-    g_last_error = msg;
+    std::snprintf(g_last_error, sizeof g_last_error, "%s", msg.c_str());
     return code;
 }
 
@@ -757,6 +757,13 @@ int parse_namelist_text(const std::string& text, mgbf_config* c, std::string& er
 
 }  // namespace
 
+namespace mgbf {
+int report_error(int code, const char* msg) {
+    std::snprintf(g_last_error, sizeof g_last_error, "%s", msg);
+    return code;
+}
+}  // namespace mgbf
+
 // ===================================================================== ABI
 
 extern "C" {
@@ -778,7 +785,7 @@ const char* mgbf_strerror(int code) {
     }
 }
 
-const char* mgbf_last_error(void) { return g_last_error.c_str(); }
+const char* mgbf_last_error(void) { return g_last_error; }
 
 int mgbf_config_init(mgbf_config* c) {
     if (!c) return fail(MGBF_ERR_ARG, "null config");

@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(128) k_hmom_st(HMomArgs a,
     constexpr int CH = 32 * (int)sizeof(T) / 16;   // 16-byte chunks per column
     constexpr int TILE = NC * 32;                  // elements per tile
     constexpr int EPC = 16 / (int)sizeof(T);       // elements per chunk
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     T* tiles = reinterpret_cast<T*>(smem_raw);
     const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
     const int lane = threadIdx.x, warp = threadIdx.y, tid = warp * 32 + lane;
@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(128) k_hmom_p2(HMomArgs a, const __grid_consta
     constexpr int CH = CB / 16;
     constexpr int TILE = NC * 64;
     constexpr int EPC = 16 / (int)sizeof(T);
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     T* tiles = reinterpret_cast<T*>(smem_raw);
     const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
     const int lane = threadIdx.x, warp = threadIdx.y, tid = warp * 32 + lane;

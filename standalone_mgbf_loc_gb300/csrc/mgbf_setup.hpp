@@ -61,4 +61,8 @@ int check_other_reaches(int p, double ampl02, double ampl03, int hx, int hy, int
 // Canonical row half-width of a disk of radius R + 1/2.
 int canonical_width(int R, int gy);
 
+// Sets the calling thread's mgbf_last_error() message (no heap use) and
+// returns code.
+int report_error(int code, const char* msg);
+
 }  // namespace mgbf
