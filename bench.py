@@ -201,6 +201,7 @@ def run_gpu(args):
     members = args.members
     gdesc = groups(members)
     batch = MGBFBatch(IM, JM, GM, WEIGHTS, gdesc)
+    batch.use_graphs(True)  # each repeated fwd / adj call replays one captured CUDA graph
     gen = torch.Generator(device=dev)
     gen.manual_seed(1000 + rank)
     fields = [torch.randn((JM, IM, g.nk), generator=gen, device=dev, dtype=torch.float32) for g in gdesc]
@@ -257,37 +258,55 @@ def run_gpu(args):
     s = 4  # bytes per FP32 element
     achieved = (2 * s * h_pts) / (h_ms * 1e-3) / 1e9 if h_ms > 0 else None
     stage_ms = {k: round(v[1] / nstep_t, 3) for k, v in stats.items()}
+    # FP32-pipe roofline of the radial kernel: the moment form costs 8R+3
+    # scalar FP operations (adds or multiply-adds) per grid point and pass
+    gen_pts = sum((IM >> g) * (JM >> g) for g in range(GM))
+    fp_ops = sum(g.nk * gen_pts * (8 * g.hx + 3) for g in gdesc) * 2 * 2 * nstep_t  # 2 passes, fwd+adj
+    fp_peak = 152 * 128 * 2.07e9  # SMs x FP32 lanes x max SM clock (one op per lane per cycle)
     # DRAM traffic of the radial kernel per grid point and pass, from the ncu
     # capture summarised in profiles/ (None until measured).
     traffic_per_pt = HMOM_DRAM_BYTES_PER_POINT
     traffic = (traffic_per_pt * h_pts / h_launch) if (traffic_per_pt and h_launch) else None
 
-    # end to end: pinned host fields -> device, forward + adjoint, device -> host
+    # end to end through the host-streaming pipeline: every step copies the
+    # whole field set from pinned host memory, filters it forward and adjoint,
+    # and copies the result back; two device sets and three streams let the
+    # copies of neighbouring steps overlap the filtering
+    from standalone_mgbf_loc_gb300.pipeline import HostStream
     host = [f.to("cpu").pin_memory() for f in fields]
-    outs = [torch.empty_like(h).pin_memory() for h in host]
-    h2d = sum(h.numel() * h.element_size() for h in host)
-    e2e_steps = max(1, min(args.steps, 5))
-    for _ in range(1):
-        for h, f in zip(host, fields):
-            f.copy_(h, non_blocking=True)
-        step()
-        for o, f in zip(outs, fields):
-            o.copy_(f, non_blocking=True)
+    outs = [torch.empty(h.shape, dtype=h.dtype).pin_memory() for h in host]
+    del fields
+    torch.cuda.empty_cache()
+    hs = HostStream(batch, torch.float32, dev, ops=("fwd", "adj"))
+    h2d = hs.bytes_per_step()
+    e2e_steps = max(2, args.steps)
+    for _ in range(2):
+        hs.submit(host, outs)
+    hs.finish()
     torch.cuda.synchronize()
     barrier()
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e2.record(stream)
+    e2.record(hs.s_h2d)
     for _ in range(e2e_steps):
-        for h, f in zip(host, fields):
-            f.copy_(h, non_blocking=True)
-        step()
-        for o, f in zip(outs, fields):
-            o.copy_(f, non_blocking=True)
-    e3.record(stream)
+        hs.submit(host, outs)
+    e3.record(hs.s_d2h)
+    hs.finish()
     torch.cuda.synchronize()
     ms_e2e = max_over_ranks(e2.elapsed_time(e3), dev)
     e2e_value = ws * 2 * pts_op / (ms_e2e / e2e_steps * 1e-3)
-    del host, outs
+    # copy bandwidth of one whole field set, each direction alone
+    c0, c1, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    with torch.cuda.stream(hs.s_h2d):
+        c0.record(hs.s_h2d)
+        for d, h in zip(hs.sets[0], host):
+            d.copy_(h, non_blocking=True)
+        c1.record(hs.s_h2d)
+        for d, h in zip(hs.sets[0], outs):
+            h.copy_(d, non_blocking=True)
+        c2.record(hs.s_h2d)
+    torch.cuda.synchronize()
+    copy_gbs = {"h2d": h2d / (c0.elapsed_time(c1) * 1e-3) / 1e9, "d2h": h2d / (c1.elapsed_time(c2) * 1e-3) / 1e9}
+    del host, outs, hs
 
     extras = {}
     if rank == 0 and not args.no_extras:
@@ -321,10 +340,17 @@ def run_gpu(args):
                          "peak_source": peak_kind,
                          "algorithmic_bytes": "2 x 4 B per grid point per launch (read + write, FP32)",
                          "launches": h_launch / nstep_t, "avg_launch_ms": h_ms / h_launch if h_launch else None},
+            "compute_roofline": {"bound": "fp32_pipe", "kernel": "k_hmom_tma",
+                                 "achieved": fp_ops / (h_ms * 1e-3) if h_ms else None, "peak": fp_peak,
+                                 "unit": "FP32 ops/s", "frac": fp_ops / (h_ms * 1e-3) / fp_peak if h_ms else None,
+                                 "ops_per_point_pass": "8R+3 (moment form; the direct disk sum costs ~pi R^2)"},
+            "step_hbm_frac": (4 * 4 * pts_op) / (ms_step * 1e-3) / (peak * 1e9),
             "stages_ms_per_step": stage_ms,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-                    "steps": e2e_steps},
+                    "steps": e2e_steps, "ms_per_step": ms_e2e / e2e_steps, "copy_gbs": copy_gbs,
+                    "pipeline": "pinned host -> device, fwd+adj, device -> host per step; uploads, filtering "
+                                "and downloads of adjacent steps overlap (two device field sets, three streams)"},
             "gpu_launches": int(round(launches_per_step * args.steps)),
             "clocks": clk.summary(),
             "rel_l2_vs_oracle": rel,

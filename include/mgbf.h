@@ -218,6 +218,11 @@ int mgbf_batch_create(int im, int jm, int gm, const double* weights, int lquart,
  * adjoint != 0 runs the transposed chain. */
 int mgbf_batch_apply(mgbf_batch* b, void* const* fields, int dtype, int adjoint, void* stream);
 int mgbf_batch_destroy(mgbf_batch* b);
+/* enable != 0: replay each distinct call (same field pointers, dtype and
+ * direction) as one CUDA graph, captured on its first call after the
+ * batch's device memory exists (the first call of a dtype runs directly);
+ * graphs are bypassed while stage timers are on.  0 releases the graphs. */
+int mgbf_batch_use_graphs(mgbf_batch* b, int enable);
 /* As mgbf_status, for a batch. */
 int mgbf_batch_status(mgbf_batch* b);
 

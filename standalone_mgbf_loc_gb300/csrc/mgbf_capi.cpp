@@ -501,6 +501,19 @@ struct mgbf_handle {
 struct mgbf_batch {
     Plan plan;
     bool filt1 = true;
+    // CUDA-graph replay of the launch sequence (mgbf_batch_use_graphs)
+    bool use_graphs = false;
+    struct GraphEntry {
+        int dtype, adjoint;
+        std::vector<void*> fields;
+        cudaGraphExec_t exec;
+    };
+    std::vector<GraphEntry> graphs;
+    cudaStream_t cap_stream = nullptr;
+    ~mgbf_batch() {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
+        if (cap_stream) cudaStreamDestroy(cap_stream);
+    }
 };
 
 namespace {
@@ -1120,26 +1133,75 @@ int mgbf_batch_create(int im, int jm, int gm, const double* weights, int lquart,
     return MGBF_OK;
 }
 
+static int batch_launch(mgbf_batch* b, void* const* fields, DType t, void* stream) {
+    Plan& P = b->plan;
+    int rc;
+    for (size_t q = 0; q < P.groups.size(); ++q) {
+        Group& G = P.groups[q];
+        View v;
+        v.p = fields[q]; v.si = G.nk; v.sj = (long long)G.nk * P.I;
+        Exec ex{P, G, t, stream};
+        const int nzcol = (G.lm > 1) ? G.nzcol : 0;
+        if ((rc = ex.forward(v, v, nzcol, b->filt1))) return rc;
+    }
+    return MGBF_OK;
+}
+
 int mgbf_batch_apply(mgbf_batch* b, void* const* fields, int dtype, int adjoint, void* stream) {
-    (void)adjoint;  // the transposed chain issues the same launches (see mgbf_filtering_procedure_adjoint)
+    // the transposed chain issues the same launches (see mgbf_filtering_procedure_adjoint)
     if (!b || !fields) return fail(MGBF_ERR_ARG, "null argument");
     if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");
     DeviceGuard dg(b->plan.device);
     const DType t = (DType)dtype;
     Plan& P = b->plan;
     int rc;
+    const size_t ng = P.groups.size();
+    for (size_t q = 0; q < ng; ++q)
+        if (!fields[q]) return fail(MGBF_ERR_ARG, "null field pointer");
+    bool first_use = false;
     for (auto& G : P.groups) {
+        if (!G.tab[t == DType::F64 ? 1 : 0].ready || G.bufs[(int)t].A.empty()) first_use = true;
         if ((rc = ensure_tables(P, G, t))) return rc;
         if ((rc = ensure_bufs(P, G, t, false))) return rc;
     }
-    for (size_t q = 0; q < P.groups.size(); ++q) {
-        Group& G = P.groups[q];
-        if (!fields[q]) return fail(MGBF_ERR_ARG, "null field pointer");
-        View v;
-        v.p = fields[q]; v.si = G.nk; v.sj = (long long)G.nk * P.I;
-        Exec ex{P, G, t, stream};
-        const int nzcol = (G.lm > 1) ? G.nzcol : 0;
-        if ((rc = ex.forward(v, v, nzcol, b->filt1))) return rc;
+    if (!b->use_graphs || g_timers.on || first_use) return batch_launch(b, fields, t, stream);
+    // replay a captured graph of this exact launch sequence, capturing it on first use
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    for (auto& g : b->graphs)
+        if (g.dtype == dtype && g.adjoint == (adjoint != 0) &&
+            std::equal(g.fields.begin(), g.fields.end(), fields)) {
+            CU(cudaGraphLaunch(g.exec, s));
+            return MGBF_OK;
+        }
+    if (!b->cap_stream) CU(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
+    CU(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
+    rc = batch_launch(b, fields, t, b->cap_stream);
+    cudaGraph_t graph = nullptr;
+    cudaError_t ec = cudaStreamEndCapture(b->cap_stream, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture");
+    mgbf_batch::GraphEntry e;
+    e.dtype = dtype;
+    e.adjoint = adjoint != 0;
+    e.fields.assign(fields, fields + ng);
+    ec = cudaGraphInstantiate(&e.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ec != cudaSuccess) return cuda_fail(ec, "cudaGraphInstantiate");
+    b->graphs.push_back(e);
+    CU(cudaGraphLaunch(e.exec, s));
+    return MGBF_OK;
+}
+
+int mgbf_batch_use_graphs(mgbf_batch* b, int enable) {
+    if (!b) return fail(MGBF_ERR_ARG, "null handle");
+    DeviceGuard dg(b->plan.device);
+    b->use_graphs = enable != 0;
+    if (!b->use_graphs) {
+        for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+        b->graphs.clear();
     }
     return MGBF_OK;
 }

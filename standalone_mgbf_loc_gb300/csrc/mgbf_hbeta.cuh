@@ -643,6 +643,18 @@ __global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_const
 // Columns per thread of the packed kernels.
 constexpr int hmom_p2_tx(int R) { return hmom_tma_tx(R); }
 
+// Opts a kernel into more than 48 KB of dynamic shared memory, once per
+// device (the attribute persists, so graph captures later need no API call).
+template <typename K>
+static cudaError_t smem_optin(K kernel, size_t bytes, unsigned long long& done /* one bit per device */) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (done >> dev & 1ull) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) done |= 1ull << dev;
+    return e;
+}
+
 template <int R, int P, typename T>
 static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t s) {
     using A = typename AccOf<T>::type;
@@ -677,8 +689,8 @@ static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t
                 constexpr size_t smt = hmom_tma_stage_bytes<R, TX2, T>();
                 // opt in above the default 48 KB (dynamic + the static mbarriers)
                 if (smt + 1024 > 48 * 1024) {
-                    cudaError_t ea = cudaFuncSetAttribute(k_hmom_tma<R, P, TX2, T>,
-                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+                    static unsigned long long done = 0;  // per instantiation
+                    cudaError_t ea = smem_optin(k_hmom_tma<R, P, TX2, T>, smt, done);
                     if (ea != cudaSuccess) return (int)ea;
                 }
                 k_hmom_tma<R, P, TX2, T><<<grid2, block, smt, s>>>(b, *static_cast<const CUtensorMap*>(a.tmap), c2);
@@ -687,8 +699,8 @@ static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t
             }
             constexpr size_t sm2 = hmom_p2_stage_bytes<R, TX2, T>();
             if (sm2 + 1024 > 48 * 1024) {
-                cudaError_t ea = cudaFuncSetAttribute(k_hmom_p2<R, P, TX2, T>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+                static unsigned long long done = 0;  // per instantiation
+                cudaError_t ea = smem_optin(k_hmom_p2<R, P, TX2, T>, sm2, done);
                 if (ea != cudaSuccess) return (int)ea;
             }
             k_hmom_p2<R, P, TX2, T><<<grid2, block, sm2, s>>>(b, c2);
@@ -700,7 +712,8 @@ static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t
         static_assert(NW == kStageWarps, "block shape");
         constexpr size_t sm = hmom_stage_bytes<R, TX, T>();
         if (sm + 1024 > 48 * 1024) {
-            cudaError_t ea = cudaFuncSetAttribute(k_hmom_st<R, P, TX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            static unsigned long long done = 0;  // per instantiation
+            cudaError_t ea = smem_optin(k_hmom_st<R, P, TX, T>, sm, done);
             if (ea != cudaSuccess) return (int)ea;
         }
         k_hmom_st<R, P, TX, T><<<grid, block, sm, s>>>(b, c);

@@ -309,6 +309,10 @@ class MGBFBatch:
     def status(self) -> None:
         _abi.check(self._lib.mgbf_batch_status(self._h), "mgbf_batch_status")
 
+    def use_graphs(self, enable: bool = True) -> None:
+        """Replay repeated calls on the same fields as captured CUDA graphs."""
+        _abi.check(self._lib.mgbf_batch_use_graphs(self._h, int(enable)), "mgbf_batch_use_graphs")
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.mgbf_batch_destroy(self._h)
