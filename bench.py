@@ -363,9 +363,11 @@ def run_gpu(args):
     return 0
 
 
-# Measured DRAM bytes per grid point and pass of k_hmom (profiles/); None if
-# not yet measured.
-HMOM_DRAM_BYTES_PER_POINT = None
+# DRAM bytes (read + write) per grid point and pass of the radial moment
+# kernel, from the ncu capture summarised in
+# profiles/k_hmom_tma_reach8_8members_512sq.md (1116.2 MB for 134.2 M points,
+# FP32); traffic grows in proportion to the points a launch processes.
+HMOM_DRAM_BYTES_PER_POINT = 8.32
 
 
 def plain_forward(torch, dev, dtype):
