@@ -201,6 +201,8 @@ def run_gpu(args):
     members = args.members
     gdesc = groups(members)
     batch = MGBFBatch(IM, JM, GM, WEIGHTS, gdesc)
+    if not args.no_autotune:
+        batch.autotune(torch.float32)  # radial-kernel variant and tile height per generation and pass
     batch.use_graphs(True)  # each repeated fwd / adj call replays one captured CUDA graph
     gen = torch.Generator(device=dev)
     gen.manual_seed(1000 + rank)
@@ -406,6 +408,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--members", type=int, default=80)
     ap.add_argument("--no-extras", action="store_true", help="skip the plain-forward and CPU-baseline legs")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default radial-kernel tiles")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -156,6 +156,14 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
  * Synchronises with the device and clears the status. */
 int mgbf_status(mgbf_handle* h);
 
+/* Autotuner of tile shapes: times the radial-filter kernel variants (TMA
+ * pipelines of one or two rows per barrier, cp.async staging) and output
+ * rows per block for every generation and pass of the handle, on the
+ * handle's own scratch buffers, and keeps the fastest for later calls.
+ * Synchronous; needs no field.  The choice changes results only by
+ * rounding (summation order). */
+int mgbf_autotune(mgbf_handle* h, int dtype, void* stream);
+
 /* Replace the per-generation weights a_1..a_n (n <= gm) without rebuilding. */
 int mgbf_set_weights(mgbf_handle* h, const double* a, int n);
 
@@ -225,6 +233,8 @@ int mgbf_batch_destroy(mgbf_batch* b);
 int mgbf_batch_use_graphs(mgbf_batch* b, int enable);
 /* As mgbf_status, for a batch. */
 int mgbf_batch_status(mgbf_batch* b);
+/* As mgbf_autotune, for a batch (releases graphs captured before). */
+int mgbf_batch_autotune(mgbf_batch* b, int dtype, void* stream);
 
 /* ------------------------------------------------------------------------
  * Allocation-free radial filtering (no counterpart in the reference).

@@ -246,6 +246,9 @@ struct Group {
     // each with the base address it was encoded for
     std::map<int, std::pair<void*, std::unique_ptr<CUtensorMap>>> tmaps;
     std::map<int, void*> tmap_failed;
+    // autotuned radial-kernel choice per (dtype, generation, pass):
+    // key = dtype*1024 + g*2 + pass -> (kernel variant, output rows per block)
+    std::map<int, std::pair<int, int>> tune;
 };
 
 struct Plan {
@@ -416,24 +419,42 @@ struct Exec {
         return 0;
     }
 
+    bool moment_path() const { return G.hs.canonical && hmom_available(t, G.hs.R, G.hs.p); }
+
+    // Default output rows per block of the moment kernel: enough blocks for
+    // about 24 warps per SM, at least 4R rows so the 2R halo rows stay cheap.
+    int default_rows(int g) const {
+        const int I = gen_I(P, g), J = gen_J(P, g);
+        const int tx = hmom_tx_for((int)acc_size(t), G.hs.R);
+        const long long w0 = (long long)((G.nk + 31) / 32) * ((I + tx - 1) / tx);
+        const long long nz = (152LL * 24 + w0 - 1) / w0;
+        const int rows = (int)((J + nz - 1) / nz);
+        return std::max(rows, std::min(J, 4 * G.hs.R));
+    }
+
+    int hmom(int g, View in, View out, double scale, int mirror, int which_in, int variant, int rows) {
+        HMomArgs a;
+        a.in = in; a.out = out; a.nk = G.nk; a.I = gen_I(P, g); a.J = gen_J(P, g);
+        a.mirror_hx = mirror; a.scale = scale * G.hs.s; a.halo = G.HXP;
+        a.tmap = tmap(g, which_in);
+        a.status = static_cast<int*>(P.status.p);
+        a.variant = variant;
+        a.rows = rows;
+        LK(launch_hmom(t, G.hs.R, G.hs.p, a, G.hs.mom, stream));
+        return 0;
+    }
+
     int hpass(int g, View in, View out, double scale, int mirror, int stage, int which_in) {
         const int I = gen_I(P, g), J = gen_J(P, g);
         StageTimer tm(stage, stream, pts(g));
-        if (G.hs.canonical && hmom_available(t, G.hs.R, G.hs.p)) {
-            HMomArgs a;
-            a.in = in; a.out = out; a.nk = G.nk; a.I = I; a.J = J;
-            a.mirror_hx = mirror; a.scale = scale * G.hs.s; a.halo = G.HXP;
-            a.tmap = tmap(g, which_in);
-            a.status = static_cast<int*>(P.status.p);
-            const int tx = hmom_tx_for((int)acc_size(t), G.hs.R);
-            const long long w0 = (long long)((G.nk + 31) / 32) * ((I + tx - 1) / tx);
-            const long long target = 152LL * 24;
-            long long nz = (target + w0 - 1) / w0;
-            int rows = (int)((J + nz - 1) / nz);
-            rows = std::max(rows, std::min(J, 4 * G.hs.R));
-            a.rows = rows;
-            LK(launch_hmom(t, G.hs.R, G.hs.p, a, G.hs.mom, stream));
-            return 0;
+        if (moment_path()) {
+            int variant = 0, rows = default_rows(g);
+            auto it = G.tune.find((int)t * 1024 + g * 2 + which_in);
+            if (it != G.tune.end()) {
+                variant = it->second.first;
+                rows = it->second.second;
+            }
+            return hmom(g, in, out, scale, mirror, which_in, variant, rows);
         }
         HDirectArgs a;
         a.in = in; a.out = out; a.nk = G.nk; a.I = I; a.J = J; a.R = G.hs.R;
@@ -1048,6 +1069,60 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
     return 0;
 }
 
+static int read_status(Plan& P);
+
+// Times the radial-kernel variants and block heights of every generation and
+// pass on the plan's own buffers (zeroed first) and keeps the fastest.
+static int autotune_plan(Plan& P, DType t, void* stream) {
+    int rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    for (auto& G : P.groups) {
+        if ((rc = ensure_tables(P, G, t)) || (rc = ensure_bufs(P, G, t, false))) return rc;
+        Exec ex{P, G, t, stream};
+        if (!ex.moment_path()) continue;
+        for (int g = 0; g < P.gm; ++g) {
+            CU(cudaMemsetAsync(G.bufs[(int)t].A[g]->p, 0, G.bufs[(int)t].A[g]->bytes, s));
+            CU(cudaMemsetAsync(G.bufs[(int)t].B[g]->p, 0, G.bufs[(int)t].B[g]->bytes, s));
+        }
+        for (int g = 0; g < P.gm; ++g)
+            for (int pass = 0; pass < 2; ++pass) {
+                const int J = gen_J(P, g);
+                const int r0 = ex.default_rows(g);
+                std::vector<int> rows = {r0, J, std::max((J + 1) / 2, std::min(J, 4 * G.hs.R)),
+                                         std::max((J + 3) / 4, std::min(J, 4 * G.hs.R))};
+                std::sort(rows.begin(), rows.end());
+                rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
+                const int nvar = t == DType::F64 ? 1 : kHMomVariants;
+                View in = pass ? ex.B(g) : ex.A(g), out = pass ? ex.A(g) : ex.B(g);
+                float best = 1e30f;
+                std::pair<int, int> choice(0, r0);
+                for (int v = 0; v < nvar; ++v)
+                    for (int r : rows) {
+                        if ((rc = ex.hmom(g, in, out, 1.0, pass ? 0 : G.hs.R, pass, v, r))) return rc;  // warm
+                        CU(cudaEventRecord(e0, s));
+                        for (int rep = 0; rep < 3; ++rep)
+                            if ((rc = ex.hmom(g, in, out, 1.0, pass ? 0 : G.hs.R, pass, v, r))) return rc;
+                        CU(cudaEventRecord(e1, s));
+                        CU(cudaEventSynchronize(e1));
+                        float ms = 0.f;
+                        CU(cudaEventElapsedTime(&ms, e0, e1));
+                        if (ms < best) {
+                            best = ms;
+                            choice = {v, r};
+                        }
+                    }
+                G.tune[(int)t * 1024 + g * 2 + pass] = choice;
+            }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CU(cudaStreamSynchronize(s));
+    return read_status(P);
+}
+
 static int read_status(Plan& P) {
     if (!P.status.p) return MGBF_OK;
     DeviceGuard dg(P.device);
@@ -1068,6 +1143,22 @@ int mgbf_status(mgbf_handle* h) {
 int mgbf_batch_status(mgbf_batch* b) {
     if (!b) return fail(MGBF_ERR_ARG, "null handle");
     return read_status(b->plan);
+}
+
+int mgbf_autotune(mgbf_handle* h, int dtype, void* stream) {
+    if (!h) return fail(MGBF_ERR_ARG, "null handle");
+    if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");
+    DeviceGuard dg(h->plan.device);
+    return autotune_plan(h->plan, (DType)dtype, stream);
+}
+
+int mgbf_batch_autotune(mgbf_batch* b, int dtype, void* stream) {
+    if (!b) return fail(MGBF_ERR_ARG, "null handle");
+    if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");
+    DeviceGuard dg(b->plan.device);
+    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);  // captured with the old choices
+    b->graphs.clear();
+    return autotune_plan(b->plan, (DType)dtype, stream);
 }
 
 int mgbf_timers_enable(int on) {

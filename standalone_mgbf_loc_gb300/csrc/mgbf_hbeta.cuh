@@ -640,6 +640,147 @@ __global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_const
     }
 }
 
+// Single-row variant of the TMA kernel (4-deep ring, one input row per
+// barrier): fewer registers, more blocks per SM; the autotuner picks
+// between the two.
+template <int R, int P, int TX, typename T>
+__global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
+                                                  const __grid_constant__ HMomCoefs2 c) {
+    constexpr int U = kStages;
+    constexpr int NS = TX + 2 * R;
+    constexpr int NR = 2 * R + U;
+    constexpr int PQ = P + 1;
+    constexpr int NC = kStageWarps * TX + 2 * R;
+    constexpr int TILE = NC * 64;
+    constexpr unsigned TILE_BYTES = TILE * sizeof(T);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long bars[kStages];
+    T* tiles = reinterpret_cast<T*>(smem_raw);
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const unsigned bbase = (unsigned)__cvta_generic_to_shared(bars);
+    const int lane = threadIdx.x, warp = threadIdx.y, tid = warp * 32 + lane;
+    const int k0 = blockIdx.x * 64;
+    const int ib = blockIdx.y * (kStageWarps * TX);
+    const int jb = blockIdx.z * a.rows;
+    const int je = min(jb + a.rows, a.J);
+    const int nrows = je - jb + 2 * R;
+    const int nrp = ((nrows + U - 1) / U) * U;  // rows read by the unrolled loop
+    if (tid == 0) {
+#pragma unroll
+        for (int s2 = 0; s2 < kStages; ++s2) mbar_init(bbase + 8 * s2, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int r) {
+        if (tid == 0 && r < nrp) {
+            const int st = r % kStages;
+            const int jr = reflect_half(jb - R + r, a.J);
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            mbar_expect_tx(bbase + 8 * st, TILE_BYTES);
+            tma_load_3d(sbase + st * TILE_BYTES, &tmap, k0, ib - R + a.halo, jr, bbase + 8 * st);
+        }
+    };
+
+    const int i0 = ib + warp * TX;
+    const int kl = k0 + 2 * lane;
+    const bool kv = kl < a.nk;
+    T* outb = static_cast<T*>(a.out.p) + kl;
+    const float2 scale = make_float2((float)a.scale, (float)a.scale);
+    float2 acc[NR][TX];
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+#pragma unroll
+        for (int q = 0; q < TX; ++q) acc[r][q] = make_float2(0.f, 0.f);
+
+    auto row = [&](const int st, const int u) {
+        const T* tp = tiles + st * TILE + warp * TX * 64 + 2 * lane;
+        float2 seg[NS];
+#pragma unroll
+        for (int s2 = 0; s2 < NS; ++s2) seg[s2] = P2<T>::lds(tp + s2 * 64);
+#pragma unroll
+        for (int q = 0; q < TX; ++q) {
+            float2 t[PQ];
+            t[0] = seg[R + q];
+#pragma unroll
+            for (int e = 1; e < PQ; ++e) t[e] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int m = 0; m <= R; ++m) {
+                if (m > 0) {
+                    const float2 pr = __fadd2_rn(seg[R + q + m], seg[R + q - m]);
+                    t[0] = __fadd2_rn(t[0], pr);
+#pragma unroll
+                    for (int e = 1; e < PQ; ++e) t[e] = __ffma2_rn(c.upow[m * PQ + e], pr, t[e]);
+                }
+#pragma unroll
+                for (int gy = 0; gy <= R; ++gy) {
+                    if (mcanon<R>(gy) == m) {
+                        float2 v = t[0];
+#pragma unroll
+                        for (int e = 1; e < PQ; ++e) v = __ffma2_rn(v, c.coef[gy], t[e]);
+                        acc[R + u - gy][q] = __fadd2_rn(acc[R + u - gy][q], v);
+                        if (gy) acc[R + u + gy][q] = __fadd2_rn(acc[R + u + gy][q], v);
+                    }
+                }
+            }
+        }
+    };
+
+#pragma unroll
+    for (int s2 = 0; s2 < kStages - 1; ++s2) issue(s2);
+    bool failed = false;
+    int waited = 0;  // rows whose barrier has been waited
+    for (int r0 = 0; r0 < nrp && !failed; r0 += U) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int r = r0 + u;
+            const bool ok = mbar_wait_bounded(bbase + 8 * u, (unsigned)((r / kStages) & 1));
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            waited = r + 1;
+            issue(r + kStages - 1);
+            row(u, u);
+        }
+        if (failed) break;
+        const int jin0 = jb - R + r0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int jo = jin0 - R + u;
+            if (kv && jo >= jb && jo < je) {
+                T* orow = outb + a.out.sj * (long long)jo;
+#pragma unroll
+                for (int q = 0; q < TX; ++q) {
+                    const int i = i0 + q;
+                    if (i < a.I) {
+                        const float2 v = __fmul2_rn(acc[u][q], scale);
+                        P2<T>::st(orow + a.out.si * (long long)i, v);
+                        if (i < a.mirror_hx) P2<T>::st(orow + a.out.si * (long long)(-1 - i), v);
+                        if (i >= a.I - a.mirror_hx) P2<T>::st(orow + a.out.si * (long long)(2 * a.I - 1 - i), v);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < NR - U; ++r)
+#pragma unroll
+            for (int q = 0; q < TX; ++q) acc[r][q] = acc[r + U][q];
+#pragma unroll
+        for (int r = NR - U; r < NR; ++r)
+#pragma unroll
+            for (int q = 0; q < TX; ++q) acc[r][q] = make_float2(0.f, 0.f);
+    }
+    if (failed) {
+        // record, then drain this block's outstanding copies (bounded) before exit
+        if (tid == 0) {
+            atomicExch(a.status, 1);
+            const int issued = min(nrp, waited + kStages - 1);
+            for (int r = waited; r < issued; ++r) mbar_wait_bounded(bbase + 8 * (r % kStages), (unsigned)((r / kStages) & 1));
+        }
+        __syncthreads();
+    }
+}
+
 // Columns per thread of the packed kernels.
 constexpr int hmom_p2_tx(int R) { return hmom_tma_tx(R); }
 
@@ -684,16 +825,27 @@ static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t
                 c2.upow[t] = make_float2((float)cd.upow[t], (float)cd.upow[t]);
             const int nstrip2 = (a.I + TX2 - 1) / TX2;
             dim3 grid2((a.nk + 63) / 64, (nstrip2 + NW - 1) / NW, (a.J + rows - 1) / rows);
-            if (a.tmap && a.status) {
+            if (a.tmap && a.status && a.variant != 2) {
                 static_assert(hmom_tma_tx(R) == TX2, "tile shape");
-                constexpr size_t smt = hmom_tma_stage_bytes<R, TX2, T>();
-                // opt in above the default 48 KB (dynamic + the static mbarriers)
-                if (smt + 1024 > 48 * 1024) {
-                    static unsigned long long done = 0;  // per instantiation
-                    cudaError_t ea = smem_optin(k_hmom_tma<R, P, TX2, T>, smt, done);
-                    if (ea != cudaSuccess) return (int)ea;
+                const CUtensorMap& tm = *static_cast<const CUtensorMap*>(a.tmap);
+                if (a.variant == 1) {  // single-row pipeline
+                    constexpr size_t smt = (size_t)kStages * (kStageWarps * TX2 + 2 * R) * 64 * sizeof(T);
+                    if (smt + 1024 > 48 * 1024) {
+                        static unsigned long long done = 0;  // per instantiation
+                        cudaError_t ea = smem_optin(k_hmom_tma1<R, P, TX2, T>, smt, done);
+                        if (ea != cudaSuccess) return (int)ea;
+                    }
+                    k_hmom_tma1<R, P, TX2, T><<<grid2, block, smt, s>>>(b, tm, c2);
+                } else {  // two rows per barrier
+                    constexpr size_t smt = hmom_tma_stage_bytes<R, TX2, T>();
+                    // opt in above the default 48 KB (dynamic + the static mbarriers)
+                    if (smt + 1024 > 48 * 1024) {
+                        static unsigned long long done = 0;  // per instantiation
+                        cudaError_t ea = smem_optin(k_hmom_tma<R, P, TX2, T>, smt, done);
+                        if (ea != cudaSuccess) return (int)ea;
+                    }
+                    k_hmom_tma<R, P, TX2, T><<<grid2, block, smt, s>>>(b, tm, c2);
                 }
-                k_hmom_tma<R, P, TX2, T><<<grid2, block, smt, s>>>(b, *static_cast<const CUtensorMap*>(a.tmap), c2);
                 cudaError_t e = cudaGetLastError();
                 return e == cudaSuccess ? 0 : (int)e;
             }

@@ -550,6 +550,121 @@ __global__ void __launch_bounds__(256) k_prolong_z(ProlongZArgs z) {
     }
 }
 
+// Vectorised fused prolongation + z forward: each lane owns 4 consecutive
+// levels (one 16-byte access), the block a tile of KT = blockDim.x * 4
+// levels (whole z columns).  Base values are fetched first, the prolonged
+// field goes to shared memory as float4 rows, and each lane then applies the
+// band rows of its four levels to a window of three vectors.
+template <typename T, int NT, int MZ>
+__global__ void __launch_bounds__(128) k_prolong_z4(ProlongZArgs z) {
+    using A = typename AccOf<T>::type;
+    constexpr int O = NT == 4 ? 1 : 0;
+    constexpr int S = NT == 4 ? 2 : 1;
+    constexpr int NC = PZ + NT - 1;
+    constexpr int NP = 4 * PZ;
+    constexpr int NB = (MZ + 3) / 4;
+    extern __shared__ unsigned char smem_raw[];
+    A* buf = reinterpret_cast<A*>(smem_raw);  // [NP][KT]
+    const ProlongArgs& a = z.p;
+    const int nv = blockDim.x;                // vectors per tile
+    const int KT = nv * 4;
+    const int tid = threadIdx.x;
+    const int k = blockIdx.x * KT + 4 * tid;
+    const bool kv = k < a.nk;
+    const int kk = kv ? k : a.nk - 4;
+    const int Ic = a.If / 2, Jc = a.Jf / 2;
+    const int m0 = blockIdx.y * PZ;
+    const int n = blockIdx.z;
+    A vals[2][2 * PZ][4];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int fj = min(max(2 * n - O + h, 0), a.Jf - 1);
+        const T* base = static_cast<const T*>(a.base.p) + a.base.sj * fj + kk;
+#pragma unroll
+        for (int q = 0; q < 2 * PZ; ++q) {
+            const int fi = min(max(2 * m0 - O + q, 0), a.If - 1);
+            V4<T>::ldc(base + a.base.si * fi, vals[h][q]);
+        }
+    }
+    int ccol[NC];
+#pragma unroll
+    for (int s2 = 0; s2 < NC; ++s2) ccol[s2] = reflect_half(m0 - S + s2, Ic);
+    const T* coarse = static_cast<const T*>(a.coarse.p) + kk;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        const T* row = coarse + a.coarse.sj * reflect_half(n - S + t, Jc);
+        A v[NC][4];
+#pragma unroll
+        for (int s2 = 0; s2 < NC; ++s2) V4<T>::ld(row + a.coarse.si * ccol[s2], v[s2]);
+        const A wy0 = (A)PCoef<NT>::c0(t), wy1 = (A)PCoef<NT>::c1(t);
+#pragma unroll
+        for (int q = 0; q < PZ; ++q)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                A x0 = A(0), x1 = A(0);
+#pragma unroll
+                for (int u = 0; u < NT; ++u) {
+                    x0 = fma((A)PCoef<NT>::c0(u), v[q + u][e], x0);
+                    x1 = fma((A)PCoef<NT>::c1(u), v[q + u][e], x1);
+                }
+                vals[0][2 * q][e] = fma(wy0, x0, vals[0][2 * q][e]);
+                vals[0][2 * q + 1][e] = fma(wy0, x1, vals[0][2 * q + 1][e]);
+                vals[1][2 * q][e] = fma(wy1, x0, vals[1][2 * q][e]);
+                vals[1][2 * q + 1][e] = fma(wy1, x1, vals[1][2 * q + 1][e]);
+            }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int q = 0; q < 2 * PZ; ++q)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) buf[(h * 2 * PZ + q) * KT + 4 * tid + e] = vals[h][q][e];
+    __syncthreads();
+    if (!kv) return;
+    A w[4][2 * MZ + 1];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int ke = k + e;
+        const bool zc = ke < z.nzk;
+        const int L = zc ? ke % z.lm : 0;
+        const A* b = static_cast<const A*>(z.band) + (size_t)L * (2 * z.mz + 1) + z.mz;
+#pragma unroll
+        for (int d = -MZ; d <= MZ; ++d) {
+            const bool ok = zc && d >= -z.mz && d <= z.mz && L + d >= 0 && L + d < z.lm;
+            w[e][d + MZ] = ok ? b[d] : ((!zc && d == 0) ? A(1) : A(0));
+        }
+    }
+    int voff[2 * NB + 1];
+#pragma unroll
+    for (int v = 0; v < 2 * NB + 1; ++v) voff[v] = 4 * min(max(tid + v - NB, 0), nv - 1);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int fj = 2 * n - O + h;
+        if (fj < 0 || fj >= a.Jf) continue;
+        T* out = static_cast<T*>(a.out.p) + a.out.sj * fj + k;
+#pragma unroll
+        for (int q = 0; q < 2 * PZ; ++q) {
+            const int fi = 2 * m0 - O + q;
+            if (fi < 0 || fi >= a.If) continue;
+            const A* col = buf + (h * 2 * PZ + q) * KT;
+            A x[4 * (2 * NB + 1)];
+#pragma unroll
+            for (int v = 0; v < 2 * NB + 1; ++v)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) x[4 * v + e] = col[voff[v] + e];
+            A y[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                A acc = A(0);
+#pragma unroll
+                for (int d = -MZ; d <= MZ; ++d) acc = fma(w[e][d + MZ], x[4 * NB + e + d], acc);
+                y[e] = acc;
+            }
+            V4<T>::st(out + a.out.si * fi, y);
+        }
+    }
+}
+
 // ------------------------------------------- direct-sum radial beta filter
 // General support table (any aspect, any integer p): the gather form of
 // fill_h + vrbeta2 (jp_pbfil.f90:888-928).  Because the radial weights are
@@ -773,14 +888,34 @@ static void pzlaunch(const ProlongZArgs& z, int KT, dim3 grid, cudaStream_t s) {
     else k_prolong_z<T, 3, MZ><<<grid, KT, sm, s>>>(z);
 }
 
+template <typename T, int MZ>
+static void pzlaunch4(const ProlongZArgs& z, int KT, dim3 grid, cudaStream_t s) {
+    const size_t sm = sizeof(typename AccOf<T>::type) * 4 * PZ * KT;
+    if (z.p.ntap == 4) k_prolong_z4<T, 4, MZ><<<grid, KT / 4, sm, s>>>(z);
+    else k_prolong_z4<T, 3, MZ><<<grid, KT / 4, sm, s>>>(z);
+}
+
 int launch_prolong_z(DType t, const ProlongZArgs& z, void* stream) {
     const ProlongArgs& a = z.p;
     if (z.lm < 2 || z.lm > 256 || z.mz > 8 || !a.has_base) return -1;
-    const int KT = (256 / z.lm) * z.lm;
     const int O = a.ntap == 4 ? 1 : 0;
     const int npx = a.If / 2 + O, npy = a.Jf / 2 + O;
-    dim3 grid((a.nk + KT - 1) / KT, (npx + PZ - 1) / PZ, npy);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // vector form: whole columns in tiles of a multiple of 4 levels (<= 512)
+    if (a.nk % 4 == 0 && aligned16(a.coarse.p) && aligned16(a.base.p) && aligned16(a.out.p)) {
+        int c = 512 / z.lm;
+        while (c > 0 && (c * z.lm) % 4) --c;
+        if (c > 0) {
+            const int KT = c * z.lm;
+            dim3 grid((a.nk + KT - 1) / KT, (npx + PZ - 1) / PZ, npy);
+            MGBF_DISPATCH(t, (z.mz <= 2 ? pzlaunch4<T, 2>(z, KT, grid, s)
+                              : z.mz <= 4 ? pzlaunch4<T, 4>(z, KT, grid, s)
+                              : pzlaunch4<T, 8>(z, KT, grid, s)));
+            return last_err();
+        }
+    }
+    const int KT = (256 / z.lm) * z.lm;
+    dim3 grid((a.nk + KT - 1) / KT, (npx + PZ - 1) / PZ, npy);
     MGBF_DISPATCH(t, (z.mz <= 2 ? pzlaunch<T, 2>(z, KT, grid, s)
                       : z.mz <= 4 ? pzlaunch<T, 4>(z, KT, grid, s)
                       : pzlaunch<T, 8>(z, KT, grid, s)));

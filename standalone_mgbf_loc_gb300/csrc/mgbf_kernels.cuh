@@ -84,7 +84,10 @@ struct HMomArgs {
     double scale;            // multiplies every output (normalisation s x generation weight)
     const void* tmap;        // host copy of a 3D TMA tensor map of the input buffer, or null
     int* status;             // device status word: set to 1 when a bounded wait runs out
+    int variant = 0;         // FP32 kernels: 0 TMA two-row, 1 TMA one-row, 2 cp.async staged
 };
+
+constexpr int kHMomVariants = 3;
 
 // Tile columns of the TMA moment kernel for reach R (box = 64 levels x this
 // many columns x 1 row); the host encodes tensor maps with this box.

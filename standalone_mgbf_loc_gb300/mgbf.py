@@ -221,6 +221,12 @@ class MGBF:
         """Raise if a bounded device wait ran out since the last check."""
         _abi.check(self._lib.mgbf_status(self._h), "mgbf_status")
 
+    def autotune(self, dtype=None) -> None:
+        """Choose radial-kernel variants and tile heights by measurement."""
+        dt = _dtype_code(dtype if dtype is not None else torch.float32)
+        stream = torch.cuda.current_stream().cuda_stream if torch is not None else None
+        _abi.check(self._lib.mgbf_autotune(self._h, dt, stream), "mgbf_autotune")
+
     def set_weights(self, a: Sequence[float]) -> None:
         arr = (ctypes.c_double * len(a))(*[float(v) for v in a])
         _abi.check(self._lib.mgbf_set_weights(self._h, arr, len(a)), "set_weights")
@@ -308,6 +314,12 @@ class MGBFBatch:
 
     def status(self) -> None:
         _abi.check(self._lib.mgbf_batch_status(self._h), "mgbf_batch_status")
+
+    def autotune(self, dtype=None) -> None:
+        """Choose radial-kernel variants and tile heights by measurement."""
+        dt = _dtype_code(dtype if dtype is not None else torch.float32)
+        stream = torch.cuda.current_stream().cuda_stream if torch is not None else None
+        _abi.check(self._lib.mgbf_batch_autotune(self._h, dt, stream), "mgbf_batch_autotune")
 
     def use_graphs(self, enable: bool = True) -> None:
         """Replay repeated calls on the same fields as captured CUDA graphs."""

@@ -240,3 +240,15 @@ def test_batch_graph_replay_matches_direct(lib, cuda):
     torch.cuda.synchronize()
     graphed.status()
     assert torch.equal(a, g)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_autotuned_choice_keeps_parity(lib, cuda, dtype):
+    c = small_config(nxPE=4, nyPE=4, im_filt=32, jm_filt=32, lm=8, km3=2, gm_max=3, hx=8, hy=8, hz=2,
+                     mg_ampl02=canonical(8))
+    op = MGBF(c)
+    op.autotune(dtype)
+    op.status()
+    x = compact_input(op, 12)
+    y = run_gpu(op, 1, x, dtype, cuda)
+    assert rel_l2(y, O.filter_compact(oracle_cfg(c, 1), x)) < TOL[dtype]
