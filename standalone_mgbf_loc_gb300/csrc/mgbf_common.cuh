@@ -78,6 +78,15 @@ template <> struct V4<__nv_bfloat16> {
     }
 };
 
+// 16-byte asynchronous global -> shared copy (L1 bypassed); `bytes` < 16
+// zero-fills the rest of the destination.
+__device__ __forceinline__ void cp_async16(unsigned saddr, const void* g, int bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(g), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // Half-sample mirror of a 0-based index into [0, n): -1 -> 0, n -> n-1
 // (the reference's physical-boundary halo fill, mg_bocos.f90:225-377),
 // clamped so that rows only used for discarded outputs stay in range.
@@ -85,6 +94,18 @@ __device__ __forceinline__ int reflect_half(int j, int n) {
     j = j < 0 ? -1 - j : j;
     j = j >= n ? 2 * n - 1 - j : j;
     return j < 0 ? 0 : (j >= n ? n - 1 : j);
+}
+
+// Opts a kernel into more than 48 KB of dynamic shared memory, once per
+// device (the attribute persists, so graph captures later need no API call).
+template <typename K>
+inline cudaError_t smem_optin(K kernel, size_t bytes, unsigned long long& done /* one bit per device */) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (done >> dev & 1ull) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) done |= 1ull << dev;
+    return e;
 }
 
 }  // namespace mgbf

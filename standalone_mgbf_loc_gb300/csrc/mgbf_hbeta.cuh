@@ -150,12 +150,6 @@ __global__ void __launch_bounds__(128) k_hmom(HMomArgs a,
 constexpr int kStages = 4;
 constexpr int kStageWarps = 4;
 
-__device__ __forceinline__ void cp_async16(unsigned saddr, const void* g, int bytes) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(g), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 template <int R, int TX, typename T>
 constexpr size_t hmom_stage_bytes() {
@@ -783,18 +777,6 @@ __global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_cons
 
 // Columns per thread of the packed kernels.
 constexpr int hmom_p2_tx(int R) { return hmom_tma_tx(R); }
-
-// Opts a kernel into more than 48 KB of dynamic shared memory, once per
-// device (the attribute persists, so graph captures later need no API call).
-template <typename K>
-static cudaError_t smem_optin(K kernel, size_t bytes, unsigned long long& done /* one bit per device */) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (done >> dev & 1ull) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess) done |= 1ull << dev;
-    return e;
-}
 
 template <int R, int P, typename T>
 static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t s) {

@@ -211,76 +211,143 @@ __global__ void __launch_bounds__(128) k_restrict(RestrictArgs a) {
     }
 }
 
-// Vectorised restriction: levels k..k+3 per thread, RV x RV coarse block.
-constexpr int RV = 2;
-template <typename T>
-__global__ void __launch_bounds__(128) k_restrict4(RestrictArgs a) {
+// Pipelined restriction.  A block takes 128 levels x 4*CX coarse columns x
+// a segment of coarse rows and walks down the rows.  Fine rows are staged
+// in shared memory by cp.async, S rows in flight (two rows per step), and
+// each warp restricts its CX coarse columns from there: lane = 4 levels, the
+// x pass (8 taps) once per fine row, then the row goes into a ring of the
+// four coarse rows it touches (fine rows 2d+3 and 2d+4 feed coarse rows
+// d..d+3 with taps 6-2s and 7-2s), and coarse row d is final once both are
+// in.  Every fine value is read from HBM once per block (plus 6 shared
+// columns and 6 rows of ring fill), and the x pass is not repeated across
+// coarse rows.
+constexpr int kRsWarps = 4;
+constexpr int kRsLevels = 128;
+template <typename T, int CX>
+__host__ __device__ constexpr int rs_cols() { return 2 * kRsWarps * CX + 6; }
+template <typename T, int CX, int S>
+constexpr size_t rs_smem() { return (size_t)S * rs_cols<T, CX>() * kRsLevels * sizeof(T); }
+
+template <typename T, int CX, int S>
+__global__ void __launch_bounds__(kRsWarps * 32) k_restrict_p(RestrictArgs a, int seg_rows) {
     using A = typename AccOf<T>::type;
-    constexpr int NF = 2 * RV + 6;
+    static_assert(S % 2 == 0 && S >= 4, "stages come in pairs of fine rows");
+    constexpr int NF = rs_cols<T, CX>();
+    constexpr int EPC = 16 / (int)sizeof(T);          // elements per 16-byte chunk
+    constexpr int CH = kRsLevels / EPC;               // chunks per staged column
+    constexpr int P2 = S / 2;                         // steps in flight
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* stg = reinterpret_cast<T*>(smem_raw);          // [S][NF][kRsLevels]
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
     const int Ic = a.If / 2, Jc = a.Jf / 2;
-    const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
-    if (k >= a.nk) return;
-    const int c0 = blockIdx.y * RV;
-    const int d0 = blockIdx.z * RV;
-    A wx[RV][8], wy[RV][8];
-#pragma unroll
-    for (int c = 0; c < RV; ++c) {
-        const int cc = min(c0 + c, Ic - 1), dd = min(d0 + c, Jc - 1);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            wx[c][q] = static_cast<const A*>(a.wx)[cc * 8 + q];
-            wy[c][q] = static_cast<const A*>(a.wy)[dd * 8 + q];
+    const int kb = blockIdx.x * kRsLevels;
+    const int chunks = (min(kRsLevels, a.nk - kb)) / EPC;
+    const int cs = blockIdx.y * (kRsWarps * CX);
+    const int d0 = blockIdx.z * seg_rows;
+    const int d1 = min(d0 + seg_rows, Jc);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c0 = cs + warp * CX;
+    const T* fine = static_cast<const T*>(a.fine.p) + kb;
+
+    auto issue = [&](int fr, int stage) {
+        const int fj = min(max(fr, 0), a.Jf - 1);
+        const T* row = fine + a.fine.sj * fj;
+        for (int t = threadIdx.x; t < NF * CH; t += kRsWarps * 32) {
+            const int col = t / CH, ch = t - col * CH;
+            if (ch < chunks) {
+                const int fc = min(max(2 * cs - 3 + col, 0), a.If - 1);
+                cp_async16(sbase + (unsigned)(((stage * NF + col) * kRsLevels + ch * EPC) * (int)sizeof(T)),
+                           row + a.fine.si * fc + ch * EPC, 16);
+            }
         }
+    };
+
+    const A* wyp = static_cast<const A*>(a.wy);
+    A wx[CX][8];
+#pragma unroll
+    for (int c = 0; c < CX; ++c) {
+        const int cc = min(c0 + c, Ic - 1);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) wx[c][q] = static_cast<const A*>(a.wx)[cc * 8 + q];
     }
-    int fcol[NF];
+    A acc[4][CX][4];
 #pragma unroll
-    for (int s = 0; s < NF; ++s) fcol[s] = min(max(2 * c0 - 3 + s, 0), a.If - 1);
-    const T* fine = static_cast<const T*>(a.fine.p) + k;
-    A acc[RV][RV][4];
+    for (int r = 0; r < 4; ++r)
 #pragma unroll
-    for (int r = 0; r < RV; ++r)
-#pragma unroll
-        for (int c = 0; c < RV; ++c)
+        for (int c = 0; c < CX; ++c)
 #pragma unroll
             for (int e = 0; e < 4; ++e) acc[r][c][e] = A(0);
+
+    const int niter = d1 - d0 + 3;  // ring base d = d0-3+it
 #pragma unroll
-    for (int rr = 0; rr < NF; ++rr) {
-        const int fj = min(max(2 * d0 - 3 + rr, 0), a.Jf - 1);
-        const T* row = fine + a.fine.sj * fj;
-        A seg[NF][4];
+    for (int q = 0; q < P2; ++q) {
+        if (q < niter) {
+            issue(2 * d0 - 3 + 2 * q, 2 * q);
+            issue(2 * d0 - 2 + 2 * q, 2 * q + 1);
+        }
+        cp_async_commit();
+    }
+    const bool kv = 4 * lane < chunks * EPC;
+    for (int it = 0; it < niter; ++it) {
+        const int d = d0 - 3 + it;
+        const int sp = it % P2;
+        cp_async_wait<P2 - 1>();
+        __syncthreads();
 #pragma unroll
-        for (int s = 0; s < NF; ++s) V4<T>::ld(row + a.fine.si * fcol[s], seg[s]);
+        for (int h = 0; h < 2; ++h) {
+            const T* srow = stg + (size_t)(2 * sp + h) * NF * kRsLevels + 4 * lane + 2 * warp * CX * kRsLevels;
+            A wy[4];
 #pragma unroll
-        for (int c = 0; c < RV; ++c) {
-            A xr[4] = {A(0), A(0), A(0), A(0)};
+            for (int r = 0; r < 4; ++r) {
+                const int dd = min(max(d + r, 0), Jc - 1);
+                wy[r] = __ldg(wyp + dd * 8 + 6 + h - 2 * r);
+            }
 #pragma unroll
-            for (int q = 0; q < 8; ++q)
+            for (int c = 0; c < CX; ++c) {
+                A xr[4] = {A(0), A(0), A(0), A(0)};
 #pragma unroll
-                for (int e = 0; e < 4; ++e) xr[e] = fma(wx[c][q], seg[2 * c + q][e], xr[e]);
+                for (int q = 0; q < 8; ++q) {
+                    A v[4];
+                    V4<T>::ldc(srow + (2 * c + q) * kRsLevels, v);
 #pragma unroll
-            for (int r = 0; r < RV; ++r) {
-                const int b = rr - 2 * r;
-                if (b >= 0 && b < 8) {
+                    for (int e = 0; e < 4; ++e) xr[e] = fma(wx[c][q], v[e], xr[e]);
+                }
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[r][c][e] = fma(wy[r][b], xr[e], acc[r][c][e]);
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) acc[r][c][e] = fma(wy[r], xr[e], acc[r][c][e]);
+            }
+        }
+        __syncthreads();  // every warp is done with stage pair sp
+        if (it + P2 < niter) {
+            issue(2 * d0 - 3 + 2 * (it + P2), 2 * sp);
+            issue(2 * d0 - 2 + 2 * (it + P2), 2 * sp + 1);
+        }
+        cp_async_commit();
+        if (d >= d0 && kv) {
+            T* out = static_cast<T*>(a.coarse.p) + a.coarse.sj * d + kb + 4 * lane;
+#pragma unroll
+            for (int c = 0; c < CX; ++c) {
+                const int cc = c0 + c;
+                if (cc < Ic) {
+                    V4<T>::st(out + a.coarse.si * cc, acc[0][c]);
+                    if (cc < a.mirror_hx) V4<T>::st(out + a.coarse.si * (-1 - cc), acc[0][c]);
+                    if (cc >= Ic - a.mirror_hx) V4<T>::st(out + a.coarse.si * (2 * Ic - 1 - cc), acc[0][c]);
                 }
             }
         }
-    }
 #pragma unroll
-    for (int r = 0; r < RV; ++r) {
-        const int d = d0 + r;
-        if (d >= Jc) break;
-        T* out = static_cast<T*>(a.coarse.p) + a.coarse.sj * d + k;
+        for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < RV; ++c) {
-            const int cc = c0 + c;
-            if (cc >= Ic) break;
-            V4<T>::st(out + a.coarse.si * cc, acc[r][c]);
-            if (cc < a.mirror_hx) V4<T>::st(out + a.coarse.si * (-1 - cc), acc[r][c]);
-            if (cc >= Ic - a.mirror_hx) V4<T>::st(out + a.coarse.si * (2 * Ic - 1 - cc), acc[r][c]);
-        }
+            for (int c = 0; c < CX; ++c)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[r][c][e] = acc[r + 1][c][e];
+#pragma unroll
+        for (int c = 0; c < CX; ++c)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[3][c][e] = A(0);
     }
+    cp_async_wait<0>();
 }
 
 // -------------------------------------------------------- prolongation
@@ -800,6 +867,7 @@ __global__ void __launch_bounds__(256) k_dot(DotArgs a) {
     }
 
 static inline size_t acc_size(DType t) { return t == DType::F64 ? 8 : 4; }
+static inline size_t elem_size(DType t) { return t == DType::F64 ? 8 : (t == DType::F32 ? 4 : 2); }
 
 static inline int last_err() {
     cudaError_t e = cudaGetLastError();
@@ -841,11 +909,32 @@ int launch_restrict(DType t, const RestrictArgs& a, void* stream) {
     const int Ic = a.If / 2, Jc = a.Jf / 2;
     if (a.nk == 0 || Ic == 0 || Jc == 0) return 0;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (a.nk % 4 == 0 && aligned16(a.fine.p) && aligned16(a.coarse.p)) {
-        const int nt = a.nk / 4;
-        dim3 block(std::min(128, ((nt + 31) / 32) * 32)), grid((nt + block.x - 1) / block.x, (Ic + RV - 1) / RV,
-                                                             (Jc + RV - 1) / RV);
-        MGBF_DISPATCH(t, (k_restrict4<T><<<grid, block, 0, s>>>(a)));
+    if ((a.nk * elem_size(t)) % 16 == 0 && aligned16(a.fine.p) && aligned16(a.coarse.p)) {
+        // Row segments: about 8 waves of blocks (2 resident per SM), at least
+        // 32 coarse rows so the 3-step ring fill stays under 10%.
+        const int cx = t == DType::F64 ? 2 : 4;
+        dim3 block(kRsWarps * 32), grid((a.nk + kRsLevels - 1) / kRsLevels, (Ic + kRsWarps * cx - 1) / (kRsWarps * cx), 1);
+        const long long tiles = (long long)grid.x * grid.y;
+        const long long nseg = (8LL * 2 * 152 + tiles - 1) / tiles;
+        int rows = (int)((Jc + nseg - 1) / nseg);
+        rows = std::max(rows, std::min(Jc, 32));
+        grid.z = (Jc + rows - 1) / rows;
+        static unsigned long long done[3] = {0, 0, 0};
+        cudaError_t e = cudaSuccess;
+        if (t == DType::F64) {
+            constexpr size_t sm = rs_smem<double, 2, 4>();
+            e = smem_optin(k_restrict_p<double, 2, 4>, sm, done[0]);
+            if (e == cudaSuccess) k_restrict_p<double, 2, 4><<<grid, block, sm, s>>>(a, rows);
+        } else if (t == DType::F32) {
+            constexpr size_t sm = rs_smem<float, 4, 4>();
+            e = smem_optin(k_restrict_p<float, 4, 4>, sm, done[1]);
+            if (e == cudaSuccess) k_restrict_p<float, 4, 4><<<grid, block, sm, s>>>(a, rows);
+        } else {
+            constexpr size_t sm = rs_smem<__nv_bfloat16, 4, 4>();
+            e = smem_optin(k_restrict_p<__nv_bfloat16, 4, 4>, sm, done[2]);
+            if (e == cudaSuccess) k_restrict_p<__nv_bfloat16, 4, 4><<<grid, block, sm, s>>>(a, rows);
+        }
+        if (e != cudaSuccess) return (int)e;
         return last_err();
     }
     constexpr int NW = 4;
