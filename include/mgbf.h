@@ -164,6 +164,13 @@ int mgbf_status(mgbf_handle* h);
  * rounding (summation order). */
 int mgbf_autotune(mgbf_handle* h, int dtype, void* stream);
 
+/* Pins the radial-filter kernel variant (0: TMA, two rows per barrier;
+ * 1: TMA, one row per barrier; 2: cp.async staging) and output rows per block
+ * (<= 0: the default) for every generation and pass; variant < 0 returns
+ * to the defaults.  FP64 always uses its one kernel.  For tests and manual
+ * tuning; mgbf_autotune chooses by measurement. */
+int mgbf_set_tuning(mgbf_handle* h, int dtype, int variant, int rows);
+
 /* Replace the per-generation weights a_1..a_n (n <= gm) without rebuilding. */
 int mgbf_set_weights(mgbf_handle* h, const double* a, int n);
 

@@ -96,6 +96,7 @@ SIGNATURES = {
     "mgbf_batch_status": (_I, [_HP]),
     "mgbf_batch_use_graphs": (_I, [_HP, _I]),
     "mgbf_autotune": (_I, [_HP, _I, _VP]),
+    "mgbf_set_tuning": (_I, [_HP, _I, _I, _I]),
     "mgbf_batch_autotune": (_I, [_HP, _I, _VP]),
     "mgbf_radial_filter_noalloc": (_I, [_VP, _VP, _I, _I, _I, _I, _D, _I, _I, _D, _VP]),
     "mgbf_timers_enable": (_I, [_I]),

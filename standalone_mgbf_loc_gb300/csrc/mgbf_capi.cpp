@@ -1152,6 +1152,26 @@ int mgbf_autotune(mgbf_handle* h, int dtype, void* stream) {
     return autotune_plan(h->plan, (DType)dtype, stream);
 }
 
+int mgbf_set_tuning(mgbf_handle* h, int dtype, int variant, int rows) {
+    if (!h) return fail(MGBF_ERR_ARG, "null handle");
+    if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");
+    if (variant >= kHMomVariants) return fail(MGBF_ERR_ARG, "unknown radial kernel variant");
+    Plan& P = h->plan;
+    for (auto& G : P.groups)
+        for (int g = 0; g < P.gm; ++g)
+            for (int pass = 0; pass < 2; ++pass) {
+                const int key = dtype * 1024 + g * 2 + pass;
+                if (variant < 0) {
+                    G.tune.erase(key);
+                } else {
+                    Exec ex{P, G, (DType)dtype, nullptr};
+                    const int J = gen_J(P, g);
+                    G.tune[key] = {variant, rows > 0 ? std::min(rows, J) : ex.default_rows(g)};
+                }
+            }
+    return MGBF_OK;
+}
+
 int mgbf_batch_autotune(mgbf_batch* b, int dtype, void* stream) {
     if (!b) return fail(MGBF_ERR_ARG, "null handle");
     if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");

@@ -68,19 +68,20 @@ __global__ void __launch_bounds__(128) k_zfilter(ZArgs a) {
     }
 }
 
-// Vectorised z filter: each thread owns levels k..k+3 (k % 4 == 0) and ZI
-// columns; the band rows of its four levels sit in registers (levels past
-// nzk get the identity row, so 2D variables are copied by the same code);
-// the window k-4NB .. k+4NB+3 comes in 2NB+1 vector loads.  Needs
-// nk % 4 == 0 and 16-byte aligned views.
+// Vectorised z filter: each thread owns levels k..k+3 (k % 4 == 0) and a
+// strip of ncol columns, taken ZI at a time; the band rows of its four
+// levels sit in registers for the whole strip (levels past nzk get the
+// identity row, so 2D variables are copied by the same code); the window
+// k-4NB .. k+4NB+3 comes in 2NB+1 vector loads.  Needs nk % 4 == 0 and
+// 16-byte aligned views.
 template <typename T, int MZ, int ZI>
-__global__ void __launch_bounds__(128) k_zfilter4(ZArgs a) {
+__global__ void __launch_bounds__(128) k_zfilter4(ZArgs a, int ncol) {
     using A = typename AccOf<T>::type;
     constexpr int NB = (MZ + 3) / 4;
     constexpr int NWIN = 4 * (2 * NB + 1);
     const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
     if (k >= a.nk) return;
-    const int i0 = blockIdx.y * ZI;
+    const int i0 = blockIdx.y * ncol;
     const int j = blockIdx.z;
     A w[4][2 * MZ + 1];
 #pragma unroll
@@ -100,10 +101,12 @@ __global__ void __launch_bounds__(128) k_zfilter4(ZArgs a) {
     for (int v = 0; v < 2 * NB + 1; ++v) voff[v] = min(max(k + 4 * (v - NB), 0), a.nk - 4);
     const T* in = static_cast<const T*>(a.in.p) + a.in.sj * j;
     T* out = static_cast<T*>(a.out.p) + a.out.sj * j + k;
+    const int i1 = min(i0 + ncol, a.I);
+    for (int ic = i0; ic < i1; ic += ZI)
 #pragma unroll
     for (int c = 0; c < ZI; ++c) {
-        const int i = i0 + c;
-        if (i >= a.I) break;
+        const int i = ic + c;
+        if (i >= i1) break;
         const T* row = in + a.in.si * i;
         A x[NWIN];
 #pragma unroll
@@ -882,9 +885,14 @@ static void zlaunch(const ZArgs& a, cudaStream_t s) {
     if constexpr (MZ <= 8) {  // the vector form keeps 4*(2MZ+1) weights in registers
         const bool vec = a.nk % 4 == 0 && aligned16(a.in.p) && aligned16(a.out.p);
         if (vec) {
+            // column strips long enough to amortise the band setup, short
+            // enough for about 8 resident waves of blocks
             const int nt = a.nk / 4;
-            dim3 block(128), grid((nt + 127) / 128, (a.I + ZI - 1) / ZI, a.J);
-            k_zfilter4<T, MZ, ZI><<<grid, block, 0, s>>>(a);
+            const long long blocks_per_col = (long long)((nt + 127) / 128) * a.J;
+            int ncol = 32;
+            while (ncol > ZI && blocks_per_col * ((a.I + ncol - 1) / ncol) < 152LL * 8 * 4) ncol /= 2;
+            dim3 block(128), grid((nt + 127) / 128, (a.I + ncol - 1) / ncol, a.J);
+            k_zfilter4<T, MZ, ZI><<<grid, block, 0, s>>>(a, ncol);
             return;
         }
     }

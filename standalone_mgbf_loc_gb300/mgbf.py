@@ -227,6 +227,11 @@ class MGBF:
         stream = torch.cuda.current_stream().cuda_stream if torch is not None else None
         _abi.check(self._lib.mgbf_autotune(self._h, dt, stream), "mgbf_autotune")
 
+    def set_tuning(self, variant: int, rows: int = 0, dtype=None) -> None:
+        """Pin the radial-kernel variant and rows per block (variant < 0: defaults)."""
+        dt = _dtype_code(dtype if dtype is not None else torch.float32)
+        _abi.check(self._lib.mgbf_set_tuning(self._h, dt, int(variant), int(rows)), "mgbf_set_tuning")
+
     def set_weights(self, a: Sequence[float]) -> None:
         arr = (ctypes.c_double * len(a))(*[float(v) for v in a])
         _abi.check(self._lib.mgbf_set_weights(self._h, arr, len(a)), "set_weights")

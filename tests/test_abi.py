@@ -181,3 +181,16 @@ def test_null_arguments_rejected(lib):
     assert lib.mgbf_filtering_procedure(None, 1, None, 0, 0, None) == _abi.MGBF_ERR_ARG
     assert lib.mgbf_create(None, None) == _abi.MGBF_ERR_ARG
     assert lib.mgbf_destroy(None) == _abi.MGBF_OK
+
+
+def test_set_tuning_validation(lib):
+    """Pinning a radial-kernel variant is host-side bookkeeping: unknown
+    variants and dtypes are rejected, valid ones and the reset are accepted."""
+    op = MGBF(small_config())
+    op.set_tuning(0)
+    op.set_tuning(2, 5)
+    op.set_tuning(-1)
+    with pytest.raises(MGBFError):
+        op.set_tuning(3)
+    assert lib.mgbf_set_tuning(None, 1, 0, 0) == _abi.MGBF_ERR_ARG
+    assert lib.mgbf_set_tuning(op._h, 7, 0, 0) == _abi.MGBF_ERR_ARG

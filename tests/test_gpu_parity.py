@@ -252,3 +252,25 @@ def test_autotuned_choice_keeps_parity(lib, cuda, dtype):
     x = compact_input(op, 12)
     y = run_gpu(op, 1, x, dtype, cuda)
     assert rel_l2(y, O.filter_compact(oracle_cfg(c, 1), x)) < TOL[dtype]
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("rows", [0, 7])
+@pytest.mark.parametrize("h", [5, 8, 12, 16])
+def test_parity_each_radial_variant(lib, cuda, dtype, variant, rows, h):
+    """Every kernel variant the autotuner may choose, with the default row
+    blocking and with short, uneven row blocks."""
+    c = small_config(nxPE=4, nyPE=4, im_filt=48, jm_filt=48, lm=8, km3=1, gm_max=3, hx=h, hy=h, hz=2,
+                     mg_ampl02=canonical(h), mg_ampl01=canonical_z(2))
+    op = MGBF(c)
+    op.set_tuning(variant, rows, dtype)
+    x = compact_input(op, 100 + h)
+    y = run_gpu(op, 1, x, dtype, cuda)
+    op.status()
+    assert rel_l2(y, O.filter_compact(oracle_cfg(c, 1), x)) < TOL[dtype]
+    # the adjoint passes run the same variant: dot-product test
+    w = compact_input(op, 200 + h)
+    ltw = run_gpu(op, 1, w, dtype, cuda, adjoint=True)
+    lhs, rhs = float(np.vdot(y, w)), float(np.vdot(x, ltw))
+    assert abs(lhs - rhs) <= (1e-6 if dtype == torch.float32 else 2e-2) * np.linalg.norm(y) * np.linalg.norm(w)
