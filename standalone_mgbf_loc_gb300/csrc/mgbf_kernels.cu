@@ -919,13 +919,15 @@ int launch_restrict(DType t, const RestrictArgs& a, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if ((a.nk * elem_size(t)) % 16 == 0 && aligned16(a.fine.p) && aligned16(a.coarse.p)) {
         // Row segments: about 8 waves of blocks (2 resident per SM), at least
-        // 32 coarse rows so the 3-step ring fill stays under 10%.
+        // 8 coarse rows (3 steps of ring fill per segment); small coarse
+        // generations get short segments and enough blocks, the finest
+        // generation long ones.
         const int cx = t == DType::F64 ? 2 : 4;
         dim3 block(kRsWarps * 32), grid((a.nk + kRsLevels - 1) / kRsLevels, (Ic + kRsWarps * cx - 1) / (kRsWarps * cx), 1);
         const long long tiles = (long long)grid.x * grid.y;
         const long long nseg = (8LL * 2 * 152 + tiles - 1) / tiles;
         int rows = (int)((Jc + nseg - 1) / nseg);
-        rows = std::max(rows, std::min(Jc, 32));
+        rows = std::max(rows, std::min(Jc, 8));
         grid.z = (Jc + rows - 1) / rows;
         static unsigned long long done[3] = {0, 0, 0};
         cudaError_t e = cudaSuccess;
