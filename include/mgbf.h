@@ -91,6 +91,7 @@ typedef struct mgbf_dims {
     int layout;
     size_t field_elems;    /* elements of one field in the handle's layout   */
     int hbeta_kernel;      /* 1: moment kernel, 0: direct-sum kernel          */
+    int reach_line;        /* fast filters' line reach (-1: procs 3/8 unusable) */
 } mgbf_dims;
 
 typedef struct mgbf_handle mgbf_handle;
@@ -121,9 +122,12 @@ int mgbf_get_dims(const mgbf_handle* h, mgbf_dims* dims);
 /*
  * filtering_procedure(mg_filt) (mg_filtering.f90:67-120) on the field in
  * place.  Supported: 1 = filtering_rad2_bckg (mg_filtering.f90:560-680),
- * 6 = filtering_rad2_ens (mg_filtering.f90:1000-1147).  2,3,4,5,7,8 return
- * MGBF_ERR_UNSUPPORTED; any other value is a no-op returning MGBF_OK, as the
- * reference's select has no default case.
+ * 6 = filtering_rad2_ens (mg_filtering.f90:1000-1147), and the fast 1D+1D
+ * variants 3 = filtering_fast_bckg (mg_filtering.f90:825-997) and
+ * 8 = filtering_fast_ens (mg_filtering.f90:1316-1506), whose horizontal
+ * filter is vrbeta1 along x and y with el = mg_ampl02 (no cholaspect).
+ * 2,4,5,7 return MGBF_ERR_UNSUPPORTED; any other value is a no-op
+ * returning MGBF_OK, as the reference's select has no default case.
  *   vall:   field pointer (device or host, per mem), laid out per the
  *           handle's layout, element type per dtype.
  *   stream: cudaStream_t (NULL = legacy default stream).  Device calls are

@@ -2,7 +2,8 @@
  * FP64 CPU oracle for the MGBF filtering pipeline -- TEST INFRASTRUCTURE ONLY.
  *
  * Restates, on one global filter grid, the reference's CPU algorithm for
- * filtering_procedure(1) and filtering_procedure(6).  Every routine below
+ * filtering_procedure(1), (6) and the fast 1D+1D variants (3) and (8).
+ * Every routine below
  * names the reference routine (file:line, paths inside the reference project)
  * whose loops it follows.  The MPI halo exchange of the reference collapses
  * into the global-edge mirror/fold that mg_bocos applies at physical
@@ -70,6 +71,8 @@ typedef struct {
     double eyx2;          /* off-diagonal (zero: no anisotropy)          */
     double ss1, ss2;      /* inverse line sums                           */
     int reach1, reach2;
+    double exxL, ssL;     /* fast filters' 1D horizontal line filter     */
+    int reachL;
 } setup_t;
 
 static const double EPS = 1.e-12;
@@ -128,15 +131,32 @@ static int setup(const orc_cfg* c, setup_t* s) {
         s->ss2 = 1.0 / sum;
         s->reach2 = reach > gym ? reach : gym;
     }
+    /* getlinesum1 on paspx / paspy (mg_intstate.f90:427-428): these aspects
+     * skip cholaspect, so el = pasp02 itself (mg_intstate.f90:370-375). */
+    {
+        s->exxL = c->ampl02 * s->rmom2_1;
+        double x = 1.0 / s->exxL;
+        int gxl = (int)ceil(-x + EPS), gxm = (int)floor(x - EPS);
+        int fast = c->proc == 3 || c->proc == 8;
+        if (fast && (gxl < -c->hx || gxm > c->hx || gxl < -c->hy || gxm > c->hy)) return ORC_ERR_REACH;
+        double sum = 0.0;
+        for (int gx = gxl; gx <= gxm; ++gx) {
+            double xx = gx, rr = (xx * s->exxL) * (xx * s->exxL);
+            sum += ipow(1.0 - rr, c->p);
+        }
+        s->ssL = 1.0 / sum;
+        s->reachL = gxm;
+    }
     return ORC_OK;
 }
 
-int orc_setup_values(const orc_cfg* c, double out[8]) {
+int orc_setup_values(const orc_cfg* c, double out[11]) {
     setup_t s;
     int rc = setup(c, &s);
     if (rc) return rc;
     out[0] = s.rmom2_1; out[1] = s.rmom2_2; out[2] = s.exx1; out[3] = s.exx2;
     out[4] = s.ss1; out[5] = s.ss2; out[6] = s.reach1; out[7] = s.reach2;
+    out[8] = s.exxL; out[9] = s.ssL; out[10] = s.reachL;
     return ORC_OK;
 }
 
@@ -249,6 +269,107 @@ static void fold_h(arr3 W, int imax, int jmax, int nbx, int nby, int k0, int k1)
         for (int i = 1; i <= imax; ++i)
             for (int k = k0; k < k1; ++k)
                 A3(W, k, i, jmax - nby + j) += A3(W, k, i, jmax + 1 + nby - j);
+}
+
+/* ------------------------------------------- fast filters: 1D line beta */
+
+/* vrbeta1 / vrbeta1t (jp_pbfil.f90:856-885, 981-1009) applied to every
+ * interior row (dir 0: along i, rbeta(km,hx,1,im,paspx,ssx,VALL(:,:,j))) or
+ * every interior column (dir 1: along j, rbeta(km,hy,1,jm,paspy,ssy,
+ * VALL(:,i,:))) of a generation array, as filtering_fast_bckg/_ens do
+ * (mg_filtering.f90:825-997, 1316-1506).  Forward: gather over the line's
+ * extended range, result on the interior, the line's halo zeroed.
+ * Adjoint: scatter from the interior into the extended line (b = 0 first).
+ * Either way the whole line, halo included, is overwritten (a = b). */
+static void line_beta(const setup_t* S, int p, arr3 a, int I, int J, int hx, int hy, int dir, int adj, int k0,
+                      int k1) {
+    const int n = dir ? J : I, h = dir ? hy : hx, m = dir ? I : J;
+    const int len = n + 2 * h;
+    const int nk = k1 - k0;
+    double* b = (double*)malloc(sizeof(double) * (size_t)nk * len);
+    const double exx = S->exxL, s = S->ssL;
+    const double x = 1.0 / exx;
+    const int gxl = (int)ceil(-x + EPS), gxm = (int)floor(x - EPS);
+#define LB(k, t) b[(size_t)((k) - k0) + (size_t)nk * (size_t)((t) + h - 1)]
+#define LA(k, t) (*(dir ? &A3(a, k, line, t) : &A3(a, k, t, line)))
+    for (int line = 1; line <= m; ++line) {
+        for (size_t t = 0; t < (size_t)nk * len; ++t) b[t] = 0.0;
+        for (int ix = 1; ix <= n; ++ix)
+            for (int gx = gxl; gx <= gxm; ++gx) {
+                int jx = ix + gx;
+                double xx = gx, rr = (xx * exx) * (xx * exx);
+                double frow = s * ipow(1.0 - rr, p);
+                if (!adj)
+                    for (int k = k0; k < k1; ++k) LB(k, ix) += frow * LA(k, jx);
+                else
+                    for (int k = k0; k < k1; ++k) LB(k, jx) += frow * LA(k, ix);
+            }
+        for (int t = 1 - h; t <= n + h; ++t)
+            for (int k = k0; k < k1; ++k) LA(k, t) = LB(k, t);
+    }
+#undef LA
+#undef LB
+    free(b);
+}
+
+/* bocox / bocoy at physical edges (mg_bocos.f90:4044-4903): half-sample
+ * mirror of the x halo on the interior rows only (dir 0), or of the y halo
+ * on the interior columns only (dir 1); the corners are not written. */
+static void fill_line(arr3 W, int imax, int jmax, int nb, int dir, int k0, int k1) {
+    if (!dir) {
+        for (int j = 1; j <= jmax; ++j)
+            for (int i = 1; i <= nb; ++i)
+                for (int k = k0; k < k1; ++k) {
+                    A3(W, k, -nb + i, j) = A3(W, k, nb + 1 - i, j);
+                    A3(W, k, imax + i, j) = A3(W, k, imax + 1 - i, j);
+                }
+    } else {
+        for (int j = 1; j <= nb; ++j)
+            for (int i = 1; i <= imax; ++i)
+                for (int k = k0; k < k1; ++k) {
+                    A3(W, k, i, jmax + j) = A3(W, k, i, jmax + 1 - j);
+                    A3(W, k, i, -nb + j) = A3(W, k, i, nb + 1 - j);
+                }
+    }
+}
+
+/* bocoTx / bocoTy at physical edges (mg_bocos.f90:4906-5718): the transpose,
+ * W(t) += W(1-t), W(M-nb+t) += W(M+nb+1-t) on the interior rows (dir 0) or
+ * columns (dir 1); halo values stay in place. */
+static void fold_line(arr3 W, int imax, int jmax, int nb, int dir, int k0, int k1) {
+    if (!dir) {
+        for (int j = 1; j <= jmax; ++j)
+            for (int i = 1; i <= nb; ++i)
+                for (int k = k0; k < k1; ++k) A3(W, k, i, j) += A3(W, k, 1 - i, j);
+        for (int j = 1; j <= jmax; ++j)
+            for (int i = 1; i <= nb; ++i)
+                for (int k = k0; k < k1; ++k) A3(W, k, imax - nb + i, j) += A3(W, k, imax + nb + 1 - i, j);
+    } else {
+        for (int j = 1; j <= nb; ++j)
+            for (int i = 1; i <= imax; ++i)
+                for (int k = k0; k < k1; ++k) A3(W, k, i, j) += A3(W, k, i, 1 - j);
+        for (int j = 1; j <= nb; ++j)
+            for (int i = 1; i <= imax; ++i)
+                for (int k = k0; k < k1; ++k) A3(W, k, i, jmax - nb + j) += A3(W, k, i, jmax + nb + 1 - j);
+    }
+}
+
+/* The fast filters' horizontal adjoint for one generation
+ * (mg_filtering.f90:859-906): rbetaT along x, bocoTx, rbetaT along y, bocoTy. */
+static void fast_adjoint(const orc_cfg* c, const setup_t* S, arr3 U, int I, int J, int k0, int k1) {
+    line_beta(S, c->p, U, I, J, c->hx, c->hy, 0, 1, k0, k1);
+    fold_line(U, I, J, c->hx, 0, k0, k1);
+    line_beta(S, c->p, U, I, J, c->hx, c->hy, 1, 1, k0, k1);
+    fold_line(U, I, J, c->hy, 1, k0, k1);
+}
+
+/* ... and its forward (mg_filtering.f90:930-975): bocoy, rbeta along y,
+ * bocox, rbeta along x. */
+static void fast_forward(const orc_cfg* c, const setup_t* S, arr3 U, int I, int J, int k0, int k1) {
+    fill_line(U, I, J, c->hy, 1, k0, k1);
+    line_beta(S, c->p, U, I, J, c->hx, c->hy, 1, 0, k0, k1);
+    fill_line(U, I, J, c->hx, 0, k0, k1);
+    line_beta(S, c->p, U, I, J, c->hx, c->hy, 0, 0, k0, k1);
 }
 
 /* ------------------------------------------------ restriction/prolongation */
@@ -501,7 +622,7 @@ typedef struct {
 static int check_cfg(const orc_cfg* c) {
     if (!c || c->I <= 0 || c->J <= 0 || c->nk <= 0 || c->gm < 1 || c->gm > ORC_MAX_GEN) return ORC_ERR_ARG;
     if (c->hx < 0 || c->hy < 0 || c->hz < 0 || c->p < 0) return ORC_ERR_ARG;
-    if (c->proc != 1 && c->proc != 6) return ORC_ERR_ARG;
+    if (c->proc != 1 && c->proc != 6 && c->proc != 3 && c->proc != 8) return ORC_ERR_ARG;
     int d = 1 << (c->gm - 1);
     if (c->I % d || c->J % d) return ORC_ERR_DIV;
     if (c->gm > 1 && (c->I / d < 2 || c->J / d < 2)) return ORC_ERR_DIV;
@@ -610,7 +731,8 @@ static void weight_gen(const orc_cfg* c, arr3 V, int I, int J, double a, double 
 
 static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G, int k0, int k1) {
     const int gm = c->gm, hx = c->hx, hy = c->hy;
-    const int filt1 = (c->proc == 1) || c->l_filt_g1;
+    const int filt1 = (c->proc == 1) || (c->proc == 3) || c->l_filt_g1;
+    const int fast = c->proc == 3 || c->proc == 8;
     double* tb = (double*)malloc(sizeof(double) * (size_t)c->nk);
     /* up: V -> H_2 -> ... -> H_gm */
     for (int g = 0; g + 1 < gm; ++g) {
@@ -622,6 +744,12 @@ static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_
         arr3 U = g ? G[g].H : V;
         int I = G[g].I, J = G[g].J;
         if (g == 0 && !filt1) continue;
+        if (fast) {
+            fast_adjoint(c, S, U, I, J, k0, k1);
+            weight_gen(c, U, I, J, c->a[g], c->b[g], k0, k1);
+            fast_forward(c, S, U, I, J, k0, k1);
+            continue;
+        }
         vrbeta2t(S, c->p, U, G[g].tmp, 1, I, 1, J, k0, k1);
         fold_h(U, I, J, hx, hy, k0, k1);
         weight_gen(c, U, I, J, c->a[g], c->b[g], k0, k1);
@@ -699,12 +827,17 @@ int orc_filter_compact(const orc_cfg* c, const double* x, double* y) {
 /* u_g = B_g R_g Bz^T x for every generation, written into G[g] (gen 0 into V). */
 static void half_chain(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G) {
     if (c->l_vertical_filter && c->nzcol > 0) vfilter(c, S, V, 1);
-    const int filt1 = (c->proc == 1) || c->l_filt_g1;
+    const int filt1 = (c->proc == 1) || (c->proc == 3) || c->l_filt_g1;
+    const int fast = c->proc == 3 || c->proc == 8;
     for (int g = 0; g + 1 < c->gm; ++g)
         restrict_gen(c, g ? G[g].H : V, &G[g], G[g + 1].H, 0, c->nk);
     for (int g = 0; g < c->gm; ++g) {
         if (g == 0 && !filt1) continue;
         arr3 U = g ? G[g].H : V;
+        if (fast) {
+            fast_adjoint(c, S, U, G[g].I, G[g].J, 0, c->nk);
+            continue;
+        }
         vrbeta2t(S, c->p, U, G[g].tmp, 1, G[g].I, 1, G[g].J, 0, c->nk);
         fold_h(U, G[g].I, G[g].J, c->hx, c->hy, 0, c->nk);
     }
@@ -725,7 +858,7 @@ int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double
     arr3 ay = {Vy, c->nk, 1 - c->hx, c->I + c->hx, 1 - c->hy, c->J + c->hy};
     half_chain(c, &S, ax, Gx);
     half_chain(c, &S, ay, Gy);
-    const int filt1 = (c->proc == 1) || c->l_filt_g1;
+    const int filt1 = (c->proc == 1) || (c->proc == 3) || c->l_filt_g1;
     for (int g = 0; g < c->gm; ++g) {
         double s = 0.0;
         if (g == 0 && !filt1) { ga[g] = 0.0; continue; }
@@ -772,6 +905,16 @@ int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y) 
         }
         from_halo(&cc, V, y);
         free(tb); a3_free(&t); free(V);
+        return ORC_OK;
+    }
+    if (which == 6 || which == 7) {
+        orc_cfg cc = *c; cc.I = I; cc.J = J;
+        double* V = to_halo(&cc, x);
+        arr3 a = {V, nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy};
+        if (which == 6) fast_forward(c, &S, a, I, J, 0, nk);
+        else fast_adjoint(c, &S, a, I, J, 0, nk);
+        from_halo(&cc, V, y);
+        free(V);
         return ORC_OK;
     }
     if (which == 4 || which == 5) {

@@ -2,8 +2,10 @@
  * FP64 CPU oracle for the MGBF filtering pipeline (test infrastructure only).
  *
  * This is a plain-C restatement of the reference's CPU algorithm for
- * filtering_procedure(1) (filtering_rad2_bckg) and filtering_procedure(6)
- * (filtering_rad2_ens), evaluated on the whole filter grid as one domain.
+ * filtering_procedure(1) (filtering_rad2_bckg), filtering_procedure(6)
+ * (filtering_rad2_ens) and the fast 1D+1D variants filtering_procedure(3)
+ * (filtering_fast_bckg) and (8) (filtering_fast_ens), evaluated on the
+ * whole filter grid as one domain.
  * It exists to check the CUDA library; only tests, the smoke check and the
  * CPU-baseline leg of the benchmark call it.  Nothing in the shipped library
  * links or executes it.
@@ -39,9 +41,9 @@ typedef struct orc_cfg {
     double a[ORC_MAX_GEN];  /* per-generation weights a_g (a[0] = gen 1)      */
     double b[ORC_MAX_GEN];  /* Helmholtz Laplacian coefficients (reference: 0) */
     int lhelm;           /* use weighting_helm form                           */
-    int proc;            /* 1 (rad2_bckg) or 6 (rad2_ens)                     */
+    int proc;            /* 1 rad2_bckg, 6 rad2_ens, 3 fast_bckg, 8 fast_ens  */
     int l_vertical_filter;
-    int l_filt_g1;       /* proc 6 only                                       */
+    int l_filt_g1;       /* procs 6 and 8 only                                */
     int lquart;          /* quadratic (3-point) interpolation                 */
     int lm;              /* levels per vertical column                        */
     int nzcol;           /* number of z columns at offsets (k-1)*lm           */
@@ -71,12 +73,16 @@ int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double
  *        2 = horizontal forward (fill + vrbeta2), 3 = horizontal adjoint
  *            (vrbeta2t + fold), on a generation-g grid (g given by gen),
  *        4 = restriction R (g -> g+1; x is gen g, y is gen g+1),
- *        5 = prolongation P (g+1 -> g; x is gen g+1, y is gen g). */
+ *        5 = prolongation P (g+1 -> g; x is gen g+1, y is gen g),
+ *        6 = fast-filter horizontal forward (bocoy, rbeta y, bocox, rbeta x),
+ *        7 = fast-filter horizontal adjoint (rbetaT x, bocoTx, rbetaT y,
+ *            bocoTy), on a generation-g grid. */
 int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y);
 
 /* Setup values (for tests): rmom2_1, rmom2_2, exx (1D), exx (2D), ss1, ss2,
- * vertical reach, horizontal reach.  Returns error if a reach exceeds a halo. */
-int orc_setup_values(const orc_cfg* c, double out[8]);
+ * vertical reach, horizontal reach, and for the fast filters' line filter
+ * exx, ss, reach.  Returns error if a reach exceeds a halo. */
+int orc_setup_values(const orc_cfg* c, double out[11]);
 
 #ifdef __cplusplus
 }

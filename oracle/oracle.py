@@ -2,7 +2,7 @@
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
 this module.  It restates the reference's CPU algorithm for
-filtering_procedure(1|6); it is the checker, never the thing measured or
+filtering_procedure(1|3|6|8); it is the checker, never the thing measured or
 shipped.  Parity with the reference itself is unpinned (see mgbf_oracle.h).
 """
 from __future__ import annotations
@@ -143,7 +143,8 @@ def weight_grads(cfg: OracleConfig, x: np.ndarray, gy: np.ndarray) -> np.ndarray
     return ga
 
 
-STAGE_Z_FWD, STAGE_Z_ADJ, STAGE_H_FWD, STAGE_H_ADJ, STAGE_RESTRICT, STAGE_PROLONG = range(6)
+(STAGE_Z_FWD, STAGE_Z_ADJ, STAGE_H_FWD, STAGE_H_ADJ, STAGE_RESTRICT, STAGE_PROLONG, STAGE_FAST_FWD,
+ STAGE_FAST_ADJ) = range(8)
 
 
 def stage(cfg: OracleConfig, which: int, gen: int, x: np.ndarray) -> np.ndarray:
@@ -162,8 +163,9 @@ def stage(cfg: OracleConfig, which: int, gen: int, x: np.ndarray) -> np.ndarray:
 
 
 def setup_values(cfg: OracleConfig) -> dict:
-    out = np.zeros(8, dtype=np.float64)
+    out = np.zeros(11, dtype=np.float64)
     c = cfg.to_c()
     _check(_load().orc_setup_values(ctypes.byref(c), _ptr(out)), "orc_setup_values")
-    keys = ["rmom2_1", "rmom2_2", "exx1", "exx2", "ss1", "ss2", "reach_z", "reach_h"]
+    keys = ["rmom2_1", "rmom2_2", "exx1", "exx2", "ss1", "ss2", "reach_z", "reach_h", "exx_line", "ss_line",
+            "reach_line"]
     return dict(zip(keys, out.tolist()))

@@ -57,7 +57,7 @@ class MgbfDims(ctypes.Structure):
     _fields_ = [
         ("im", _I), ("jm", _I), ("km_all", _I), ("km", _I), ("km3_all", _I), ("gm", _I),
         ("hx", _I), ("hy", _I), ("hz", _I), ("reach_h", _I), ("reach_z", _I), ("layout", _I),
-        ("field_elems", ctypes.c_size_t), ("hbeta_kernel", _I),
+        ("field_elems", ctypes.c_size_t), ("hbeta_kernel", _I), ("reach_line", _I),
     ]
 
 

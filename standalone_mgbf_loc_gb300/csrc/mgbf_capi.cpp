@@ -235,12 +235,14 @@ struct Group {
     double ampl01 = 1, ampl02 = 1;
     HStencil hs;
     ZStencil zs;
+    LStencil ls;         // fast filters' line beta (procs 3, 8)
+    std::string ls_err;  // why ls is unusable (reach beyond hx/hy), or empty
     int HXP = 0;  // x padding of internal generation buffers
     DevBuf mrow;  // int table, shared by all types
     AccTables tab[2];  // [0] float, [1] double
     // internal buffers per storage type and generation: A, B, C
     struct Set {
-        std::vector<std::unique_ptr<DevBuf>> A, B, C;
+        std::vector<std::unique_ptr<DevBuf>> A, B, C, D;  // D: between the fast filters' two line passes
     } bufs[3];
     // TMA maps of the A/B buffers: key = dtype*64 + gen*2 + (0: A, 1: B),
     // each with the base address it was encoded for
@@ -314,7 +316,7 @@ View gen_view(const Plan& P, const Group& G, void* base, DType t, int g) {
     return v;
 }
 
-int ensure_bufs(Plan& P, Group& G, DType t, bool needC) {
+int ensure_bufs(Plan& P, Group& G, DType t, bool needC, bool needD = false) {
     auto& S = G.bufs[(int)t];
     auto grow = [&](std::vector<std::unique_ptr<DevBuf>>& v) -> int {
         if ((int)v.size() < P.gm) v.resize(P.gm);
@@ -329,6 +331,7 @@ int ensure_bufs(Plan& P, Group& G, DType t, bool needC) {
     if ((rc = grow(S.A))) return rc;
     if ((rc = grow(S.B))) return rc;
     if (needC && (rc = grow(S.C))) return rc;
+    if (needD && (rc = grow(S.D))) return rc;
     return 0;
 }
 
@@ -343,6 +346,8 @@ struct Exec {
     View A(int g) { return gen_view(P, G, G.bufs[(int)t].A[g]->p, t, g); }
     View B(int g) { return gen_view(P, G, G.bufs[(int)t].B[g]->p, t, g); }
     View C(int g) { return gen_view(P, G, G.bufs[(int)t].C[g]->p, t, g); }
+    View D(int g) { return gen_view(P, G, G.bufs[(int)t].D[g]->p, t, g); }
+    bool fast = false;  // procs 3 and 8: separable line filters instead of the radial disk
 
     double pts(int g) const { return (double)G.nk * gen_I(P, g) * gen_J(P, g); }
 
@@ -444,9 +449,27 @@ struct Exec {
         return 0;
     }
 
+    // One line pass of the fast filters: dir 0 along x, 1 along y.
+    int line(int g, View in, View out, int dir, double scale) {
+        LineArgs a;
+        a.in = in; a.out = out; a.nk = G.nk; a.I = gen_I(P, g); a.J = gen_J(P, g);
+        a.dir = dir; a.R = G.ls.R; a.scale = scale;
+        for (int d = 0; d <= G.ls.R; ++d) a.w[d] = G.ls.w[d];
+        LK(launch_line(t, a, stream));
+        return 0;
+    }
+
     int hpass(int g, View in, View out, double scale, int mirror, int stage, int which_in) {
         const int I = gen_I(P, g), J = gen_J(P, g);
         StageTimer tm(stage, stream, pts(g));
+        if (fast) {
+            // adjoint side (rbetaT x, bocoTx, rbetaT y, bocoTy): x first;
+            // forward side (bocoy, rbeta y, bocox, rbeta x): y first
+            const int first = which_in == 0 ? 0 : 1;
+            int rc;
+            if ((rc = line(g, in, D(g), first, 1.0))) return rc;
+            return line(g, D(g), out, 1 - first, scale);
+        }
         if (moment_path()) {
             int variant = 0, rows = default_rows(g);
             auto it = G.tune.find((int)t * 1024 + g * 2 + which_in);
@@ -590,6 +613,20 @@ int build_group(Plan& P, Group& G, bool zneeded) {
                                                " exceeds the coarsest generation " +
                                                std::to_string(IG) + "x" + std::to_string(JG));
     G.HXP = G.hs.R + 8;
+    // the fast filters' line stencil: an error only when procs 3/8 run
+    // (mgbf_create rejects it up front, as def_mg_weights does)
+    G.ls_err.clear();
+    if (build_lstencil(G.p, G.ampl02, G.hx, G.hy, G.ls, err)) {
+        G.ls_err = err;
+        G.ls.R = -1;
+    } else if (G.ls.R > kMaxLineReach) {
+        G.ls_err = "line filter reach " + std::to_string(G.ls.R) + " above " + std::to_string(kMaxLineReach);
+        G.ls.R = -1;
+    } else if (G.ls.R > IG || G.ls.R > JG) {
+        G.ls_err = "line filter reach " + std::to_string(G.ls.R) + " exceeds the coarsest generation " +
+                   std::to_string(IG) + "x" + std::to_string(JG);
+        G.ls.R = -1;
+    }
     return 0;
 }
 
@@ -931,6 +968,7 @@ int mgbf_get_dims(const mgbf_handle* h, mgbf_dims* d) {
     d->reach_h = G.hs.R; d->reach_z = G.zs.mz; d->layout = h->cfg.layout;
     d->field_elems = h->field_elems;
     d->hbeta_kernel = (G.hs.canonical && hmom_available(DType::F32, G.hs.R, G.hs.p)) ? 1 : 0;
+    d->reach_line = G.ls.R;
     return MGBF_OK;
 }
 
@@ -940,17 +978,22 @@ int mgbf_set_weights(mgbf_handle* h, const double* a, int n) {
     return MGBF_OK;
 }
 
+static bool is_fast(int mg_filt) { return mg_filt == 3 || mg_filt == 8; }
+static bool is_bckg(int mg_filt) { return mg_filt == 1 || mg_filt == 3; }
+
 static int check_proc(mgbf_handle* h, int mg_filt, bool& noop) {
     noop = false;
-    if (mg_filt == 1 || mg_filt == 6) {
-        if (mg_filt == 1 && h->cfg.n_ens != 1)
-            return fail(MGBF_ERR_CONFIG, "filtering_rad2_bckg (proc 1) needs n_ens = 1: its arrays are dimensioned km, not km_all");
-        if (mg_filt == 6 && h->cfg.l_vertical_filter && h->cfg.km2 > 0 && h->cfg.km3 > 0)
-            return fail(MGBF_ERR_CONFIG, "filtering_rad2_ens (proc 6) with the vertical filter needs km2 = 0: sup_vrbeta1_ens views VALL with leading dimension km3_all*lm");
+    if (mg_filt == 1 || mg_filt == 6 || mg_filt == 3 || mg_filt == 8) {
+        if (is_bckg(mg_filt) && h->cfg.n_ens != 1)
+            return fail(MGBF_ERR_CONFIG, "filtering_rad2_bckg / filtering_fast_bckg (procs 1, 3) need n_ens = 1: their arrays are dimensioned km, not km_all");
+        if (!is_bckg(mg_filt) && h->cfg.l_vertical_filter && h->cfg.km2 > 0 && h->cfg.km3 > 0)
+            return fail(MGBF_ERR_CONFIG, "filtering_rad2_ens / filtering_fast_ens (procs 6, 8) with the vertical filter need km2 = 0: sup_vrbeta1_ens views VALL with leading dimension km3_all*lm");
+        if (is_fast(mg_filt) && h->plan.groups[0].ls.R < 0)
+            return fail(MGBF_ERR_DIVISIBILITY, h->plan.groups[0].ls_err);
         return MGBF_OK;
     }
     if (mg_filt >= 2 && mg_filt <= 8)
-        return fail(MGBF_ERR_UNSUPPORTED, "filtering procedure " + std::to_string(mg_filt) + " is not implemented (supported: 1, 6)");
+        return fail(MGBF_ERR_UNSUPPORTED, "filtering procedure " + std::to_string(mg_filt) + " is not implemented (supported: 1, 3, 6, 8)");
     noop = true;  // no case default in the reference's select
     return MGBF_OK;
 }
@@ -960,16 +1003,22 @@ static int run_proc(mgbf_handle* h, int mg_filt, const void* xin, void* yout, DT
     Group& G = P.groups[0];
     int rc;
     if ((rc = ensure_tables(P, G, t))) return rc;
-    if ((rc = ensure_bufs(P, G, t, false))) return rc;
-    const int nzcol = (h->cfg.l_vertical_filter && h->cfg.lm > 1) ? (mg_filt == 1 ? h->nzcol_proc1 : h->nzcol_proc6) : 0;
-    const bool filt1 = mg_filt == 1 || h->cfg.l_filt_g1;
+    if ((rc = ensure_bufs(P, G, t, false, is_fast(mg_filt)))) return rc;
+    const int nzcol = (h->cfg.l_vertical_filter && h->cfg.lm > 1) ? (is_bckg(mg_filt) ? h->nzcol_proc1 : h->nzcol_proc6) : 0;
+    const bool filt1 = is_bckg(mg_filt) || h->cfg.l_filt_g1;
     Exec ex{P, G, t, stream};
+    ex.fast = is_fast(mg_filt);
     View x = field_view(h, const_cast<void*>(xin), t);
     View y = field_view(h, yout, t);
     if ((rc = ex.forward(x, y, nzcol, filt1))) return rc;
     if (h->cfg.layout == MGBF_LAYOUT_HALO && filt1) {
+        // vrbeta2 zeroes the whole halo; the line filters leave its corners
         StageTimer tm(ST_HALO, stream, 0.0);
-        LK(launch_zero_halo(t, y, G.nk, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
+        if (ex.fast) {
+            LK(launch_zero_halo_edges(t, y, G.nk, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
+        } else {
+            LK(launch_zero_halo(t, y, G.nk, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
+        }
     }
     return 0;
 }
@@ -1022,7 +1071,7 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
     Plan& P = h->plan;
     Group& G = P.groups[0];
     if ((rc = ensure_tables(P, G, t))) return rc;
-    if ((rc = ensure_bufs(P, G, t, true))) return rc;
+    if ((rc = ensure_bufs(P, G, t, true, is_fast(mg_filt)))) return rc;
     const void *dx = x, *dgy = gy;
     void* dgx = gx;
     const size_t bytes = h->field_elems * elem_size(t);
@@ -1034,9 +1083,10 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
         dgy = h->stage2[(int)t].p;
         dgx = h->stage2[(int)t].p;
     }
-    const int nzcol = (h->cfg.l_vertical_filter && h->cfg.lm > 1) ? (mg_filt == 1 ? h->nzcol_proc1 : h->nzcol_proc6) : 0;
-    const bool filt1 = mg_filt == 1 || h->cfg.l_filt_g1;
+    const int nzcol = (h->cfg.l_vertical_filter && h->cfg.lm > 1) ? (is_bckg(mg_filt) ? h->nzcol_proc1 : h->nzcol_proc6) : 0;
+    const bool filt1 = is_bckg(mg_filt) || h->cfg.l_filt_g1;
     Exec ex{P, G, t, stream};
+    ex.fast = is_fast(mg_filt);
     View vx = field_view(h, const_cast<void*>(dx), t);
     View vg = field_view(h, const_cast<void*>(dgy), t);
     View vo = field_view(h, dgx, t);
@@ -1060,7 +1110,11 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
     if ((rc = ex.second_half(vo, nzcol, filt1, P.a))) return rc;
     if (h->cfg.layout == MGBF_LAYOUT_HALO && filt1) {
         StageTimer tm(ST_HALO, stream, 0.0);
-        LK(launch_zero_halo(t, vo, G.nk, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
+        if (ex.fast) {
+            LK(launch_zero_halo_edges(t, vo, G.nk, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
+        } else {
+            LK(launch_zero_halo(t, vo, G.nk, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
+        }
     }
     CU(cudaMemcpyAsync(ga, P.dot.p, sizeof(double) * P.gm, cudaMemcpyDeviceToHost, s));
     if (mem == MGBF_MEM_HOST)

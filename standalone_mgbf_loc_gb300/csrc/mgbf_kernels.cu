@@ -735,6 +735,87 @@ __global__ void __launch_bounds__(128) k_prolong_z4(ProlongZArgs z) {
     }
 }
 
+// ------------------------------------------------- fast filters: line beta
+// vrbeta1 along one horizontal axis (jp_pbfil.f90:856-885) as the fast
+// filters apply it (mg_filtering.f90:825-997, 1316-1506): the mirror fill of
+// bocox/bocoy is an index reflection, so the kernel reads the interior only.
+// The stencil is symmetric and the mirror half-sample, so the same gather
+// also gives the adjoint (rbetaT then bocoTx/bocoTy).  Each thread owns
+// levels k..k+3 and TL consecutive outputs of one line; its window of
+// TL+2MR inputs sits in registers (MR = compile-time reach bound, taps past
+// the runtime reach carry weight 0).
+template <typename T, int MR, int TL>
+__global__ void __launch_bounds__(128) k_line_w(LineArgs a) {
+    using A = typename AccOf<T>::type;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (k >= a.nk) return;
+    const int n = a.dir ? a.J : a.I;
+    const int t0 = blockIdx.y * TL;
+    const int line = blockIdx.z;
+    const long long ls_in = a.dir ? a.in.sj : a.in.si, os_in = a.dir ? a.in.si : a.in.sj;
+    const long long ls_out = a.dir ? a.out.sj : a.out.si, os_out = a.dir ? a.out.si : a.out.sj;
+    const T* in = static_cast<const T*>(a.in.p) + k + os_in * line;
+    T* out = static_cast<T*>(a.out.p) + k + os_out * line;
+    A w[MR + 1];
+#pragma unroll
+    for (int d = 0; d <= MR; ++d) w[d] = d <= a.R ? static_cast<A>(a.w[d]) : A(0);
+    A x[TL + 2 * MR][4];
+#pragma unroll
+    for (int s2 = 0; s2 < TL + 2 * MR; ++s2) V4<T>::ld(in + ls_in * reflect_half(t0 - MR + s2, n), x[s2]);
+    const A sc = static_cast<A>(a.scale);
+#pragma unroll
+    for (int q = 0; q < TL; ++q) {
+        if (t0 + q >= n) break;
+        A y[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            A acc = w[0] * x[q + MR][e];
+#pragma unroll
+            for (int d = 1; d <= MR; ++d) acc = fma(w[d], x[q + MR + d][e] + x[q + MR - d][e], acc);
+            y[e] = acc * sc;
+        }
+        V4<T>::st(out + ls_out * (t0 + q), y);
+    }
+}
+
+// Any reach: taps read through L1, four outputs per thread.
+template <typename T>
+__global__ void __launch_bounds__(128) k_line_g(LineArgs a) {
+    using A = typename AccOf<T>::type;
+    constexpr int TL = 4;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (k >= a.nk) return;
+    const int n = a.dir ? a.J : a.I;
+    const int t0 = blockIdx.y * TL;
+    const int line = blockIdx.z;
+    const long long ls_in = a.dir ? a.in.sj : a.in.si, os_in = a.dir ? a.in.si : a.in.sj;
+    const long long ls_out = a.dir ? a.out.sj : a.out.si, os_out = a.dir ? a.out.si : a.out.sj;
+    const T* in = static_cast<const T*>(a.in.p) + k + os_in * line;
+    T* out = static_cast<T*>(a.out.p) + k + os_out * line;
+    const A sc = static_cast<A>(a.scale);
+#pragma unroll
+    for (int q = 0; q < TL; ++q) {
+        const int t = t0 + q;
+        if (t >= n) break;
+        A acc[4], v[4];
+        V4<T>::ld(in + ls_in * t, v);
+        const A w0 = static_cast<A>(a.w[0]);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[e] = w0 * v[e];
+        for (int d = 1; d <= a.R; ++d) {
+            A u[4];
+            V4<T>::ld(in + ls_in * reflect_half(t + d, n), u);
+            V4<T>::ld(in + ls_in * reflect_half(t - d, n), v);
+            const A wd = static_cast<A>(a.w[d]);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[e] = fma(wd, u[e] + v[e], acc[e]);
+        }
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[e] *= sc;
+        V4<T>::st(out + ls_out * t, acc);
+    }
+}
+
 // ------------------------------------------- direct-sum radial beta filter
 // General support table (any aspect, any integer p): the gather form of
 // fill_h + vrbeta2 (jp_pbfil.f90:888-928).  Because the radial weights are
@@ -833,6 +914,21 @@ __global__ void __launch_bounds__(256) k_zero_halo(View v, int nk, int I, int J,
     const int j = (int)blockIdx.y - hy;
     const bool halo = i < 0 || i >= I || j < 0 || j >= J;
     if (halo) static_cast<T*>(v.p)[v.sj * j + v.si * i + k] = T(0);
+}
+
+// The fast filters leave the halo corners as they were (bocox/bocoy write
+// the x halo of interior rows and the y halo of interior columns only) and
+// zero the rest of the halo (vrbeta1's a = b on each line).
+template <typename T>
+__global__ void __launch_bounds__(256) k_zero_halo_edges(View v, int nk, int I, int J, int hx, int hy) {
+    const int ni = I + 2 * hx;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nk * ni) return;
+    const int i = (int)(t / nk) - hx;
+    const int k = (int)(t - (long long)(i + hx) * nk);
+    const int j = (int)blockIdx.y - hy;
+    const bool iin = i >= 0 && i < I, jin = j >= 0 && j < J;
+    if (iin != jin) static_cast<T*>(v.p)[v.sj * j + v.si * i + k] = T(0);
 }
 
 template <typename T>
@@ -1087,6 +1183,93 @@ int launch_zero_halo(DType t, View v, int nk, int I, int J, int hx, int hy, void
     dim3 block(256), grid((unsigned)((n + 255) / 256), J + 2 * hy);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     MGBF_DISPATCH(t, (k_zero_halo<T><<<grid, block, 0, s>>>(v, nk, I, J, hx, hy)));
+    return last_err();
+}
+
+int launch_zero_halo_edges(DType t, View v, int nk, int I, int J, int hx, int hy, void* stream) {
+    const long long n = (long long)nk * (I + 2 * hx);
+    if (n == 0 || (hx == 0 && hy == 0)) return 0;
+    dim3 block(256), grid((unsigned)((n + 255) / 256), J + 2 * hy);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    MGBF_DISPATCH(t, (k_zero_halo_edges<T><<<grid, block, 0, s>>>(v, nk, I, J, hx, hy)));
+    return last_err();
+}
+
+// One level per thread (any nk, any alignment), four outputs, any reach.
+template <typename T>
+__global__ void __launch_bounds__(128) k_line_s(LineArgs a) {
+    using A = typename AccOf<T>::type;
+    constexpr int TL = 4;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.nk) return;
+    const int n = a.dir ? a.J : a.I;
+    const int t0 = blockIdx.y * TL;
+    const int line = blockIdx.z;
+    const long long ls_in = a.dir ? a.in.sj : a.in.si, os_in = a.dir ? a.in.si : a.in.sj;
+    const long long ls_out = a.dir ? a.out.sj : a.out.si, os_out = a.dir ? a.out.si : a.out.sj;
+    const T* in = static_cast<const T*>(a.in.p) + k + os_in * line;
+    T* out = static_cast<T*>(a.out.p) + k + os_out * line;
+    const A sc = static_cast<A>(a.scale);
+#pragma unroll
+    for (int q = 0; q < TL; ++q) {
+        const int t = t0 + q;
+        if (t >= n) break;
+        A acc = static_cast<A>(a.w[0]) * ldv(in + ls_in * t);
+        for (int d = 1; d <= a.R; ++d)
+            acc = fma(static_cast<A>(a.w[d]),
+                      ldv(in + ls_in * reflect_half(t + d, n)) + ldv(in + ls_in * reflect_half(t - d, n)), acc);
+        stv(out + ls_out * t, acc * sc);
+    }
+}
+
+template <typename T, int MR, int TL>
+static void line_launch(const LineArgs& a, int n, int m, cudaStream_t s) {
+    const int nt = a.nk / 4;
+    dim3 block(std::min(128, ((nt + 31) / 32) * 32));
+    dim3 grid((nt + block.x - 1) / block.x, (n + TL - 1) / TL, m);
+    k_line_w<T, MR, TL><<<grid, block, 0, s>>>(a);
+}
+
+int launch_line(DType t, const LineArgs& a, void* stream) {
+    if (a.nk == 0 || a.I == 0 || a.J == 0) return 0;
+    if (a.R < 0 || a.R > kMaxLineReach) return (int)cudaErrorInvalidValue;
+    const int n = a.dir ? a.J : a.I, m = a.dir ? a.I : a.J;
+    if (a.R > n) return (int)cudaErrorInvalidValue;  // one mirror image at most
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t es = elem_size(t);
+    const bool vec = a.nk % 4 == 0 && aligned16(a.in.p) && aligned16(a.out.p) && (a.in.si * es) % 16 == 0 &&
+                     (a.in.sj * es) % 16 == 0 && (a.out.si * es) % 16 == 0 && (a.out.sj * es) % 16 == 0;
+    if (!vec || (t == DType::BF16 && (a.nk % 8 || !aligned16(a.in.p)))) {
+        dim3 block(128), grid((a.nk + 127) / 128, (n + 3) / 4, m);
+        MGBF_DISPATCH(t, (k_line_s<T><<<grid, block, 0, s>>>(a)));
+        return last_err();
+    }
+    if (t == DType::F64) {
+        if (a.R <= 4) line_launch<double, 4, 4>(a, n, m, s);
+        else if (a.R <= 8) line_launch<double, 8, 4>(a, n, m, s);
+        else {
+            const int nt = a.nk / 4;
+            dim3 block(std::min(128, ((nt + 31) / 32) * 32)), grid((nt + block.x - 1) / block.x, (n + 3) / 4, m);
+            k_line_g<double><<<grid, block, 0, s>>>(a);
+        }
+        return last_err();
+    }
+    auto run = [&](auto tag) {
+        using T = decltype(tag);
+        if (a.R <= 4) {
+            line_launch<T, 4, 16>(a, n, m, s);
+        } else if (a.R <= 8) {
+            line_launch<T, 8, 8>(a, n, m, s);
+        } else if (a.R <= 16) {
+            line_launch<T, 16, 8>(a, n, m, s);
+        } else {
+            const int nt = a.nk / 4;
+            dim3 block(std::min(128, ((nt + 31) / 32) * 32)), grid((nt + block.x - 1) / block.x, (n + 3) / 4, m);
+            k_line_g<T><<<grid, block, 0, s>>>(a);
+        }
+    };
+    if (t == DType::F32) run(float());
+    else run(__nv_bfloat16());
     return last_err();
 }
 

@@ -32,6 +32,19 @@ struct ZArgs {
     int mirror_hx;      // write a mirrored x halo of this width (0: none)
 };
 
+// 1D line beta of the fast filters along x (dir 0: i, stride si) or y
+// (dir 1: j, stride sj) of an interior (nk, I, J) view, half-sample mirror
+// at both ends: out = scale * sum_{|d|<=R} w[|d|] in(mirror(t+d)).
+constexpr int kMaxLineReach = 64;
+struct LineArgs {
+    View in, out;
+    int nk, I, J;
+    int dir;
+    int R;
+    double w[kMaxLineReach + 1];  // w[0..R], already normalised
+    double scale;
+};
+
 struct RestrictArgs {
     View fine, coarse;
     int nk, If, Jf;     // fine interior sizes; coarse = If/2, Jf/2
@@ -119,6 +132,8 @@ int launch_prolong_z(DType t, const ProlongZArgs& a, void* stream);
 int launch_hdirect(DType t, const HDirectArgs& a, void* stream);
 int launch_mirror_x(DType t, View v, int nk, int I, int J, int hx, void* stream);
 int launch_copy(DType t, View in, View out, int nk, int I, int J, int mirror_hx, void* stream);
+int launch_line(DType t, const LineArgs& a, void* stream);
+int launch_zero_halo_edges(DType t, View v, int nk, int I, int J, int hx, int hy, void* stream);
 int launch_zero_halo(DType t, View v, int nk, int I, int J, int hx, int hy, void* stream);
 int launch_dot(DType t, const DotArgs& a, void* stream);
 

@@ -243,6 +243,37 @@ int build_interp(int nf, bool quart, Interp1D& T, std::string& err) {
     return MGBF_OK;
 }
 
+// getlinesum1 (jp_pbfil.f90:149-180) and the vrbeta1 weights
+// (jp_pbfil.f90:856-885) for el = paspx = paspy = pasp02.
+int build_lstencil(int p, double ampl02, int hx, int hy, LStencil& out, std::string& err) {
+    if (!(ampl02 > 0.0)) {
+        err = "mg_ampl02 must be positive";
+        return MGBF_ERR_CONFIG;
+    }
+    out = LStencil{};
+    out.p = p;
+    out.exx = ampl02 * (1.0 / std::sqrt(2.0 * p + 3.0));
+    const double x = 1.0 / out.exx;
+    const int lo = (int)std::ceil(-x + kEps), hi = (int)std::floor(x - kEps);
+    if (lo < -hx || hi > hx || lo < -hy || hi > hy) {
+        err = "getlinesum1 on paspx/paspy: reach " + std::to_string(std::max(-lo, hi)) + " exceeds hx/hy";
+        return MGBF_ERR_REACH;
+    }
+    double sum = 0.0;
+    for (int g = lo; g <= hi; ++g) {
+        const double rr = (g * out.exx) * (g * out.exx);
+        sum += std::pow(1.0 - rr, p);
+    }
+    out.s = 1.0 / sum;
+    out.R = hi;
+    out.w.resize(hi + 1);
+    for (int g = 0; g <= hi; ++g) {
+        const double rr = (g * out.exx) * (g * out.exx);
+        out.w[g] = out.s * std::pow(1.0 - rr, p);
+    }
+    return MGBF_OK;
+}
+
 int check_other_reaches(int p, double ampl02, double ampl03, int hx, int hy, int hz, std::string& err) {
     // getlinesum(hx,1,im,paspx,ssx) / (hy,...,paspy,ssy): paspx = pasp02 is
     // used without cholaspect (mg_intstate.f90:370-375,427-428).

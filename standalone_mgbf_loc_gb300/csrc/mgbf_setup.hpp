@@ -3,6 +3,7 @@
 // Restates the reference's setup arithmetic (all FP64, as in the reference):
 //   rmom2_k            mg_parameter.f90:567-572
 //   cholaspect1/2      jp_pbfil.f90:74-107 (diagonal aspect tensors)
+//   paspx / paspy      mg_intstate.f90:370-375, 427-428 (no cholaspect)
 //   getlinesum1/2      jp_pbfil.f90:149-218 (support and normalisation)
 //   vrbeta1/2 weights  jp_pbfil.f90:856-928 (frow = s*(1-rr)^p)
 //   def_offset_coef    mg_interpolate.f90:61-86
@@ -31,6 +32,16 @@ struct HStencil {
     HMomCoefs<double> mom{};    // moment coefficients (valid if canonical)
 };
 
+// The fast filters' (procs 3 and 8) 1D horizontal line beta: vrbeta1 along
+// x and y with paspx = paspy = pasp02 taken WITHOUT cholaspect
+// (mg_intstate.f90:370-375), so exx = mg_ampl02 * rmom2_1.
+struct LStencil {
+    int p = 2;
+    double exx = 0, s = 0;
+    int R = 0;                  // reach: taps -R..R
+    std::vector<double> w;      // R+1 normalised weights s*(1-(g exx)^2)^p, g = 0..R
+};
+
 struct ZStencil {
     int lm = 0, mz = 0;
     double exx = 0, s = 0;
@@ -51,6 +62,7 @@ int build_hstencil(int p, double ampl02, int hx, int hy, HStencil& out, std::str
 int build_zstencil(int p, double ampl01, int hz, int lm, bool need_mirror, ZStencil& out,
                    std::string& err);
 int build_interp(int nf, bool quart, Interp1D& out, std::string& err);
+int build_lstencil(int p, double ampl02, int hx, int hy, LStencil& out, std::string& err);
 
 // Reach checks def_mg_weights performs for the other filters of the
 // reference (getlinesum on paspx/paspy, mg_intstate.f90:427-428, which skip

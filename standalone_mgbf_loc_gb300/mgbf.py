@@ -135,6 +135,7 @@ class MGBFDims:
     layout: int
     field_elems: int
     hbeta_kernel: int
+    reach_line: int
 
     def field_shape(self):
         if self.layout == _abi.MGBF_LAYOUT_HALO:

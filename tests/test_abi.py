@@ -144,7 +144,7 @@ def test_reach_larger_than_coarsest_generation(lib):
 def test_unsupported_and_unknown_procedures(lib):
     op = MGBF(small_config())
     x = np.zeros(op.field_shape())
-    for proc in (2, 3, 4, 5, 7, 8):
+    for proc in (2, 4, 5, 7):
         with pytest.raises(MGBFError) as e:
             op.filtering_procedure(proc, x)
         assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
@@ -194,3 +194,17 @@ def test_set_tuning_validation(lib):
         op.set_tuning(3)
     assert lib.mgbf_set_tuning(None, 1, 0, 0) == _abi.MGBF_ERR_ARG
     assert lib.mgbf_set_tuning(op._h, 7, 0, 0) == _abi.MGBF_ERR_ARG
+
+
+def test_fast_line_reach_beyond_coarsest_generation(lib):
+    """Procs 3/8 need the line reach within the coarsest generation (one
+    mirror image); the handle still serves procs 1/6.  Checked before any
+    device work, so no GPU is needed."""
+    c = small_config(nxPE=4, nyPE=4, im_filt=16, jm_filt=16, gm_max=4, gm_uncapped=True, hx=13, hy=13,
+                     mg_ampl02=0.2)
+    op = MGBF(c)
+    assert op.dims.gm == 4 and op.dims.reach_line == -1
+    with pytest.raises(MGBFError) as e:
+        op.filtering_procedure(3, np.zeros(op.field_shape()))
+    assert e.value.code == _abi.MGBF_ERR_DIVISIBILITY
+    assert "coarsest generation" in str(e.value)
