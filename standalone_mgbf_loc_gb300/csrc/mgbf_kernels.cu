@@ -744,25 +744,52 @@ __global__ void __launch_bounds__(128) k_prolong_z4(ProlongZArgs z) {
 // levels k..k+3 and TL consecutive outputs of one line; its window of
 // TL+2MR inputs sits in registers (MR = compile-time reach bound, taps past
 // the runtime reach carry weight 0).
+// Flat thread index -> (level group, strip of TL outputs, line), level
+// group fastest: warps stay full whatever nk is, and neighbouring warps take
+// neighbouring strips (their windows overlap in L1).
+template <typename A> __device__ __forceinline__ A line_w(const LineArgs& a, int d);
+template <> __device__ __forceinline__ float line_w<float>(const LineArgs& a, int d) { return a.wf[d]; }
+template <> __device__ __forceinline__ double line_w<double>(const LineArgs& a, int d) { return a.w[d]; }
+template <typename A> __device__ __forceinline__ A line_scale(const LineArgs& a);
+template <> __device__ __forceinline__ float line_scale<float>(const LineArgs& a) { return a.scalef; }
+template <> __device__ __forceinline__ double line_scale<double>(const LineArgs& a) { return a.scale; }
+
+struct LinePos {
+    int q, t0, line;
+    bool ok;
+};
+__device__ __forceinline__ LinePos line_pos(int nq, int n, int m, int TL) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nstrip = (n + TL - 1) / TL;
+    LinePos r;
+    r.q = (int)(idx % nq);
+    const long long rest = idx / nq;
+    r.t0 = (int)(rest % nstrip) * TL;
+    r.line = (int)(rest / nstrip);
+    r.ok = r.line < m;
+    return r;
+}
+
 template <typename T, int MR, int TL>
 __global__ void __launch_bounds__(128) k_line_w(LineArgs a) {
     using A = typename AccOf<T>::type;
-    const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
-    if (k >= a.nk) return;
     const int n = a.dir ? a.J : a.I;
-    const int t0 = blockIdx.y * TL;
-    const int line = blockIdx.z;
+    const LinePos lp = line_pos(a.nk / 4, n, a.dir ? a.I : a.J, TL);
+    if (!lp.ok) return;
+    const int k = 4 * lp.q;
+    const int t0 = lp.t0;
+    const int line = lp.line;
     const long long ls_in = a.dir ? a.in.sj : a.in.si, os_in = a.dir ? a.in.si : a.in.sj;
     const long long ls_out = a.dir ? a.out.sj : a.out.si, os_out = a.dir ? a.out.si : a.out.sj;
     const T* in = static_cast<const T*>(a.in.p) + k + os_in * line;
     T* out = static_cast<T*>(a.out.p) + k + os_out * line;
     A w[MR + 1];
 #pragma unroll
-    for (int d = 0; d <= MR; ++d) w[d] = d <= a.R ? static_cast<A>(a.w[d]) : A(0);
+    for (int d = 0; d <= MR; ++d) w[d] = d <= a.R ? line_w<A>(a, d) : A(0);
     A x[TL + 2 * MR][4];
 #pragma unroll
     for (int s2 = 0; s2 < TL + 2 * MR; ++s2) V4<T>::ld(in + ls_in * reflect_half(t0 - MR + s2, n), x[s2]);
-    const A sc = static_cast<A>(a.scale);
+    const A sc = line_scale<A>(a);
 #pragma unroll
     for (int q = 0; q < TL; ++q) {
         if (t0 + q >= n) break;
@@ -783,30 +810,31 @@ template <typename T>
 __global__ void __launch_bounds__(128) k_line_g(LineArgs a) {
     using A = typename AccOf<T>::type;
     constexpr int TL = 4;
-    const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
-    if (k >= a.nk) return;
     const int n = a.dir ? a.J : a.I;
-    const int t0 = blockIdx.y * TL;
-    const int line = blockIdx.z;
+    const LinePos lp = line_pos(a.nk / 4, n, a.dir ? a.I : a.J, TL);
+    if (!lp.ok) return;
+    const int k = 4 * lp.q;
+    const int t0 = lp.t0;
+    const int line = lp.line;
     const long long ls_in = a.dir ? a.in.sj : a.in.si, os_in = a.dir ? a.in.si : a.in.sj;
     const long long ls_out = a.dir ? a.out.sj : a.out.si, os_out = a.dir ? a.out.si : a.out.sj;
     const T* in = static_cast<const T*>(a.in.p) + k + os_in * line;
     T* out = static_cast<T*>(a.out.p) + k + os_out * line;
-    const A sc = static_cast<A>(a.scale);
+    const A sc = line_scale<A>(a);
 #pragma unroll
     for (int q = 0; q < TL; ++q) {
         const int t = t0 + q;
         if (t >= n) break;
         A acc[4], v[4];
         V4<T>::ld(in + ls_in * t, v);
-        const A w0 = static_cast<A>(a.w[0]);
+        const A w0 = line_w<A>(a, 0);
 #pragma unroll
         for (int e = 0; e < 4; ++e) acc[e] = w0 * v[e];
         for (int d = 1; d <= a.R; ++d) {
             A u[4];
             V4<T>::ld(in + ls_in * reflect_half(t + d, n), u);
             V4<T>::ld(in + ls_in * reflect_half(t - d, n), v);
-            const A wd = static_cast<A>(a.w[d]);
+            const A wd = line_w<A>(a, d);
 #pragma unroll
             for (int e = 0; e < 4; ++e) acc[e] = fma(wd, u[e] + v[e], acc[e]);
         }
@@ -1200,39 +1228,45 @@ template <typename T>
 __global__ void __launch_bounds__(128) k_line_s(LineArgs a) {
     using A = typename AccOf<T>::type;
     constexpr int TL = 4;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.nk) return;
     const int n = a.dir ? a.J : a.I;
-    const int t0 = blockIdx.y * TL;
-    const int line = blockIdx.z;
+    const LinePos lp = line_pos(a.nk, n, a.dir ? a.I : a.J, TL);
+    if (!lp.ok) return;
+    const int k = lp.q;
+    const int t0 = lp.t0;
+    const int line = lp.line;
     const long long ls_in = a.dir ? a.in.sj : a.in.si, os_in = a.dir ? a.in.si : a.in.sj;
     const long long ls_out = a.dir ? a.out.sj : a.out.si, os_out = a.dir ? a.out.si : a.out.sj;
     const T* in = static_cast<const T*>(a.in.p) + k + os_in * line;
     T* out = static_cast<T*>(a.out.p) + k + os_out * line;
-    const A sc = static_cast<A>(a.scale);
+    const A sc = line_scale<A>(a);
 #pragma unroll
     for (int q = 0; q < TL; ++q) {
         const int t = t0 + q;
         if (t >= n) break;
-        A acc = static_cast<A>(a.w[0]) * ldv(in + ls_in * t);
+        A acc = line_w<A>(a, 0) * ldv(in + ls_in * t);
         for (int d = 1; d <= a.R; ++d)
-            acc = fma(static_cast<A>(a.w[d]),
+            acc = fma(line_w<A>(a, d),
                       ldv(in + ls_in * reflect_half(t + d, n)) + ldv(in + ls_in * reflect_half(t - d, n)), acc);
         stv(out + ls_out * t, acc * sc);
     }
 }
 
-template <typename T, int MR, int TL>
-static void line_launch(const LineArgs& a, int n, int m, cudaStream_t s) {
-    const int nt = a.nk / 4;
-    dim3 block(std::min(128, ((nt + 31) / 32) * 32));
-    dim3 grid((nt + block.x - 1) / block.x, (n + TL - 1) / TL, m);
-    k_line_w<T, MR, TL><<<grid, block, 0, s>>>(a);
+static dim3 line_grid(long long nq, int n, int m, int TL) {
+    const long long threads = nq * ((n + TL - 1) / TL) * (long long)m;
+    return dim3((unsigned)((threads + 127) / 128));
 }
 
-int launch_line(DType t, const LineArgs& a, void* stream) {
-    if (a.nk == 0 || a.I == 0 || a.J == 0) return 0;
-    if (a.R < 0 || a.R > kMaxLineReach) return (int)cudaErrorInvalidValue;
+template <typename T, int MR, int TL>
+static void line_launch(const LineArgs& a, int n, int m, cudaStream_t s) {
+    k_line_w<T, MR, TL><<<line_grid(a.nk / 4, n, m, TL), 128, 0, s>>>(a);
+}
+
+int launch_line(DType t, const LineArgs& args, void* stream) {
+    if (args.nk == 0 || args.I == 0 || args.J == 0) return 0;
+    if (args.R < 0 || args.R > kMaxLineReach) return (int)cudaErrorInvalidValue;
+    LineArgs a = args;
+    for (int d = 0; d <= kMaxLineReach; ++d) a.wf[d] = d <= a.R ? (float)a.w[d] : 0.f;
+    a.scalef = (float)a.scale;
     const int n = a.dir ? a.J : a.I, m = a.dir ? a.I : a.J;
     if (a.R > n) return (int)cudaErrorInvalidValue;  // one mirror image at most
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1240,32 +1274,34 @@ int launch_line(DType t, const LineArgs& a, void* stream) {
     const bool vec = a.nk % 4 == 0 && aligned16(a.in.p) && aligned16(a.out.p) && (a.in.si * es) % 16 == 0 &&
                      (a.in.sj * es) % 16 == 0 && (a.out.si * es) % 16 == 0 && (a.out.sj * es) % 16 == 0;
     if (!vec || (t == DType::BF16 && (a.nk % 8 || !aligned16(a.in.p)))) {
-        dim3 block(128), grid((a.nk + 127) / 128, (n + 3) / 4, m);
-        MGBF_DISPATCH(t, (k_line_s<T><<<grid, block, 0, s>>>(a)));
+        MGBF_DISPATCH(t, (k_line_s<T><<<line_grid(a.nk, n, m, 4), 128, 0, s>>>(a)));
         return last_err();
     }
     if (t == DType::F64) {
         if (a.R <= 4) line_launch<double, 4, 4>(a, n, m, s);
         else if (a.R <= 8) line_launch<double, 8, 4>(a, n, m, s);
-        else {
-            const int nt = a.nk / 4;
-            dim3 block(std::min(128, ((nt + 31) / 32) * 32)), grid((nt + block.x - 1) / block.x, (n + 3) / 4, m);
-            k_line_g<double><<<grid, block, 0, s>>>(a);
-        }
+        else k_line_g<double><<<line_grid(a.nk / 4, n, m, 4), 128, 0, s>>>(a);
         return last_err();
     }
+    // reach buckets; the register window TL + 2MR stays at <= 32 inputs
     auto run = [&](auto tag) {
         using T = decltype(tag);
-        if (a.R <= 4) {
+        if (a.R <= 2) {
+            line_launch<T, 2, 16>(a, n, m, s);
+        } else if (a.R <= 4) {
             line_launch<T, 4, 16>(a, n, m, s);
+        } else if (a.R <= 6) {
+            line_launch<T, 6, 16>(a, n, m, s);
         } else if (a.R <= 8) {
-            line_launch<T, 8, 8>(a, n, m, s);
+            line_launch<T, 8, 16>(a, n, m, s);
+        } else if (a.R <= 12) {
+            line_launch<T, 12, 8>(a, n, m, s);
+        } else if (a.R <= 14) {
+            line_launch<T, 14, 4>(a, n, m, s);
         } else if (a.R <= 16) {
-            line_launch<T, 16, 8>(a, n, m, s);
+            line_launch<T, 16, 4>(a, n, m, s);
         } else {
-            const int nt = a.nk / 4;
-            dim3 block(std::min(128, ((nt + 31) / 32) * 32)), grid((nt + block.x - 1) / block.x, (n + 3) / 4, m);
-            k_line_g<T><<<grid, block, 0, s>>>(a);
+            k_line_g<T><<<line_grid(a.nk / 4, n, m, 4), 128, 0, s>>>(a);
         }
     };
     if (t == DType::F32) run(float());

@@ -43,6 +43,10 @@ struct LineArgs {
     int R;
     double w[kMaxLineReach + 1];  // w[0..R], already normalised
     double scale;
+    // float copies (made by launch_line): converting FP64 in every thread
+    // would load the small FP64 pipe
+    float wf[kMaxLineReach + 1];
+    float scalef;
 };
 
 struct RestrictArgs {
