@@ -242,6 +242,13 @@ int mgbf_batch_destroy(mgbf_batch* b);
  * batch's device memory exists (the first call of a dtype runs directly);
  * graphs are bypassed while stage timers are on.  0 releases the graphs. */
 int mgbf_batch_use_graphs(mgbf_batch* b, int enable);
+/* Procedure a batch runs: 6 (filtering_rad2_ens, the default) or 8
+ * (filtering_fast_ens, mg_filtering.f90:1316-1506: the 1D+1D line filters
+ * with el = mg_ampl02).  8 fails with MGBF_ERR_DIVISIBILITY when a group's
+ * line reach exceeds its hx/hy or the coarsest generation.  Releases graphs
+ * captured before. */
+int mgbf_batch_set_procedure(mgbf_batch* b, int mg_filt);
+
 /* As mgbf_status, for a batch. */
 int mgbf_batch_status(mgbf_batch* b);
 /* As mgbf_autotune, for a batch (releases graphs captured before). */

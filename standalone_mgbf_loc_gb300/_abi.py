@@ -95,6 +95,7 @@ SIGNATURES = {
     "mgbf_status": (_I, [_HP]),
     "mgbf_batch_status": (_I, [_HP]),
     "mgbf_batch_use_graphs": (_I, [_HP, _I]),
+    "mgbf_batch_set_procedure": (_I, [_HP, _I]),
     "mgbf_autotune": (_I, [_HP, _I, _VP]),
     "mgbf_set_tuning": (_I, [_HP, _I, _I, _I]),
     "mgbf_batch_autotune": (_I, [_HP, _I, _VP]),

@@ -545,6 +545,7 @@ struct mgbf_handle {
 struct mgbf_batch {
     Plan plan;
     bool filt1 = true;
+    int proc = 6;  // 6: radial (filtering_rad2_ens), 8: fast 1D+1D (filtering_fast_ens)
     // CUDA-graph replay of the launch sequence (mgbf_batch_use_graphs)
     bool use_graphs = false;
     struct GraphEntry {
@@ -1306,6 +1307,7 @@ static int batch_launch(mgbf_batch* b, void* const* fields, DType t, void* strea
         View v;
         v.p = fields[q]; v.si = G.nk; v.sj = (long long)G.nk * P.I;
         Exec ex{P, G, t, stream};
+        ex.fast = b->proc == 8;
         const int nzcol = (G.lm > 1) ? G.nzcol : 0;
         if ((rc = ex.forward(v, v, nzcol, b->filt1))) return rc;
     }
@@ -1327,7 +1329,7 @@ int mgbf_batch_apply(mgbf_batch* b, void* const* fields, int dtype, int adjoint,
     for (auto& G : P.groups) {
         if (!G.tab[t == DType::F64 ? 1 : 0].ready || G.bufs[(int)t].A.empty()) first_use = true;
         if ((rc = ensure_tables(P, G, t))) return rc;
-        if ((rc = ensure_bufs(P, G, t, false))) return rc;
+        if ((rc = ensure_bufs(P, G, t, false, b->proc == 8))) return rc;
     }
     if (!b->use_graphs || g_timers.on || first_use) return batch_launch(b, fields, t, stream);
     // replay a captured graph of this exact launch sequence, capturing it on first use
@@ -1357,6 +1359,21 @@ int mgbf_batch_apply(mgbf_batch* b, void* const* fields, int dtype, int adjoint,
     if (ec != cudaSuccess) return cuda_fail(ec, "cudaGraphInstantiate");
     b->graphs.push_back(e);
     CU(cudaGraphLaunch(e.exec, s));
+    return MGBF_OK;
+}
+
+int mgbf_batch_set_procedure(mgbf_batch* b, int mg_filt) {
+    if (!b) return fail(MGBF_ERR_ARG, "null handle");
+    if (mg_filt != 6 && mg_filt != 8)
+        return fail(MGBF_ERR_UNSUPPORTED, "batches run filtering_procedure 6 or 8, not " + std::to_string(mg_filt));
+    if (mg_filt == 8)
+        for (size_t q = 0; q < b->plan.groups.size(); ++q)
+            if (b->plan.groups[q].ls.R < 0)
+                return fail(MGBF_ERR_DIVISIBILITY, "group " + std::to_string(q) + ": " + b->plan.groups[q].ls_err);
+    DeviceGuard dg(b->plan.device);
+    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);  // captured for the other procedure
+    b->graphs.clear();
+    b->proc = mg_filt;
     return MGBF_OK;
 }
 

@@ -327,6 +327,10 @@ class MGBFBatch:
         stream = torch.cuda.current_stream().cuda_stream if torch is not None else None
         _abi.check(self._lib.mgbf_batch_autotune(self._h, dt, stream), "mgbf_batch_autotune")
 
+    def set_procedure(self, mg_filt: int) -> None:
+        """6: radial filters (default); 8: the fast 1D+1D line filters."""
+        _abi.check(self._lib.mgbf_batch_set_procedure(self._h, int(mg_filt)), "mgbf_batch_set_procedure")
+
     def use_graphs(self, enable: bool = True) -> None:
         """Replay repeated calls on the same fields as captured CUDA graphs."""
         _abi.check(self._lib.mgbf_batch_use_graphs(self._h, int(enable)), "mgbf_batch_use_graphs")

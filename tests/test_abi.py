@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig, MGBFError, _abi
-from tests.helpers import canonical, small_config
+from tests.helpers import canonical, canonical_z, small_config
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -208,3 +208,21 @@ def test_fast_line_reach_beyond_coarsest_generation(lib):
         op.filtering_procedure(3, np.zeros(op.field_shape()))
     assert e.value.code == _abi.MGBF_ERR_DIVISIBILITY
     assert "coarsest generation" in str(e.value)
+
+
+def test_batch_set_procedure_validation(lib):
+    from standalone_mgbf_loc_gb300 import GroupDesc, MGBFBatch
+    ok = GroupDesc(nk=8, lm=8, nzcol=1, hx=6, hy=6, hz=2, p=2, mg_ampl01=canonical_z(2), mg_ampl02=0.4)
+    b = MGBFBatch(64, 64, 3, [1.0, 0.5, 0.25], [ok])
+    b.set_procedure(8)
+    b.set_procedure(6)
+    for bad in (1, 3, 7):
+        with pytest.raises(MGBFError) as e:
+            b.set_procedure(bad)
+        assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
+    # line reach 6 > hx = 4: the radial procedure still works, 8 is refused
+    short = GroupDesc(nk=8, lm=8, nzcol=1, hx=4, hy=4, hz=2, p=2, mg_ampl01=canonical_z(2), mg_ampl02=0.4)
+    b2 = MGBFBatch(64, 64, 3, [1.0, 0.5, 0.25], [short])
+    with pytest.raises(MGBFError) as e:
+        b2.set_procedure(8)
+    assert e.value.code == _abi.MGBF_ERR_DIVISIBILITY

@@ -111,3 +111,33 @@ def test_fast_weight_gradients(lib, cuda):
     oc = oracle_cfg(c, 8)
     assert np.allclose(ga, O.weight_grads(oc, x, gy), rtol=1e-10, atol=1e-10)
     assert rel_l2(gx.cpu().numpy(), O.filter_compact(oc, gy)) < 1e-12
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+def test_fast_batch_groups(lib, cuda, graphs):
+    """A batch switched to procedure 8: every group == its own oracle run."""
+    from standalone_mgbf_loc_gb300 import GroupDesc, MGBFBatch
+    I = J = 64
+    gm = 3
+    w = [1.0, 0.5, 0.25]
+    groups = [
+        GroupDesc(nk=3 * 8, lm=8, nzcol=3, hx=6, hy=6, hz=2, p=2, mg_ampl01=canonical_z(2), mg_ampl02=0.4),
+        GroupDesc(nk=5, lm=1, nzcol=0, hx=9, hy=9, hz=2, p=2, mg_ampl01=canonical_z(2), mg_ampl02=0.3),
+    ]
+    b = MGBFBatch(I, J, gm, w, groups)
+    b.set_procedure(8)
+    b.use_graphs(graphs)
+    rng = np.random.default_rng(12)
+    xs = [rng.standard_normal((J, I, g.nk)) for g in groups]
+    ts = [torch.empty((J, I, g.nk), device=cuda, dtype=torch.float32) for g in groups]
+    for _ in range(3 if graphs else 1):  # with graphs: direct, capture, replay (same pointers)
+        for t, x in zip(ts, xs):
+            t.copy_(torch.from_numpy(x))
+        b.apply(ts)
+    torch.cuda.synchronize()
+    b.status()
+    for g, x, t in zip(groups, xs, ts):
+        oc = O.OracleConfig(I=I, J=J, nk=g.nk, hx=g.hx, hy=g.hy, hz=g.hz, p=g.p, ampl01=g.mg_ampl01,
+                            ampl02=g.mg_ampl02, gm=gm, weights=w, proc=8, lm=g.lm, nzcol=g.nzcol,
+                            l_vertical_filter=g.nzcol > 0)
+        assert rel_l2(t.double().cpu().numpy(), O.filter_compact(oc, x)) < 1e-5
