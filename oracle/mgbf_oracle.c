@@ -941,3 +941,209 @@ int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y) 
     }
     return ORC_ERR_ARG;
 }
+
+/* ------------------------------------------- analysis <-> filter transfers */
+
+#define XF_IB 6 /* ib = jb = 6 (mg_parameter.f90:520-521): range of the xf table */
+
+typedef struct {
+    int ref;      /* first filter tap, rank-local 1-based index */
+    double c[4];  /* weights of taps ref .. ref+order */
+} xcoef;
+
+/* lsqr_mg_coef (mg_interpolate.f90:89-298) along one axis of one rank:
+ * lengthx = na (mg_parameter.f90:515-541), so dxa = 1, dxf = na/nf, both
+ * grids offset by half a cell.  order 3: the blend of two quadratic
+ * Lagrange interpolants (cx0..cx3, first tap iref); 2: quadratic (qx,
+ * irefq); 1: linear (Lx, irefL). */
+static void axis_coef(int na, int nf, int order, xcoef* out) {
+    const double length = 1.0 * na;
+    const double da = length / na, df = length / nf;
+    const double a0 = da * 0.5, f0 = df * 0.5;
+    for (int n = 1; n <= na; ++n) {
+        const double x = a0 + da * (n - 1);
+        int ifound = 1 - XF_IB;
+        for (int i = 1 - XF_IB; i <= nf + XF_IB - 1; ++i)
+            if (x < f0 + df * (i - 1)) { ifound = i; break; }
+        xcoef* o = &out[n - 1];
+        o->c[0] = o->c[1] = o->c[2] = o->c[3] = 0.0;
+        if (order == 3) {
+            const int i = ifound - 2;
+            const double x1 = f0 + df * (i - 1), x2 = f0 + df * i, x3 = f0 + df * (i + 1), x4 = f0 + df * (i + 2);
+            const double x1x = x1 - x, x2x = x2 - x, x3x = x3 - x, x4x = x4 - x;
+            const double rx2x1 = 1. / (x2 - x1), rx3x1 = 1. / (x3 - x1);
+            const double rx3x2 = 1. / (x3 - x2), rx4x2 = 1. / (x4 - x2), rx4x3 = 1. / (x4 - x3);
+            const double cfl1 = x2x * x3x * rx2x1 * rx3x1;
+            const double cfl2 = -(x1x * x3x * rx2x1 * rx3x2);
+            const double cfl3 = x1x * x2x * rx3x1 * rx3x2;
+            const double cll = x3x * rx3x2;
+            const double cfr1 = x3x * x4x * rx3x2 * rx4x2;
+            const double cfr2 = -(x2x * x4x * rx3x2 * rx4x3);
+            const double cfr3 = x2x * x3x * rx4x2 * rx4x3;
+            const double crr = -(x2x * rx3x2);
+            o->ref = i;
+            o->c[0] = cfl1 * cll;
+            o->c[1] = cfl2 * cll + cfr1 * crr;
+            o->c[2] = cfl3 * cll + cfr2 * crr;
+            o->c[3] = cfr3 * crr;
+        } else if (order == 2) {
+            const int i = ifound - 1;
+            const double x1 = f0 + df * (i - 1), x2 = f0 + df * i, x3 = f0 + df * (i + 1);
+            const double x1_x = x1 - x, x2_x = x2 - x, x3_x = x3 - x;
+            const double rx2x1 = 1. / (x2 - x1), rx3x1 = 1. / (x3 - x1), rx3x2 = 1. / (x3 - x2);
+            o->ref = i;
+            o->c[0] = x2_x * x3_x * rx2x1 * rx3x1;
+            o->c[1] = -(x1_x * x3_x * rx2x1 * rx3x2);
+            o->c[2] = x1_x * x2_x * rx3x1 * rx3x2;
+        } else {
+            const int i = ifound - 1;
+            const double x1 = f0 + df * (i - 1), x2 = f0 + df * i;
+            const double x1_x = x1 - x, x2_x = x2 - x;
+            const double rx2x1 = 1. / (x2 - x1);
+            o->ref = i;
+            o->c[0] = x2_x * rx2x1;
+            o->c[1] = -(x1_x * rx2x1);
+        }
+    }
+}
+
+static int xfer_check(const orc_xfer* c) {
+    if (!c || c->nm0 <= 0 || c->mm0 <= 0 || c->nxpe <= 0 || c->nype <= 0 || c->im <= 0 || c->jm <= 0) return ORC_ERR_ARG;
+    if (c->nm0 % c->nxpe || c->mm0 % c->nype) return ORC_ERR_ARG;
+    if (c->order < 1 || c->order > 3 || c->hx < c->order || c->hy < c->order) return ORC_ERR_ARG;
+    if (c->lm_a > c->lm && (c->lm_a != 2 * c->lm - 1 || (size_t)c->en * c->lm > (size_t)c->nkf ||
+                            (size_t)c->en * c->lm_a > (size_t)c->nka))
+        return ORC_ERR_ARG;
+    if (c->lm_a <= c->lm && c->nka != c->nkf) return ORC_ERR_ARG;
+    return ORC_OK;
+}
+
+/* filt_to_anal_all2 / filt_to_anal (mg_transfer.f90:184-203, 406-464):
+ * boco_2d with the interpolation halo, lsqr/quad/lin_direct_offset
+ * (mg_interpolate.f90:634-681, 750-795, 858-903), then
+ * l_vertical_direct_spec2 (mg_interpolate.f90:1006-1044) when lm_a > lm. */
+int orc_filt_to_anal(const orc_xfer* c, double* vall, double* worka) {
+    int rc = xfer_check(c);
+    if (rc) return rc;
+    const int I = c->nxpe * c->im, J = c->nype * c->jm, nm = c->nm0 / c->nxpe, mm = c->mm0 / c->nype;
+    const int ib = c->order, nt = c->order + 1, nk = c->nkf;
+    arr3 V = {vall, nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy};
+    fill_h(V, I, J, ib, ib, 0, nk);
+    xcoef* cx = (xcoef*)malloc(sizeof(xcoef) * nm);
+    xcoef* cy = (xcoef*)malloc(sizeof(xcoef) * mm);
+    axis_coef(nm, c->im, c->order, cx);
+    axis_coef(mm, c->jm, c->order, cy);
+    const int vert = c->lm_a > c->lm;
+    double* work = vert ? (double*)malloc(sizeof(double) * (size_t)nk * c->nm0 * c->mm0) : worka;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int M = 1; M <= c->mm0; ++M) {
+        const int rj = (M - 1) / mm;
+        const xcoef* ky = &cy[M - 1 - rj * mm];
+        const int j0 = rj * c->jm + ky->ref;
+        double vx[4];
+        for (int N = 1; N <= c->nm0; ++N) {
+            const int ri = (N - 1) / nm;
+            const xcoef* kx = &cx[N - 1 - ri * nm];
+            const int i0 = ri * c->im + kx->ref;
+            double* w = work + (size_t)nk * ((size_t)(N - 1) + (size_t)c->nm0 * (M - 1));
+            for (int k = 0; k < nk; ++k) {
+                for (int s = 0; s < nt; ++s) {
+                    double v = kx->c[0] * A3(V, k, i0, j0 + s);
+                    for (int t = 1; t < nt; ++t) v += kx->c[t] * A3(V, k, i0 + t, j0 + s);
+                    vx[s] = v;
+                }
+                double r = ky->c[0] * vx[0];
+                for (int s = 1; s < nt; ++s) r += ky->c[s] * vx[s];
+                w[k] = r;
+            }
+        }
+    }
+    if (vert) {
+        const size_t npts = (size_t)c->nm0 * c->mm0;
+        for (size_t q = 0; q < npts; ++q) {
+            const double* F = work + (size_t)nk * q;
+            double* W = worka + (size_t)c->nka * q;
+            for (int e = 0; e < c->en; ++e) {
+                const int enm = e * c->lm_a, ekm = e * c->lm;
+                int k = 1;
+                for (int n = 1; n <= c->lm_a; n += 2) W[enm + n - 1] = F[ekm + k - 1], ++k;
+                k = 1;
+                for (int n = 2; n <= c->lm_a - 1; n += 2) W[enm + n - 1] = 0.5 * (F[ekm + k - 1] + F[ekm + k]), ++k;
+            }
+        }
+        free(work);
+    }
+    free(cx);
+    free(cy);
+    return ORC_OK;
+}
+
+/* anal_to_filt_all2 / anal_to_filt (mg_transfer.f90:154-181, 339-403):
+ * l_vertical_adjoint_spec2 (mg_interpolate.f90:963-1003) when lm_a > lm,
+ * VALL = 0, lsqr/quad/lin_adjoint_offset (mg_interpolate.f90:684-747,
+ * 798-855, 906-960), bocoT_2d with the interpolation halo (the halo keeps
+ * its scattered values).  The ranks' scatters into each other's halos sum
+ * into the one global array. */
+int orc_anal_to_filt(const orc_xfer* c, const double* worka, double* vall) {
+    int rc = xfer_check(c);
+    if (rc) return rc;
+    const int I = c->nxpe * c->im, J = c->nype * c->jm, nm = c->nm0 / c->nxpe, mm = c->mm0 / c->nype;
+    const int ib = c->order, nt = c->order + 1, nk = c->nkf;
+    const size_t npts = (size_t)c->nm0 * c->mm0;
+    const double* work = worka;
+    double* wbuf = NULL;
+    if (c->lm_a > c->lm) {
+        wbuf = (double*)calloc((size_t)nk * npts, sizeof(double));
+        for (size_t q = 0; q < npts; ++q) {
+            const double* W = worka + (size_t)c->nka * q;
+            double* F = wbuf + (size_t)nk * q;
+            for (int e = 0; e < c->en; ++e) {
+                const int enm = e * c->lm_a, ekm = e * c->lm;
+                int k = 1;
+                for (int n = 2; n <= c->lm_a - 1; n += 2) {
+                    F[ekm + k - 1] += 0.5 * W[enm + n - 1];
+                    F[ekm + k] += 0.5 * W[enm + n - 1];
+                    ++k;
+                }
+                k = 1;
+                for (int n = 1; n <= c->lm_a; n += 2) F[ekm + k - 1] += W[enm + n - 1], ++k;
+            }
+        }
+        work = wbuf;
+    }
+    arr3 V = {vall, nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy};
+    memset(vall, 0, sizeof(double) * (size_t)nk * (I + 2 * c->hx) * (size_t)(J + 2 * c->hy));
+    xcoef* cx = (xcoef*)malloc(sizeof(xcoef) * nm);
+    xcoef* cy = (xcoef*)malloc(sizeof(xcoef) * mm);
+    axis_coef(nm, c->im, c->order, cx);
+    axis_coef(mm, c->jm, c->order, cy);
+    /* VX(nk, 1:nm0, 1-ib:J+ib) */
+    arr3 VX = a3_alloc(nk, 1, c->nm0, 1 - ib, J + ib);
+    a3_zero(VX, 0, nk);
+    for (int M = 1; M <= c->mm0; ++M) {
+        const int rj = (M - 1) / mm;
+        const xcoef* ky = &cy[M - 1 - rj * mm];
+        const int j0 = rj * c->jm + ky->ref;
+        for (int N = 1; N <= c->nm0; ++N) {
+            const double* w = work + (size_t)nk * ((size_t)(N - 1) + (size_t)c->nm0 * (M - 1));
+            for (int s = 0; s < nt; ++s)
+                for (int k = 0; k < nk; ++k) A3(VX, k, N, j0 + s) += w[k] * ky->c[s];
+        }
+    }
+    for (int N = 1; N <= c->nm0; ++N) {
+        const int ri = (N - 1) / nm;
+        const xcoef* kx = &cx[N - 1 - ri * nm];
+        const int i0 = ri * c->im + kx->ref;
+        for (int j = 1 - ib; j <= J + ib; ++j)
+            for (int t = 0; t < nt; ++t)
+                for (int k = 0; k < nk; ++k) A3(V, k, i0 + t, j) += A3(VX, k, N, j) * kx->c[t];
+    }
+    fold_h(V, I, J, ib, ib, 0, nk);
+    a3_free(&VX);
+    free(cx);
+    free(cy);
+    free(wbuf);
+    return ORC_OK;
+}

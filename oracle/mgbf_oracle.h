@@ -84,6 +84,30 @@ int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y);
  * exx, ss, reach.  Returns error if a reach exceeds a halo. */
 int orc_setup_values(const orc_cfg* c, double out[11]);
 
+/* ----------------------------------------------------------------------
+ * Transfers between the analysis grid and the filter grid (the new map,
+ * l_new_map: anal_to_filt_all2 / filt_to_anal_all2, mg_transfer.f90:154-203,
+ * 339-464; offset interpolations mg_interpolate.f90:89-298, 634-960;
+ * vertical l_vertical_*_spec2, mg_interpolate.f90:963-1044).
+ * WORKA is (nka, nm0, mm0) with the level index fastest. */
+typedef struct orc_xfer {
+    int nm0, mm0;     /* analysis grid                                         */
+    int nxpe, nype;   /* rank layout: nm = nm0/nxpe analysis points per rank   */
+    int im, jm;       /* filter points per rank (im_filt, jm_filt)             */
+    int hx, hy;       /* VALL halo widths                                      */
+    int nkf, nka;     /* leading dims: filter km_all, analysis km_a_all         */
+    int lm, lm_a, en; /* vertical: en = km3*n_ens blocks of lm_a / lm levels    */
+    int order;        /* 3 = lsqr (default), 2 = quad, 1 = lin                  */
+} orc_xfer;
+
+/* anal_to_filt_all2: VALL (nkf, 1-hx:I+hx, 1-hy:J+hy) = 0, then the
+ * adjoint interpolation of WORKA and bocoT_2d over the interpolation halo. */
+int orc_anal_to_filt(const orc_xfer* c, const double* worka, double* vall);
+
+/* filt_to_anal_all2: boco_2d fills VALL's halo (interpolation width), then
+ * the direct interpolation into WORKA. */
+int orc_filt_to_anal(const orc_xfer* c, double* vall, double* worka);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,8 +49,11 @@ def _load():
         lib.orc_weight_grads.argtypes = [cp, dp, dp, dp]
         lib.orc_stage.argtypes = [cp, ctypes.c_int, ctypes.c_int, dp, dp]
         lib.orc_setup_values.argtypes = [cp, dp]
+        xp = ctypes.POINTER(_CXfer)
+        lib.orc_anal_to_filt.argtypes = [xp, dp, dp]
+        lib.orc_filt_to_anal.argtypes = [xp, dp, dp]
         for f in (lib.orc_filtering_procedure, lib.orc_filter_compact, lib.orc_weight_grads,
-                  lib.orc_stage, lib.orc_setup_values):
+                  lib.orc_stage, lib.orc_setup_values, lib.orc_anal_to_filt, lib.orc_filt_to_anal):
             f.restype = ctypes.c_int
         _lib = lib
     return _lib
@@ -169,3 +172,74 @@ def setup_values(cfg: OracleConfig) -> dict:
     keys = ["rmom2_1", "rmom2_2", "exx1", "exx2", "ss1", "ss2", "reach_z", "reach_h", "exx_line", "ss_line",
             "reach_line"]
     return dict(zip(keys, out.tolist()))
+
+
+# ------------------------------------------------ analysis <-> filter grid
+
+
+class _CXfer(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("nm0", "mm0", "nxpe", "nype", "im", "jm", "hx", "hy", "nkf", "nka",
+                                            "lm", "lm_a", "en", "order")]
+
+
+@dataclass
+class XferConfig:
+    """Transfer geometry (mg_parameter.f90:357-358, 515-541): nm0 x mm0
+    analysis points and nxpe*im x nype*jm filter points; order 3 = lsqr,
+    2 = quadratic (l_quad_horizontal), 1 = linear (l_lin_horizontal)."""
+    nm0: int
+    mm0: int
+    nxpe: int
+    nype: int
+    im: int
+    jm: int
+    hx: int
+    hy: int
+    nkf: int
+    nka: int = 0
+    lm: int = 1
+    lm_a: int = 1
+    en: int = 0
+    order: int = 3
+
+    def to_c(self):
+        c = _CXfer()
+        for n, _ in _CXfer._fields_:
+            setattr(c, n, int(getattr(self, n)))
+        if not self.nka:
+            c.nka = self.nkf
+        return c
+
+    @property
+    def I(self):
+        return self.nxpe * self.im
+
+    @property
+    def J(self):
+        return self.nype * self.jm
+
+    def vall_shape(self):
+        return (self.J + 2 * self.hy, self.I + 2 * self.hx, self.nkf)
+
+    def worka_shape(self):
+        return (self.mm0, self.nm0, self.nka or self.nkf)
+
+
+def filt_to_anal(cfg: XferConfig, vall: np.ndarray) -> np.ndarray:
+    """filt_to_anal_all2: VALL (halo layout; its interpolation halo is filled
+    in place, as in the reference) -> WORKA."""
+    assert vall.shape == cfg.vall_shape() and vall.dtype == np.float64 and vall.flags.c_contiguous
+    w = np.zeros(cfg.worka_shape(), dtype=np.float64)
+    c = cfg.to_c()
+    _check(_load().orc_filt_to_anal(ctypes.byref(c), _ptr(vall), _ptr(w)), "orc_filt_to_anal")
+    return w
+
+
+def anal_to_filt(cfg: XferConfig, worka: np.ndarray) -> np.ndarray:
+    """anal_to_filt_all2: WORKA -> VALL (halo layout)."""
+    worka = np.ascontiguousarray(worka, dtype=np.float64)
+    assert worka.shape == cfg.worka_shape()
+    v = np.zeros(cfg.vall_shape(), dtype=np.float64)
+    c = cfg.to_c()
+    _check(_load().orc_anal_to_filt(ctypes.byref(c), _ptr(worka), _ptr(v)), "orc_anal_to_filt")
+    return v
