@@ -92,6 +92,9 @@ typedef struct mgbf_dims {
     size_t field_elems;    /* elements of one field in the handle's layout   */
     int hbeta_kernel;      /* 1: moment kernel, 0: direct-sum kernel          */
     int reach_line;        /* fast filters' line reach (-1: procs 3/8 unusable) */
+    int nm0, mm0;          /* analysis grid of the transfers                  */
+    int km_a_all;          /* leading dimension of WORKA: (km2+lm_a*km3)*n_ens */
+    size_t anal_elems;     /* elements of WORKA(km_a_all, nm0, mm0)           */
 } mgbf_dims;
 
 typedef struct mgbf_handle mgbf_handle;
@@ -136,6 +139,25 @@ int mgbf_get_dims(const mgbf_handle* h, mgbf_dims* dims);
  */
 int mgbf_filtering_procedure(mgbf_handle* h, int mg_filt, void* vall, int dtype, int mem,
                              void* stream);
+
+/*
+ * Transfers between the analysis grid WORKA(km_a_all, nm0, mm0) (level
+ * index fastest) and the filter field VALL, the new map of the reference's
+ * driver (RBETA_TEST.f90:46-98 with l_new_map):
+ *   mgbf_anal_to_filt  = anal_to_filt_all2 (mg_transfer.f90:154-181, 339-403):
+ *     l_vertical_adjoint_spec2 when lm_a = 2*lm-1, VALL = 0, the adjoint
+ *     offset interpolation (lsqr, or quad / lin per l_quad_horizontal /
+ *     l_lin_horizontal) and bocoT_2d over the interpolation halo (3/2/1).
+ *   mgbf_filt_to_anal  = filt_to_anal_all2 (mg_transfer.f90:184-203, 406-464):
+ *     boco_2d fills VALL's interpolation halo (in place, halo layout), the
+ *     direct interpolation, l_vertical_direct_spec2 when lm_a = 2*lm-1.
+ * The analysis grid is nm0 x mm0 over nxPE x nyPE ranks, each rank's nm0/nxPE
+ * points over the same length as its im_filt filter points.  lm_a must be
+ * lm, or 2*lm-1 with km2 = 0; l_new_map = false (the old map) returns
+ * MGBF_ERR_UNSUPPORTED.  dtype/mem/stream as in mgbf_filtering_procedure.
+ */
+int mgbf_anal_to_filt(mgbf_handle* h, const void* worka, void* vall, int dtype, int mem, void* stream);
+int mgbf_filt_to_anal(mgbf_handle* h, void* vall, void* worka, int dtype, int mem, void* stream);
 
 /* Adjoint of filtering_procedure(mg_filt), run through the explicit
  * transposed chain (no reference counterpart: the reference's adjoint test

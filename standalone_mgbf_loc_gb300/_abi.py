@@ -58,6 +58,7 @@ class MgbfDims(ctypes.Structure):
         ("im", _I), ("jm", _I), ("km_all", _I), ("km", _I), ("km3_all", _I), ("gm", _I),
         ("hx", _I), ("hy", _I), ("hz", _I), ("reach_h", _I), ("reach_z", _I), ("layout", _I),
         ("field_elems", ctypes.c_size_t), ("hbeta_kernel", _I), ("reach_line", _I),
+        ("nm0", _I), ("mm0", _I), ("km_a_all", _I), ("anal_elems", ctypes.c_size_t),
     ]
 
 
@@ -97,6 +98,8 @@ SIGNATURES = {
     "mgbf_batch_use_graphs": (_I, [_HP, _I]),
     "mgbf_batch_set_procedure": (_I, [_HP, _I]),
     "mgbf_autotune": (_I, [_HP, _I, _VP]),
+    "mgbf_anal_to_filt": (_I, [_HP, _VP, _VP, _I, _I, _VP]),
+    "mgbf_filt_to_anal": (_I, [_HP, _VP, _VP, _I, _I, _VP]),
     "mgbf_set_tuning": (_I, [_HP, _I, _I, _I]),
     "mgbf_batch_autotune": (_I, [_HP, _I, _VP]),
     "mgbf_radial_filter_noalloc": (_I, [_VP, _VP, _I, _I, _I, _I, _D, _I, _I, _D, _VP]),

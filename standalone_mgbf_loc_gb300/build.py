@@ -28,6 +28,7 @@ SOURCES = [
     "mgbf_hbeta_f64.cu",
     "mgbf_hbeta_bf16.cu",
     "mgbf_noalloc.cu",
+    "mgbf_xfer.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

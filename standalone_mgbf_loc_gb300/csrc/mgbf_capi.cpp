@@ -160,8 +160,10 @@ bool make_tmap(CUtensorMap* m, void* base, DType t, int nk, int ncols, int nrows
 
 // ------------------------------------------------------------ stage timers
 
-enum Stage { ST_VFILTT, ST_UPSEND, ST_HFILTT, ST_HFILT, ST_DNSEND, ST_VFILT, ST_DNSEND_VFILT, ST_COPY, ST_HALO, ST_WGRAD, ST_N };
-const char* kStageNames[ST_N] = {"vfiltT", "upsend", "hfiltT", "hfilt", "dnsend", "vfilt", "dnsend+vfilt", "copy", "halo", "wgrad"};
+enum Stage { ST_VFILTT, ST_UPSEND, ST_HFILTT, ST_HFILT, ST_DNSEND, ST_VFILT, ST_DNSEND_VFILT, ST_COPY, ST_HALO, ST_WGRAD,
+             ST_AN2FILT, ST_FILT2AN, ST_N };
+const char* kStageNames[ST_N] = {"vfiltT", "upsend", "hfiltT", "hfilt", "dnsend", "vfilt", "dnsend+vfilt", "copy", "halo", "wgrad",
+                                 "an2filt", "filt2an"};
 
 struct TimerEvent {
     cudaEvent_t a, b;
@@ -534,12 +536,25 @@ struct Exec {
 
 }  // namespace
 
+// Analysis <-> filter transfer state of a handle (built at first use).
+struct XferState {
+    bool built = false;
+    int order = 3, nm0 = 0, mm0 = 0, nka = 0, en = 0;
+    bool vert = false;
+    XferAxis ax, ay;
+    DevBuf rx, ry, offx, srcx, offy, srcy;
+    DevBuf cx[2], cy[2], wx[2], wy[2];  // [0] float, [1] double
+    DevBuf vx[3], vext[3], fv[3];       // per storage type
+    DevBuf anal[3];                     // host-memory calls: the analysis field
+};
+
 struct mgbf_handle {
     mgbf_config cfg;
     Plan plan;
     int nzcol_proc1 = 0, nzcol_proc6 = 0;
     size_t field_elems = 0;
     DevBuf stage[3], stage2[3], stage3[3];
+    XferState xf;
 };
 
 struct mgbf_batch {
@@ -970,6 +985,10 @@ int mgbf_get_dims(const mgbf_handle* h, mgbf_dims* d) {
     d->field_elems = h->field_elems;
     d->hbeta_kernel = (G.hs.canonical && hmom_available(DType::F32, G.hs.R, G.hs.p)) ? 1 : 0;
     d->reach_line = G.ls.R;
+    const mgbf_config& c = h->cfg;
+    d->nm0 = c.nm0; d->mm0 = c.mm0;
+    d->km_a_all = (c.km2 + c.lm_a * c.km3) * c.n_ens;  // mg_parameter.f90:293-296
+    d->anal_elems = (size_t)d->km_a_all * (size_t)(c.nm0 > 0 ? c.nm0 : 0) * (size_t)(c.mm0 > 0 ? c.mm0 : 0);
     return MGBF_OK;
 }
 
@@ -1122,6 +1141,194 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
         CU(cudaMemcpyAsync(gx, h->stage2[(int)t].p, bytes, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
     return 0;
+}
+
+// ------------------------------------------ analysis <-> filter transfers
+
+// Validation and host tables (first use): the new map only (l_new_map),
+// interpolation order from l_lin_horizontal / l_quad_horizontal, analysis
+// levels lm_a = lm or 2*lm-1 (l_vertical_*_spec2).
+static int xfer_prepare(mgbf_handle* h) {
+    XferState& X = h->xf;
+    if (X.built) return MGBF_OK;
+    const mgbf_config& c = h->cfg;
+    const Plan& P = h->plan;
+    if (c.nm0 <= 0 || c.mm0 <= 0) return fail(MGBF_ERR_CONFIG, "the transfers need the analysis grid nm0 x mm0 (> 0)");
+    if (!c.l_new_map)
+        return fail(MGBF_ERR_UNSUPPORTED,
+                    "only the new map (l_new_map: anal_to_filt_all2 / filt_to_anal_all2) is implemented");
+    const int order = c.l_lin_horizontal ? 1 : (c.l_quad_horizontal ? 2 : 3);
+    if (c.layout == MGBF_LAYOUT_HALO && (c.hx < order || c.hy < order))
+        return fail(MGBF_ERR_CONFIG, "hx and hy must hold the interpolation halo (" + std::to_string(order) + ")");
+    if (P.I < 2 * order || P.J < 2 * order)
+        return fail(MGBF_ERR_CONFIG, "filter grid smaller than twice the interpolation halo");
+    int nka = (c.km2 + c.lm * c.km3) * c.n_ens;
+    bool vert = false;
+    if (c.lm_a > c.lm) {
+        if (c.lm_a != 2 * c.lm - 1) return fail(MGBF_ERR_CONFIG, "lm_a must be lm or 2*lm-1 (l_vertical_*_spec2)");
+        if (c.km2 > 0)
+            return fail(MGBF_ERR_UNSUPPORTED,
+                        "lm_a > lm with 2D variables: l_vertical_*_spec2 take the whole leading dimension as blocks "
+                        "of lm_a levels, which the stacked 2D variables break");
+        vert = true;
+        nka = c.lm_a * c.km3 * c.n_ens;
+    } else if (c.lm_a != c.lm) {
+        return fail(MGBF_ERR_CONFIG, "lm_a < lm: the reference copies WORKA to WORK without a vertical map");
+    }
+    X.order = order;
+    X.nm0 = c.nm0;
+    X.mm0 = c.mm0;
+    X.nka = nka;
+    X.en = c.km3 * c.n_ens;
+    X.vert = vert;
+    build_xfer_axis(c.nm0 / c.nxPE, c.im_filt, c.nxPE, order, X.ax);
+    build_xfer_axis(c.mm0 / c.nyPE, c.jm_filt, c.nyPE, order, X.ay);
+    X.built = true;
+    return MGBF_OK;
+}
+
+static int xfer_tables(mgbf_handle* h, DType t) {
+    XferState& X = h->xf;
+    const int ai = t == DType::F64 ? 1 : 0;
+    int rc;
+    if (!X.rx.p) {
+        if ((rc = upload(X.rx, X.ax.ref)) || (rc = upload(X.ry, X.ay.ref)) || (rc = upload(X.offx, X.ax.off)) ||
+            (rc = upload(X.srcx, X.ax.src)) || (rc = upload(X.offy, X.ay.off)) || (rc = upload(X.srcy, X.ay.src)))
+            return rc;
+    }
+    if (!X.cx[ai].p) {
+        if ((rc = upload_acc(X.cx[ai], X.ax.c, t)) || (rc = upload_acc(X.cy[ai], X.ay.c, t)) ||
+            (rc = upload_acc(X.wx[ai], X.ax.w, t)) || (rc = upload_acc(X.wy[ai], X.ay.w, t)))
+            return rc;
+    }
+    return 0;
+}
+
+static View shifted(View v, int da, int db, DType t) {
+    v.p = static_cast<char*>(v.p) + (long long)elem_size(t) * (v.si * da + v.sj * db);
+    return v;
+}
+
+// filt_to_anal_all2: boco_2d on VALL's interpolation halo (halo layout), the
+// vertical map on the filter grid (it commutes with the horizontal one), the
+// offset interpolation into WORKA.
+static int xfer_f2a(mgbf_handle* h, void* vall, void* worka, DType t, void* stream) {
+    XferState& X = h->xf;
+    Plan& P = h->plan;
+    const int nkf = P.groups[0].nk, ai = t == DType::F64 ? 1 : 0;
+    int rc;
+    StageTimer tm(ST_FILT2AN, stream, (double)X.nm0 * X.mm0);
+    View v = field_view(h, vall, t);
+    if (h->cfg.layout == MGBF_LAYOUT_HALO) LK(launch_xfer_fill(t, v, nkf, P.I, P.J, X.order, stream));
+    View src = v;
+    int nk = nkf;
+    if (X.vert) {
+        DevBuf& F = X.fv[(int)t];
+        if ((rc = F.ensure((size_t)X.nka * P.I * P.J * elem_size(t)))) return rc;
+        View f;
+        f.p = F.p; f.si = X.nka; f.sj = (long long)X.nka * P.I;
+        XferVertArgs va;
+        va.in = v; va.out = f; va.nkf = nkf; va.nka = X.nka; va.lm = h->cfg.lm; va.en = X.en; va.adjoint = 0;
+        va.na = P.I; va.nb = P.J; va.a0 = 0; va.b0 = 0;
+        LK(launch_xfer_vert(t, va, stream));
+        src = f;
+        nk = X.nka;
+    }
+    XferDirectArgs da;
+    da.in = src;
+    da.out.p = worka; da.out.si = X.nka; da.out.sj = (long long)X.nka * X.nm0;
+    da.nk = nk; da.I = P.I; da.J = P.J; da.nm0 = X.nm0; da.mm0 = X.mm0; da.order = X.order;
+    da.rx = static_cast<const int*>(X.rx.p); da.ry = static_cast<const int*>(X.ry.p);
+    da.cx = X.cx[ai].p; da.cy = X.cy[ai].p;
+    LK(launch_xfer_direct(t, da, stream));
+    return 0;
+}
+
+// anal_to_filt_all2: the adjoint interpolation as two gathers (y, then x)
+// into the extended filter array, bocoT_2d on its interpolation halo, the
+// vertical adjoint, VALL = 0 outside the interpolation halo.
+static int xfer_a2f(mgbf_handle* h, const void* worka, void* vall, DType t, void* stream) {
+    XferState& X = h->xf;
+    Plan& P = h->plan;
+    const int nkf = P.groups[0].nk, ai = t == DType::F64 ? 1 : 0, ib = X.order;
+    const int IE = P.I + 2 * ib, JE = P.J + 2 * ib;
+    const size_t es = elem_size(t);
+    int rc;
+    StageTimer tm(ST_AN2FILT, stream, (double)X.nm0 * X.mm0);
+    View wa;
+    wa.p = const_cast<void*>(worka); wa.si = X.nka; wa.sj = (long long)X.nka * X.nm0;
+    DevBuf& VX = X.vx[(int)t];
+    DevBuf& VE = X.vext[(int)t];
+    if ((rc = VX.ensure((size_t)X.nka * X.nm0 * JE * es)) || (rc = VE.ensure((size_t)X.nka * IE * JE * es))) return rc;
+    View vx;
+    vx.p = VX.p; vx.si = X.nka; vx.sj = (long long)X.nka * X.nm0;
+    XferGatherArgs g;
+    g.in = wa; g.out = vx; g.nk = X.nka; g.na = X.nm0; g.nb = JE; g.dir = 1;
+    g.off = static_cast<const int*>(X.offy.p); g.src = static_cast<const int*>(X.srcy.p); g.w = X.wy[ai].p;
+    g.out_a0 = 0; g.out_b0 = 0;
+    LK(launch_xfer_gather(t, g, stream));
+    View ve;
+    ve.p = VE.p; ve.si = X.nka; ve.sj = (long long)X.nka * IE;
+    ve = shifted(ve, ib, ib, t);  // origin at the first interior point
+    g.in = vx; g.out = ve; g.na = IE; g.nb = JE; g.dir = 0;
+    g.off = static_cast<const int*>(X.offx.p); g.src = static_cast<const int*>(X.srcx.p); g.w = X.wx[ai].p;
+    g.out_a0 = ib; g.out_b0 = ib;
+    LK(launch_xfer_gather(t, g, stream));
+    LK(launch_xfer_fold(t, ve, X.nka, P.I, P.J, ib, stream));
+    View v = field_view(h, vall, t);
+    const bool halo = h->cfg.layout == MGBF_LAYOUT_HALO;
+    if (halo) CU(cudaMemsetAsync(vall, 0, h->field_elems * es, static_cast<cudaStream_t>(stream)));
+    const int r0 = halo ? -ib : 0, na = halo ? IE : P.I, nb = halo ? JE : P.J;
+    if (X.vert) {
+        XferVertArgs va;
+        va.in = ve; va.out = v; va.nkf = nkf; va.nka = X.nka; va.lm = h->cfg.lm; va.en = X.en; va.adjoint = 1;
+        va.na = na; va.nb = nb; va.a0 = r0; va.b0 = r0;
+        LK(launch_xfer_vert(t, va, stream));
+    } else {
+        LK(launch_copy(t, shifted(ve, r0, r0, t), shifted(v, r0, r0, t), nkf, na, nb, 0, stream));
+    }
+    return 0;
+}
+
+static int xfer_call(mgbf_handle* h, bool to_anal, const void* in, void* out, int dtype, int mem, void* stream) {
+    if (!h || !in || !out) return fail(MGBF_ERR_ARG, "null argument");
+    if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");
+    if (mem != MGBF_MEM_DEVICE && mem != MGBF_MEM_HOST) return fail(MGBF_ERR_ARG, "bad memory space");
+    int rc;
+    if ((rc = xfer_prepare(h))) return rc;
+    DeviceGuard dg(h->plan.device);
+    const DType t = (DType)dtype;
+    if ((rc = ensure_tables(h->plan, h->plan.groups[0], t)) || (rc = xfer_tables(h, t))) return rc;
+    XferState& X = h->xf;
+    const size_t es = elem_size(t);
+    const size_t fbytes = h->field_elems * es, abytes = (size_t)X.nka * X.nm0 * X.mm0 * es;
+    if (mem == MGBF_MEM_DEVICE)
+        return to_anal ? xfer_f2a(h, const_cast<void*>(in), out, t, stream) : xfer_a2f(h, in, out, t, stream);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    DevBuf& F = h->stage[(int)t];
+    DevBuf& A = X.anal[(int)t];
+    if ((rc = F.ensure(fbytes)) || (rc = A.ensure(abytes))) return rc;
+    if (to_anal) {
+        CU(cudaMemcpyAsync(F.p, in, fbytes, cudaMemcpyHostToDevice, s));
+        if ((rc = xfer_f2a(h, F.p, A.p, t, stream))) return rc;
+        CU(cudaMemcpyAsync(out, A.p, abytes, cudaMemcpyDeviceToHost, s));
+        if (h->cfg.layout == MGBF_LAYOUT_HALO)  // VALL's halo was filled, as in the reference
+            CU(cudaMemcpyAsync(const_cast<void*>(in), F.p, fbytes, cudaMemcpyDeviceToHost, s));
+    } else {
+        CU(cudaMemcpyAsync(A.p, in, abytes, cudaMemcpyHostToDevice, s));
+        if ((rc = xfer_a2f(h, A.p, F.p, t, stream))) return rc;
+        CU(cudaMemcpyAsync(out, F.p, fbytes, cudaMemcpyDeviceToHost, s));
+    }
+    CU(cudaStreamSynchronize(s));
+    return 0;
+}
+
+int mgbf_anal_to_filt(mgbf_handle* h, const void* worka, void* vall, int dtype, int mem, void* stream) {
+    return xfer_call(h, false, worka, vall, dtype, mem, stream);
+}
+
+int mgbf_filt_to_anal(mgbf_handle* h, void* vall, void* worka, int dtype, int mem, void* stream) {
+    return xfer_call(h, true, vall, worka, dtype, mem, stream);
 }
 
 static int read_status(Plan& P);

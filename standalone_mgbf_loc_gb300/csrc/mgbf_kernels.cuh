@@ -49,6 +49,32 @@ struct LineArgs {
     float scalef;
 };
 
+// Analysis <-> filter grid transfers (mgbf_xfer.cu).
+struct XferDirectArgs {
+    View in, out;      // in: filter field (interior origin), out: analysis field
+    int nk, I, J, nm0, mm0;
+    int order;         // 3 lsqr (4 taps), 2 quad, 1 lin
+    const int* rx;     // first filter tap per analysis column (0-based, may leave [0, I))
+    const int* ry;
+    const void* cx;    // 4 weights per analysis column (accumulation type)
+    const void* cy;
+};
+struct XferGatherArgs {
+    View in, out;
+    int nk, na, nb;    // targets: na x nb points
+    int dir;           // 0: list over the first point index (sources along in.si); 1: over the second (in.sj)
+    const int* off;    // list offsets per target, size n+1
+    const int* src;    // source index per entry
+    const void* w;     // weight per entry (accumulation type)
+    int out_a0, out_b0;  // output view coordinate = target index - out_*0
+};
+struct XferVertArgs {
+    View in, out;
+    int nkf, nka, lm, en;  // en blocks of lm filter / 2lm-1 analysis levels
+    int adjoint;           // 0: filter -> analysis levels, 1: the transpose
+    int na, nb, a0, b0;    // points a0 .. a0+na-1, b0 .. b0+nb-1 (view coordinates)
+};
+
 struct RestrictArgs {
     View fine, coarse;
     int nk, If, Jf;     // fine interior sizes; coarse = If/2, Jf/2
@@ -137,6 +163,11 @@ int launch_hdirect(DType t, const HDirectArgs& a, void* stream);
 int launch_mirror_x(DType t, View v, int nk, int I, int J, int hx, void* stream);
 int launch_copy(DType t, View in, View out, int nk, int I, int J, int mirror_hx, void* stream);
 int launch_line(DType t, const LineArgs& a, void* stream);
+int launch_xfer_direct(DType t, const XferDirectArgs& a, void* stream);
+int launch_xfer_gather(DType t, const XferGatherArgs& a, void* stream);
+int launch_xfer_fold(DType t, View v, int nk, int I, int J, int b, void* stream);
+int launch_xfer_fill(DType t, View v, int nk, int I, int J, int b, void* stream);
+int launch_xfer_vert(DType t, const XferVertArgs& a, void* stream);
 int launch_zero_halo_edges(DType t, View v, int nk, int I, int J, int hx, int hy, void* stream);
 int launch_zero_halo(DType t, View v, int nk, int I, int J, int hx, int hy, void* stream);
 int launch_dot(DType t, const DotArgs& a, void* stream);

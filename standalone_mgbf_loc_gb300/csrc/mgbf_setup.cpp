@@ -274,6 +274,86 @@ int build_lstencil(int p, double ampl02, int hx, int hy, LStencil& out, std::str
     return MGBF_OK;
 }
 
+void build_xfer_axis(int na, int nf, int nranks, int order, XferAxis& out) {
+    constexpr int ib = 6;  // xf table range 1-ib .. nf+ib (mg_parameter.f90:520-521)
+    const double length = 1.0 * na;
+    const double da = length / na, df = length / nf;
+    const double a0 = da * 0.5, f0 = df * 0.5;
+    std::vector<int> lref(na);
+    std::vector<double> lc(4 * (size_t)na, 0.0);
+    for (int n = 1; n <= na; ++n) {
+        const double x = a0 + da * (n - 1);
+        int ifound = 1 - ib;
+        for (int i = 1 - ib; i <= nf + ib - 1; ++i)
+            if (x < f0 + df * (i - 1)) {
+                ifound = i;
+                break;
+            }
+        double* c = &lc[4 * (size_t)(n - 1)];
+        if (order == 3) {
+            const int i = ifound - 2;
+            const double x1 = f0 + df * (i - 1), x2 = f0 + df * i, x3 = f0 + df * (i + 1), x4 = f0 + df * (i + 2);
+            const double x1x = x1 - x, x2x = x2 - x, x3x = x3 - x, x4x = x4 - x;
+            const double rx2x1 = 1. / (x2 - x1), rx3x1 = 1. / (x3 - x1);
+            const double rx3x2 = 1. / (x3 - x2), rx4x2 = 1. / (x4 - x2), rx4x3 = 1. / (x4 - x3);
+            const double cfl1 = x2x * x3x * rx2x1 * rx3x1;
+            const double cfl2 = -(x1x * x3x * rx2x1 * rx3x2);
+            const double cfl3 = x1x * x2x * rx3x1 * rx3x2;
+            const double cll = x3x * rx3x2;
+            const double cfr1 = x3x * x4x * rx3x2 * rx4x2;
+            const double cfr2 = -(x2x * x4x * rx3x2 * rx4x3);
+            const double cfr3 = x2x * x3x * rx4x2 * rx4x3;
+            const double crr = -(x2x * rx3x2);
+            lref[n - 1] = i;
+            c[0] = cfl1 * cll;
+            c[1] = cfl2 * cll + cfr1 * crr;
+            c[2] = cfl3 * cll + cfr2 * crr;
+            c[3] = cfr3 * crr;
+        } else if (order == 2) {
+            const int i = ifound - 1;
+            const double x1 = f0 + df * (i - 1), x2 = f0 + df * i, x3 = f0 + df * (i + 1);
+            const double x1_x = x1 - x, x2_x = x2 - x, x3_x = x3 - x;
+            const double rx2x1 = 1. / (x2 - x1), rx3x1 = 1. / (x3 - x1), rx3x2 = 1. / (x3 - x2);
+            lref[n - 1] = i;
+            c[0] = x2_x * x3_x * rx2x1 * rx3x1;
+            c[1] = -(x1_x * x3_x * rx2x1 * rx3x2);
+            c[2] = x1_x * x2_x * rx3x1 * rx3x2;
+        } else {
+            const int i = ifound - 1;
+            const double x1 = f0 + df * (i - 1), x2 = f0 + df * i;
+            const double x1_x = x1 - x, x2_x = x2 - x;
+            const double rx2x1 = 1. / (x2 - x1);
+            lref[n - 1] = i;
+            c[0] = x2_x * rx2x1;
+            c[1] = -(x1_x * rx2x1);
+        }
+    }
+    out = XferAxis{};
+    out.order = order;
+    const int ntot = na * nranks, nft = nf * nranks, ne = nft + 2 * order;
+    out.ref.resize(ntot);
+    out.c.resize(4 * (size_t)ntot);
+    std::vector<std::vector<std::pair<int, double>>> lists(ne);
+    for (int r = 0; r < nranks; ++r)
+        for (int n = 0; n < na; ++n) {
+            const int N = r * na + n;
+            out.ref[N] = r * nf + lref[n] - 1;  // global, 0-based
+            for (int t = 0; t < 4; ++t) out.c[4 * (size_t)N + t] = lc[4 * (size_t)n + t];
+            for (int t = 0; t <= order; ++t) {
+                const int e = out.ref[N] + t + order;
+                if (e >= 0 && e < ne) lists[e].push_back({N, lc[4 * (size_t)n + t]});
+            }
+        }
+    out.off.assign(ne + 1, 0);
+    for (int e = 0; e < ne; ++e) {
+        out.off[e + 1] = out.off[e] + (int)lists[e].size();
+        for (auto& pr : lists[e]) {
+            out.src.push_back(pr.first);
+            out.w.push_back(pr.second);
+        }
+    }
+}
+
 int check_other_reaches(int p, double ampl02, double ampl03, int hx, int hy, int hz, std::string& err) {
     // getlinesum(hx,1,im,paspx,ssx) / (hy,...,paspy,ssy): paspx = pasp02 is
     // used without cholaspect (mg_intstate.f90:370-375,427-428).

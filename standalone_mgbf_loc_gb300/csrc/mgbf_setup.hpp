@@ -57,6 +57,22 @@ struct Interp1D {
     std::vector<double> pw;     // nf x ntap prolongation weights
 };
 
+// One axis of the analysis <-> filter transfer, global over nranks ranks:
+// per analysis point the first filter tap (global, 0-based; may lie in the
+// mirror halo) and 4 weights (order+1 used).  lsqr_mg_coef
+// (mg_interpolate.f90:89-298) on each rank's local grid, lengthx = na
+// (mg_parameter.f90:515-541).
+struct XferAxis {
+    int order = 3;
+    std::vector<int> ref;     // na * nranks
+    std::vector<double> c;    // 4 per point
+    // adjoint lists over the extended filter index e = ref + t + order,
+    // e in [0, nf*nranks + 2*order): offsets, source analysis index, weight
+    std::vector<int> off, src;
+    std::vector<double> w;
+};
+void build_xfer_axis(int na, int nf, int nranks, int order, XferAxis& out);
+
 // Returns 0 or an MGBF_ERR_* code with a message in err.
 int build_hstencil(int p, double ampl02, int hx, int hy, HStencil& out, std::string& err);
 int build_zstencil(int p, double ampl01, int hz, int lm, bool need_mirror, ZStencil& out,

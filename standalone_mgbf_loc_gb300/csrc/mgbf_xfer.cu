@@ -1,0 +1,287 @@
+// Transfers between the analysis grid and the first filter generation
+// (anal_to_filt_all2 / filt_to_anal_all2, mg_transfer.f90:154-203, 339-464).
+//
+// Direct (filter -> analysis): each analysis point gathers the separable
+// 2/3/4-tap offset interpolation (lin/quad/lsqr_direct_offset,
+// mg_interpolate.f90:634-681, 750-795, 858-903) from the filter field, with
+// the half-sample mirror of boco_2d as an index reflection.
+// Adjoint (analysis -> filter): the reference scatters (..._adjoint_offset,
+// mg_interpolate.f90:684-747, 798-855, 906-960); here every target gathers
+// its sources from host-built lists, first along y into an intermediate on
+// the analysis x-grid, then along x into the extended filter array, so no
+// two threads write one element.  bocoT_2d's fold then runs on the halo
+// bands only.
+// Vertical (lm_a = 2 lm - 1): l_vertical_direct/adjoint_spec2
+// (mg_interpolate.f90:963-1044) per point and block of levels.
+#include <cuda_runtime.h>
+
+#include "mgbf_common.cuh"
+#include "mgbf_kernels.cuh"
+
+namespace mgbf {
+
+namespace {
+
+// V levels per thread: 4 (vector loads) or 1.
+template <typename T, int V> struct Lv;
+template <typename T> struct Lv<T, 4> {
+    using A = typename AccOf<T>::type;
+    static __device__ __forceinline__ void ld(const T* p, A (&v)[4]) { V4<T>::ld(p, v); }
+    static __device__ __forceinline__ void st(T* p, const A (&v)[4]) { V4<T>::st(p, v); }
+};
+template <typename T> struct Lv<T, 1> {
+    using A = typename AccOf<T>::type;
+    static __device__ __forceinline__ void ld(const T* p, A (&v)[1]) { v[0] = ldv(p); }
+    static __device__ __forceinline__ void st(T* p, const A (&v)[1]) { stv(p, v[0]); }
+};
+
+// Flat thread index -> (level group q, point a, point b), q fastest.
+struct Pos3 {
+    int q, a, b;
+    bool ok;
+};
+__device__ __forceinline__ Pos3 pos3(int nq, int na, int nb) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    Pos3 r;
+    r.q = (int)(idx % nq);
+    const long long rest = idx / nq;
+    r.a = (int)(rest % na);
+    r.b = (int)(rest / na);
+    r.ok = r.b < nb;
+    return r;
+}
+
+// W(k, N, M) = sum_s cy_s(M) sum_t cx_t(N) V(k, reflect(rx(N)+t), reflect(ry(M)+s))
+template <typename T, int V>
+__global__ void __launch_bounds__(128) k_xfer_direct(XferDirectArgs a) {
+    using A = typename AccOf<T>::type;
+    const Pos3 p = pos3(a.nk / V, a.nm0, a.mm0);
+    if (!p.ok) return;
+    const int k = V * p.q;
+    const int nt = a.order + 1;
+    const int rx = a.rx[p.a], ry = a.ry[p.b];
+    const A* cx = static_cast<const A*>(a.cx) + 4 * p.a;
+    const A* cy = static_cast<const A*>(a.cy) + 4 * p.b;
+    const T* in = static_cast<const T*>(a.in.p) + k;
+    A acc[V], vx[V], v[V];
+    for (int s = 0; s < nt; ++s) {
+        const T* row = in + a.in.sj * reflect_half(ry + s, a.J);
+#pragma unroll
+        for (int e = 0; e < V; ++e) vx[e] = A(0);
+        for (int t = 0; t < nt; ++t) {
+            Lv<T, V>::ld(row + a.in.si * reflect_half(rx + t, a.I), v);
+            const A c = cx[t];
+#pragma unroll
+            for (int e = 0; e < V; ++e) vx[e] = t ? fma(c, v[e], vx[e]) : c * v[e];
+        }
+        const A c = cy[s];
+#pragma unroll
+        for (int e = 0; e < V; ++e) acc[e] = s ? fma(c, vx[e], acc[e]) : c * vx[e];
+    }
+    Lv<T, V>::st(static_cast<T*>(a.out.p) + k + a.out.si * p.a + a.out.sj * p.b, acc);
+}
+
+// out(k, a, b) = sum over the list of target `lt` of w * in(k, src, b) (dir 0:
+// list over the first point index, sources along `in.si`) or
+// sum w * in(k, a, src) (dir 1: sources along `in.sj`).  Targets with an
+// empty list give 0.
+template <typename T, int V>
+__global__ void __launch_bounds__(128) k_xfer_gather(XferGatherArgs a) {
+    using A = typename AccOf<T>::type;
+    const Pos3 p = pos3(a.nk / V, a.na, a.nb);
+    if (!p.ok) return;
+    const int k = V * p.q;
+    const int lt = a.dir ? p.b : p.a;
+    const int o0 = a.off[lt], o1 = a.off[lt + 1];
+    const A* w = static_cast<const A*>(a.w);
+    const T* in = static_cast<const T*>(a.in.p) + k + (a.dir ? a.in.si * p.a : a.in.sj * p.b);
+    const long long ls = a.dir ? a.in.sj : a.in.si;
+    A acc[V], v[V];
+#pragma unroll
+    for (int e = 0; e < V; ++e) acc[e] = A(0);
+    for (int o = o0; o < o1; ++o) {
+        Lv<T, V>::ld(in + ls * a.src[o], v);
+        const A c = w[o];
+#pragma unroll
+        for (int e = 0; e < V; ++e) acc[e] = fma(c, v[e], acc[e]);
+    }
+    Lv<T, V>::st(static_cast<T*>(a.out.p) + k + a.out.si * (p.a - a.out_a0) + a.out.sj * (p.b - a.out_b0), acc);
+}
+
+// bocoT_2d on the halo band b of an extended array whose view origin is the
+// first interior point: x first on every row of the band's range, then y
+// on the interior columns.  One thread per (level, row or column, t).
+template <typename T>
+__global__ void __launch_bounds__(256) k_fold_x(View v, int nk, int I, int J, int b) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n = (long long)nk * b * (J + 2 * b);
+    if (idx >= n) return;
+    const int k = (int)(idx % nk);
+    const long long r = idx / nk;
+    const int t = (int)(r % b);
+    const int j = (int)(r / b) - b;
+    T* row = static_cast<T*>(v.p) + k + v.sj * j;
+    // west: W(t) += W(1-t); east: W(I-b+t) += W(I+b+1-t)  (1-based, t = 1..b)
+    stv(row + v.si * t, ldv(row + v.si * t) + ldv(row + v.si * (-1 - t)));
+    stv(row + v.si * (I - 1 - t), ldv(row + v.si * (I - 1 - t)) + ldv(row + v.si * (I + t)));
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_fold_y(View v, int nk, int I, int J, int b) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n = (long long)nk * b * I;
+    if (idx >= n) return;
+    const int k = (int)(idx % nk);
+    const long long r = idx / nk;
+    const int t = (int)(r % b);
+    const int i = (int)(r / b);
+    T* col = static_cast<T*>(v.p) + k + v.si * i;
+    stv(col + v.sj * t, ldv(col + v.sj * t) + ldv(col + v.sj * (-1 - t)));
+    stv(col + v.sj * (J - 1 - t), ldv(col + v.sj * (J - 1 - t)) + ldv(col + v.sj * (J + t)));
+}
+
+// boco_2d on a halo band b: y first on the interior columns, then x on every
+// row including the y-halo rows (mg_bocos.f90:225-377).
+template <typename T>
+__global__ void __launch_bounds__(256) k_fill_y(View v, int nk, int I, int J, int b) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)nk * b * I) return;
+    const int k = (int)(idx % nk);
+    const long long r = idx / nk;
+    const int t = (int)(r % b);
+    const int i = (int)(r / b);
+    T* col = static_cast<T*>(v.p) + k + v.si * i;
+    stv(col + v.sj * (-1 - t), ldv(col + v.sj * t));
+    stv(col + v.sj * (J + t), ldv(col + v.sj * (J - 1 - t)));
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_fill_x(View v, int nk, int I, int J, int b) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)nk * b * (J + 2 * b)) return;
+    const int k = (int)(idx % nk);
+    const long long r = idx / nk;
+    const int t = (int)(r % b);
+    const int j = (int)(r / b) - b;
+    T* row = static_cast<T*>(v.p) + k + v.sj * j;
+    stv(row + v.si * (-1 - t), ldv(row + v.si * t));
+    stv(row + v.si * (I + t), ldv(row + v.si * (I - 1 - t)));
+}
+
+// l_vertical_direct_spec2 / l_vertical_adjoint_spec2 at every point of an
+// (a, b) range: en blocks of lm filter levels <-> en blocks of lm_a = 2lm-1
+// analysis levels; levels past the blocks are copied (direct) or left 0.
+template <typename T>
+__global__ void __launch_bounds__(256) k_vert(XferVertArgs a) {
+    using A = typename AccOf<T>::type;
+    const int nko = a.adjoint ? a.nkf : a.nka;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)nko * a.na * a.nb) return;
+    const int ko = (int)(idx % nko);
+    const long long r = idx / nko;
+    const int pa = (int)(r % a.na) + a.a0, pb = (int)(r / a.na) + a.b0;
+    const T* in = static_cast<const T*>(a.in.p) + a.in.si * pa + a.in.sj * pb;
+    T* out = static_cast<T*>(a.out.p) + a.out.si * pa + a.out.sj * pb;
+    const int lm = a.lm, lma = 2 * a.lm - 1;
+    A v = A(0);
+    if (!a.adjoint) {
+        if (ko < a.en * lma) {
+            const int e = ko / lma, n = ko - e * lma;  // 0-based analysis level
+            if (n % 2 == 0) v = ldv(in + e * lm + n / 2);
+            else v = A(0.5) * (ldv(in + e * lm + (n - 1) / 2) + ldv(in + e * lm + (n + 1) / 2));
+        } else {
+            v = ldv(in + ko - a.en * lma + a.en * lm);
+        }
+    } else {
+        if (ko < a.en * lm) {
+            const int e = ko / lm, kk = ko - e * lm;
+            const T* w = in + e * lma;
+            // reference order: the halves of the even levels (increasing), then the odd level
+            if (kk >= 1) v += A(0.5) * ldv(w + 2 * kk - 1);
+            if (2 * kk + 1 <= lma - 1) v += A(0.5) * ldv(w + 2 * kk + 1);
+            v += ldv(w + 2 * kk);
+        } else {
+            v = ldv(in + ko - a.en * lm + a.en * lma);
+        }
+    }
+    stv(out + ko, v);
+}
+
+inline int last_err() {
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : (int)e;
+}
+inline bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+inline size_t esz(DType t) { return t == DType::F64 ? 8 : (t == DType::F32 ? 4 : 2); }
+inline bool vec_ok(DType t, int nk, const View& a, const View& b) {
+    const size_t e = esz(t);
+    return nk % 4 == 0 && al16(a.p) && al16(b.p) && (a.si * e) % 16 == 0 && (a.sj * e) % 16 == 0 &&
+           (b.si * e) % 16 == 0 && (b.sj * e) % 16 == 0;
+}
+inline unsigned blocks(long long threads, int bs) { return (unsigned)((threads + bs - 1) / bs); }
+
+template <typename F>
+void dispatch(DType t, F&& f) {
+    switch (t) {
+        case DType::F64: f(double()); break;
+        case DType::F32: f(float()); break;
+        case DType::BF16: f(__nv_bfloat16()); break;
+    }
+}
+
+}  // namespace
+
+int launch_xfer_direct(DType t, const XferDirectArgs& a, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const bool vec = vec_ok(t, a.nk, a.in, a.out);
+    dispatch(t, [&](auto tag) {
+        using T = decltype(tag);
+        if (vec) k_xfer_direct<T, 4><<<blocks((long long)a.nk / 4 * a.nm0 * a.mm0, 128), 128, 0, s>>>(a);
+        else k_xfer_direct<T, 1><<<blocks((long long)a.nk * a.nm0 * a.mm0, 128), 128, 0, s>>>(a);
+    });
+    return last_err();
+}
+
+int launch_xfer_gather(DType t, const XferGatherArgs& a, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const bool vec = vec_ok(t, a.nk, a.in, a.out);
+    dispatch(t, [&](auto tag) {
+        using T = decltype(tag);
+        if (vec) k_xfer_gather<T, 4><<<blocks((long long)a.nk / 4 * a.na * a.nb, 128), 128, 0, s>>>(a);
+        else k_xfer_gather<T, 1><<<blocks((long long)a.nk * a.na * a.nb, 128), 128, 0, s>>>(a);
+    });
+    return last_err();
+}
+
+int launch_xfer_fold(DType t, View v, int nk, int I, int J, int b, void* stream) {
+    if (b <= 0) return 0;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    dispatch(t, [&](auto tag) {
+        using T = decltype(tag);
+        k_fold_x<T><<<blocks((long long)nk * b * (J + 2 * b), 256), 256, 0, s>>>(v, nk, I, J, b);
+        k_fold_y<T><<<blocks((long long)nk * b * I, 256), 256, 0, s>>>(v, nk, I, J, b);
+    });
+    return last_err();
+}
+
+int launch_xfer_fill(DType t, View v, int nk, int I, int J, int b, void* stream) {
+    if (b <= 0) return 0;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    dispatch(t, [&](auto tag) {
+        using T = decltype(tag);
+        k_fill_y<T><<<blocks((long long)nk * b * I, 256), 256, 0, s>>>(v, nk, I, J, b);
+        k_fill_x<T><<<blocks((long long)nk * b * (J + 2 * b), 256), 256, 0, s>>>(v, nk, I, J, b);
+    });
+    return last_err();
+}
+
+int launch_xfer_vert(DType t, const XferVertArgs& a, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const long long n = (long long)(a.adjoint ? a.nkf : a.nka) * a.na * a.nb;
+    if (n == 0) return 0;
+    dispatch(t, [&](auto tag) {
+        using T = decltype(tag);
+        k_vert<T><<<blocks(n, 256), 256, 0, s>>>(a);
+    });
+    return last_err();
+}
+
+}  // namespace mgbf

@@ -136,6 +136,14 @@ class MGBFDims:
     field_elems: int
     hbeta_kernel: int
     reach_line: int
+    nm0: int
+    mm0: int
+    km_a_all: int
+    anal_elems: int
+
+    def analysis_shape(self):
+        """WORKA(km_a_all, nm0, mm0) in C order."""
+        return (self.mm0, self.nm0, self.km_a_all)
 
     def field_shape(self):
         if self.layout == _abi.MGBF_LAYOUT_HALO:
@@ -227,6 +235,32 @@ class MGBF:
         dt = _dtype_code(dtype if dtype is not None else torch.float32)
         stream = torch.cuda.current_stream().cuda_stream if torch is not None else None
         _abi.check(self._lib.mgbf_autotune(self._h, dt, stream), "mgbf_autotune")
+
+    def analysis_shape(self):
+        return self.dims.analysis_shape()
+
+    def anal_to_filt(self, worka, vall) -> None:
+        """anal_to_filt_all2: WORKA (analysis grid) -> VALL (overwritten)."""
+        if tuple(worka.shape) != self.analysis_shape():
+            raise MGBFError(_abi.MGBF_ERR_ARG, f"WORKA shape {tuple(worka.shape)} != {self.analysis_shape()}")
+        self._check_shape(vall)
+        pa, dt, mem, st = _field_args(worka)
+        pv, dt2, mem2, _ = _field_args(vall)
+        if dt != dt2 or mem != mem2:
+            raise MGBFError(_abi.MGBF_ERR_ARG, "WORKA and VALL must share dtype and memory space")
+        _abi.check(self._lib.mgbf_anal_to_filt(self._h, pa, pv, dt, mem, st), "mgbf_anal_to_filt")
+
+    def filt_to_anal(self, vall, worka) -> None:
+        """filt_to_anal_all2: VALL -> WORKA (VALL's interpolation halo is
+        filled in place, as in the reference)."""
+        if tuple(worka.shape) != self.analysis_shape():
+            raise MGBFError(_abi.MGBF_ERR_ARG, f"WORKA shape {tuple(worka.shape)} != {self.analysis_shape()}")
+        self._check_shape(vall)
+        pv, dt, mem, st = _field_args(vall)
+        pa, dt2, mem2, _ = _field_args(worka)
+        if dt != dt2 or mem != mem2:
+            raise MGBFError(_abi.MGBF_ERR_ARG, "WORKA and VALL must share dtype and memory space")
+        _abi.check(self._lib.mgbf_filt_to_anal(self._h, pv, pa, dt, mem, st), "mgbf_filt_to_anal")
 
     def set_tuning(self, variant: int, rows: int = 0, dtype=None) -> None:
         """Pin the radial-kernel variant and rows per block (variant < 0: defaults)."""

@@ -226,3 +226,20 @@ def test_batch_set_procedure_validation(lib):
     with pytest.raises(MGBFError) as e:
         b2.set_procedure(8)
     assert e.value.code == _abi.MGBF_ERR_DIVISIBILITY
+
+
+@pytest.mark.parametrize("change,code", [
+    (dict(nm0=0, mm0=0), _abi.MGBF_ERR_CONFIG),
+    (dict(l_new_map=False), _abi.MGBF_ERR_UNSUPPORTED),
+    (dict(lm_a=5), _abi.MGBF_ERR_CONFIG),                       # neither lm nor 2*lm-1
+    (dict(lm_a=15, km2=1), _abi.MGBF_ERR_UNSUPPORTED),          # spec2 blocks break with 2D variables
+    (dict(hx=2, layout=_abi.MGBF_LAYOUT_HALO), _abi.MGBF_ERR_CONFIG),  # lsqr needs a halo of 3
+])
+def test_transfer_validation(lib, change, code):
+    """Checked before any device work."""
+    d = dict(nm0=72, mm0=48, lm=8, lm_a=8, km3=2, hx=4, hy=4, mg_ampl02=1.0)  # every reach 2
+    d.update(change)
+    op = MGBF(small_config(**d))
+    with pytest.raises(MGBFError) as e:
+        op.filt_to_anal(np.zeros(op.field_shape()), np.zeros(op.analysis_shape()))
+    assert e.value.code == code
