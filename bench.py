@@ -317,6 +317,7 @@ def run_gpu(args):
         extras["fp64_plain"] = plain_forward(torch, dev, torch.float64)
         extras["fp32_plain"] = plain_forward(torch, dev, torch.float32)
         extras["fast_fp32"] = fast_forward(torch, dev, torch.float32, peak)
+        extras["transfers_fp32"] = transfers(torch, dev, torch.float32, peak)
 
     result = None
     if rank == 0:
@@ -444,6 +445,44 @@ def fast_forward(torch, dev, dtype, peak_gbs):
             "line_kernel": {"bound": "hbm", "ms_per_call": line_ms, "achieved": gbs, "peak": peak_gbs,
                             "unit": "GB/s", "frac": gbs / peak_gbs if gbs else None,
                             "algorithmic_bytes": "2 passes x 2 x 4 B per point of each generation"}}
+
+
+def transfers(torch, dev, dtype, peak_gbs):
+    """anal_to_filt_all2 / filt_to_anal_all2 on the shipped namelist's grids:
+    analysis 1440x960, filter 20x20 ranks of 64x32 (1280x640), 4 3D
+    variables of 65 levels (lm_a = lm), lsqr interpolation.  HBM-bound:
+    each direction reads one field and writes the other once."""
+    from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig
+    cfg = MGBFConfig(nxPE=20, nyPE=20, im_filt=64, jm_filt=32, nm0=1440, mm0=960, lm=65, lm_a=65, km3=4, km2=0,
+                     n_ens=1, gm_max=4, hx=6, hy=6, hz=4, p=2, mg_ampl02=ampl02(6), mg_ampl01=ampl01(4),
+                     layout=0)  # VALL with its halo, as the reference holds it
+    op = MGBF(cfg)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(9)
+    v = torch.randn(op.field_shape(), generator=gen, device=dev, dtype=dtype)
+    w = torch.randn(op.analysis_shape(), generator=gen, device=dev, dtype=dtype)
+    es = v.element_size()
+    out = {"workload": "transfers, analysis 1440x960 <-> filter 1280x640 (20x20 ranks of 64x32), 260 levels, lsqr, "
+                       "VALL with halo 6",
+           "dtype": str(dtype).replace("torch.", "")}
+    for name, fn in (("anal_to_filt", lambda: op.anal_to_filt(w, v)), ("filt_to_anal", lambda: op.filt_to_anal(v, w))):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        n = 10
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(n):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / n
+        nbytes = (v.numel() + w.numel()) * es  # one field read, the other written
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        out[name] = {"ms": ms, "achieved": gbs, "peak": peak_gbs, "unit": "GB/s", "frac": gbs / peak_gbs,
+                     "algorithmic_bytes": nbytes}
+    op.close()
+    return out
 
 
 def main():

@@ -1259,7 +1259,8 @@ static int xfer_a2f(mgbf_handle* h, const void* worka, void* vall, DType t, void
     wa.p = const_cast<void*>(worka); wa.si = X.nka; wa.sj = (long long)X.nka * X.nm0;
     DevBuf& VX = X.vx[(int)t];
     DevBuf& VE = X.vext[(int)t];
-    if ((rc = VX.ensure((size_t)X.nka * X.nm0 * JE * es)) || (rc = VE.ensure((size_t)X.nka * IE * JE * es))) return rc;
+    if ((rc = VX.ensure((size_t)X.nka * X.nm0 * JE * es))) return rc;
+    if ((h->cfg.layout != MGBF_LAYOUT_HALO || X.vert) && (rc = VE.ensure((size_t)X.nka * IE * JE * es))) return rc;
     View vx;
     vx.p = VX.p; vx.si = X.nka; vx.sj = (long long)X.nka * X.nm0;
     XferGatherArgs g;
@@ -1267,17 +1268,27 @@ static int xfer_a2f(mgbf_handle* h, const void* worka, void* vall, DType t, void
     g.off = static_cast<const int*>(X.offy.p); g.src = static_cast<const int*>(X.srcy.p); g.w = X.wy[ai].p;
     g.out_a0 = 0; g.out_b0 = 0;
     LK(launch_xfer_gather(t, g, stream));
+    View v = field_view(h, vall, t);
+    const bool halo = h->cfg.layout == MGBF_LAYOUT_HALO;
+    // VALL = 0 beyond the interpolation halo; everything inside is written
+    if (halo)
+        LK(launch_zero_halo(t, shifted(v, -ib, -ib, t), nkf, IE, JE, h->cfg.hx - ib, h->cfg.hy - ib, stream));
+    // the x gather writes the extended array: VALL itself when it has the
+    // halo and the levels match, else a temporary
+    const bool direct_out = halo && !X.vert;
     View ve;
-    ve.p = VE.p; ve.si = X.nka; ve.sj = (long long)X.nka * IE;
-    ve = shifted(ve, ib, ib, t);  // origin at the first interior point
+    if (direct_out) {
+        ve = v;
+    } else {
+        ve.p = VE.p; ve.si = X.nka; ve.sj = (long long)X.nka * IE;
+        ve = shifted(ve, ib, ib, t);  // origin at the first interior point
+    }
     g.in = vx; g.out = ve; g.na = IE; g.nb = JE; g.dir = 0;
     g.off = static_cast<const int*>(X.offx.p); g.src = static_cast<const int*>(X.srcx.p); g.w = X.wx[ai].p;
     g.out_a0 = ib; g.out_b0 = ib;
     LK(launch_xfer_gather(t, g, stream));
     LK(launch_xfer_fold(t, ve, X.nka, P.I, P.J, ib, stream));
-    View v = field_view(h, vall, t);
-    const bool halo = h->cfg.layout == MGBF_LAYOUT_HALO;
-    if (halo) CU(cudaMemsetAsync(vall, 0, h->field_elems * es, static_cast<cudaStream_t>(stream)));
+    if (direct_out) return 0;
     const int r0 = halo ? -ib : 0, na = halo ? IE : P.I, nb = halo ? JE : P.J;
     if (X.vert) {
         XferVertArgs va;

@@ -52,22 +52,24 @@ __device__ __forceinline__ Pos3 pos3(int nq, int na, int nb) {
 }
 
 // W(k, N, M) = sum_s cy_s(M) sum_t cx_t(N) V(k, reflect(rx(N)+t), reflect(ry(M)+s))
-template <typename T, int V>
+template <typename T, int V, int ORDER>
 __global__ void __launch_bounds__(128) k_xfer_direct(XferDirectArgs a) {
     using A = typename AccOf<T>::type;
     const Pos3 p = pos3(a.nk / V, a.nm0, a.mm0);
     if (!p.ok) return;
     const int k = V * p.q;
-    const int nt = a.order + 1;
+    constexpr int nt = ORDER + 1;
     const int rx = a.rx[p.a], ry = a.ry[p.b];
     const A* cx = static_cast<const A*>(a.cx) + 4 * p.a;
     const A* cy = static_cast<const A*>(a.cy) + 4 * p.b;
     const T* in = static_cast<const T*>(a.in.p) + k;
     A acc[V], vx[V], v[V];
+#pragma unroll
     for (int s = 0; s < nt; ++s) {
         const T* row = in + a.in.sj * reflect_half(ry + s, a.J);
 #pragma unroll
         for (int e = 0; e < V; ++e) vx[e] = A(0);
+#pragma unroll
         for (int t = 0; t < nt; ++t) {
             Lv<T, V>::ld(row + a.in.si * reflect_half(rx + t, a.I), v);
             const A c = cx[t];
@@ -234,8 +236,15 @@ int launch_xfer_direct(DType t, const XferDirectArgs& a, void* stream) {
     const bool vec = vec_ok(t, a.nk, a.in, a.out);
     dispatch(t, [&](auto tag) {
         using T = decltype(tag);
-        if (vec) k_xfer_direct<T, 4><<<blocks((long long)a.nk / 4 * a.nm0 * a.mm0, 128), 128, 0, s>>>(a);
-        else k_xfer_direct<T, 1><<<blocks((long long)a.nk * a.nm0 * a.mm0, 128), 128, 0, s>>>(a);
+        const unsigned gv = blocks((long long)a.nk / 4 * a.nm0 * a.mm0, 128), gs = blocks((long long)a.nk * a.nm0 * a.mm0, 128);
+        switch (a.order * 2 + (vec ? 1 : 0)) {
+            case 7: k_xfer_direct<T, 4, 3><<<gv, 128, 0, s>>>(a); break;
+            case 6: k_xfer_direct<T, 1, 3><<<gs, 128, 0, s>>>(a); break;
+            case 5: k_xfer_direct<T, 4, 2><<<gv, 128, 0, s>>>(a); break;
+            case 4: k_xfer_direct<T, 1, 2><<<gs, 128, 0, s>>>(a); break;
+            case 3: k_xfer_direct<T, 4, 1><<<gv, 128, 0, s>>>(a); break;
+            default: k_xfer_direct<T, 1, 1><<<gs, 128, 0, s>>>(a); break;
+        }
     });
     return last_err();
 }
