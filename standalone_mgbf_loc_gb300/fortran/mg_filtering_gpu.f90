@@ -4,6 +4,8 @@
 ! Drop-in for the filtering path of the reference's modules:
 !   mg_initialize            (mg_entrymod.f90:36)   -> mg_initialize_gpu
 !   filtering_procedure(mg_filt) (mg_filtering.f90:67) -> filtering_procedure
+!   anal_to_filt_all2 / filt_to_anal_all2 (mg_transfer.f90:154-203)
+!                                                   -> anal_to_filt_all2 / filt_to_anal_all2
 !   mg_finalize              (mg_entrymod.f90:222)  -> mg_finalize_gpu
 ! A caller such as RBETA_TEST keeps `call filtering_procedure(mgbf_proc)`
 ! and passes its VALL array (km_all, 1-hx:im+hx, 1-hy:jm+hy) in real(8),
@@ -21,6 +23,7 @@ module mg_filtering_gpu
   implicit none
   private
   public :: mg_initialize_gpu, filtering_procedure, filtering_procedure_adjoint, mg_finalize_gpu
+  public :: anal_to_filt_all2, filt_to_anal_all2
   public :: mgbf_ok
 
   integer(c_int), parameter :: mgbf_ok = 0
@@ -47,6 +50,18 @@ module mg_filtering_gpu
       type(c_ptr), value :: h
       integer(c_int), value :: mg_filt, dtype, mem
       type(c_ptr), value :: vall, stream
+    end function
+    integer(c_int) function mgbf_anal_to_filt(h, worka, vall, dtype, mem, stream) bind(C, name="mgbf_anal_to_filt")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      type(c_ptr), value :: worka, vall, stream
+      integer(c_int), value :: dtype, mem
+    end function
+    integer(c_int) function mgbf_filt_to_anal(h, vall, worka, dtype, mem, stream) bind(C, name="mgbf_filt_to_anal")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      type(c_ptr), value :: vall, worka, stream
+      integer(c_int), value :: dtype, mem
     end function
     integer(c_int) function mgbf_destroy(h) bind(C, name="mgbf_destroy")
       import :: c_int, c_ptr
@@ -90,6 +105,25 @@ contains
     rc = mgbf_filtering_procedure_adjoint(handle, int(mg_filt, c_int), c_loc(vall), mgbf_f64, mgbf_mem_host, &
                                           c_null_ptr)
     if (rc /= mgbf_ok) call fail(rc, 'filtering_procedure_adjoint')
+  end subroutine
+
+  ! anal_to_filt_all2: WORKA(km_a_all, nm0, mm0) -> VALL (overwritten).
+  subroutine anal_to_filt_all2(worka, vall)
+    real(c_double), dimension(:,:,:), contiguous, target, intent(in) :: worka
+    real(c_double), dimension(:,:,:), contiguous, target, intent(inout) :: vall
+    integer(c_int) :: rc
+    rc = mgbf_anal_to_filt(handle, c_loc(worka), c_loc(vall), mgbf_f64, mgbf_mem_host, c_null_ptr)
+    if (rc /= mgbf_ok) call fail(rc, 'anal_to_filt_all2')
+  end subroutine
+
+  ! filt_to_anal_all2: VALL -> WORKA; VALL's interpolation halo is filled,
+  ! as boco_2d does in the reference.
+  subroutine filt_to_anal_all2(vall, worka)
+    real(c_double), dimension(:,:,:), contiguous, target, intent(inout) :: vall
+    real(c_double), dimension(:,:,:), contiguous, target, intent(inout) :: worka
+    integer(c_int) :: rc
+    rc = mgbf_filt_to_anal(handle, c_loc(vall), c_loc(worka), mgbf_f64, mgbf_mem_host, c_null_ptr)
+    if (rc /= mgbf_ok) call fail(rc, 'filt_to_anal_all2')
   end subroutine
 
   subroutine mg_finalize_gpu()
