@@ -73,6 +73,8 @@ typedef struct {
     int reach1, reach2;
     double exxL, ssL;     /* fast filters' 1D horizontal line filter     */
     int reachL;
+    double e3, ss3;       /* filtering_rad3's ball: el*rmom2_3, 1/sum    */
+    int reach3;
 } setup_t;
 
 static const double EPS = 1.e-12;
@@ -146,6 +148,33 @@ static int setup(const orc_cfg* c, setup_t* s) {
         }
         s->ssL = 1.0 / sum;
         s->reachL = gxm;
+    }
+    /* cholaspect3 (jp_pbfil.f90:109-126) on pasp3 = diag(pasp03) and
+     * getlinesum3 (jp_pbfil.f90:220-268); rmom2_3 = 1/sqrt(2p+5). */
+    {
+        const double e = sqrt(1.0 / c->ampl03) * (1.0 / sqrt(pee2 + 5.0));
+        s->e3 = e;
+        double z = 1.0 / e;
+        int gzl = (int)ceil(-z + EPS), gzm = (int)floor(z - EPS);
+        int bad = gzl < -c->hz || gzm > c->hz;
+        double sum = 0.0;
+        for (int gz = gzl; gz <= gzm; ++gz) {
+            double zz = gz, rry = (zz * e) * (zz * e), y = sqrt(1.0 - rry);
+            int gyl = (int)ceil((0.0 - y) / e + EPS), gym = (int)floor((0.0 + y) / e - EPS);
+            if (gyl < -c->hy || gym > c->hy) bad = 1;
+            for (int gy = gyl; gy <= gym; ++gy) {
+                double yy = gy, rrx = rry + (yy * e - 0.0) * (yy * e - 0.0), x = sqrt(1.0 - rrx);
+                int gxl = (int)ceil((0.0 - x) / e + EPS), gxm = (int)floor((0.0 + x) / e - EPS);
+                if (gxl < -c->hx || gxm > c->hx) bad = 1;
+                for (int gx = gxl; gx <= gxm; ++gx) {
+                    double xx = gx, rr = rrx + (xx * e - 0.0) * (xx * e - 0.0);
+                    sum += ipow(1.0 - rr, c->p);
+                }
+            }
+        }
+        if (c->proc == 4 && bad) return ORC_ERR_REACH;
+        s->ss3 = 1.0 / sum;
+        s->reach3 = gzm;
     }
     return ORC_OK;
 }
@@ -370,6 +399,89 @@ static void fast_forward(const orc_cfg* c, const setup_t* S, arr3 U, int I, int 
     line_beta(S, c->p, U, I, J, c->hx, c->hy, 1, 0, k0, k1);
     fill_line(U, I, J, c->hx, 0, k0, k1);
     line_beta(S, c->p, U, I, J, c->hx, c->hy, 0, 0, k0, k1);
+}
+
+/* ----------------------------------------------- filtering_rad3: 3D ball */
+
+/* sup_vrbeta3 / sup_vrbeta3T (mg_filtering.f90:1923-2039) on the 3D
+ * variables of a generation array, column by column (levels k = v*lm+L-1):
+ * copy the column with its x/y halo, whole-sample mirror in L over hz
+ * levels, vrbeta3 (gather, jp_pbfil.f90:930-977) or vrbeta3t (scatter from
+ * the interior into the extended box, jp_pbfil.f90:1053-1100, then the L
+ * fold), and copy back the INTERIOR only: the x/y halo of U keeps what it
+ * held (the scatter's x/y-halo part is dropped). */
+static void ball3(const orc_cfg* c, const setup_t* S, arr3 U, int I, int J, int adj) {
+    const int lm = c->lm, hz = c->hz, hx = c->hx, hy = c->hy, p = c->p;
+    const size_t ni = (size_t)I + 2 * hx, nj = (size_t)J + 2 * hy, nz = (size_t)lm + 2 * hz;
+    double* W = (double*)malloc(sizeof(double) * ni * nj * nz);
+    double* B = (double*)malloc(sizeof(double) * ni * nj * nz);
+#define BX(a, i, j, L) a[((size_t)((L) + hz - 1) * nj + (size_t)((j) + hy - 1)) * ni + (size_t)((i) + hx - 1)]
+    const double e = S->e3, s = S->ss3;
+    const double z0 = 1.0 / e;
+    const int gzl = (int)ceil(-z0 + EPS), gzm = (int)floor(z0 - EPS);
+    for (int v = 0; v < c->nzcol; ++v) {
+        for (int L = 1; L <= lm; ++L)
+            for (int j = 1 - hy; j <= J + hy; ++j)
+                for (int i = 1 - hx; i <= I + hx; ++i) BX(W, i, j, L) = A3(U, v * lm + L - 1, i, j);
+        for (int L = 1; L <= hz; ++L)
+            for (int j = 1 - hy; j <= J + hy; ++j)
+                for (int i = 1 - hx; i <= I + hx; ++i) {
+                    BX(W, i, j, 1 - L) = BX(W, i, j, 1 + L);
+                    BX(W, i, j, lm + L) = BX(W, i, j, lm - L);
+                }
+        for (size_t t = 0; t < ni * nj * nz; ++t) B[t] = 0.0;
+        for (int iz = 1; iz <= lm; ++iz)
+            for (int iy = 1; iy <= J; ++iy)
+                for (int ix = 1; ix <= I; ++ix) {
+                    const double ta = BX(W, ix, iy, iz);
+                    double tb = 0.0;
+                    for (int gz = gzl; gz <= gzm; ++gz) {
+                        const double zz = gz, rry = (zz * e) * (zz * e), y = sqrt(1.0 - rry);
+                        const int gyl = (int)ceil((0.0 - y) / e + EPS), gym = (int)floor((0.0 + y) / e - EPS);
+                        for (int gy = gyl; gy <= gym; ++gy) {
+                            const double yy = gy, rrx = rry + (yy * e - 0.0) * (yy * e - 0.0), x = sqrt(1.0 - rrx);
+                            const int gxl = (int)ceil((0.0 - x) / e + EPS), gxm = (int)floor((0.0 + x) / e - EPS);
+                            for (int gx = gxl; gx <= gxm; ++gx) {
+                                const double xx = gx, rr = rrx + (xx * e - 0.0) * (xx * e - 0.0);
+                                const double frow = s * ipow(1.0 - rr, p);
+                                if (adj) BX(B, ix + gx, iy + gy, iz + gz) += frow * ta;
+                                else tb += frow * BX(W, ix + gx, iy + gy, iz + gz);
+                            }
+                        }
+                    }
+                    if (!adj) BX(B, ix, iy, iz) = tb;
+                }
+        if (adj)
+            for (int L = 1; L <= hz; ++L)
+                for (int j = 1 - hy; j <= J + hy; ++j)
+                    for (int i = 1 - hx; i <= I + hx; ++i) {
+                        BX(B, i, j, 1 + L) += BX(B, i, j, 1 - L);
+                        BX(B, i, j, lm - L) += BX(B, i, j, lm + L);
+                    }
+        for (int L = 1; L <= lm; ++L)
+            for (int j = 1; j <= J; ++j)
+                for (int i = 1; i <= I; ++i) A3(U, v * lm + L - 1, i, j) = BX(B, i, j, L);
+    }
+#undef BX
+    free(W);
+    free(B);
+}
+
+static void weight_gen(const orc_cfg* c, arr3 V, int I, int J, double a, double b, int k0, int k1);
+
+/* One generation of filtering_rad3 (mg_filtering.f90:123-257): the 2D
+ * variables through vrbeta2t / vrbeta2, the 3D variables through the ball,
+ * bocoT_2d / weighting / boco_2d over all levels in between. */
+static void rad3_generation(const orc_cfg* c, const setup_t* S, arr3 U, arr3 tmp, int I, int J, double a, double b,
+                            double* tb) {
+    const int n3 = c->nzcol * c->lm, nk = c->nk;
+    if (n3 < nk) vrbeta2t(S, c->p, U, tmp, 1, I, 1, J, n3, nk);
+    if (n3 > 0) ball3(c, S, U, I, J, 1);
+    fold_h(U, I, J, c->hx, c->hy, 0, nk);
+    weight_gen(c, U, I, J, a, b, 0, nk);
+    fill_h(U, I, J, c->hx, c->hy, 0, nk);
+    if (n3 < nk) vrbeta2(S, c->p, U, tmp, 1, I, 1, J, n3, nk, tb);
+    if (n3 > 0) ball3(c, S, U, I, J, 0);
 }
 
 /* ------------------------------------------------ restriction/prolongation */
@@ -622,7 +734,12 @@ typedef struct {
 static int check_cfg(const orc_cfg* c) {
     if (!c || c->I <= 0 || c->J <= 0 || c->nk <= 0 || c->gm < 1 || c->gm > ORC_MAX_GEN) return ORC_ERR_ARG;
     if (c->hx < 0 || c->hy < 0 || c->hz < 0 || c->p < 0) return ORC_ERR_ARG;
-    if (c->proc != 1 && c->proc != 6 && c->proc != 3 && c->proc != 8) return ORC_ERR_ARG;
+    if (c->proc != 1 && c->proc != 6 && c->proc != 3 && c->proc != 8 && c->proc != 4) return ORC_ERR_ARG;
+    if (c->proc == 4) {
+        if (c->nzcol < 0 || c->lm < 1 || (size_t)c->nzcol * c->lm > (size_t)c->nk) return ORC_ERR_ARG;
+        if (c->nzcol > 0 && c->hz >= c->lm) return ORC_ERR_ARG;
+        if (!(c->ampl03 > 0.0)) return ORC_ERR_ARG;
+    }
     int d = 1 << (c->gm - 1);
     if (c->I % d || c->J % d) return ORC_ERR_DIV;
     if (c->gm > 1 && (c->I / d < 2 || c->J / d < 2)) return ORC_ERR_DIV;
@@ -731,7 +848,7 @@ static void weight_gen(const orc_cfg* c, arr3 V, int I, int J, double a, double 
 
 static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G, int k0, int k1) {
     const int gm = c->gm, hx = c->hx, hy = c->hy;
-    const int filt1 = (c->proc == 1) || (c->proc == 3) || c->l_filt_g1;
+    const int filt1 = (c->proc == 1) || (c->proc == 3) || (c->proc == 4) || c->l_filt_g1;
     const int fast = c->proc == 3 || c->proc == 8;
     double* tb = (double*)malloc(sizeof(double) * (size_t)c->nk);
     /* up: V -> H_2 -> ... -> H_gm */
@@ -744,6 +861,10 @@ static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_
         arr3 U = g ? G[g].H : V;
         int I = G[g].I, J = G[g].J;
         if (g == 0 && !filt1) continue;
+        if (c->proc == 4) {  /* whole columns: the caller runs one k-range */
+            rad3_generation(c, S, U, G[g].tmp, I, J, c->a[g], c->b[g], tb);
+            continue;
+        }
         if (fast) {
             fast_adjoint(c, S, U, I, J, k0, k1);
             weight_gen(c, U, I, J, c->a[g], c->b[g], k0, k1);
@@ -771,7 +892,8 @@ int orc_filtering_procedure(const orc_cfg* c, double* Vd) {
     rc = setup(c, &S);
     if (rc) return rc;
     arr3 V = {Vd, c->nk, 1 - c->hx, c->I + c->hx, 1 - c->hy, c->J + c->hy};
-    if (c->l_vertical_filter && c->nzcol > 0) vfilter(c, &S, V, 1);
+    const int zfilt = c->proc != 4 && c->l_vertical_filter && c->nzcol > 0;  /* rad3 has no separate z filter */
+    if (zfilt) vfilter(c, &S, V, 1);
     gen_t G[ORC_MAX_GEN];
     memset(G, 0, sizeof(G));
     gens_alloc(c, G);
@@ -779,6 +901,7 @@ int orc_filtering_procedure(const orc_cfg* c, double* Vd) {
 #ifdef _OPENMP
     nth = c->nthreads > 0 ? c->nthreads : omp_get_max_threads();
     if (nth > c->nk) nth = c->nk;
+    if (c->proc == 4) nth = 1;
 #pragma omp parallel num_threads(nth)
     {
         int t = omp_get_thread_num(), nt = omp_get_num_threads();
@@ -790,7 +913,7 @@ int orc_filtering_procedure(const orc_cfg* c, double* Vd) {
     horizontal_pipeline(c, &S, V, G, 0, c->nk);
 #endif
     gens_free(c, G);
-    if (c->l_vertical_filter && c->nzcol > 0) vfilter(c, &S, V, 0);
+    if (zfilt) vfilter(c, &S, V, 0);
     return ORC_OK;
 }
 
@@ -846,6 +969,7 @@ static void half_chain(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G) {
 int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double* ga) {
     int rc = check_cfg(c);
     if (rc) return rc;
+    if (c->proc == 4) return ORC_ERR_ARG;  /* its adjoint side is not the transpose of its forward side */
     setup_t S;
     rc = setup(c, &S);
     if (rc) return rc;

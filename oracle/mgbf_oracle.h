@@ -41,13 +41,14 @@ typedef struct orc_cfg {
     double a[ORC_MAX_GEN];  /* per-generation weights a_g (a[0] = gen 1)      */
     double b[ORC_MAX_GEN];  /* Helmholtz Laplacian coefficients (reference: 0) */
     int lhelm;           /* use weighting_helm form                           */
-    int proc;            /* 1 rad2_bckg, 6 rad2_ens, 3 fast_bckg, 8 fast_ens  */
+    int proc;            /* 1 rad2_bckg, 6 rad2_ens, 3 fast_bckg, 8 fast_ens, 4 rad3 */
     int l_vertical_filter;
     int l_filt_g1;       /* procs 6 and 8 only                                */
     int lquart;          /* quadratic (3-point) interpolation                 */
     int lm;              /* levels per vertical column                        */
     int nzcol;           /* number of z columns at offsets (k-1)*lm           */
     int nthreads;        /* OpenMP threads (<=0: runtime default)             */
+    double ampl03;       /* mg_ampl03: aspect of the 3D filter (proc 4)       */
 } orc_cfg;
 
 /* Error codes (negative), mirroring the library's. */

@@ -30,7 +30,7 @@ class _Cfg(ctypes.Structure):
         ("lhelm", ctypes.c_int), ("proc", ctypes.c_int),
         ("l_vertical_filter", ctypes.c_int), ("l_filt_g1", ctypes.c_int),
         ("lquart", ctypes.c_int), ("lm", ctypes.c_int), ("nzcol", ctypes.c_int),
-        ("nthreads", ctypes.c_int),
+        ("nthreads", ctypes.c_int), ("ampl03", ctypes.c_double),
     ]
 
 
@@ -86,6 +86,7 @@ class OracleConfig:
     lhelm: bool = False
     helm_b: Optional[List[float]] = None
     nthreads: int = 0
+    ampl03: float = 1.0
 
     def to_c(self) -> _Cfg:
         c = _Cfg()
@@ -104,6 +105,7 @@ class OracleConfig:
         c.lm = self.lm
         c.nzcol = self.nzcol
         c.nthreads = self.nthreads
+        c.ampl03 = float(self.ampl03)
         return c
 
     def gen_shape(self, g: int):
