@@ -128,9 +128,14 @@ int mgbf_get_dims(const mgbf_handle* h, mgbf_dims* dims);
  * 6 = filtering_rad2_ens (mg_filtering.f90:1000-1147), and the fast 1D+1D
  * variants 3 = filtering_fast_bckg (mg_filtering.f90:825-997) and
  * 8 = filtering_fast_ens (mg_filtering.f90:1316-1506), whose horizontal
- * filter is vrbeta1 along x and y with el = mg_ampl02 (no cholaspect).
- * 2,4,5,7 return MGBF_ERR_UNSUPPORTED; any other value is a no-op
- * returning MGBF_OK, as the reference's select has no default case.
+ * filter is vrbeta1 along x and y with el = mg_ampl02 (no cholaspect), and
+ * 4 = filtering_rad3 (mg_filtering.f90:123-257: the 3D ball vrbeta3 with
+ * aspect mg_ampl03 on the 3D variables, the 2D radial filter on the 2D
+ * ones, no separate vertical filter; like the reference, its adjoint side
+ * keeps only the interior of the 3D scatter and folds the caller's VALL
+ * halo, so the operator is not symmetric).  2,5,7 return
+ * MGBF_ERR_UNSUPPORTED; any other value is a no-op returning MGBF_OK, as
+ * the reference's select has no default case.
  *   vall:   field pointer (device or host, per mem), laid out per the
  *           handle's layout, element type per dtype.
  *   stream: cudaStream_t (NULL = legacy default stream).  Device calls are

@@ -29,6 +29,7 @@ SOURCES = [
     "mgbf_hbeta_bf16.cu",
     "mgbf_noalloc.cu",
     "mgbf_xfer.cu",
+    "mgbf_rad3.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

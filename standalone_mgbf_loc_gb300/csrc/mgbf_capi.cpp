@@ -239,6 +239,10 @@ struct Group {
     ZStencil zs;
     LStencil ls;         // fast filters' line beta (procs 3, 8)
     std::string ls_err;  // why ls is unusable (reach beyond hx/hy), or empty
+    double ampl03 = 0;   // filtering_rad3's 3D ball (proc 4)
+    BStencil bs;
+    std::string bs_err;
+    DevBuf btaps, bw[2];  // ball taps (int4) and weights per accumulation type
     int HXP = 0;  // x padding of internal generation buffers
     DevBuf mrow;  // int table, shared by all types
     AccTables tab[2];  // [0] float, [1] double
@@ -350,6 +354,37 @@ struct Exec {
     View C(int g) { return gen_view(P, G, G.bufs[(int)t].C[g]->p, t, g); }
     View D(int g) { return gen_view(P, G, G.bufs[(int)t].D[g]->p, t, g); }
     bool fast = false;  // procs 3 and 8: separable line filters instead of the radial disk
+    int n3 = -1;        // proc 4: levels of the 3D variables (ball); the rest take the 2D radial filter
+    bool has_prev = false;  // proc 4, generation 1: the caller's halo, folded by the adjoint side
+    View prev;
+    int hx = 0, hy = 0;
+
+    // proc 4: 2D radial direct sum on the levels past n3, 3D ball on the first n3
+    int rad3_pass(int g, View in, View out, double scale, int mirror, int which_in) {
+        const int I = gen_I(P, g), J = gen_J(P, g);
+        if (n3 < G.nk) {
+            HDirectArgs a;
+            a.in = in; a.out = out;
+            a.in.p = static_cast<char*>(in.p) + elem_size(t) * (size_t)n3;
+            a.out.p = static_cast<char*>(out.p) + elem_size(t) * (size_t)n3;
+            a.nk = G.nk - n3; a.I = I; a.J = J; a.R = G.hs.R;
+            a.mrow = static_cast<const int*>(G.mrow.p);
+            a.w = G.tab[ai()].hw.p; a.mirror_hx = mirror; a.scale = scale;
+            LK(launch_hdirect(t, a, stream));
+        }
+        if (n3 > 0) {
+            BallArgs b;
+            b.in = in; b.out = out; b.prev = prev;
+            b.ncol = n3 / G.lm; b.lm = G.lm; b.I = I; b.J = J;
+            b.adjoint = which_in == 0; b.has_prev = which_in == 0 && g == 0 && has_prev; b.hx = hx; b.hy = hy;
+            b.ntaps = (int)G.bs.w.size();
+            b.taps = static_cast<const int4*>(G.btaps.p);
+            b.w = G.bw[ai()].p;
+            b.scale = scale;
+            LK(launch_ball(t, b, stream));
+        }
+        return 0;
+    }
 
     double pts(int g) const { return (double)G.nk * gen_I(P, g) * gen_J(P, g); }
 
@@ -464,6 +499,7 @@ struct Exec {
     int hpass(int g, View in, View out, double scale, int mirror, int stage, int which_in) {
         const int I = gen_I(P, g), J = gen_J(P, g);
         StageTimer tm(stage, stream, pts(g));
+        if (n3 >= 0) return rad3_pass(g, in, out, scale, mirror, which_in);
         if (fast) {
             // adjoint side (rbetaT x, bocoTx, rbetaT y, bocoTy): x first;
             // forward side (bocoy, rbeta y, bocox, rbeta x): y first
@@ -642,6 +678,19 @@ int build_group(Plan& P, Group& G, bool zneeded) {
         G.ls_err = "line filter reach " + std::to_string(G.ls.R) + " exceeds the coarsest generation " +
                    std::to_string(IG) + "x" + std::to_string(JG);
         G.ls.R = -1;
+    }
+    // filtering_rad3's ball: an error only when proc 4 runs
+    G.bs_err.clear();
+    if (G.ampl03 > 0.0) {
+        if (build_bstencil(G.p, G.ampl03, G.hx, G.hy, G.hz, G.bs, err)) {
+            G.bs_err = err;
+            G.bs.R = -1;
+        } else if (G.bs.R > IG || G.bs.R > JG) {
+            G.bs_err = "3D filter reach " + std::to_string(G.bs.R) + " exceeds the coarsest generation";
+            G.bs.R = -1;
+        }
+    } else {
+        G.bs_err = "mg_ampl03 must be positive";
     }
     return 0;
 }
@@ -954,7 +1003,7 @@ int mgbf_create(const mgbf_config* cfg, mgbf_handle** out) {
     Group& G = P.groups[0];
     G.nk = km_all; G.lm = c.lm; G.nzcol = c.km3 * c.n_ens;
     G.hx = c.hx; G.hy = c.hy; G.hz = c.hz; G.p = c.p;
-    G.ampl01 = c.mg_ampl01; G.ampl02 = c.mg_ampl02;
+    G.ampl01 = c.mg_ampl01; G.ampl02 = c.mg_ampl02; G.ampl03 = c.mg_ampl03;
     if ((rc = build_group(P, G, zneeded))) return rc;
     if ((rc = build_interps(P))) return rc;
     h->field_elems = c.layout == MGBF_LAYOUT_HALO
@@ -999,13 +1048,22 @@ int mgbf_set_weights(mgbf_handle* h, const double* a, int n) {
 }
 
 static bool is_fast(int mg_filt) { return mg_filt == 3 || mg_filt == 8; }
-static bool is_bckg(int mg_filt) { return mg_filt == 1 || mg_filt == 3; }
+static bool is_bckg(int mg_filt) { return mg_filt == 1 || mg_filt == 3 || mg_filt == 4; }
 
 static int check_proc(mgbf_handle* h, int mg_filt, bool& noop) {
     noop = false;
-    if (mg_filt == 1 || mg_filt == 6 || mg_filt == 3 || mg_filt == 8) {
+    if (mg_filt == 1 || mg_filt == 6 || mg_filt == 3 || mg_filt == 8 || mg_filt == 4) {
         if (is_bckg(mg_filt) && h->cfg.n_ens != 1)
-            return fail(MGBF_ERR_CONFIG, "filtering_rad2_bckg / filtering_fast_bckg (procs 1, 3) need n_ens = 1: their arrays are dimensioned km, not km_all");
+            return fail(MGBF_ERR_CONFIG, "filtering_rad2_bckg / filtering_fast_bckg / filtering_rad3 (procs 1, 3, 4) need n_ens = 1: their arrays are dimensioned km, not km_all");
+        if (mg_filt == 4) {
+            const Group& G = h->plan.groups[0];
+            if (G.bs.R < 0) return fail(MGBF_ERR_DIVISIBILITY, "filtering_rad3: " + G.bs_err);
+            if (h->cfg.km3 > 0 && h->cfg.hz >= h->cfg.lm)
+                return fail(MGBF_ERR_CONFIG, "filtering_rad3: sup_vrbeta3 mirrors hz levels, which needs hz < lm");
+            if (h->cfg.layout == MGBF_LAYOUT_HALO && (h->plan.I < 2 * h->cfg.hx || h->plan.J < 2 * h->cfg.hy))
+                return fail(MGBF_ERR_CONFIG, "filtering_rad3 on VALL with halos needs im >= 2*hx and jm >= 2*hy");
+            return MGBF_OK;
+        }
         if (!is_bckg(mg_filt) && h->cfg.l_vertical_filter && h->cfg.km2 > 0 && h->cfg.km3 > 0)
             return fail(MGBF_ERR_CONFIG, "filtering_rad2_ens / filtering_fast_ens (procs 6, 8) with the vertical filter need km2 = 0: sup_vrbeta1_ens views VALL with leading dimension km3_all*lm");
         if (is_fast(mg_filt) && h->plan.groups[0].ls.R < 0)
@@ -1013,9 +1071,17 @@ static int check_proc(mgbf_handle* h, int mg_filt, bool& noop) {
         return MGBF_OK;
     }
     if (mg_filt >= 2 && mg_filt <= 8)
-        return fail(MGBF_ERR_UNSUPPORTED, "filtering procedure " + std::to_string(mg_filt) + " is not implemented (supported: 1, 3, 6, 8)");
+        return fail(MGBF_ERR_UNSUPPORTED, "filtering procedure " + std::to_string(mg_filt) + " is not implemented (supported: 1, 3, 4, 6, 8)");
     noop = true;  // no case default in the reference's select
     return MGBF_OK;
+}
+
+static int rad3_tables(Group& G, DType t) {
+    int rc;
+    const int ai = t == DType::F64 ? 1 : 0;
+    if (!G.btaps.p && (rc = upload(G.btaps, G.bs.taps))) return rc;
+    if (!G.bw[ai].p && (rc = upload_acc(G.bw[ai], G.bs.w, t))) return rc;
+    return 0;
 }
 
 static int run_proc(mgbf_handle* h, int mg_filt, const void* xin, void* yout, DType t, void* stream) {
@@ -1024,13 +1090,29 @@ static int run_proc(mgbf_handle* h, int mg_filt, const void* xin, void* yout, DT
     int rc;
     if ((rc = ensure_tables(P, G, t))) return rc;
     if ((rc = ensure_bufs(P, G, t, false, is_fast(mg_filt)))) return rc;
-    const int nzcol = (h->cfg.l_vertical_filter && h->cfg.lm > 1) ? (is_bckg(mg_filt) ? h->nzcol_proc1 : h->nzcol_proc6) : 0;
+    const bool rad3 = mg_filt == 4;
+    const int nzcol = (!rad3 && h->cfg.l_vertical_filter && h->cfg.lm > 1)
+                          ? (is_bckg(mg_filt) ? h->nzcol_proc1 : h->nzcol_proc6) : 0;  // rad3: no separate z filter
     const bool filt1 = is_bckg(mg_filt) || h->cfg.l_filt_g1;
     Exec ex{P, G, t, stream};
     ex.fast = is_fast(mg_filt);
     View x = field_view(h, const_cast<void*>(xin), t);
     View y = field_view(h, yout, t);
+    if (rad3) {
+        if ((rc = rad3_tables(G, t))) return rc;
+        ex.n3 = h->cfg.km3 * h->cfg.lm;
+        ex.hx = h->cfg.hx; ex.hy = h->cfg.hy;
+        ex.has_prev = h->cfg.layout == MGBF_LAYOUT_HALO;
+        ex.prev = x;
+    }
     if ((rc = ex.forward(x, y, nzcol, filt1))) return rc;
+    if (rad3) {
+        if (h->cfg.layout == MGBF_LAYOUT_HALO) {
+            StageTimer tm(ST_HALO, stream, 0.0);
+            LK(launch_rad3_halo(t, y, ex.B(0), G.nk, ex.n3, P.I, P.J, h->cfg.hx, h->cfg.hy, stream));
+        }
+        return 0;
+    }
     if (h->cfg.layout == MGBF_LAYOUT_HALO && filt1) {
         // vrbeta2 zeroes the whole halo; the line filters leave its corners
         StageTimer tm(ST_HALO, stream, 0.0);
@@ -1085,6 +1167,9 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
     int rc = check_proc(h, mg_filt, noop);
     if (rc) return rc;
     if (noop) return fail(MGBF_ERR_UNSUPPORTED, "no filtering procedure " + std::to_string(mg_filt));
+    if (mg_filt == 4)
+        return fail(MGBF_ERR_UNSUPPORTED,
+                    "weight gradients of filtering_rad3: its adjoint side is not the transpose of its forward side");
     DeviceGuard dg(h->plan.device);
     const DType t = (DType)dtype;
     cudaStream_t s = static_cast<cudaStream_t>(stream);

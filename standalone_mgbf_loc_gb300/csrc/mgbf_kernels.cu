@@ -1041,7 +1041,10 @@ int launch_restrict(DType t, const RestrictArgs& a, void* stream) {
     const int Ic = a.If / 2, Jc = a.Jf / 2;
     if (a.nk == 0 || Ic == 0 || Jc == 0) return 0;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if ((a.nk * elem_size(t)) % 16 == 0 && aligned16(a.fine.p) && aligned16(a.coarse.p)) {
+    // lanes work in groups of 4 levels: nk % 4 == 0 (the 16-byte condition
+    // alone admits nk = 2 mod 4 in FP64, whose last group would spill into
+    // the next column)
+    if (a.nk % 4 == 0 && (a.nk * elem_size(t)) % 16 == 0 && aligned16(a.fine.p) && aligned16(a.coarse.p)) {
         // Row segments: about 8 waves of blocks (2 resident per SM), at least
         // 8 coarse rows (3 steps of ring fill per segment); small coarse
         // generations get short segments and enough blocks, the finest

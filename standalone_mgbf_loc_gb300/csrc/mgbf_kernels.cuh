@@ -75,6 +75,19 @@ struct XferVertArgs {
     int na, nb, a0, b0;    // points a0 .. a0+na-1, b0 .. b0+nb-1 (view coordinates)
 };
 
+// filtering_rad3's 3D ball (mgbf_rad3.cu) on the ncol*lm leading levels.
+struct BallArgs {
+    View in, out;
+    View prev;          // adjoint, generation 1: the caller's halo to fold (has_prev)
+    int ncol, lm, I, J;
+    int adjoint, has_prev, hx, hy;
+    int ntaps;
+    const int4* taps;   // (gx, gy, gz, 0) per tap
+    const void* w;      // weight per tap (accumulation type)
+    double scale;
+    float scalef;       // set by launch_ball
+};
+
 struct RestrictArgs {
     View fine, coarse;
     int nk, If, Jf;     // fine interior sizes; coarse = If/2, Jf/2
@@ -163,6 +176,8 @@ int launch_hdirect(DType t, const HDirectArgs& a, void* stream);
 int launch_mirror_x(DType t, View v, int nk, int I, int J, int hx, void* stream);
 int launch_copy(DType t, View in, View out, int nk, int I, int J, int mirror_hx, void* stream);
 int launch_line(DType t, const LineArgs& a, void* stream);
+int launch_ball(DType t, const BallArgs& a, void* stream);
+int launch_rad3_halo(DType t, View out, View src, int nk, int n3, int I, int J, int hx, int hy, void* stream);
 int launch_xfer_direct(DType t, const XferDirectArgs& a, void* stream);
 int launch_xfer_gather(DType t, const XferGatherArgs& a, void* stream);
 int launch_xfer_fold(DType t, View v, int nk, int I, int J, int b, void* stream);

@@ -274,6 +274,51 @@ int build_lstencil(int p, double ampl02, int hx, int hy, LStencil& out, std::str
     return MGBF_OK;
 }
 
+int build_bstencil(int p, double ampl03, int hx, int hy, int hz, BStencil& out, std::string& err) {
+    out = BStencil{};
+    if (!(ampl03 > 0.0)) {
+        err = "mg_ampl03 must be positive";
+        return MGBF_ERR_CONFIG;
+    }
+    const double e = std::sqrt(1.0 / ampl03) * (1.0 / std::sqrt(2.0 * p + 5.0));
+    const double z = 1.0 / e;
+    const int gzl = (int)std::ceil(-z + kEps), gzm = (int)std::floor(z - kEps);
+    if (gzl < -hz || gzm > hz) {
+        err = "getlinesum3: filter reach becomes too large for hz";
+        return MGBF_ERR_REACH;
+    }
+    double sum = 0.0;
+    std::vector<double> raw;
+    for (int gz = gzl; gz <= gzm; ++gz) {
+        const double rry = (gz * e) * (gz * e), y = std::sqrt(1.0 - rry);
+        const int gyl = (int)std::ceil((0.0 - y) / e + kEps), gym = (int)std::floor((0.0 + y) / e - kEps);
+        if (gyl < -hy || gym > hy) {
+            err = "getlinesum3: filter reach becomes too large for hy";
+            return MGBF_ERR_REACH;
+        }
+        for (int gy = gyl; gy <= gym; ++gy) {
+            const double rrx = rry + (gy * e - 0.0) * (gy * e - 0.0), x = std::sqrt(1.0 - rrx);
+            const int gxl = (int)std::ceil((0.0 - x) / e + kEps), gxm = (int)std::floor((0.0 + x) / e - kEps);
+            if (gxl < -hx || gxm > hx) {
+                err = "getlinesum3: filter reach becomes too large for hx";
+                return MGBF_ERR_REACH;
+            }
+            for (int gx = gxl; gx <= gxm; ++gx) {
+                const double rr = rrx + (gx * e - 0.0) * (gx * e - 0.0);
+                const double v = std::pow(1.0 - rr, p);
+                sum += v;
+                raw.push_back(v);
+                out.taps.insert(out.taps.end(), {gx, gy, gz, 0});
+            }
+        }
+    }
+    out.e = e;
+    out.s = 1.0 / sum;
+    out.R = gzm;
+    for (double v : raw) out.w.push_back(out.s * v);
+    return MGBF_OK;
+}
+
 void build_xfer_axis(int na, int nf, int nranks, int order, XferAxis& out) {
     constexpr int ib = 6;  // xf table range 1-ib .. nf+ib (mg_parameter.f90:520-521)
     const double length = 1.0 * na;

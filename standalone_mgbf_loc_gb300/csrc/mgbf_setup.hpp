@@ -42,6 +42,17 @@ struct LStencil {
     std::vector<double> w;      // R+1 normalised weights s*(1-(g exx)^2)^p, g = 0..R
 };
 
+// filtering_rad3's 3D ball: vrbeta3 (jp_pbfil.f90:930-977) with el from
+// cholaspect3 of pasp3 = diag(mg_ampl03) (jp_pbfil.f90:109-126), normalised
+// by getlinesum3 (jp_pbfil.f90:220-268); taps in the reference's gz, gy, gx
+// loop order.
+struct BStencil {
+    int R = -1;                 // reach in every direction (-1: none)
+    double e = 0, s = 0;
+    std::vector<int> taps;      // (gx, gy, gz, 0) per tap
+    std::vector<double> w;      // normalised weight per tap
+};
+
 struct ZStencil {
     int lm = 0, mz = 0;
     double exx = 0, s = 0;
@@ -79,6 +90,7 @@ int build_zstencil(int p, double ampl01, int hz, int lm, bool need_mirror, ZSten
                    std::string& err);
 int build_interp(int nf, bool quart, Interp1D& out, std::string& err);
 int build_lstencil(int p, double ampl02, int hx, int hy, LStencil& out, std::string& err);
+int build_bstencil(int p, double ampl03, int hx, int hy, int hz, BStencil& out, std::string& err);
 
 // Reach checks def_mg_weights performs for the other filters of the
 // reference (getlinesum on paspx/paspy, mg_intstate.f90:427-428, which skip

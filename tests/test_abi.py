@@ -144,7 +144,7 @@ def test_reach_larger_than_coarsest_generation(lib):
 def test_unsupported_and_unknown_procedures(lib):
     op = MGBF(small_config())
     x = np.zeros(op.field_shape())
-    for proc in (2, 4, 5, 7):
+    for proc in (2, 5, 7):
         with pytest.raises(MGBFError) as e:
             op.filtering_procedure(proc, x)
         assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
@@ -243,3 +243,17 @@ def test_transfer_validation(lib, change, code):
     with pytest.raises(MGBFError) as e:
         op.filt_to_anal(np.zeros(op.field_shape()), np.zeros(op.analysis_shape()))
     assert e.value.code == code
+
+
+def test_rad3_validation(lib):
+    """filtering_rad3: weight gradients are refused (its adjoint side is not
+    the transpose of its forward side); a ball reach beyond hz is refused when
+    the handle is created (getlinesum3 in def_mg_weights)."""
+    op = MGBF(small_config(lm=6, km3=2, hz=2, hx=3, hy=3, mg_ampl02=canonical(3), mg_ampl03=1.0))
+    x = np.zeros(op.field_shape())
+    with pytest.raises(MGBFError) as e:
+        op.apply_with_weight_grads(4, x, x)
+    assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
+    with pytest.raises(MGBFError) as e:
+        MGBF(small_config(lm=6, km3=2, hz=2, hx=3, hy=3, mg_ampl02=canonical(3), mg_ampl03=1.5))
+    assert e.value.code == _abi.MGBF_ERR_REACH

@@ -274,3 +274,16 @@ def test_parity_each_radial_variant(lib, cuda, dtype, variant, rows, h):
     ltw = run_gpu(op, 1, w, dtype, cuda, adjoint=True)
     lhs, rhs = float(np.vdot(y, w)), float(np.vdot(x, ltw))
     assert abs(lhs - rhs) <= (1e-6 if dtype == torch.float32 else 2e-2) * np.linalg.norm(y) * np.linalg.norm(w)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("nk_levels", [(7, 2), (5, 2), (9, 1)])
+def test_level_counts_not_multiple_of_four(lib, cuda, dtype, nk_levels):
+    """Leading dimensions 14, 10, 9 (2 or 1 mod 4) through every generation:
+    the vectorised kernels take 4 levels per lane and must not be chosen."""
+    lm, km3 = nk_levels
+    c = small_config(lm=lm, km3=km3, gm_max=3, hz=2)
+    op = MGBF(c)
+    x = compact_input(op, 60 + lm)
+    y = run_gpu(op, 1, x, dtype, cuda)
+    assert rel_l2(y, O.filter_compact(oracle_cfg(c, 1), x)) < TOL[dtype]
