@@ -318,6 +318,7 @@ def run_gpu(args):
         extras["fp32_plain"] = plain_forward(torch, dev, torch.float32)
         extras["fast_fp32"] = fast_forward(torch, dev, torch.float32, peak)
         extras["transfers_fp32"] = transfers(torch, dev, torch.float32, peak)
+        extras["rad3_fp32"] = rad3_forward(torch, dev, torch.float32)
 
     result = None
     if rank == 0:
@@ -445,6 +446,43 @@ def fast_forward(torch, dev, dtype, peak_gbs):
             "line_kernel": {"bound": "hbm", "ms_per_call": line_ms, "achieved": gbs, "peak": peak_gbs,
                             "unit": "GB/s", "frac": gbs / peak_gbs if gbs else None,
                             "algorithmic_bytes": "2 passes x 2 x 4 B per point of each generation"}}
+
+
+def rad3_forward(torch, dev, dtype):
+    """filtering_procedure(4) (filtering_rad3) on a 768x768 field with one
+    64-level 3D variable (3D ball, mg_ampl03 = 1: reach 2) and one 2D
+    variable (disk reach 4), 5 generations.  The ball is a direct sum
+    (~120 taps per point); the stage timers give its share."""
+    from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig, _abi
+    cfg = MGBFConfig(nxPE=16, nyPE=16, im_filt=48, jm_filt=48, lm=64, km3=1, km2=1, n_ens=1, gm_max=5,
+                     hx=4, hy=4, hz=4, p=2, mg_ampl02=ampl02(4), mg_ampl01=ampl01(4), mg_ampl03=1.0,
+                     mg_weig1=1.0, mg_weig2=0.5, mg_weig3=0.25, mg_weig4=0.125, mg_weig5=0.0625, layout=1)
+    op = MGBF(cfg)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(10)
+    x = torch.randn(op.field_shape(), generator=gen, device=dev, dtype=dtype)
+    for _ in range(2):
+        op.filtering_procedure(4, x)
+    torch.cuda.synchronize()
+    n = 5
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(n):
+        op.filtering_procedure(4, x)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / n
+    _abi.timers_enable(True)
+    op.filtering_procedure(4, x)
+    torch.cuda.synchronize()
+    st = _abi.timers_read()
+    _abi.timers_enable(False)
+    pts = float(np.prod(op.field_shape()))
+    op.close()
+    return {"workload": "filtering_rad3 (proc 4), 768x768, one 64-level 3D variable (ball reach 2) + one 2D "
+                        "variable (disk reach 4), 5 generations",
+            "dtype": str(dtype).replace("torch.", ""), "ms": ms, "value": pts / (ms * 1e-3), "unit": UNIT,
+            "stages_ms": {k: v[1] for k, v in st.items()}}
 
 
 def transfers(torch, dev, dtype, peak_gbs):
