@@ -576,6 +576,7 @@ struct Exec {
 struct XferState {
     bool built = false;
     int order = 3, nm0 = 0, mm0 = 0, nka = 0, en = 0;
+    int strip_rows = 0;  // max filter rows used by 8 consecutive analysis rows
     bool vert = false;
     XferAxis ax, ay;
     DevBuf rx, ry, offx, srcx, offy, srcy;
@@ -1268,6 +1269,11 @@ static int xfer_prepare(mgbf_handle* h) {
     X.vert = vert;
     build_xfer_axis(c.nm0 / c.nxPE, c.im_filt, c.nxPE, order, X.ax);
     build_xfer_axis(c.mm0 / c.nyPE, c.jm_filt, c.nyPE, order, X.ay);
+    X.strip_rows = 0;
+    for (int M0 = 0; M0 < c.mm0; M0 += 8) {
+        const int M1 = std::min(M0 + 8, c.mm0);
+        X.strip_rows = std::max(X.strip_rows, X.ay.ref[M1 - 1] + order + 1 - X.ay.ref[M0]);
+    }
     X.built = true;
     return MGBF_OK;
 }
@@ -1325,6 +1331,7 @@ static int xfer_f2a(mgbf_handle* h, void* vall, void* worka, DType t, void* stre
     da.nk = nk; da.I = P.I; da.J = P.J; da.nm0 = X.nm0; da.mm0 = X.mm0; da.order = X.order;
     da.rx = static_cast<const int*>(X.rx.p); da.ry = static_cast<const int*>(X.ry.p);
     da.cx = X.cx[ai].p; da.cy = X.cy[ai].p;
+    da.max_strip_rows = X.strip_rows;
     LK(launch_xfer_direct(t, da, stream));
     return 0;
 }

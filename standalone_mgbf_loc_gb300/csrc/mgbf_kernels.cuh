@@ -58,6 +58,7 @@ struct XferDirectArgs {
     const int* ry;
     const void* cx;    // 4 weights per analysis column (accumulation type)
     const void* cy;
+    int max_strip_rows;  // filter rows needed by 8 consecutive analysis rows (0: unknown)
 };
 struct XferGatherArgs {
     View in, out;

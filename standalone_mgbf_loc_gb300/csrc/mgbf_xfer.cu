@@ -15,6 +15,8 @@
 // (mg_interpolate.f90:963-1044) per point and block of levels.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "mgbf_common.cuh"
 #include "mgbf_kernels.cuh"
 
@@ -81,6 +83,67 @@ __global__ void __launch_bounds__(128) k_xfer_direct(XferDirectArgs a) {
         for (int e = 0; e < V; ++e) acc[e] = s ? fma(c, vx[e], acc[e]) : c * vx[e];
     }
     Lv<T, V>::st(static_cast<T*>(a.out.p) + k + a.out.si * p.a + a.out.sj * p.b, acc);
+}
+
+// Strip form of the direct interpolation: a thread owns V levels of one
+// analysis column N and TM consecutive analysis rows.  The filter rows those
+// rows need (first taps ry(M) are nondecreasing in M) are x-interpolated
+// once each into registers, then every output row combines its order+1 of
+// them.  Loads per output drop from (order+1)^2 to about
+// (order+1) * (filter rows per analysis row + (order+1)/TM).
+template <typename T, int V, int ORDER, int TM, int NRMAX>
+__global__ void __launch_bounds__(128) k_xfer_direct_strip(XferDirectArgs a) {
+    using A = typename AccOf<T>::type;
+    constexpr int nt = ORDER + 1;
+    const int nstrip = (a.mm0 + TM - 1) / TM;
+    const Pos3 p = pos3(a.nk / V, a.nm0, nstrip);
+    if (!p.ok) return;
+    const int k = V * p.q;
+    const int M0 = p.b * TM, M1 = min(M0 + TM, a.mm0);
+    const int j_lo = a.ry[M0];
+    const int rx = a.rx[p.a];
+    const A* cx = static_cast<const A*>(a.cx) + 4 * p.a;
+    const T* in = static_cast<const T*>(a.in.p) + k;
+    int coff[nt];
+#pragma unroll
+    for (int t = 0; t < nt; ++t) coff[t] = reflect_half(rx + t, a.I);
+    A c[nt];
+#pragma unroll
+    for (int t = 0; t < nt; ++t) c[t] = cx[t];
+    A vx[NRMAX][V];
+    const int nr = a.ry[M1 - 1] + nt - j_lo;  // filter rows of the strip (<= NRMAX, checked by the launcher)
+#pragma unroll
+    for (int r = 0; r < NRMAX; ++r) {
+        if (r < nr) {
+            const T* row = in + a.in.sj * reflect_half(j_lo + r, a.J);
+            A v[V];
+#pragma unroll
+            for (int t = 0; t < nt; ++t) {
+                Lv<T, V>::ld(row + a.in.si * coff[t], v);
+#pragma unroll
+                for (int e = 0; e < V; ++e) vx[r][e] = t ? fma(c[t], v[e], vx[r][e]) : c[t] * v[e];
+            }
+        }
+    }
+    T* outp = static_cast<T*>(a.out.p) + k + a.out.si * p.a;
+    for (int M = M0; M < M1; ++M) {
+        const int r0 = a.ry[M] - j_lo;
+        const A* cy = static_cast<const A*>(a.cy) + 4 * M;
+        A acc[V];
+#pragma unroll
+        for (int e = 0; e < V; ++e) acc[e] = A(0);
+        // registers are indexed statically: select the rows r0 .. r0+ORDER
+#pragma unroll
+        for (int r = 0; r < NRMAX; ++r) {
+            const int s = r - r0;
+            if (s >= 0 && s < nt) {
+                const A w = cy[s];
+#pragma unroll
+                for (int e = 0; e < V; ++e) acc[e] = fma(w, vx[r][e], acc[e]);
+            }
+        }
+        Lv<T, V>::st(outp + a.out.sj * M, acc);
+    }
 }
 
 // out(k, a, b) = sum over the list of target `lt` of w * in(k, src, b) (dir 0:
@@ -234,6 +297,22 @@ void dispatch(DType t, F&& f) {
 int launch_xfer_direct(DType t, const XferDirectArgs& a, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const bool vec = vec_ok(t, a.nk, a.in, a.out);
+    // strip form when every strip's filter rows fit the register window
+    constexpr int TM = 8, NRMAX = 16;
+    if (vec && a.max_strip_rows > 0 && a.max_strip_rows <= NRMAX && t != DType::F64) {
+        const unsigned g = blocks((long long)a.nk / 4 * a.nm0 * ((a.mm0 + TM - 1) / TM), 128);
+        dispatch(t, [&](auto tag) {
+            using T = decltype(tag);
+            if constexpr (!std::is_same<T, double>::value) {
+                switch (a.order) {
+                    case 3: k_xfer_direct_strip<T, 4, 3, TM, NRMAX><<<g, 128, 0, s>>>(a); break;
+                    case 2: k_xfer_direct_strip<T, 4, 2, TM, NRMAX><<<g, 128, 0, s>>>(a); break;
+                    default: k_xfer_direct_strip<T, 4, 1, TM, NRMAX><<<g, 128, 0, s>>>(a); break;
+                }
+            }
+        });
+        return last_err();
+    }
     dispatch(t, [&](auto tag) {
         using T = decltype(tag);
         const unsigned gv = blocks((long long)a.nk / 4 * a.nm0 * a.mm0, 128), gs = blocks((long long)a.nk * a.nm0 * a.mm0, 128);
