@@ -532,12 +532,33 @@ def main():
     ap.add_argument("--members", type=int, default=80)
     ap.add_argument("--no-extras", action="store_true", help="skip the plain-forward and CPU-baseline legs")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default radial-kernel tiles")
+    ap.add_argument("--leg", choices=sorted(LEGS), help="run one secondary leg alone (fp32) and print its JSON line")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    if args.leg:
+        return run_leg(args.leg)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
+
+
+# secondary legs, each runnable alone (used for kernel profiles)
+LEGS = {
+    "fast": lambda torch, dev, peak: fast_forward(torch, dev, torch.float32, peak),
+    "transfers": lambda torch, dev, peak: transfers(torch, dev, torch.float32, peak),
+    "rad3": lambda torch, dev, peak: rad3_forward(torch, dev, torch.float32),
+    "plain": lambda torch, dev, peak: plain_forward(torch, dev, torch.float32),
+}
+
+
+def run_leg(name):
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    peak, _ = measured_peaks()
+    print(json.dumps({"leg": name, **LEGS[name](torch, dev, peak)}), flush=True)
+    return 0
 
 
 if __name__ == "__main__":

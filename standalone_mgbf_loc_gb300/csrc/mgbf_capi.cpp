@@ -243,6 +243,7 @@ struct Group {
     BStencil bs;
     std::string bs_err;
     DevBuf btaps, bw[2];  // ball taps (int4) and weights per accumulation type
+    DevBuf brows, brw[2];  // the ball's rows along x (int2) and their weights
     int HXP = 0;  // x padding of internal generation buffers
     DevBuf mrow;  // int table, shared by all types
     AccTables tab[2];  // [0] float, [1] double
@@ -380,6 +381,9 @@ struct Exec {
             b.ntaps = (int)G.bs.w.size();
             b.taps = static_cast<const int4*>(G.btaps.p);
             b.w = G.bw[ai()].p;
+            b.R = G.bs.R; b.nrows = (int)G.bs.rows.size() / 2;
+            b.rows = static_cast<const int2*>(G.brows.p);
+            b.rw = G.brw[ai()].p;
             b.scale = scale;
             LK(launch_ball(t, b, stream));
         }
@@ -1082,6 +1086,8 @@ static int rad3_tables(Group& G, DType t) {
     const int ai = t == DType::F64 ? 1 : 0;
     if (!G.btaps.p && (rc = upload(G.btaps, G.bs.taps))) return rc;
     if (!G.bw[ai].p && (rc = upload_acc(G.bw[ai], G.bs.w, t))) return rc;
+    if (!G.brows.p && (rc = upload(G.brows, G.bs.rows))) return rc;
+    if (!G.brw[ai].p && (rc = upload_acc(G.brw[ai], G.bs.rw, t))) return rc;
     return 0;
 }
 

@@ -85,6 +85,9 @@ struct BallArgs {
     int ntaps;
     const int4* taps;   // (gx, gy, gz, 0) per tap
     const void* w;      // weight per tap (accumulation type)
+    int R, nrows;       // reach; rows of taps along x
+    const int2* rows;   // (gy, gz) per row
+    const void* rw;     // 2R+1 weights per row (accumulation type)
     double scale;
     float scalef;       // set by launch_ball
 };

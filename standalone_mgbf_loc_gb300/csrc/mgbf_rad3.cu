@@ -89,6 +89,111 @@ __global__ void __launch_bounds__(128) k_ball(BallArgs a) {
     stv(static_cast<T*>(a.out.p) + a.out.si * i + a.out.sj * j + k, acc * ball_scale<A>(a));
 }
 
+// The same sums in rows along x.  A thread owns LC consecutive x positions
+// of one level (consecutive threads: consecutive levels, so every load of a
+// warp is one contiguous run).  For each row (gy, gz) of the ball it loads
+// the LC + 2R column window of that row once and applies the row's 2R+1 gx
+// weights from registers.  The rows keep the taps' order and the weights a
+// row lacks are zero (fma(0, x, acc) == acc), so the result is bit-identical
+// to k_ball's.
+template <typename T, int R, int LC>
+__global__ void __launch_bounds__(128) k_ball_rows(BallArgs a) {
+    using A = typename AccOf<T>::type;
+    constexpr int W = LC + 2 * R, NW = 2 * R + 1;
+    const int n3 = a.ncol * a.lm;
+    const int nch = (a.I + LC - 1) / LC;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)n3 * nch * a.J) return;
+    const int k = (int)(idx % n3);
+    const long long r = idx / n3;
+    const int i0 = (int)(r % nch) * LC, j = (int)(r / nch);
+    const int L = k % a.lm, base = k - L;
+    const T* in = static_cast<const T*>(a.in.p) + base;
+    const A* rw = static_cast<const A*>(a.rw);
+    // column offsets of the window: source x = i0 - R + m; for the adjoint a
+    // source outside the interior contributes nothing
+    // (32-bit: the launcher checks that si * I fits)
+    int xo[W];
+#pragma unroll
+    for (int m = 0; m < W; ++m) xo[m] = (int)a.in.si * reflect_half(i0 - R + m, a.I);
+    auto xv = [&](int m) { return (unsigned)(i0 - R + m) < (unsigned)a.I; };
+    A acc[LC];
+#pragma unroll
+    for (int l = 0; l < LC; ++l) acc[l] = A(0);
+    const int top = 2 * (a.lm - 1);
+    // adjoint: every source of the window lies in the x interior (uniform
+    // over a warp whenever a chunk holds at least 32 levels)
+    const bool xin = i0 - R >= 0 && i0 + LC + R <= a.I;
+    for (int t = 0; t < a.nrows; ++t) {
+        const int2 row = a.rows[t];  // (gy, gz)
+        A wl[NW];
+#pragma unroll
+        for (int d = 0; d < NW; ++d) wl[d] = rw[t * NW + d];
+        A win[W];
+        if (!a.adjoint) {
+            const T* src = in + a.in.sj * reflect_half(j + row.x, a.J) + mirror_whole(L + row.y, a.lm);
+#pragma unroll
+            for (int m = 0; m < W; ++m) win[m] = ldv(src + xo[m]);
+            // target i0 + l reads x = i0 + l + gx: window index l + gx + R
+#pragma unroll
+            for (int l = 0; l < LC; ++l)
+#pragma unroll
+                for (int d = 0; d < NW; ++d) acc[l] = fma(wl[d], win[l + d], acc[l]);
+        } else {
+            const int js = j - row.x;
+            if (js < 0 || js >= a.J) continue;  // the whole row's sources lie outside the interior
+            const T* src = in + a.in.sj * js;
+            // source levels whose target Ls + gz lands on L directly or folds onto it
+            const int l1 = L - row.y, l2 = -L - row.y, l3 = top - L - row.y;
+            const bool v1 = l1 >= 0 && l1 < a.lm;
+            const bool v2 = L >= 1 && l2 >= 0 && l2 < a.lm;
+            const bool v3 = L <= a.lm - 2 && l3 >= 0 && l3 < a.lm;
+            // direct pre-image, predicated per lane (0 + x == x, so the sum
+            // below keeps k_ball's order: direct, then fold from below, then above)
+            if (xin) {
+#pragma unroll
+                for (int m = 0; m < W; ++m) win[m] = v1 ? ldv(src + xo[m] + l1) : A(0);
+            } else {
+#pragma unroll
+                for (int m = 0; m < W; ++m) win[m] = (v1 && xv(m)) ? ldv(src + xo[m] + l1) : A(0);
+            }
+            // folded pre-images: only lanes within R of a column end, on rows
+            // whose gz points out of the column
+            if (v2 || v3) {
+#pragma unroll
+                for (int m = 0; m < W; ++m) {
+                    if (xv(m)) {
+                        const T* c = src + xo[m];
+                        if (v2) win[m] += ldv(c + l2);
+                        if (v3) win[m] += ldv(c + l3);
+                    }
+                }
+            }
+            // target i0 + l takes x = i0 + l - gx: window index l - gx + R
+#pragma unroll
+            for (int l = 0; l < LC; ++l)
+#pragma unroll
+                for (int d = 0; d < NW; ++d) acc[l] = fma(wl[d], win[l + 2 * R - d], acc[l]);
+        }
+    }
+    const A sc = ball_scale<A>(a);
+#pragma unroll
+    for (int l = 0; l < LC; ++l) {
+        const int i = i0 + l;
+        if (i >= a.I) break;
+        A v = acc[l];
+        if (a.adjoint && a.has_prev) {
+            const T* h = static_cast<const T*>(a.prev.p) + k;
+            const int px = i < a.hx ? -1 - i : (i >= a.I - a.hx ? 2 * a.I - 1 - i : INT_MIN);
+            const int py = j < a.hy ? -1 - j : (j >= a.J - a.hy ? 2 * a.J - 1 - j : INT_MIN);
+            if (px != INT_MIN) v += ldv(h + a.prev.si * px + a.prev.sj * j);
+            if (py != INT_MIN) v += ldv(h + a.prev.si * i + a.prev.sj * py);
+            if (px != INT_MIN && py != INT_MIN) v += ldv(h + a.prev.si * px + a.prev.sj * py);
+        }
+        stv(static_cast<T*>(a.out.p) + a.out.si * i + a.out.sj * j + k, v * sc);
+    }
+}
+
 // VALL's halo after procedure 4: the 3D variables keep boco_2d's mirror fill
 // of the field the ball forward pass read, the 2D variables hold zero.
 template <typename T>
@@ -122,9 +227,19 @@ int launch_ball(DType t, const BallArgs& args, void* stream) {
     BallArgs a = args;
     a.scalef = (float)a.scale;  // no FP64 conversion in the threads
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    constexpr int LC = 16;  // x positions per thread (16 measured faster than 8 in every type)
+    const long long nr = (long long)args.ncol * args.lm * ((args.I + LC - 1) / LC) * args.J;
+    const unsigned gr = (unsigned)((nr + 127) / 128);
     dispatch(t, [&](auto tag) {
         using T = decltype(tag);
-        k_ball<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+        if (a.rows == nullptr || a.nrows <= 0 || a.in.si * a.I >= INT_MAX) a.R = 0;
+        switch (a.R) {
+            case 1: k_ball_rows<T, 1, LC><<<gr, 128, 0, s>>>(a); break;
+            case 2: k_ball_rows<T, 2, LC><<<gr, 128, 0, s>>>(a); break;
+            case 3: k_ball_rows<T, 3, LC><<<gr, 128, 0, s>>>(a); break;
+            case 4: k_ball_rows<T, 4, LC><<<gr, 128, 0, s>>>(a); break;
+            default: k_ball<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a); break;
+        }
     });
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? 0 : (int)e;

@@ -316,6 +316,16 @@ int build_bstencil(int p, double ampl03, int hx, int hy, int hz, BStencil& out, 
     out.s = 1.0 / sum;
     out.R = gzm;
     for (double v : raw) out.w.push_back(out.s * v);
+    const int nw = 2 * out.R + 1;
+    for (size_t e = 0; e < out.w.size(); ++e) {
+        const int gx = out.taps[4 * e], gy = out.taps[4 * e + 1], gz = out.taps[4 * e + 2];
+        const size_t nr = out.rows.size() / 2;
+        if (nr == 0 || out.rows[2 * nr - 2] != gy || out.rows[2 * nr - 1] != gz) {
+            out.rows.insert(out.rows.end(), {gy, gz});
+            out.rw.resize(out.rw.size() + nw, 0.0);
+        }
+        out.rw[out.rw.size() - nw + gx + out.R] = out.w[e];
+    }
     return MGBF_OK;
 }
 

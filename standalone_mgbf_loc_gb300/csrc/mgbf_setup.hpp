@@ -51,6 +51,10 @@ struct BStencil {
     double e = 0, s = 0;
     std::vector<int> taps;      // (gx, gy, gz, 0) per tap
     std::vector<double> w;      // normalised weight per tap
+    // the same taps grouped in rows along x: (gy, gz) per row, in tap order,
+    // and 2R+1 weights per row for gx = -R..R (zero where the ball has no tap)
+    std::vector<int> rows;
+    std::vector<double> rw;
 };
 
 struct ZStencil {

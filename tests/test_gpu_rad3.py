@@ -56,8 +56,9 @@ def test_rad3_parity_halo_layout(lib, cuda, dtype, gm):
 
 
 def test_rad3_ball_reaches(lib, cuda):
-    """Ball reach 1 (mg_ampl03 = 0.3) and 3 (mg_ampl03 = 1.5, hz = 3)."""
-    for a3, hz, h in ((0.3, 2, 3), (1.5, 3, 3)):
+    """Ball reach 1 (mg_ampl03 = 0.3), 3 (1.5), 4 (2.0, the widest row
+    kernel) and 5 (3.0, beyond the row kernels: the per-tap kernel)."""
+    for a3, hz, h in ((0.3, 2, 3), (1.5, 3, 3), (2.0, 4, 4), (3.0, 5, 5)):
         c = rad3_config(mg_ampl03=a3, hz=hz, hx=h, hy=h, layout=_abi.MGBF_LAYOUT_COMPACT)
         op = MGBF(c)
         x = np.random.default_rng(42).standard_normal(op.field_shape())
