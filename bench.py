@@ -485,13 +485,16 @@ def rad3_forward(torch, dev, dtype):
             "stages_ms": {k: v[1] for k, v in st.items()}}
 
 
-def transfers(torch, dev, dtype, peak_gbs):
+def transfers(torch, dev, dtype, peak_gbs, half=False):
     """anal_to_filt_all2 / filt_to_anal_all2 on the shipped namelist's grids:
     analysis 1440x960, filter 20x20 ranks of 64x32 (1280x640), 4 3D
     variables of 65 levels (lm_a = lm), lsqr interpolation.  HBM-bound:
-    each direction reads one field and writes the other once."""
+    each direction reads one field and writes the other once.  `half`:
+    both grids halved in x and y (720x480 <-> 10x10 ranks), for profiles."""
     from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig
-    cfg = MGBFConfig(nxPE=20, nyPE=20, im_filt=64, jm_filt=32, nm0=1440, mm0=960, lm=65, lm_a=65, km3=4, km2=0,
+    d = 2 if half else 1
+    cfg = MGBFConfig(nxPE=20 // d, nyPE=20 // d, im_filt=64, jm_filt=32, nm0=1440 // d, mm0=960 // d, lm=65, lm_a=65,
+                     km3=4, km2=0,
                      n_ens=1, gm_max=4, hx=6, hy=6, hz=4, p=2, mg_ampl02=ampl02(6), mg_ampl01=ampl01(4),
                      layout=0)  # VALL with its halo, as the reference holds it
     op = MGBF(cfg)
@@ -500,8 +503,8 @@ def transfers(torch, dev, dtype, peak_gbs):
     v = torch.randn(op.field_shape(), generator=gen, device=dev, dtype=dtype)
     w = torch.randn(op.analysis_shape(), generator=gen, device=dev, dtype=dtype)
     es = v.element_size()
-    out = {"workload": "transfers, analysis 1440x960 <-> filter 1280x640 (20x20 ranks of 64x32), 260 levels, lsqr, "
-                       "VALL with halo 6",
+    out = {"workload": f"transfers, analysis {1440 // d}x{960 // d} <-> filter {1280 // d}x{640 // d} "
+                       f"({20 // d}x{20 // d} ranks of 64x32), 260 levels, lsqr, VALL with halo 6",
            "dtype": str(dtype).replace("torch.", "")}
     for name, fn in (("anal_to_filt", lambda: op.anal_to_filt(w, v)), ("filt_to_anal", lambda: op.filt_to_anal(v, w))):
         for _ in range(3):
@@ -547,6 +550,7 @@ def main():
 LEGS = {
     "fast": lambda torch, dev, peak: fast_forward(torch, dev, torch.float32, peak),
     "transfers": lambda torch, dev, peak: transfers(torch, dev, torch.float32, peak),
+    "transfers_half": lambda torch, dev, peak: transfers(torch, dev, torch.float32, peak, half=True),
     "rad3": lambda torch, dev, peak: rad3_forward(torch, dev, torch.float32),
     "plain": lambda torch, dev, peak: plain_forward(torch, dev, torch.float32),
 }

@@ -851,24 +851,25 @@ __global__ void __launch_bounds__(128) k_line_g(LineArgs a) {
 // equals vrbeta2t + fold_h (jp_pbfil.f90:1011-1050); the tests check this
 // against the oracle's literal scatter form.  Each lane owns one k and TX
 // consecutive columns; the input carries an x halo >= R + TX - 1.
-template <typename T, int TX>
-__global__ void __launch_bounds__(128) k_hdirect(HDirectArgs a) {
-    using A = typename AccOf<T>::type;
-    extern __shared__ unsigned char smem_raw[];
+
+// Weights and row half-widths of the support table into shared memory.
+template <typename A>
+__device__ __forceinline__ void hdirect_stage(const HDirectArgs& a, A* w, int* mrow) {
     const int W = 2 * a.R + 1;
-    A* w = reinterpret_cast<A*>(smem_raw);
-    int* mrow = reinterpret_cast<int*>(w + W * W);
     const int nthreads = blockDim.x * blockDim.y;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     for (int t = tid; t < W * W; t += nthreads) w[t] = static_cast<const A*>(a.w)[t];
     for (int t = tid; t < W; t += nthreads) mrow[t] = a.mrow[t];
     __syncthreads();
-    int k = blockIdx.x * 32 + threadIdx.x;
-    const bool kv = k < a.nk;
-    if (!kv) k = a.nk - 1;
-    const int i0 = (blockIdx.y * blockDim.y + threadIdx.y) * TX;
-    if (i0 >= a.I) return;
-    const int j = blockIdx.z;
+}
+
+// One thread's sum: level k, columns i0 .. i0+TX-1 of row j (kv false: a
+// padding lane that computes on a valid level but stores nothing).
+template <typename T, int TX>
+__device__ __forceinline__ void hdirect_strip(const HDirectArgs& a, const typename AccOf<T>::type* w,
+                                              const int* mrow, int k, bool kv, int i0, int j) {
+    using A = typename AccOf<T>::type;
+    const int W = 2 * a.R + 1;
     A acc[TX];
 #pragma unroll
     for (int q = 0; q < TX; ++q) acc[q] = A(0);
@@ -901,6 +902,38 @@ __global__ void __launch_bounds__(128) k_hdirect(HDirectArgs a) {
         if (i < a.mirror_hx) stv(out + a.out.si * (-1 - i), v);
         if (i >= a.I - a.mirror_hx) stv(out + a.out.si * (2 * a.I - 1 - i), v);
     }
+}
+
+template <typename T, int TX>
+__global__ void __launch_bounds__(128) k_hdirect(HDirectArgs a) {
+    using A = typename AccOf<T>::type;
+    extern __shared__ unsigned char smem_raw[];
+    A* w = reinterpret_cast<A*>(smem_raw);
+    int* mrow = reinterpret_cast<int*>(w + (2 * a.R + 1) * (2 * a.R + 1));
+    hdirect_stage(a, w, mrow);
+    int k = blockIdx.x * 32 + threadIdx.x;
+    const bool kv = k < a.nk;
+    if (!kv) k = a.nk - 1;
+    const int i0 = (blockIdx.y * blockDim.y + threadIdx.y) * TX;
+    if (i0 >= a.I) return;
+    hdirect_strip<T, TX>(a, w, mrow, k, kv, i0, blockIdx.z);
+}
+
+// Few levels (the 2D variables of filtering_rad3: often one): lanes of a
+// warp cover (level, strip) pairs instead of 32 levels, so none idles.
+template <typename T, int TX>
+__global__ void __launch_bounds__(128) k_hdirect_flat(HDirectArgs a) {
+    using A = typename AccOf<T>::type;
+    extern __shared__ unsigned char smem_raw[];
+    A* w = reinterpret_cast<A*>(smem_raw);
+    int* mrow = reinterpret_cast<int*>(w + (2 * a.R + 1) * (2 * a.R + 1));
+    hdirect_stage(a, w, mrow);
+    const int nstrip = (a.I + TX - 1) / TX;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)a.nk * nstrip * a.J) return;
+    const int k = (int)(idx % a.nk);
+    const long long r = idx / a.nk;
+    hdirect_strip<T, TX>(a, w, mrow, k, true, (int)(r % nstrip) * TX, (int)(r / nstrip));
 }
 
 // ---------------------------------------------------------------- helpers
@@ -1180,8 +1213,18 @@ int launch_hdirect(DType t, const HDirectArgs& a, void* stream) {
     const int W = 2 * a.R + 1;
     const size_t sm = acc_size(t) * W * W + sizeof(int) * W;
     const int nstrip = (a.I + TX - 1) / TX;
-    dim3 block(32, NW), grid((a.nk + 31) / 32, (nstrip + NW - 1) / NW, a.J);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (a.nk < 16) {
+        const long long n = (long long)a.nk * nstrip * a.J;
+        if (n == 0) return 0;
+        if (sm > 48 * 1024) {
+            MGBF_DISPATCH(t, (cudaFuncSetAttribute(k_hdirect_flat<T, TX>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)));
+        }
+        MGBF_DISPATCH(t, (k_hdirect_flat<T, TX><<<(unsigned)((n + 127) / 128), 128, sm, s>>>(a)));
+        return last_err();
+    }
+    dim3 block(32, NW), grid((a.nk + 31) / 32, (nstrip + NW - 1) / NW, a.J);
     if (sm > 48 * 1024) {
         MGBF_DISPATCH(t, (cudaFuncSetAttribute(k_hdirect<T, TX>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)));

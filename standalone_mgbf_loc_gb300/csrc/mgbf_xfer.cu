@@ -85,16 +85,19 @@ __global__ void __launch_bounds__(128) k_xfer_direct(XferDirectArgs a) {
     Lv<T, V>::st(static_cast<T*>(a.out.p) + k + a.out.si * p.a + a.out.sj * p.b, acc);
 }
 
-// Strip form of the direct interpolation: a thread owns V levels of one
+// Strip form of the direct interpolation: a thread owns V = 4 levels of one
 // analysis column N and TM consecutive analysis rows.  The filter rows those
 // rows need (first taps ry(M) are nondecreasing in M) are x-interpolated
-// once each into registers, then every output row combines its order+1 of
-// them.  Loads per output drop from (order+1)^2 to about
-// (order+1) * (filter rows per analysis row + (order+1)/TM).
+// once each into the thread's own slice of shared memory, then every output
+// row reads its order+1 of them by index.  Loads per output drop from
+// (order+1)^2 to about (order+1) * (filter rows per analysis row +
+// (order+1)/TM).  No thread reads another's slice: no barrier is needed.
 template <typename T, int V, int ORDER, int TM, int NRMAX>
 __global__ void __launch_bounds__(128) k_xfer_direct_strip(XferDirectArgs a) {
     using A = typename AccOf<T>::type;
+    static_assert(V == 4 && std::is_same<A, float>::value, "strip form: 4 float accumulators per thread");
     constexpr int nt = ORDER + 1;
+    extern __shared__ float4 sx[];  // x-interpolated filter rows, [row][thread]: max_strip_rows x 128
     const int nstrip = (a.mm0 + TM - 1) / TM;
     const Pos3 p = pos3(a.nk / V, a.nm0, nstrip);
     if (!p.ok) return;
@@ -110,37 +113,35 @@ __global__ void __launch_bounds__(128) k_xfer_direct_strip(XferDirectArgs a) {
     A c[nt];
 #pragma unroll
     for (int t = 0; t < nt; ++t) c[t] = cx[t];
-    A vx[NRMAX][V];
     const int nr = a.ry[M1 - 1] + nt - j_lo;  // filter rows of the strip (<= NRMAX, checked by the launcher)
+    float4* mine = sx + threadIdx.x;
+#pragma unroll 2
+    for (int r = 0; r < nr; ++r) {
+        const T* row = in + a.in.sj * reflect_half(j_lo + r, a.J);
+        A v[V], vx[V];
 #pragma unroll
-    for (int r = 0; r < NRMAX; ++r) {
-        if (r < nr) {
-            const T* row = in + a.in.sj * reflect_half(j_lo + r, a.J);
-            A v[V];
+        for (int t = 0; t < nt; ++t) {
+            Lv<T, V>::ld(row + a.in.si * coff[t], v);
 #pragma unroll
-            for (int t = 0; t < nt; ++t) {
-                Lv<T, V>::ld(row + a.in.si * coff[t], v);
-#pragma unroll
-                for (int e = 0; e < V; ++e) vx[r][e] = t ? fma(c[t], v[e], vx[r][e]) : c[t] * v[e];
-            }
+            for (int e = 0; e < V; ++e) vx[e] = t ? fma(c[t], v[e], vx[e]) : c[t] * v[e];
         }
+        mine[r * 128] = make_float4(vx[0], vx[1], vx[2], vx[3]);
     }
     T* outp = static_cast<T*>(a.out.p) + k + a.out.si * p.a;
     for (int M = M0; M < M1; ++M) {
-        const int r0 = a.ry[M] - j_lo;
+        const float4* rows = mine + (a.ry[M] - j_lo) * 128;
         const A* cy = static_cast<const A*>(a.cy) + 4 * M;
         A acc[V];
 #pragma unroll
         for (int e = 0; e < V; ++e) acc[e] = A(0);
-        // registers are indexed statically: select the rows r0 .. r0+ORDER
 #pragma unroll
-        for (int r = 0; r < NRMAX; ++r) {
-            const int s = r - r0;
-            if (s >= 0 && s < nt) {
-                const A w = cy[s];
-#pragma unroll
-                for (int e = 0; e < V; ++e) acc[e] = fma(w, vx[r][e], acc[e]);
-            }
+        for (int s = 0; s < nt; ++s) {
+            const float4 f = rows[s * 128];
+            const A w = cy[s];
+            acc[0] = fma(w, f.x, acc[0]);
+            acc[1] = fma(w, f.y, acc[1]);
+            acc[2] = fma(w, f.z, acc[2]);
+            acc[3] = fma(w, f.w, acc[3]);
         }
         Lv<T, V>::st(outp + a.out.sj * M, acc);
     }
@@ -301,13 +302,14 @@ int launch_xfer_direct(DType t, const XferDirectArgs& a, void* stream) {
     constexpr int TM = 8, NRMAX = 16;
     if (vec && a.max_strip_rows > 0 && a.max_strip_rows <= NRMAX && t != DType::F64) {
         const unsigned g = blocks((long long)a.nk / 4 * a.nm0 * ((a.mm0 + TM - 1) / TM), 128);
+        const size_t sm = sizeof(float4) * 128 * (size_t)a.max_strip_rows;  // <= 32 KB
         dispatch(t, [&](auto tag) {
             using T = decltype(tag);
             if constexpr (!std::is_same<T, double>::value) {
                 switch (a.order) {
-                    case 3: k_xfer_direct_strip<T, 4, 3, TM, NRMAX><<<g, 128, 0, s>>>(a); break;
-                    case 2: k_xfer_direct_strip<T, 4, 2, TM, NRMAX><<<g, 128, 0, s>>>(a); break;
-                    default: k_xfer_direct_strip<T, 4, 1, TM, NRMAX><<<g, 128, 0, s>>>(a); break;
+                    case 3: k_xfer_direct_strip<T, 4, 3, TM, NRMAX><<<g, 128, sm, s>>>(a); break;
+                    case 2: k_xfer_direct_strip<T, 4, 2, TM, NRMAX><<<g, 128, sm, s>>>(a); break;
+                    default: k_xfer_direct_strip<T, 4, 1, TM, NRMAX><<<g, 128, sm, s>>>(a); break;
                 }
             }
         });
