@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -577,10 +578,17 @@ struct Exec {
 }  // namespace
 
 // Analysis <-> filter transfer state of a handle (built at first use).
+constexpr int kFusedTile = 64;  // extended filter columns per block of the fused anal_to_filt
+
 struct XferState {
     bool built = false;
     int order = 3, nm0 = 0, mm0 = 0, nka = 0, en = 0;
     int strip_rows = 0;  // max filter rows used by 8 consecutive analysis rows
+    // fused anal_to_filt: tiles of kFusedTile extended filter columns, the
+    // analysis columns each tile's x lists touch, and the widest tile
+    std::vector<int> tile_c0, tile_nc;
+    int ncmax = 0;
+    DevBuf dtile_c0, dtile_nc;
     bool vert = false;
     XferAxis ax, ay;
     DevBuf rx, ry, offx, srcx, offy, srcy;
@@ -1280,6 +1288,18 @@ static int xfer_prepare(mgbf_handle* h) {
         const int M1 = std::min(M0 + 8, c.mm0);
         X.strip_rows = std::max(X.strip_rows, X.ay.ref[M1 - 1] + order + 1 - X.ay.ref[M0]);
     }
+    X.tile_c0.clear(); X.tile_nc.clear(); X.ncmax = 0;
+    const int IE = (int)X.ax.off.size() - 1;
+    for (int a0 = 0; a0 < IE; a0 += kFusedTile) {
+        int lo = INT_MAX, hi = -1;
+        for (int o = X.ax.off[a0]; o < X.ax.off[std::min(a0 + kFusedTile, IE)]; ++o) {
+            lo = std::min(lo, X.ax.src[o]);
+            hi = std::max(hi, X.ax.src[o]);
+        }
+        X.tile_c0.push_back(hi < 0 ? 0 : lo);
+        X.tile_nc.push_back(hi < 0 ? 0 : hi - lo + 1);
+        X.ncmax = std::max(X.ncmax, X.tile_nc.back());
+    }
     X.built = true;
     return MGBF_OK;
 }
@@ -1290,7 +1310,8 @@ static int xfer_tables(mgbf_handle* h, DType t) {
     int rc;
     if (!X.rx.p) {
         if ((rc = upload(X.rx, X.ax.ref)) || (rc = upload(X.ry, X.ay.ref)) || (rc = upload(X.offx, X.ax.off)) ||
-            (rc = upload(X.srcx, X.ax.src)) || (rc = upload(X.offy, X.ay.off)) || (rc = upload(X.srcy, X.ay.src)))
+            (rc = upload(X.srcx, X.ax.src)) || (rc = upload(X.offy, X.ay.off)) || (rc = upload(X.srcy, X.ay.src)) ||
+            (rc = upload(X.dtile_c0, X.tile_c0)) || (rc = upload(X.dtile_nc, X.tile_nc)))
             return rc;
     }
     if (!X.cx[ai].p) {
@@ -1357,15 +1378,7 @@ static int xfer_a2f(mgbf_handle* h, const void* worka, void* vall, DType t, void
     wa.p = const_cast<void*>(worka); wa.si = X.nka; wa.sj = (long long)X.nka * X.nm0;
     DevBuf& VX = X.vx[(int)t];
     DevBuf& VE = X.vext[(int)t];
-    if ((rc = VX.ensure((size_t)X.nka * X.nm0 * JE * es))) return rc;
     if ((h->cfg.layout != MGBF_LAYOUT_HALO || X.vert) && (rc = VE.ensure((size_t)X.nka * IE * JE * es))) return rc;
-    View vx;
-    vx.p = VX.p; vx.si = X.nka; vx.sj = (long long)X.nka * X.nm0;
-    XferGatherArgs g;
-    g.in = wa; g.out = vx; g.nk = X.nka; g.na = X.nm0; g.nb = JE; g.dir = 1;
-    g.off = static_cast<const int*>(X.offy.p); g.src = static_cast<const int*>(X.srcy.p); g.w = X.wy[ai].p;
-    g.out_a0 = 0; g.out_b0 = 0;
-    LK(launch_xfer_gather(t, g, stream));
     View v = field_view(h, vall, t);
     const bool halo = h->cfg.layout == MGBF_LAYOUT_HALO;
     // VALL = 0 beyond the interpolation halo; everything inside is written
@@ -1381,10 +1394,32 @@ static int xfer_a2f(mgbf_handle* h, const void* worka, void* vall, DType t, void
         ve.p = VE.p; ve.si = X.nka; ve.sj = (long long)X.nka * IE;
         ve = shifted(ve, ib, ib, t);  // origin at the first interior point
     }
-    g.in = vx; g.out = ve; g.na = IE; g.nb = JE; g.dir = 0;
-    g.off = static_cast<const int*>(X.offx.p); g.src = static_cast<const int*>(X.srcx.p); g.w = X.wx[ai].p;
-    g.out_a0 = ib; g.out_b0 = ib;
-    LK(launch_xfer_gather(t, g, stream));
+    // both gathers in one kernel where the shape allows, else y into the
+    // intermediate VX and x from there
+    XferFusedArgs fa;
+    fa.in = wa; fa.out = ve; fa.nk = X.nka; fa.IE = IE; fa.JE = JE; fa.ib = ib; fa.ta = kFusedTile;
+    const int nl = X.nka / 4, ngrp = (nl + 15) / 16;
+    fa.lanes = ngrp > 0 ? (nl + ngrp - 1) / ngrp : 0;
+    fa.ncmax = X.ncmax;
+    fa.offx = static_cast<const int*>(X.offx.p); fa.srcx = static_cast<const int*>(X.srcx.p); fa.wx = X.wx[ai].p;
+    fa.offy = static_cast<const int*>(X.offy.p); fa.srcy = static_cast<const int*>(X.srcy.p); fa.wy = X.wy[ai].p;
+    fa.tile_c0 = static_cast<const int*>(X.dtile_c0.p); fa.tile_nc = static_cast<const int*>(X.dtile_nc.p);
+    const int frc = launch_xfer_a2f_fused(t, fa, stream);
+    if (frc > 0) LK(frc);
+    if (frc < 0) {
+        if ((rc = VX.ensure((size_t)X.nka * X.nm0 * JE * es))) return rc;
+        View vx;
+        vx.p = VX.p; vx.si = X.nka; vx.sj = (long long)X.nka * X.nm0;
+        XferGatherArgs g;
+        g.in = wa; g.out = vx; g.nk = X.nka; g.na = X.nm0; g.nb = JE; g.dir = 1;
+        g.off = static_cast<const int*>(X.offy.p); g.src = static_cast<const int*>(X.srcy.p); g.w = X.wy[ai].p;
+        g.out_a0 = 0; g.out_b0 = 0;
+        LK(launch_xfer_gather(t, g, stream));
+        g.in = vx; g.out = ve; g.na = IE; g.nb = JE; g.dir = 0;
+        g.off = static_cast<const int*>(X.offx.p); g.src = static_cast<const int*>(X.srcx.p); g.w = X.wx[ai].p;
+        g.out_a0 = ib; g.out_b0 = ib;
+        LK(launch_xfer_gather(t, g, stream));
+    }
     LK(launch_xfer_fold(t, ve, X.nka, P.I, P.J, ib, stream));
     if (direct_out) return 0;
     const int r0 = halo ? -ib : 0, na = halo ? IE : P.I, nb = halo ? JE : P.J;

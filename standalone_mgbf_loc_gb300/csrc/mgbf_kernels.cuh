@@ -69,6 +69,23 @@ struct XferGatherArgs {
     const void* w;     // weight per entry (accumulation type)
     int out_a0, out_b0;  // output view coordinate = target index - out_*0
 };
+// anal_to_filt's two gathers in one kernel: per block one filter row b, a
+// tile of target columns and a group of levels; the y gather of the tile's
+// analysis columns goes to shared memory, the x gather reads it from there.
+struct XferFusedArgs {
+    View in;             // analysis field (k, c, r)
+    View out;            // extended filter array, origin at the first interior point
+    int nk;              // levels (multiple of 4)
+    int IE, JE;          // targets: IE x JE extended filter points
+    int ib;              // output coordinate = target index - ib
+    int ta;              // target columns per tile
+    int lanes;           // 4-level lanes per level group
+    int ncmax;           // analysis columns of the widest tile (shared memory rows)
+    const int *offx, *srcx, *offy, *srcy;
+    const void *wx, *wy;  // FP32 weights
+    const int* tile_c0;  // first analysis column per tile
+    const int* tile_nc;  // analysis columns per tile
+};
 struct XferVertArgs {
     View in, out;
     int nkf, nka, lm, en;  // en blocks of lm filter / 2lm-1 analysis levels
@@ -184,6 +201,9 @@ int launch_ball(DType t, const BallArgs& a, void* stream);
 int launch_rad3_halo(DType t, View out, View src, int nk, int n3, int I, int J, int hx, int hy, void* stream);
 int launch_xfer_direct(DType t, const XferDirectArgs& a, void* stream);
 int launch_xfer_gather(DType t, const XferGatherArgs& a, void* stream);
+// FP32 / BF16 with 16-byte aligned 4-level vectors; returns -1 (nothing
+// launched) when the shape does not fit, so the caller runs the two gathers.
+int launch_xfer_a2f_fused(DType t, const XferFusedArgs& a, void* stream);
 int launch_xfer_fold(DType t, View v, int nk, int I, int J, int b, void* stream);
 int launch_xfer_fill(DType t, View v, int nk, int I, int J, int b, void* stream);
 int launch_xfer_vert(DType t, const XferVertArgs& a, void* stream);

@@ -174,6 +174,54 @@ __global__ void __launch_bounds__(128) k_xfer_gather(XferGatherArgs a) {
     Lv<T, V>::st(static_cast<T*>(a.out.p) + k + a.out.si * (p.a - a.out_a0) + a.out.sj * (p.b - a.out_b0), acc);
 }
 
+// Both adjoint gathers of anal_to_filt in one pass.  Block: filter row b
+// (blockIdx.y), target columns [tile*ta, tile*ta + ta) (blockIdx.x), level
+// lanes [grp*lanes, ...) (blockIdx.z).  Phase 1 y-gathers the analysis
+// columns the tile's x lists touch into shared memory (what the separate y
+// gather writes to the intermediate, kept in FP32); phase 2 x-gathers each
+// target from there.  Both sums run in list order, as the separate gathers'.
+template <typename T>
+__global__ void __launch_bounds__(256) k_xfer_a2f_fused(XferFusedArgs a) {
+    extern __shared__ float4 vs[];  // [column - c0][lane]
+    const int tile = blockIdx.x, b = blockIdx.y;
+    const int l0 = blockIdx.z * a.lanes;
+    const int nlg = min(a.lanes, a.nk / 4 - l0);
+    if (nlg <= 0) return;  // uniform over the block
+    const int c0 = a.tile_c0[tile], nc = a.tile_nc[tile];
+    const int oy0 = a.offy[b], oy1 = a.offy[b + 1];
+    const float* wy = static_cast<const float*>(a.wy);
+    const T* W = static_cast<const T*>(a.in.p) + 4 * l0;
+    for (int p = threadIdx.x; p < nc * nlg; p += blockDim.x) {
+        const int e = p % nlg, c = p / nlg;
+        const T* col = W + 4 * e + a.in.si * (c0 + c);
+        float acc[4] = {0.f, 0.f, 0.f, 0.f}, v[4];
+        for (int o = oy0; o < oy1; ++o) {
+            V4<T>::ld(col + a.in.sj * a.srcy[o], v);
+            const float w = wy[o];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[q] = fma(w, v[q], acc[q]);
+        }
+        vs[c * nlg + e] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    }
+    __syncthreads();
+    const int a0 = tile * a.ta, a1 = min(a0 + a.ta, a.IE);
+    const float* wx = static_cast<const float*>(a.wx);
+    T* out = static_cast<T*>(a.out.p) + 4 * l0 + a.out.sj * (b - a.ib);
+    for (int p = threadIdx.x; p < (a1 - a0) * nlg; p += blockDim.x) {
+        const int e = p % nlg, t = a0 + p / nlg;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int o = a.offx[t]; o < a.offx[t + 1]; ++o) {
+            const float4 f = vs[(a.srcx[o] - c0) * nlg + e];
+            const float w = wx[o];
+            acc[0] = fma(w, f.x, acc[0]);
+            acc[1] = fma(w, f.y, acc[1]);
+            acc[2] = fma(w, f.z, acc[2]);
+            acc[3] = fma(w, f.w, acc[3]);
+        }
+        V4<T>::st(out + 4 * e + a.out.si * (t - a.ib), acc);
+    }
+}
+
 // bocoT_2d on the halo band b of an extended array whose view origin is the
 // first interior point: x first on every row of the band's range, then y
 // on the interior columns.  One thread per (level, row or column, t).
@@ -337,6 +385,21 @@ int launch_xfer_gather(DType t, const XferGatherArgs& a, void* stream) {
         using T = decltype(tag);
         if (vec) k_xfer_gather<T, 4><<<blocks((long long)a.nk / 4 * a.na * a.nb, 128), 128, 0, s>>>(a);
         else k_xfer_gather<T, 1><<<blocks((long long)a.nk * a.na * a.nb, 128), 128, 0, s>>>(a);
+    });
+    return last_err();
+}
+
+int launch_xfer_a2f_fused(DType t, const XferFusedArgs& a, void* stream) {
+    if (t == DType::F64 || a.lanes <= 0 || a.ta <= 0 || !vec_ok(t, a.nk, a.in, a.out)) return -1;
+    const size_t sm = sizeof(float4) * (size_t)a.ncmax * a.lanes;
+    if (sm > 48 * 1024 || a.JE > 65535) return -1;
+    const int nl = a.nk / 4;
+    dim3 grid((unsigned)((a.IE + a.ta - 1) / a.ta), (unsigned)a.JE, (unsigned)((nl + a.lanes - 1) / a.lanes));
+    if (grid.z > 65535) return -1;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    dispatch(t, [&](auto tag) {
+        using T = decltype(tag);
+        if constexpr (!std::is_same<T, double>::value) k_xfer_a2f_fused<T><<<grid, 256, sm, s>>>(a);
     });
     return last_err();
 }
