@@ -2,7 +2,8 @@
  * FP64 CPU oracle for the MGBF filtering pipeline -- TEST INFRASTRUCTURE ONLY.
  *
  * Restates, on one global filter grid, the reference's CPU algorithm for
- * filtering_procedure(1), (6) and the fast 1D+1D variants (3) and (8).
+ * filtering_procedure(1), (6), the fast 1D+1D variants (3) and (8),
+ * filtering_rad3 (4) and the line-filter procedure filtering_lin2_bckg (2).
  * Every routine below
  * names the reference routine (file:line, paths inside the reference project)
  * whose loops it follows.  The MPI halo exchange of the reference collapses
@@ -75,9 +76,15 @@ typedef struct {
     int reachL;
     double e3, ss3;       /* filtering_rad3's ball: el*rmom2_3, 1/sum    */
     int reach3;
+    /* filtering_lin2_bckg's three line filters (colors): generator, integer
+     * half-span, formal half-span and dibeta weights fil[0..h] */
+    int ddx[3], ddy[3], dh[3];
+    double dhs[3];
+    double dfil[3][ORC_DIB_NFIL + 1];
 } setup_t;
 
 static const double EPS = 1.e-12;
+static int dibeta_setup(const orc_cfg* c, setup_t* s);
 
 /* mg_parameter.f90:567-572 (rmom2), mg_intstate.f90:360-431 (pasp, cholaspect,
  * getlinesum), jp_pbfil.f90:74-107 (cholaspect1/2), 149-218 (getlinesum1/2). */
@@ -175,6 +182,122 @@ static int setup(const orc_cfg* c, setup_t* s) {
         if (c->proc == 4 && bad) return ORC_ERR_REACH;
         s->ss3 = 1.0 / sum;
         s->reach3 = gzm;
+    }
+    if (c->proc == 2) return dibeta_setup(c, s);
+    return ORC_OK;
+}
+
+/* ------------------------------------------ proc 2 line-filter setup */
+
+/* Moment tables of inimomtab (jp_pbfil3.f90:378-457) for the beta filters of
+ * integer half-span h = 1..nh: bnorm(h) = 1 / sum_i (1-(i/h)^2)^p and
+ * bsprds(h) = sum_i i^2 (1-(i/h)^2)^p / sum_i (1-(i/h)^2)^p over i = -h..h.
+ * The reference evaluates the continuum moments plus their Euler-Maclaurin
+ * corrections, which for these polynomial weights are the exact sums. */
+static void dib_moments(int p, double* bnorm, double* bsprd) {
+    for (int h = 1; h <= ORC_DIB_NH; ++h) {
+        double s0 = 0.0, s2 = 0.0;
+        for (int i = -h; i <= h; ++i) {
+            double z = (double)i / h, w = ipow(1.0 - z * z, p);
+            s0 += w;
+            s2 += (double)i * i * w;
+        }
+        bnorm[h] = 1.0 / s0;
+        bsprd[h] = s2 / s0;
+    }
+}
+
+/* triad (jp_pbfil3.f90:573-624): resolve the aspect 3-vector (A11, A22, A12)
+ * onto three integer line generators lt[q] with weights w[q] >= 0 (up to
+ * -1e-14) such that A = sum_q w[q] lt[q] lt[q]^T.  Starts from the generators
+ * (1,0), (0,1), (-1,-1); while the smallest weight is negative, flips and
+ * recombines the generators and updates the projection rows. */
+int orc_triad(const double asp[3], int lt_out[6], double w_out[3]) {
+    int lt[3][2] = {{1, 0}, {0, 1}, {-1, -1}};
+    int lu[3][3] = {{1, 0, -1}, {0, 1, -1}, {0, 0, 1}};  /* lu[col][row] */
+    double w[3];
+    for (int q = 0; q < 3; ++q) w[q] = asp[0] * lu[q][0] + asp[1] * lu[q][1] + asp[2] * lu[q][2];
+    int it;
+    for (it = 1; it <= 200; ++it) {
+        int k = 0;
+        for (int q = 1; q < 3; ++q)
+            if (w[q] < w[k]) k = q;  /* first minimum */
+        const double dw = 2.0 * w[k];
+        if (dw >= -1.e-14) break;
+        const int l = (k + 1) % 3, m = (l + 1) % 3;
+        int dl[3];
+        for (int r = 0; r < 3; ++r) dl[r] = 2 * lu[k][r];
+        lt[l][0] = -lt[l][0]; lt[l][1] = -lt[l][1];
+        lt[k][0] = -lt[l][0] - lt[m][0]; lt[k][1] = -lt[l][1] - lt[m][1];
+        for (int q = 0; q < 3; ++q) {
+            const int sg = q == k ? -1 : 1;
+            for (int r = 0; r < 3; ++r) lu[q][r] += dl[r] * sg;
+            w[q] += sg * dw;
+        }
+    }
+    for (int q = 0; q < 3; ++q) {
+        lt_out[2 * q] = lt[q][0]; lt_out[2 * q + 1] = lt[q][1];
+        w_out[q] = w[q];
+    }
+    return it > 200 ? ORC_ERR_ARG : ORC_OK;
+}
+
+/* init_mg_line (mg_intstate.f90:436-480) for proc 2.  It runs after
+ * def_mg_weights has replaced pasp2 = diag(mg_ampl02) by the Cholesky factor
+ * of its inverse (mg_intstate.f90:385-388, 423), so the triad sees
+ * (c, c, 0), c = 1/sqrt(mg_ampl02).  Each color's spread^2 then goes
+ * through hstform (jp_pbfil3.f90:1399-1430: the formal half-span between
+ * consecutive table entries) and blinfil (1463-1501: the weights of the
+ * two-beta "dibeta" filter).  A spread beyond the table, a half-span the
+ * table cannot hold, or a reach beyond the halo is an error here; the
+ * reference prints and carries on (or reads outside its arrays). */
+static int dibeta_setup(const orc_cfg* c, setup_t* s) {
+    double bnorm[ORC_DIB_NH + 1], bsprd[ORC_DIB_NH + 1];
+    dib_moments(c->p, bnorm, bsprd);
+    const double el = sqrt(1.0 / c->ampl02);
+    const double asp[3] = {el, el, 0.0};
+    int lt[6];
+    double w[3];
+    if (orc_triad(asp, lt, w)) return ORC_ERR_ARG;
+    for (int q = 0; q < 3; ++q) {
+        double hs = w[q];
+        int found = 0;
+        if (hs >= 0.0)
+            for (int h = 2; h <= ORC_DIB_NH && !found; ++h)
+                if (bsprd[h] >= hs) {
+                    hs = h - (bsprd[h] - hs) / (bsprd[h] - bsprd[h - 1]);
+                    found = 1;
+                }
+        if (!found) return ORC_ERR_REACH;
+        const int h = (int)hs, hp = h + 1;
+        if (h < 1 || hp > ORC_DIB_NH || hp > ORC_DIB_NFIL) return ORC_ERR_REACH;
+        const double whp = (hs - h) * bnorm[hp], wh = (hp - hs) * bnorm[h];
+        double* f = s->dfil[q];
+        for (int i = 0; i <= ORC_DIB_NFIL; ++i) f[i] = 0.0;
+        for (int i = 0; i <= h; ++i) {
+            double z = (double)i / hp;
+            f[i] = whp * ipow(1.0 - z * z, c->p);
+        }
+        for (int i = 0; i < h; ++i) {
+            double z = (double)i / h;
+            f[i] += wh * ipow(1.0 - z * z, c->p);
+        }
+        s->ddx[q] = lt[2 * q]; s->ddy[q] = lt[2 * q + 1];
+        s->dh[q] = h; s->dhs[q] = hs;
+        if (h * abs(s->ddx[q]) > c->hx || h * abs(s->ddy[q]) > c->hy) return ORC_ERR_REACH;
+    }
+    return ORC_OK;
+}
+
+int orc_dibeta_values(const orc_cfg* c, int gen[6], int h[3], double hs[3], double fil[3 * (ORC_DIB_NFIL + 1)]) {
+    setup_t s;
+    int rc = setup(c, &s);
+    if (rc) return rc;
+    if (c->proc != 2 && (rc = dibeta_setup(c, &s))) return rc;
+    for (int q = 0; q < 3; ++q) {
+        gen[2 * q] = s.ddx[q]; gen[2 * q + 1] = s.ddy[q];
+        h[q] = s.dh[q]; hs[q] = s.dhs[q];
+        for (int i = 0; i <= ORC_DIB_NFIL; ++i) fil[q * (ORC_DIB_NFIL + 1) + i] = s.dfil[q][i];
     }
     return ORC_OK;
 }
@@ -399,6 +522,64 @@ static void fast_forward(const orc_cfg* c, const setup_t* S, arr3 U, int I, int 
     line_beta(S, c->p, U, I, J, c->hx, c->hy, 1, 0, k0, k1);
     fill_line(U, I, J, c->hx, 0, k0, k1);
     line_beta(S, c->p, U, I, J, c->hx, c->hy, 0, 0, k0, k1);
+}
+
+/* ------------------------------- proc 2: dibeta line filters by color */
+
+/* vdibeta2 / vdibeta2t (jp_pbfil3.f90:1801-1837, 2345-2382) for color q on
+ * a generation array, as filtering_lin2_bckg calls them
+ * (mg_filtering.f90:683-822): interior points only, b = 0 first, then
+ * a = b.  Forward: b(x) = fil0 a(x) + sum_t fil_t (a(x + t d) + a(x - t d)),
+ * reading the filled halo; the halo of the result is zero.  Adjoint: the
+ * scatter of the same weights from every interior point into the extended
+ * array. */
+static void dibeta_pass(const setup_t* S, int q, arr3 a, arr3 b, int I, int J, int adj, int k0, int k1) {
+    a3_zero(b, k0, k1);
+    const int dx = S->ddx[q], dy = S->ddy[q], h = S->dh[q];
+    const double* f = S->dfil[q];
+    for (int iy = 1; iy <= J; ++iy)
+        for (int ix = 1; ix <= I; ++ix) {
+            if (!adj) {
+                double* dst = &A3(b, 0, ix, iy);
+                const double* c0 = &A3(a, 0, ix, iy);
+                for (int k = k0; k < k1; ++k) dst[k] = f[0] * c0[k];
+                for (int t = 1; t <= h; ++t) {
+                    const double* up = &A3(a, 0, ix + dx * t, iy + dy * t);
+                    const double* dn = &A3(a, 0, ix - dx * t, iy - dy * t);
+                    for (int k = k0; k < k1; ++k) dst[k] += f[t] * (up[k] + dn[k]);
+                }
+            } else {
+                const double* at = &A3(a, 0, ix, iy);
+                double* c0 = &A3(b, 0, ix, iy);
+                for (int k = k0; k < k1; ++k) c0[k] += f[0] * at[k];
+                for (int t = 1; t <= h; ++t) {
+                    double* up = &A3(b, 0, ix + dx * t, iy + dy * t);
+                    double* dn = &A3(b, 0, ix - dx * t, iy - dy * t);
+                    for (int k = k0; k < k1; ++k) {
+                        const double v = f[t] * at[k];
+                        up[k] += v;
+                        dn[k] += v;
+                    }
+                }
+            }
+        }
+    a3_copy(a, b, k0, k1);
+}
+
+/* One generation of filtering_lin2_bckg's horizontal part: for colors 3, 2,
+ * 1 the adjoint line filter and bocoT_2d; weighting; for colors 1, 2, 3
+ * boco_2d and the forward line filter (mg_filtering.f90:725-797). */
+static void lin2_adjoint(const orc_cfg* c, const setup_t* S, arr3 U, arr3 T, int I, int J, int k0, int k1) {
+    for (int q = 2; q >= 0; --q) {
+        dibeta_pass(S, q, U, T, I, J, 1, k0, k1);
+        fold_h(U, I, J, c->hx, c->hy, k0, k1);
+    }
+}
+static void lin2_forward(const orc_cfg* c, const setup_t* S, arr3 U, arr3 T, int I, int J, int k0, int k1) {
+    for (int q = 0; q < 3; ++q) {
+        fill_h(U, I, J, c->hx, c->hy, k0, k1);
+        dibeta_pass(S, q, U, T, I, J, 0, k0, k1);
+    }
 }
 
 /* ----------------------------------------------- filtering_rad3: 3D ball */
@@ -734,7 +915,8 @@ typedef struct {
 static int check_cfg(const orc_cfg* c) {
     if (!c || c->I <= 0 || c->J <= 0 || c->nk <= 0 || c->gm < 1 || c->gm > ORC_MAX_GEN) return ORC_ERR_ARG;
     if (c->hx < 0 || c->hy < 0 || c->hz < 0 || c->p < 0) return ORC_ERR_ARG;
-    if (c->proc != 1 && c->proc != 6 && c->proc != 3 && c->proc != 8 && c->proc != 4) return ORC_ERR_ARG;
+    if (c->proc != 1 && c->proc != 6 && c->proc != 3 && c->proc != 8 && c->proc != 4 && c->proc != 2)
+        return ORC_ERR_ARG;
     if (c->proc == 4) {
         if (c->nzcol < 0 || c->lm < 1 || (size_t)c->nzcol * c->lm > (size_t)c->nk) return ORC_ERR_ARG;
         if (c->nzcol > 0 && c->hz >= c->lm) return ORC_ERR_ARG;
@@ -848,7 +1030,7 @@ static void weight_gen(const orc_cfg* c, arr3 V, int I, int J, double a, double 
 
 static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G, int k0, int k1) {
     const int gm = c->gm, hx = c->hx, hy = c->hy;
-    const int filt1 = (c->proc == 1) || (c->proc == 3) || (c->proc == 4) || c->l_filt_g1;
+    const int filt1 = (c->proc == 1) || (c->proc == 2) || (c->proc == 3) || (c->proc == 4) || c->l_filt_g1;
     const int fast = c->proc == 3 || c->proc == 8;
     double* tb = (double*)malloc(sizeof(double) * (size_t)c->nk);
     /* up: V -> H_2 -> ... -> H_gm */
@@ -869,6 +1051,12 @@ static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_
             fast_adjoint(c, S, U, I, J, k0, k1);
             weight_gen(c, U, I, J, c->a[g], c->b[g], k0, k1);
             fast_forward(c, S, U, I, J, k0, k1);
+            continue;
+        }
+        if (c->proc == 2) {
+            lin2_adjoint(c, S, U, G[g].tmp, I, J, k0, k1);
+            weight_gen(c, U, I, J, c->a[g], c->b[g], k0, k1);
+            lin2_forward(c, S, U, G[g].tmp, I, J, k0, k1);
             continue;
         }
         vrbeta2t(S, c->p, U, G[g].tmp, 1, I, 1, J, k0, k1);
@@ -950,7 +1138,7 @@ int orc_filter_compact(const orc_cfg* c, const double* x, double* y) {
 /* u_g = B_g R_g Bz^T x for every generation, written into G[g] (gen 0 into V). */
 static void half_chain(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G) {
     if (c->l_vertical_filter && c->nzcol > 0) vfilter(c, S, V, 1);
-    const int filt1 = (c->proc == 1) || (c->proc == 3) || c->l_filt_g1;
+    const int filt1 = (c->proc == 1) || (c->proc == 2) || (c->proc == 3) || c->l_filt_g1;
     const int fast = c->proc == 3 || c->proc == 8;
     for (int g = 0; g + 1 < c->gm; ++g)
         restrict_gen(c, g ? G[g].H : V, &G[g], G[g + 1].H, 0, c->nk);
@@ -959,6 +1147,10 @@ static void half_chain(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G) {
         arr3 U = g ? G[g].H : V;
         if (fast) {
             fast_adjoint(c, S, U, G[g].I, G[g].J, 0, c->nk);
+            continue;
+        }
+        if (c->proc == 2) {
+            lin2_adjoint(c, S, U, G[g].tmp, G[g].I, G[g].J, 0, c->nk);
             continue;
         }
         vrbeta2t(S, c->p, U, G[g].tmp, 1, G[g].I, 1, G[g].J, 0, c->nk);
@@ -982,7 +1174,7 @@ int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double
     arr3 ay = {Vy, c->nk, 1 - c->hx, c->I + c->hx, 1 - c->hy, c->J + c->hy};
     half_chain(c, &S, ax, Gx);
     half_chain(c, &S, ay, Gy);
-    const int filt1 = (c->proc == 1) || (c->proc == 3) || c->l_filt_g1;
+    const int filt1 = (c->proc == 1) || (c->proc == 2) || (c->proc == 3) || c->l_filt_g1;
     for (int g = 0; g < c->gm; ++g) {
         double s = 0.0;
         if (g == 0 && !filt1) { ga[g] = 0.0; continue; }
@@ -1039,6 +1231,18 @@ int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y) 
         else fast_adjoint(c, &S, a, I, J, 0, nk);
         from_halo(&cc, V, y);
         free(V);
+        return ORC_OK;
+    }
+    if (which == 8 || which == 9) {
+        if (c->proc != 2) return ORC_ERR_ARG;
+        orc_cfg cc = *c; cc.I = I; cc.J = J;
+        double* V = to_halo(&cc, x);
+        arr3 a = {V, nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy};
+        arr3 t = a3_alloc(nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy);
+        if (which == 8) lin2_forward(c, &S, a, t, I, J, 0, nk);
+        else lin2_adjoint(c, &S, a, t, I, J, 0, nk);
+        from_halo(&cc, V, y);
+        a3_free(&t); free(V);
         return ORC_OK;
     }
     if (which == 4 || which == 5) {

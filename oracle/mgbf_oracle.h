@@ -29,6 +29,10 @@ extern "C" {
 #endif
 
 #define ORC_MAX_GEN 16
+/* proc 2 line filters: moment-table size nh and filter buffer nfil
+ * (mg_parameter.f90:562-563) */
+#define ORC_DIB_NH 6
+#define ORC_DIB_NFIL (ORC_DIB_NH + 2)
 
 typedef struct orc_cfg {
     int I, J;            /* generation-1 filter grid (im00 x jm00)            */
@@ -41,7 +45,7 @@ typedef struct orc_cfg {
     double a[ORC_MAX_GEN];  /* per-generation weights a_g (a[0] = gen 1)      */
     double b[ORC_MAX_GEN];  /* Helmholtz Laplacian coefficients (reference: 0) */
     int lhelm;           /* use weighting_helm form                           */
-    int proc;            /* 1 rad2_bckg, 6 rad2_ens, 3 fast_bckg, 8 fast_ens, 4 rad3 */
+    int proc;            /* 1 rad2_bckg, 6 rad2_ens, 3 fast_bckg, 8 fast_ens, 4 rad3, 2 lin2_bckg */
     int l_vertical_filter;
     int l_filt_g1;       /* procs 6 and 8 only                                */
     int lquart;          /* quadratic (3-point) interpolation                 */
@@ -77,13 +81,24 @@ int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double
  *        5 = prolongation P (g+1 -> g; x is gen g+1, y is gen g),
  *        6 = fast-filter horizontal forward (bocoy, rbeta y, bocox, rbeta x),
  *        7 = fast-filter horizontal adjoint (rbetaT x, bocoTx, rbetaT y,
- *            bocoTy), on a generation-g grid. */
+ *            bocoTy), on a generation-g grid,
+ *        8 = proc 2 line filters forward (boco_2d + dibeta, colors 1..3),
+ *        9 = their adjoint (dibetat + bocoT_2d, colors 3..1). */
 int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y);
 
 /* Setup values (for tests): rmom2_1, rmom2_2, exx (1D), exx (2D), ss1, ss2,
  * vertical reach, horizontal reach, and for the fast filters' line filter
  * exx, ss, reach.  Returns error if a reach exceeds a halo. */
 int orc_setup_values(const orc_cfg* c, double out[11]);
+
+/* Proc 2 (filtering_lin2_bckg) line filters, for tests: the three colors'
+ * generators (dx, dy), integer half-spans h, formal half-spans hs and
+ * dibeta weights fil[q*(ORC_DIB_NFIL+1) + i], i = 0..h (zero beyond). */
+int orc_dibeta_values(const orc_cfg* c, int gen[6], int h[3], double hs[3], double fil[3 * (ORC_DIB_NFIL + 1)]);
+
+/* The triad decomposition alone: asp = (A11, A22, A12) -> generators
+ * lt = (dx0, dy0, dx1, dy1, dx2, dy2) and weights w. */
+int orc_triad(const double asp[3], int lt[6], double w[3]);
 
 /* ----------------------------------------------------------------------
  * Transfers between the analysis grid and the filter grid (the new map,

@@ -2,7 +2,8 @@
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
 this module.  It restates the reference's CPU algorithm for
-filtering_procedure(1|3|6|8); it is the checker, never the thing measured or
+filtering_procedure(1|2|3|4|6|8) and the analysis<->filter transfers; it is
+the checker, never the thing measured or
 shipped.  Parity with the reference itself is unpinned (see mgbf_oracle.h).
 """
 from __future__ import annotations
@@ -49,6 +50,11 @@ def _load():
         lib.orc_weight_grads.argtypes = [cp, dp, dp, dp]
         lib.orc_stage.argtypes = [cp, ctypes.c_int, ctypes.c_int, dp, dp]
         lib.orc_setup_values.argtypes = [cp, dp]
+        ip = ctypes.POINTER(ctypes.c_int)
+        lib.orc_dibeta_values.argtypes = [cp, ip, ip, dp, dp]
+        lib.orc_triad.argtypes = [dp, ip, dp]
+        lib.orc_dibeta_values.restype = ctypes.c_int
+        lib.orc_triad.restype = ctypes.c_int
         xp = ctypes.POINTER(_CXfer)
         lib.orc_anal_to_filt.argtypes = [xp, dp, dp]
         lib.orc_filt_to_anal.argtypes = [xp, dp, dp]
@@ -149,7 +155,9 @@ def weight_grads(cfg: OracleConfig, x: np.ndarray, gy: np.ndarray) -> np.ndarray
 
 
 (STAGE_Z_FWD, STAGE_Z_ADJ, STAGE_H_FWD, STAGE_H_ADJ, STAGE_RESTRICT, STAGE_PROLONG, STAGE_FAST_FWD,
- STAGE_FAST_ADJ) = range(8)
+ STAGE_FAST_ADJ, STAGE_LIN2_FWD, STAGE_LIN2_ADJ) = range(10)
+DIB_NH = 6
+DIB_NFIL = DIB_NH + 2
 
 
 def stage(cfg: OracleConfig, which: int, gen: int, x: np.ndarray) -> np.ndarray:
@@ -174,6 +182,28 @@ def setup_values(cfg: OracleConfig) -> dict:
     keys = ["rmom2_1", "rmom2_2", "exx1", "exx2", "ss1", "ss2", "reach_z", "reach_h", "exx_line", "ss_line",
             "reach_line"]
     return dict(zip(keys, out.tolist()))
+
+
+def dibeta_values(cfg: OracleConfig) -> list:
+    """Proc 2's three line filters (colors 1..3): dicts with the generator
+    (dx, dy), integer half-span h, formal half-span hs and weights fil[0..h]."""
+    gen = (ctypes.c_int * 6)()
+    h = (ctypes.c_int * 3)()
+    hs = np.zeros(3)
+    fil = np.zeros(3 * (DIB_NFIL + 1))
+    c = cfg.to_c()
+    _check(_load().orc_dibeta_values(ctypes.byref(c), gen, h, _ptr(hs), _ptr(fil)), "orc_dibeta_values")
+    return [{"d": (gen[2 * q], gen[2 * q + 1]), "h": h[q], "hs": float(hs[q]),
+             "fil": fil[q * (DIB_NFIL + 1):q * (DIB_NFIL + 1) + h[q] + 1].copy()} for q in range(3)]
+
+
+def triad(aspect) -> tuple:
+    """The triad decomposition of (A11, A22, A12): (generators 3x2, weights 3)."""
+    a = np.ascontiguousarray(aspect, dtype=np.float64)
+    lt = (ctypes.c_int * 6)()
+    w = np.zeros(3)
+    _check(_load().orc_triad(_ptr(a), lt, _ptr(w)), "orc_triad")
+    return np.array(list(lt)).reshape(3, 2), w
 
 
 # ------------------------------------------------ analysis <-> filter grid
