@@ -485,6 +485,42 @@ def rad3_forward(torch, dev, dtype):
             "stages_ms": {k: v[1] for k, v in st.items()}}
 
 
+def lin2_forward(torch, dev, dtype):
+    """filtering_procedure(2) (filtering_lin2_bckg) on one 768x768x64 field,
+    5 generations, hz=4, mg_ampl02 = 0.3: per generation three dibeta line
+    filters, half-span 3 along x and y and the identity on the diagonal
+    (the triad of the Cholesky factor of the inverse aspect)."""
+    from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig, _abi
+    cfg = MGBFConfig(nxPE=16, nyPE=16, im_filt=48, jm_filt=48, lm=64, km3=1, km2=0, n_ens=1, gm_max=5,
+                     hx=12, hy=12, hz=4, p=2, mg_ampl02=0.3, mg_ampl01=ampl01(4),
+                     mg_weig1=1.0, mg_weig2=0.5, mg_weig3=0.25, mg_weig4=0.125, mg_weig5=0.0625, layout=1)
+    op = MGBF(cfg)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(11)
+    x = torch.randn(op.field_shape(), generator=gen, device=dev, dtype=dtype)
+    for _ in range(2):
+        op.filtering_procedure(2, x)
+    torch.cuda.synchronize()
+    n = 5
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(n):
+        op.filtering_procedure(2, x)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / n
+    _abi.timers_enable(True)
+    op.filtering_procedure(2, x)
+    torch.cuda.synchronize()
+    st = _abi.timers_read()
+    _abi.timers_enable(False)
+    pts = float(np.prod(op.field_shape()))
+    op.close()
+    return {"workload": "filtering_lin2_bckg (proc 2), one 3D field 768x768x64, 5 generations, line half-span 3",
+            "dtype": str(dtype).replace("torch.", ""), "ms": ms, "value": pts / (ms * 1e-3), "unit": UNIT,
+            "stages_ms": {k: v[1] for k, v in st.items()}}
+
+
 def transfers(torch, dev, dtype, peak_gbs, half=False):
     """anal_to_filt_all2 / filt_to_anal_all2 on the shipped namelist's grids:
     analysis 1440x960, filter 20x20 ranks of 64x32 (1280x640), 4 3D
@@ -552,6 +588,7 @@ LEGS = {
     "transfers": lambda torch, dev, peak: transfers(torch, dev, torch.float32, peak),
     "transfers_half": lambda torch, dev, peak: transfers(torch, dev, torch.float32, peak, half=True),
     "rad3": lambda torch, dev, peak: rad3_forward(torch, dev, torch.float32),
+    "lin2": lambda torch, dev, peak: lin2_forward(torch, dev, torch.float32),
     "plain": lambda torch, dev, peak: plain_forward(torch, dev, torch.float32),
 }
 

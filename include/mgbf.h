@@ -133,9 +133,14 @@ int mgbf_get_dims(const mgbf_handle* h, mgbf_dims* dims);
  * aspect mg_ampl03 on the 3D variables, the 2D radial filter on the 2D
  * ones, no separate vertical filter; like the reference, its adjoint side
  * keeps only the interior of the 3D scatter and folds the caller's VALL
- * halo, so the operator is not symmetric).  2,5,7 return
- * MGBF_ERR_UNSUPPORTED; any other value is a no-op returning MGBF_OK, as
- * the reference's select has no default case.
+ * halo, so the operator is not symmetric), and
+ * 2 = filtering_lin2_bckg (mg_filtering.f90:683-822: per generation the
+ * three "dibeta" line filters of the triad decomposition, jp_pbfil3.f90,
+ * of the Cholesky factor of the inverse aspect that init_mg_line sees;
+ * MGBF_ERR_REACH when a line filter's spread is beyond the moment table or
+ * its reach beyond the halo).  5 and 7 return MGBF_ERR_UNSUPPORTED; any
+ * other value is a no-op returning MGBF_OK, as the reference's select has
+ * no default case.
  *   vall:   field pointer (device or host, per mem), laid out per the
  *           handle's layout, element type per dtype.
  *   stream: cudaStream_t (NULL = legacy default stream).  Device calls are
@@ -166,8 +171,9 @@ int mgbf_filt_to_anal(mgbf_handle* h, void* vall, void* worka, int dtype, int me
 
 /* Adjoint of filtering_procedure(mg_filt), run through the explicit
  * transposed chain (no reference counterpart: the reference's adjoint test
- * is an empty stub, RBETA_TEST.f90:64-69).  The operator is self-adjoint,
- * so the result equals the forward up to rounding. */
+ * is an empty stub, RBETA_TEST.f90:64-69).  Procedures 1, 2, 3, 6 and 8 are
+ * self-adjoint, so the result equals the forward up to rounding; 4 is not
+ * and returns MGBF_ERR_UNSUPPORTED. */
 int mgbf_filtering_procedure_adjoint(mgbf_handle* h, int mg_filt, void* vall, int dtype, int mem,
                                      void* stream);
 

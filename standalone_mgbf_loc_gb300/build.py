@@ -30,6 +30,7 @@ SOURCES = [
     "mgbf_noalloc.cu",
     "mgbf_xfer.cu",
     "mgbf_rad3.cu",
+    "mgbf_dibeta.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

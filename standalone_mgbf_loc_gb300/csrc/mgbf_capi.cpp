@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -243,6 +244,9 @@ struct Group {
     double ampl03 = 0;   // filtering_rad3's 3D ball (proc 4)
     BStencil bs;
     std::string bs_err;
+    DStencil ds;         // filtering_lin2_bckg's three line filters (proc 2)
+    std::string ds_err;
+    int ds_rc = 0;
     DevBuf btaps, bw[2];  // ball taps (int4) and weights per accumulation type
     DevBuf brows, brw[2];  // the ball's rows along x (int2) and their weights
     int HXP = 0;  // x padding of internal generation buffers
@@ -356,6 +360,7 @@ struct Exec {
     View C(int g) { return gen_view(P, G, G.bufs[(int)t].C[g]->p, t, g); }
     View D(int g) { return gen_view(P, G, G.bufs[(int)t].D[g]->p, t, g); }
     bool fast = false;  // procs 3 and 8: separable line filters instead of the radial disk
+    bool lin2 = false;  // proc 2: three line filters along the triad's generators
     int n3 = -1;        // proc 4: levels of the 3D variables (ball); the rest take the 2D radial filter
     bool has_prev = false;  // proc 4, generation 1: the caller's halo, folded by the adjoint side
     View prev;
@@ -501,10 +506,33 @@ struct Exec {
         return 0;
     }
 
+    // One color q of proc 2's line filters (adjoint: dibetat + bocoT_2d;
+    // forward: boco_2d + dibeta).
+    int dib(int g, View in, View out, int q, bool adjoint, double scale) {
+        DibArgs a;
+        a.in = in; a.out = out; a.nk = G.nk; a.I = gen_I(P, g); a.J = gen_J(P, g);
+        a.dx = G.ds.dx[q]; a.dy = G.ds.dy[q]; a.h = G.ds.h[q];
+        a.hx = G.hx; a.hy = G.hy; a.adjoint = adjoint ? 1 : 0;
+        for (int i = 0; i < 9; ++i) a.fil[i] = G.ds.fil[q][i];
+        a.scale = scale;
+        LK(launch_dibeta(t, a, stream));
+        return 0;
+    }
+
     int hpass(int g, View in, View out, double scale, int mirror, int stage, int which_in) {
         const int I = gen_I(P, g), J = gen_J(P, g);
         StageTimer tm(stage, stream, pts(g));
         if (n3 >= 0) return rad3_pass(g, in, out, scale, mirror, which_in);
+        if (lin2) {
+            // adjoint side: colors 3, 2, 1; forward side: colors 1, 2, 3;
+            // in -> out -> D -> out, the generation weight on the last pass
+            const bool adj = which_in == 0;
+            const int q0 = adj ? 2 : 0, dq = adj ? -1 : 1;
+            int rc;
+            if ((rc = dib(g, in, out, q0, adj, 1.0))) return rc;
+            if ((rc = dib(g, out, D(g), q0 + dq, adj, 1.0))) return rc;
+            return dib(g, D(g), out, q0 + 2 * dq, adj, scale);
+        }
         if (fast) {
             // adjoint side (rbetaT x, bocoTx, rbetaT y, bocoTy): x first;
             // forward side (bocoy, rbeta y, bocox, rbeta x): y first
@@ -704,6 +732,21 @@ int build_group(Plan& P, Group& G, bool zneeded) {
         }
     } else {
         G.bs_err = "mg_ampl03 must be positive";
+    }
+    // filtering_lin2_bckg's line filters: an error only when proc 2 runs
+    G.ds_err.clear();
+    G.ds_rc = build_dstencil(G.p, G.ampl02, G.hx, G.hy, G.ds, err);
+    if (G.ds_rc) {
+        G.ds_err = err;
+        G.ds.ok = false;
+    } else {
+        for (int q = 0; q < 3 && G.ds.ok; ++q)
+            if (G.ds.h[q] * std::abs(G.ds.dx[q]) > IG || G.ds.h[q] * std::abs(G.ds.dy[q]) > JG) {
+                G.ds_err = "line filter " + std::to_string(q + 1) + " reaches beyond the coarsest generation " +
+                           std::to_string(IG) + "x" + std::to_string(JG);
+                G.ds_rc = MGBF_ERR_DIVISIBILITY;
+                G.ds.ok = false;
+            }
     }
     return 0;
 }
@@ -1061,13 +1104,17 @@ int mgbf_set_weights(mgbf_handle* h, const double* a, int n) {
 }
 
 static bool is_fast(int mg_filt) { return mg_filt == 3 || mg_filt == 8; }
-static bool is_bckg(int mg_filt) { return mg_filt == 1 || mg_filt == 3 || mg_filt == 4; }
+static bool is_bckg(int mg_filt) { return mg_filt == 1 || mg_filt == 2 || mg_filt == 3 || mg_filt == 4; }
+static bool needs_d(int mg_filt) { return is_fast(mg_filt) || mg_filt == 2; }
 
 static int check_proc(mgbf_handle* h, int mg_filt, bool& noop) {
     noop = false;
-    if (mg_filt == 1 || mg_filt == 6 || mg_filt == 3 || mg_filt == 8 || mg_filt == 4) {
+    if (mg_filt == 1 || mg_filt == 2 || mg_filt == 6 || mg_filt == 3 || mg_filt == 8 || mg_filt == 4) {
         if (is_bckg(mg_filt) && h->cfg.n_ens != 1)
-            return fail(MGBF_ERR_CONFIG, "filtering_rad2_bckg / filtering_fast_bckg / filtering_rad3 (procs 1, 3, 4) need n_ens = 1: their arrays are dimensioned km, not km_all");
+            return fail(MGBF_ERR_CONFIG, "filtering_rad2_bckg / filtering_lin2_bckg / filtering_fast_bckg / filtering_rad3 (procs 1, 2, 3, 4) need n_ens = 1: their arrays are dimensioned km, not km_all");
+        if (mg_filt == 2 && !h->plan.groups[0].ds.ok)
+            return fail(h->plan.groups[0].ds_rc ? h->plan.groups[0].ds_rc : MGBF_ERR_CONFIG,
+                        "filtering_lin2_bckg: " + h->plan.groups[0].ds_err);
         if (mg_filt == 4) {
             const Group& G = h->plan.groups[0];
             if (G.bs.R < 0) return fail(MGBF_ERR_DIVISIBILITY, "filtering_rad3: " + G.bs_err);
@@ -1084,7 +1131,7 @@ static int check_proc(mgbf_handle* h, int mg_filt, bool& noop) {
         return MGBF_OK;
     }
     if (mg_filt >= 2 && mg_filt <= 8)
-        return fail(MGBF_ERR_UNSUPPORTED, "filtering procedure " + std::to_string(mg_filt) + " is not implemented (supported: 1, 3, 4, 6, 8)");
+        return fail(MGBF_ERR_UNSUPPORTED, "filtering procedure " + std::to_string(mg_filt) + " is not implemented (supported: 1, 2, 3, 4, 6, 8)");
     noop = true;  // no case default in the reference's select
     return MGBF_OK;
 }
@@ -1104,13 +1151,14 @@ static int run_proc(mgbf_handle* h, int mg_filt, const void* xin, void* yout, DT
     Group& G = P.groups[0];
     int rc;
     if ((rc = ensure_tables(P, G, t))) return rc;
-    if ((rc = ensure_bufs(P, G, t, false, is_fast(mg_filt)))) return rc;
+    if ((rc = ensure_bufs(P, G, t, false, needs_d(mg_filt)))) return rc;
     const bool rad3 = mg_filt == 4;
     const int nzcol = (!rad3 && h->cfg.l_vertical_filter && h->cfg.lm > 1)
                           ? (is_bckg(mg_filt) ? h->nzcol_proc1 : h->nzcol_proc6) : 0;  // rad3: no separate z filter
     const bool filt1 = is_bckg(mg_filt) || h->cfg.l_filt_g1;
     Exec ex{P, G, t, stream};
     ex.fast = is_fast(mg_filt);
+    ex.lin2 = mg_filt == 2;
     View x = field_view(h, const_cast<void*>(xin), t);
     View y = field_view(h, yout, t);
     if (rad3) {
@@ -1170,6 +1218,9 @@ int mgbf_filtering_procedure_adjoint(mgbf_handle* h, int mg_filt, void* vall, in
     // L^T = (Bz M Bz^T)^T = Bz M^T Bz^T with M = sum_g P_g B_g a_g B_g^T R_g;
     // transposing each stage in reverse order reproduces the same launch
     // sequence (Bz^T first, restriction = P^T, B^T = B, a_g, B, P, Bz).
+    // filtering_rad3's adjoint side is not the transpose of its forward side.
+    if (mg_filt == 4)
+        return fail(MGBF_ERR_UNSUPPORTED, "adjoint of filtering_rad3: the operator is not self-adjoint");
     return with_field(h, mg_filt, vall, dtype, mem, stream);
 }
 
@@ -1191,7 +1242,7 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
     Plan& P = h->plan;
     Group& G = P.groups[0];
     if ((rc = ensure_tables(P, G, t))) return rc;
-    if ((rc = ensure_bufs(P, G, t, true, is_fast(mg_filt)))) return rc;
+    if ((rc = ensure_bufs(P, G, t, true, needs_d(mg_filt)))) return rc;
     const void *dx = x, *dgy = gy;
     void* dgx = gx;
     const size_t bytes = h->field_elems * elem_size(t);
@@ -1207,6 +1258,7 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
     const bool filt1 = is_bckg(mg_filt) || h->cfg.l_filt_g1;
     Exec ex{P, G, t, stream};
     ex.fast = is_fast(mg_filt);
+    ex.lin2 = mg_filt == 2;
     View vx = field_view(h, const_cast<void*>(dx), t);
     View vg = field_view(h, const_cast<void*>(dgy), t);
     View vo = field_view(h, dgx, t);

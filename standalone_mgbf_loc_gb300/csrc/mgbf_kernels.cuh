@@ -109,6 +109,24 @@ struct BallArgs {
     float scalef;       // set by launch_ball
 };
 
+// One color of filtering_lin2_bckg's line filters (jp_pbfil3.f90:1801-1837
+// vdibeta2, 2345-2382 vdibeta2t) on a generation: generator (dx, dy),
+// half-span h, symmetric weights fil[0..h].  Forward: boco_2d's mirror fill
+// as an index reflection, then the gather on the interior.  Adjoint: the
+// scatter from the interior followed by bocoT_2d (fold widths hx, hy), as a
+// gather over the target's mirror images.
+struct DibArgs {
+    View in, out;
+    int nk, I, J;
+    int dx, dy, h;
+    int hx, hy;
+    int adjoint;
+    double fil[9];
+    float filf[9];      // set by launch_dibeta
+    double scale;
+    float scalef;       // set by launch_dibeta
+};
+
 struct RestrictArgs {
     View fine, coarse;
     int nk, If, Jf;     // fine interior sizes; coarse = If/2, Jf/2
@@ -198,6 +216,7 @@ int launch_mirror_x(DType t, View v, int nk, int I, int J, int hx, void* stream)
 int launch_copy(DType t, View in, View out, int nk, int I, int J, int mirror_hx, void* stream);
 int launch_line(DType t, const LineArgs& a, void* stream);
 int launch_ball(DType t, const BallArgs& a, void* stream);
+int launch_dibeta(DType t, const DibArgs& a, void* stream);
 int launch_rad3_halo(DType t, View out, View src, int nk, int n3, int I, int J, int hx, int hy, void* stream);
 int launch_xfer_direct(DType t, const XferDirectArgs& a, void* stream);
 int launch_xfer_gather(DType t, const XferGatherArgs& a, void* stream);

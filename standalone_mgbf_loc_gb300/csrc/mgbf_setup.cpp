@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 
 #include "../../include/mgbf.h"
@@ -245,6 +246,97 @@ int build_interp(int nf, bool quart, Interp1D& T, std::string& err) {
 
 // getlinesum1 (jp_pbfil.f90:149-180) and the vrbeta1 weights
 // (jp_pbfil.f90:856-885) for el = paspx = paspy = pasp02.
+int build_dstencil(int p, double ampl02, int hx, int hy, DStencil& out, std::string& err) {
+    out = DStencil{};
+    if (!(ampl02 > 0.0) || p < 1) {
+        err = "line filters need mg_ampl02 > 0 and p >= 1";
+        return MGBF_ERR_CONFIG;
+    }
+    // beta filters of integer half-span m: normalisation and spread^2 (the
+    // corrected moments of inimomtab are these exact sums)
+    double norm[kDibNH + 1], spread[kDibNH + 1];
+    for (int m = 1; m <= kDibNH; ++m) {
+        double s0 = 0.0, s2 = 0.0;
+        for (int i = -m; i <= m; ++i) {
+            const double u = 1.0 - (double(i) / m) * (double(i) / m);
+            const double w = std::pow(u, p);
+            s0 += w;
+            s2 += double(i) * i * w;
+        }
+        norm[m] = 1.0 / s0;
+        spread[m] = s2 / s0;
+    }
+    // triad of (A11, A22, A12): generators g[q], projections lu[q] (rows of
+    // the inverse basis), weights w[q] = A . lu[q]
+    const double c = std::sqrt(1.0 / ampl02);
+    const double A[3] = {c, c, 0.0};
+    int g[3][2] = {{1, 0}, {0, 1}, {-1, -1}};
+    int lu[3][3] = {{1, 0, -1}, {0, 1, -1}, {0, 0, 1}};
+    double w[3];
+    for (int q = 0; q < 3; ++q) w[q] = A[0] * lu[q][0] + A[1] * lu[q][1] + A[2] * lu[q][2];
+    bool done = false;
+    for (int it = 0; it < 200 && !done; ++it) {
+        int k = 0;
+        for (int q = 1; q < 3; ++q)
+            if (w[q] < w[k]) k = q;
+        const double dw = 2.0 * w[k];
+        if (dw >= -1e-14) {
+            done = true;
+            break;
+        }
+        const int l = (k + 1) % 3, m = (l + 1) % 3;
+        int d2[3];
+        for (int r = 0; r < 3; ++r) d2[r] = 2 * lu[k][r];
+        for (int e = 0; e < 2; ++e) {
+            g[l][e] = -g[l][e];
+            g[k][e] = -g[l][e] - g[m][e];
+        }
+        for (int q = 0; q < 3; ++q) {
+            const int sg = q == k ? -1 : 1;
+            for (int r = 0; r < 3; ++r) lu[q][r] += sg * d2[r];
+            w[q] += sg * dw;
+        }
+    }
+    if (!done) {
+        err = "triad: the aspect tensor did not resolve into three line filters";
+        return MGBF_ERR_CONFIG;
+    }
+    for (int q = 0; q < 3; ++q) {
+        // spread^2 -> formal half-span between the table entries around it
+        double hs = -1.0;
+        if (w[q] >= 0.0)
+            for (int m = 2; m <= kDibNH; ++m)
+                if (spread[m] >= w[q]) {
+                    hs = m - (spread[m] - w[q]) / (spread[m] - spread[m - 1]);
+                    break;
+                }
+        const int h = hs < 0.0 ? 0 : int(hs), hp = h + 1;
+        if (hs < 0.0 || h < 1 || hp > kDibNH || hp > kDibNFil) {
+            err = "line filter spread^2 " + std::to_string(w[q]) + " (mg_ampl02) is beyond the moment table (nh = " +
+                  std::to_string(kDibNH) + ")";
+            return MGBF_ERR_REACH;
+        }
+        const double whp = (hs - h) * norm[hp], wh = (hp - hs) * norm[h];
+        for (int i = 0; i <= h; ++i) {
+            const double u = 1.0 - (double(i) / hp) * (double(i) / hp);
+            out.fil[q][i] = whp * std::pow(u, p);
+        }
+        for (int i = 0; i < h; ++i) {
+            const double u = 1.0 - (double(i) / h) * (double(i) / h);
+            out.fil[q][i] += wh * std::pow(u, p);
+        }
+        out.dx[q] = g[q][0]; out.dy[q] = g[q][1]; out.h[q] = h; out.hs[q] = hs;
+        if (h * std::abs(g[q][0]) > hx || h * std::abs(g[q][1]) > hy) {
+            err = "line filter " + std::to_string(q + 1) + " reaches " + std::to_string(h) + " steps of (" +
+                  std::to_string(g[q][0]) + "," + std::to_string(g[q][1]) + "), beyond the halo hx=" +
+                  std::to_string(hx) + ", hy=" + std::to_string(hy);
+            return MGBF_ERR_REACH;
+        }
+    }
+    out.ok = true;
+    return MGBF_OK;
+}
+
 int build_lstencil(int p, double ampl02, int hx, int hy, LStencil& out, std::string& err) {
     if (!(ampl02 > 0.0)) {
         err = "mg_ampl02 must be positive";

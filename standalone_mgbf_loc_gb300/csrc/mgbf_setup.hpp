@@ -42,6 +42,21 @@ struct LStencil {
     std::vector<double> w;      // R+1 normalised weights s*(1-(g exx)^2)^p, g = 0..R
 };
 
+// filtering_lin2_bckg's three line filters ("colors"), as init_mg_line sets
+// them up (mg_intstate.f90:436-480; jp_pbfil3.f90:378-457, 573-624,
+// 1399-1501): the triad decomposition of the Cholesky factor of the inverse
+// aspect, (c, c, 0) with c = 1/sqrt(mg_ampl02), into integer generators
+// (dx, dy) and spreads^2; each spread^2 -> formal half-span hs between two
+// integer beta filters -> the dibeta weights fil[0..h].
+constexpr int kDibNH = 6;             // moment-table size nh (mg_parameter.f90:562)
+constexpr int kDibNFil = kDibNH + 2;  // nfil (mg_parameter.f90:563)
+struct DStencil {
+    bool ok = false;
+    int dx[3] = {0, 0, 0}, dy[3] = {0, 0, 0}, h[3] = {0, 0, 0};
+    double hs[3] = {0, 0, 0};
+    double fil[3][kDibNFil + 1] = {};
+};
+
 // filtering_rad3's 3D ball: vrbeta3 (jp_pbfil.f90:930-977) with el from
 // cholaspect3 of pasp3 = diag(mg_ampl03) (jp_pbfil.f90:109-126), normalised
 // by getlinesum3 (jp_pbfil.f90:220-268); taps in the reference's gz, gy, gx
@@ -94,6 +109,7 @@ int build_zstencil(int p, double ampl01, int hz, int lm, bool need_mirror, ZSten
                    std::string& err);
 int build_interp(int nf, bool quart, Interp1D& out, std::string& err);
 int build_lstencil(int p, double ampl02, int hx, int hy, LStencil& out, std::string& err);
+int build_dstencil(int p, double ampl02, int hx, int hy, DStencil& out, std::string& err);
 int build_bstencil(int p, double ampl03, int hx, int hy, int hz, BStencil& out, std::string& err);
 
 // Reach checks def_mg_weights performs for the other filters of the

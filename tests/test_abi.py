@@ -144,7 +144,7 @@ def test_reach_larger_than_coarsest_generation(lib):
 def test_unsupported_and_unknown_procedures(lib):
     op = MGBF(small_config())
     x = np.zeros(op.field_shape())
-    for proc in (2, 5, 7):
+    for proc in (5, 7):
         with pytest.raises(MGBFError) as e:
             op.filtering_procedure(proc, x)
         assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
@@ -153,6 +153,28 @@ def test_unsupported_and_unknown_procedures(lib):
     op.filtering_procedure(0, x)
     op.filtering_procedure(9, x)
     assert (x == 1.0).all()
+
+
+def test_line_filter_procedure_validation(lib):
+    """filtering_lin2_bckg (proc 2): a spread beyond the moment table or a
+    line reach beyond the halo is refused before any device work."""
+    # spread^2 1/sqrt(0.035) = 5.3 lies beyond the table's largest (half-span
+    # 6: 5.14); the fast filters' line reach 75 that every handle checks
+    # (def_mg_weights) needs the 80-point halo
+    op = MGBF(small_config(mg_ampl02=0.035, hx=80, hy=80, im_filt=32, jm_filt=32, gm_max=1))
+    with pytest.raises(MGBFError) as e:
+        op.filtering_procedure(2, np.zeros(op.field_shape()))
+    assert e.value.code == _abi.MGBF_ERR_REACH
+    with pytest.raises(MGBFError) as e:  # proc 2 is a single-member procedure
+        MGBF(small_config(n_ens=2)).filtering_procedure(2, np.zeros(MGBF(small_config(n_ens=2)).field_shape()))
+    assert e.value.code == _abi.MGBF_ERR_CONFIG
+
+
+def test_adjoint_of_rad3_is_refused(lib):
+    op = MGBF(small_config(lm=6, km3=2, km2=2, hz=2, mg_ampl03=1.0, layout=_abi.MGBF_LAYOUT_COMPACT))
+    with pytest.raises(MGBFError) as e:
+        op.filtering_procedure_adjoint(4, np.zeros(op.field_shape()))
+    assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
 
 
 def test_proc1_requires_single_member(lib):
