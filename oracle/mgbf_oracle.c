@@ -3,7 +3,8 @@
  *
  * Restates, on one global filter grid, the reference's CPU algorithm for
  * filtering_procedure(1), (6), the fast 1D+1D variants (3) and (8),
- * filtering_rad3 (4) and the line-filter procedure filtering_lin2_bckg (2).
+ * filtering_rad3 (4) and the line-filter procedures filtering_lin2_bckg (2)
+ * and filtering_lin2_ens (7).
  * Every routine below
  * names the reference routine (file:line, paths inside the reference project)
  * whose loops it follows.  The MPI halo exchange of the reference collapses
@@ -183,7 +184,7 @@ static int setup(const orc_cfg* c, setup_t* s) {
         s->ss3 = 1.0 / sum;
         s->reach3 = gzm;
     }
-    if (c->proc == 2) return dibeta_setup(c, s);
+    if (c->proc == 2 || c->proc == 7) return dibeta_setup(c, s);
     return ORC_OK;
 }
 
@@ -293,7 +294,7 @@ int orc_dibeta_values(const orc_cfg* c, int gen[6], int h[3], double hs[3], doub
     setup_t s;
     int rc = setup(c, &s);
     if (rc) return rc;
-    if (c->proc != 2 && (rc = dibeta_setup(c, &s))) return rc;
+    if (c->proc != 2 && c->proc != 7 && (rc = dibeta_setup(c, &s))) return rc;
     for (int q = 0; q < 3; ++q) {
         gen[2 * q] = s.ddx[q]; gen[2 * q + 1] = s.ddy[q];
         h[q] = s.dh[q]; hs[q] = s.dhs[q];
@@ -915,7 +916,8 @@ typedef struct {
 static int check_cfg(const orc_cfg* c) {
     if (!c || c->I <= 0 || c->J <= 0 || c->nk <= 0 || c->gm < 1 || c->gm > ORC_MAX_GEN) return ORC_ERR_ARG;
     if (c->hx < 0 || c->hy < 0 || c->hz < 0 || c->p < 0) return ORC_ERR_ARG;
-    if (c->proc != 1 && c->proc != 6 && c->proc != 3 && c->proc != 8 && c->proc != 4 && c->proc != 2)
+    if (c->proc != 1 && c->proc != 6 && c->proc != 3 && c->proc != 8 && c->proc != 4 && c->proc != 2 &&
+        c->proc != 7)
         return ORC_ERR_ARG;
     if (c->proc == 4) {
         if (c->nzcol < 0 || c->lm < 1 || (size_t)c->nzcol * c->lm > (size_t)c->nk) return ORC_ERR_ARG;
@@ -1053,7 +1055,7 @@ static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_
             fast_forward(c, S, U, I, J, k0, k1);
             continue;
         }
-        if (c->proc == 2) {
+        if (c->proc == 2 || c->proc == 7) {
             lin2_adjoint(c, S, U, G[g].tmp, I, J, k0, k1);
             weight_gen(c, U, I, J, c->a[g], c->b[g], k0, k1);
             lin2_forward(c, S, U, G[g].tmp, I, J, k0, k1);
@@ -1101,7 +1103,9 @@ int orc_filtering_procedure(const orc_cfg* c, double* Vd) {
     horizontal_pipeline(c, &S, V, G, 0, c->nk);
 #endif
     gens_free(c, G);
-    if (zfilt) vfilter(c, &S, V, 0);
+    /* filtering_lin2_ens (proc 7) ends with the ADJOINT vertical filter
+     * (sup_vrbeta1T_ens, mg_filtering.f90:1304), as the reference does */
+    if (zfilt) vfilter(c, &S, V, c->proc == 7);
     return ORC_OK;
 }
 
@@ -1149,7 +1153,7 @@ static void half_chain(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G) {
             fast_adjoint(c, S, U, G[g].I, G[g].J, 0, c->nk);
             continue;
         }
-        if (c->proc == 2) {
+        if (c->proc == 2 || c->proc == 7) {
             lin2_adjoint(c, S, U, G[g].tmp, G[g].I, G[g].J, 0, c->nk);
             continue;
         }
@@ -1161,7 +1165,9 @@ static void half_chain(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G) {
 int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double* ga) {
     int rc = check_cfg(c);
     if (rc) return rc;
-    if (c->proc == 4) return ORC_ERR_ARG;  /* its adjoint side is not the transpose of its forward side */
+    /* proc 4: its adjoint side is not the transpose of its forward side;
+     * proc 7: Bz^T M Bz^T, so the gy chain would need Bz, not Bz^T */
+    if (c->proc == 4 || c->proc == 7) return ORC_ERR_ARG;
     setup_t S;
     rc = setup(c, &S);
     if (rc) return rc;
@@ -1234,7 +1240,7 @@ int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y) 
         return ORC_OK;
     }
     if (which == 8 || which == 9) {
-        if (c->proc != 2) return ORC_ERR_ARG;
+        if (c->proc != 2 && c->proc != 7) return ORC_ERR_ARG;
         orc_cfg cc = *c; cc.I = I; cc.J = J;
         double* V = to_halo(&cc, x);
         arr3 a = {V, nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy};

@@ -45,7 +45,8 @@ typedef struct orc_cfg {
     double a[ORC_MAX_GEN];  /* per-generation weights a_g (a[0] = gen 1)      */
     double b[ORC_MAX_GEN];  /* Helmholtz Laplacian coefficients (reference: 0) */
     int lhelm;           /* use weighting_helm form                           */
-    int proc;            /* 1 rad2_bckg, 6 rad2_ens, 3 fast_bckg, 8 fast_ens, 4 rad3, 2 lin2_bckg */
+    int proc;            /* 1 rad2_bckg, 6 rad2_ens, 3 fast_bckg, 8 fast_ens, 4 rad3, 2 lin2_bckg,
+                            7 lin2_ens */
     int l_vertical_filter;
     int l_filt_g1;       /* procs 6 and 8 only                                */
     int lquart;          /* quadratic (3-point) interpolation                 */

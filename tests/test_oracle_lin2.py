@@ -199,3 +199,38 @@ def test_errors():
         O.filter_compact(cfg(hx=2), np.zeros((20, 24, 5)))
     with pytest.raises(O.OracleError):  # spread^2 beyond the moment table
         O.filter_compact(cfg(ampl02=0.02, hx=8, hy=8), np.zeros((20, 24, 5)))
+
+
+# ------------------------------------------- proc 7: filtering_lin2_ens
+
+@pytest.mark.parametrize("lquart", [False, True])
+def test_proc7_is_proc2_between_two_adjoint_vertical_filters(lquart):
+    """filtering_lin2_ens (mg_filtering.f90:1150-1313) runs proc 2's
+    horizontal part (generation 1 filtered: l_filt_g1) and ends with the
+    adjoint vertical filter sup_vrbeta1T_ens (:1304), so L7 = Bz^T M Bz^T."""
+    kw = dict(I=32, J=32, nk=6, gm=3, weights=[1.0, 0.5, 0.25], lquart=lquart, lm=3, nzcol=2, ampl01=0.8, hz=2)
+    c7 = cfg(proc=7, l_vertical_filter=True, l_filt_g1=True, **kw)
+    c2 = cfg(proc=2, l_vertical_filter=False, **kw)
+    cz = cfg(proc=7, l_vertical_filter=True, **kw)
+    x = rng.standard_normal((32, 32, 6))
+    ref = O.stage(cz, O.STAGE_Z_ADJ, 1, O.filter_compact(c2, O.stage(cz, O.STAGE_Z_ADJ, 1, x)))
+    assert np.abs(O.filter_compact(c7, x) - ref).max() < 1e-13
+    # not self-adjoint
+    a, b = rng.standard_normal((32, 32, 6)), rng.standard_normal((32, 32, 6))
+    la, lb = O.filter_compact(c7, a), O.filter_compact(c7, b)
+    assert abs((la * b).sum() - (a * lb).sum()) > 1e-6 * np.abs(la * b).sum()
+
+
+def test_proc7_generation1_unfiltered_without_filt_g1():
+    """With l_filt_g1 false, generation 1 is neither filtered nor weighted
+    (weighting_ens, mg_generations.f90:1012-1052): one generation and no
+    vertical filter leave the field unchanged."""
+    c = cfg(proc=7, l_filt_g1=False, weights=[0.3])
+    x = rng.standard_normal((c.J, c.I, c.nk))
+    assert np.abs(O.filter_compact(c, x) - x).max() == 0.0
+
+
+def test_proc7_weight_grads_refused():
+    c = cfg(proc=7)
+    with pytest.raises(O.OracleError):
+        O.weight_grads(c, np.zeros((c.J, c.I, c.nk)), np.zeros((c.J, c.I, c.nk)))
