@@ -138,9 +138,12 @@ int mgbf_get_dims(const mgbf_handle* h, mgbf_dims* dims);
  * three "dibeta" line filters of the triad decomposition, jp_pbfil3.f90,
  * of the Cholesky factor of the inverse aspect that init_mg_line sees;
  * MGBF_ERR_REACH when a line filter's spread is beyond the moment table or
- * its reach beyond the halo).  5 and 7 return MGBF_ERR_UNSUPPORTED; any
- * other value is a no-op returning MGBF_OK, as the reference's select has
- * no default case.
+ * its reach beyond the halo), and 7 = filtering_lin2_ens
+ * (mg_filtering.f90:1150-1313: the same line filters over the stacked
+ * members, l_filt_g1 and lquart as for 6, ending like the reference with the
+ * ADJOINT vertical filter sup_vrbeta1T_ens, so the operator is not
+ * symmetric).  5 returns MGBF_ERR_UNSUPPORTED; any other value is a no-op
+ * returning MGBF_OK, as the reference's select has no default case.
  *   vall:   field pointer (device or host, per mem), laid out per the
  *           handle's layout, element type per dtype.
  *   stream: cudaStream_t (NULL = legacy default stream).  Device calls are
@@ -172,8 +175,8 @@ int mgbf_filt_to_anal(mgbf_handle* h, void* vall, void* worka, int dtype, int me
 /* Adjoint of filtering_procedure(mg_filt), run through the explicit
  * transposed chain (no reference counterpart: the reference's adjoint test
  * is an empty stub, RBETA_TEST.f90:64-69).  Procedures 1, 2, 3, 6 and 8 are
- * self-adjoint, so the result equals the forward up to rounding; 4 is not
- * and returns MGBF_ERR_UNSUPPORTED. */
+ * self-adjoint, so the result equals the forward up to rounding; 4 and 7
+ * are not and return MGBF_ERR_UNSUPPORTED. */
 int mgbf_filtering_procedure_adjoint(mgbf_handle* h, int mg_filt, void* vall, int dtype, int mem,
                                      void* stream);
 
@@ -183,7 +186,8 @@ int mgbf_filtering_procedure_adjoint(mgbf_handle* h, int mg_filt, void* vall, in
  *   u_g = B_g R_g Bz^T x, v_g = B_g R_g Bz^T gy, for g = 1..gm.
  * x, gy, gx: fields in the handle's layout (gx may alias gy).  ga: host
  * array of gm doubles.  Coarse generations are recomputed from x.
- * Returns after ga is on the host.
+ * Returns after ga is on the host.  Procedures 4 and 7 (not self-adjoint)
+ * return MGBF_ERR_UNSUPPORTED.
  */
 int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, const void* gy,
                                  void* gx, double* ga, int dtype, int mem, void* stream);

@@ -360,7 +360,8 @@ struct Exec {
     View C(int g) { return gen_view(P, G, G.bufs[(int)t].C[g]->p, t, g); }
     View D(int g) { return gen_view(P, G, G.bufs[(int)t].D[g]->p, t, g); }
     bool fast = false;  // procs 3 and 8: separable line filters instead of the radial disk
-    bool lin2 = false;  // proc 2: three line filters along the triad's generators
+    bool lin2 = false;  // procs 2, 7: three line filters along the triad's generators
+    bool zadj_out = false;  // proc 7: ends with the adjoint vertical filter (mg_filtering.f90:1304)
     int n3 = -1;        // proc 4: levels of the 3D variables (ball); the rest take the 2D radial filter
     bool has_prev = false;  // proc 4, generation 1: the caller's halo, folded by the adjoint side
     View prev;
@@ -584,13 +585,15 @@ struct Exec {
         const bool z = nzcol > 0 && !G.zs.fwd.empty();
         for (int g = P.gm - 1; g >= 2; --g)
             if ((rc = prolong(g - 1, A(g), A(g - 1), A(g - 1)))) return rc;
-        if (P.gm == 1) return zstage(A(0), y, false, z ? nzcol : 0, 0);
+        if (P.gm == 1) return zstage(A(0), y, zadj_out, z ? nzcol : 0, 0);
         if (!z) return prolong(0, A(1), A(0), y);
-        // last prolongation and the vertical forward filter in one pass
-        int r = prolong_z(A(1), A(0), y, nzcol);
-        if (r != -1) return r;
+        if (!zadj_out) {
+            // last prolongation and the vertical forward filter in one pass
+            int r = prolong_z(A(1), A(0), y, nzcol);
+            if (r != -1) return r;
+        }
         if ((rc = prolong(0, A(1), A(0), A(0)))) return rc;
-        return zstage(A(0), y, false, nzcol, 0);
+        return zstage(A(0), y, zadj_out, nzcol, 0);
     }
 
     int forward(View x, View y, int nzcol, bool filt1) {
@@ -1105,16 +1108,17 @@ int mgbf_set_weights(mgbf_handle* h, const double* a, int n) {
 
 static bool is_fast(int mg_filt) { return mg_filt == 3 || mg_filt == 8; }
 static bool is_bckg(int mg_filt) { return mg_filt == 1 || mg_filt == 2 || mg_filt == 3 || mg_filt == 4; }
-static bool needs_d(int mg_filt) { return is_fast(mg_filt) || mg_filt == 2; }
+static bool is_lin2(int mg_filt) { return mg_filt == 2 || mg_filt == 7; }
+static bool needs_d(int mg_filt) { return is_fast(mg_filt) || is_lin2(mg_filt); }
 
 static int check_proc(mgbf_handle* h, int mg_filt, bool& noop) {
     noop = false;
-    if (mg_filt == 1 || mg_filt == 2 || mg_filt == 6 || mg_filt == 3 || mg_filt == 8 || mg_filt == 4) {
+    if (mg_filt == 1 || mg_filt == 2 || mg_filt == 6 || mg_filt == 7 || mg_filt == 3 || mg_filt == 8 || mg_filt == 4) {
         if (is_bckg(mg_filt) && h->cfg.n_ens != 1)
             return fail(MGBF_ERR_CONFIG, "filtering_rad2_bckg / filtering_lin2_bckg / filtering_fast_bckg / filtering_rad3 (procs 1, 2, 3, 4) need n_ens = 1: their arrays are dimensioned km, not km_all");
-        if (mg_filt == 2 && !h->plan.groups[0].ds.ok)
+        if (is_lin2(mg_filt) && !h->plan.groups[0].ds.ok)
             return fail(h->plan.groups[0].ds_rc ? h->plan.groups[0].ds_rc : MGBF_ERR_CONFIG,
-                        "filtering_lin2_bckg: " + h->plan.groups[0].ds_err);
+                        (mg_filt == 2 ? "filtering_lin2_bckg: " : "filtering_lin2_ens: ") + h->plan.groups[0].ds_err);
         if (mg_filt == 4) {
             const Group& G = h->plan.groups[0];
             if (G.bs.R < 0) return fail(MGBF_ERR_DIVISIBILITY, "filtering_rad3: " + G.bs_err);
@@ -1125,13 +1129,13 @@ static int check_proc(mgbf_handle* h, int mg_filt, bool& noop) {
             return MGBF_OK;
         }
         if (!is_bckg(mg_filt) && h->cfg.l_vertical_filter && h->cfg.km2 > 0 && h->cfg.km3 > 0)
-            return fail(MGBF_ERR_CONFIG, "filtering_rad2_ens / filtering_fast_ens (procs 6, 8) with the vertical filter need km2 = 0: sup_vrbeta1_ens views VALL with leading dimension km3_all*lm");
+            return fail(MGBF_ERR_CONFIG, "filtering_rad2_ens / filtering_lin2_ens / filtering_fast_ens (procs 6, 7, 8) with the vertical filter need km2 = 0: sup_vrbeta1_ens views VALL with leading dimension km3_all*lm");
         if (is_fast(mg_filt) && h->plan.groups[0].ls.R < 0)
             return fail(MGBF_ERR_DIVISIBILITY, h->plan.groups[0].ls_err);
         return MGBF_OK;
     }
     if (mg_filt >= 2 && mg_filt <= 8)
-        return fail(MGBF_ERR_UNSUPPORTED, "filtering procedure " + std::to_string(mg_filt) + " is not implemented (supported: 1, 2, 3, 4, 6, 8)");
+        return fail(MGBF_ERR_UNSUPPORTED, "filtering procedure " + std::to_string(mg_filt) + " is not implemented (supported: 1, 2, 3, 4, 6, 7, 8)");
     noop = true;  // no case default in the reference's select
     return MGBF_OK;
 }
@@ -1158,7 +1162,8 @@ static int run_proc(mgbf_handle* h, int mg_filt, const void* xin, void* yout, DT
     const bool filt1 = is_bckg(mg_filt) || h->cfg.l_filt_g1;
     Exec ex{P, G, t, stream};
     ex.fast = is_fast(mg_filt);
-    ex.lin2 = mg_filt == 2;
+    ex.lin2 = is_lin2(mg_filt);
+    ex.zadj_out = mg_filt == 7;
     View x = field_view(h, const_cast<void*>(xin), t);
     View y = field_view(h, yout, t);
     if (rad3) {
@@ -1219,8 +1224,10 @@ int mgbf_filtering_procedure_adjoint(mgbf_handle* h, int mg_filt, void* vall, in
     // transposing each stage in reverse order reproduces the same launch
     // sequence (Bz^T first, restriction = P^T, B^T = B, a_g, B, P, Bz).
     // filtering_rad3's adjoint side is not the transpose of its forward side.
-    if (mg_filt == 4)
-        return fail(MGBF_ERR_UNSUPPORTED, "adjoint of filtering_rad3: the operator is not self-adjoint");
+    if (mg_filt == 4 || mg_filt == 7)
+        return fail(MGBF_ERR_UNSUPPORTED, std::string("adjoint of ") +
+                                              (mg_filt == 4 ? "filtering_rad3" : "filtering_lin2_ens") +
+                                              ": the operator is not self-adjoint");
     return with_field(h, mg_filt, vall, dtype, mem, stream);
 }
 
@@ -1236,6 +1243,9 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
     if (mg_filt == 4)
         return fail(MGBF_ERR_UNSUPPORTED,
                     "weight gradients of filtering_rad3: its adjoint side is not the transpose of its forward side");
+    if (mg_filt == 7)
+        return fail(MGBF_ERR_UNSUPPORTED,
+                    "weight gradients of filtering_lin2_ens: it ends with the adjoint vertical filter, so it is not self-adjoint");
     DeviceGuard dg(h->plan.device);
     const DType t = (DType)dtype;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1258,7 +1268,8 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
     const bool filt1 = is_bckg(mg_filt) || h->cfg.l_filt_g1;
     Exec ex{P, G, t, stream};
     ex.fast = is_fast(mg_filt);
-    ex.lin2 = mg_filt == 2;
+    ex.lin2 = is_lin2(mg_filt);
+    ex.zadj_out = mg_filt == 7;
     View vx = field_view(h, const_cast<void*>(dx), t);
     View vg = field_view(h, const_cast<void*>(dgy), t);
     View vo = field_view(h, dgx, t);

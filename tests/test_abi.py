@@ -144,7 +144,7 @@ def test_reach_larger_than_coarsest_generation(lib):
 def test_unsupported_and_unknown_procedures(lib):
     op = MGBF(small_config())
     x = np.zeros(op.field_shape())
-    for proc in (5, 7):
+    for proc in (5,):
         with pytest.raises(MGBFError) as e:
             op.filtering_procedure(proc, x)
         assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
@@ -174,6 +174,19 @@ def test_adjoint_of_rad3_is_refused(lib):
     op = MGBF(small_config(lm=6, km3=2, km2=2, hz=2, mg_ampl03=1.0, layout=_abi.MGBF_LAYOUT_COMPACT))
     with pytest.raises(MGBFError) as e:
         op.filtering_procedure_adjoint(4, np.zeros(op.field_shape()))
+    assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
+
+
+def test_lin2_ens_not_self_adjoint_calls_refused(lib):
+    """filtering_lin2_ens (proc 7) ends with the adjoint vertical filter:
+    neither its adjoint nor its weight gradients are the symmetric chain."""
+    op = MGBF(small_config(n_ens=2, layout=_abi.MGBF_LAYOUT_COMPACT))
+    x = np.zeros(op.field_shape())
+    with pytest.raises(MGBFError) as e:
+        op.filtering_procedure_adjoint(7, x)
+    assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
+    with pytest.raises(MGBFError) as e:
+        op.apply_with_weight_grads(7, x, x.copy())
     assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
 
 

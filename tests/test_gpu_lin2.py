@@ -107,3 +107,26 @@ def test_lin2_host_memory(lib, cuda):
     y = x.copy()
     op.filtering_procedure(2, y)
     assert rel_l2(y, O.filter_compact(oracle_cfg(c, 2), x)) < 1e-12
+
+
+# ------------------------------------------- proc 7: filtering_lin2_ens
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("lquart", [False, True])
+@pytest.mark.parametrize("filt_g1", [True, False])
+def test_lin2_ens_parity_compact(lib, cuda, dtype, lquart, filt_g1):
+    """Proc 7: two members stacked, ending with the adjoint vertical filter."""
+    c = lin2_config(n_ens=2, lquart=lquart, l_filt_g1=filt_g1)
+    op = MGBF(c)
+    x = np.random.default_rng(60).standard_normal(op.field_shape())
+    assert rel_l2(run(op, x, dtype, proc=7), O.filter_compact(oracle_cfg(c, 7), x)) < TOL[dtype]
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_lin2_ens_parity_halo_layout(lib, cuda, dtype):
+    c = lin2_config(n_ens=2, layout=_abi.MGBF_LAYOUT_HALO)
+    op = MGBF(c)
+    v = np.random.default_rng(61).standard_normal(op.field_shape())
+    ref = v.copy()
+    O.filtering_procedure(oracle_cfg(c, 7), ref)
+    assert rel_l2(run(op, v, dtype, proc=7), ref) < TOL[dtype]
