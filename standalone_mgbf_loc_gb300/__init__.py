@@ -1,5 +1,5 @@
-"""GB300-native MGBF filtering path (filtering_procedure procs 1, 2, 3, 4, 6
-and 8; the analysis<->filter transfers).
+"""GB300-native MGBF filtering path (filtering_procedure procs 1, 2, 3, 4, 6,
+7 and 8; the analysis<->filter transfers).
 
 The compute path is libmgbf.so (hand-written sm_103a CUDA + C++ host
 orchestration) reached through its C-ABI; this package is the Python host
