@@ -21,6 +21,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -81,7 +82,10 @@ class ClockSampler:
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu}.csv")
+        # the raw samples go to MGBF_CLOCK_LOG_DIR (default: the temp dir);
+        # their summary is the JSON line's "clocks" entry
+        log_dir = os.environ.get("MGBF_CLOCK_LOG_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(log_dir, f"mgbf_clocks_rank{gpu}.csv")
 
     def __enter__(self):
         try:
