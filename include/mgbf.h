@@ -122,6 +122,13 @@ int mgbf_create_from_namelist(const char* path, mgbf_handle** out);
 /* Sizes derived at creation. */
 int mgbf_get_dims(const mgbf_handle* h, mgbf_dims* dims);
 
+/* The three line filters of procedures 2 and 7 as set up at creation
+ * (init_mg_line, mg_intstate.f90:436-480): per color q = 0..2 the
+ * generator (gen[2q], gen[2q+1]), integer half-span h[q], formal half-span
+ * hs[q] and weights fil[9q + i], i = 0..h[q] (zero beyond).  Returns the
+ * setup's error (MGBF_ERR_REACH, ...) when those procedures cannot run. */
+int mgbf_get_line_filters(const mgbf_handle* h, int gen[6], int hspan[3], double hs[3], double fil[27]);
+
 /*
  * filtering_procedure(mg_filt) (mg_filtering.f90:67-120) on the field in
  * place.  Supported: 1 = filtering_rad2_bckg (mg_filtering.f90:560-680),

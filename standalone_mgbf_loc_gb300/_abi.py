@@ -82,6 +82,8 @@ SIGNATURES = {
     "mgbf_create": (_I, [ctypes.POINTER(MgbfConfig), ctypes.POINTER(_HP)]),
     "mgbf_create_from_namelist": (_I, [ctypes.c_char_p, ctypes.POINTER(_HP)]),
     "mgbf_get_dims": (_I, [_HP, ctypes.POINTER(MgbfDims)]),
+    "mgbf_get_line_filters": (_I, [_HP, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "mgbf_filtering_procedure": (_I, [_HP, _I, _VP, _I, _I, _VP]),
     "mgbf_filtering_procedure_adjoint": (_I, [_HP, _I, _VP, _I, _I, _VP]),
     "mgbf_apply_with_weight_grads": (_I, [_HP, _I, _VP, _VP, _VP, ctypes.POINTER(_D), _I, _I, _VP]),

@@ -1080,6 +1080,18 @@ int mgbf_create_from_namelist(const char* path, mgbf_handle** out) {
     return mgbf_create(&c, out);
 }
 
+int mgbf_get_line_filters(const mgbf_handle* h, int gen[6], int hspan[3], double hs[3], double fil[27]) {
+    if (!h || !gen || !hspan || !hs || !fil) return fail(MGBF_ERR_ARG, "null argument");
+    const Group& G = h->plan.groups[0];
+    if (!G.ds.ok) return fail(G.ds_rc ? G.ds_rc : MGBF_ERR_CONFIG, "line filters: " + G.ds_err);
+    for (int q = 0; q < 3; ++q) {
+        gen[2 * q] = G.ds.dx[q]; gen[2 * q + 1] = G.ds.dy[q];
+        hspan[q] = G.ds.h[q]; hs[q] = G.ds.hs[q];
+        for (int i = 0; i < 9; ++i) fil[9 * q + i] = G.ds.fil[q][i];
+    }
+    return MGBF_OK;
+}
+
 int mgbf_get_dims(const mgbf_handle* h, mgbf_dims* d) {
     if (!h || !d) return fail(MGBF_ERR_ARG, "null argument");
     const Plan& P = h->plan;

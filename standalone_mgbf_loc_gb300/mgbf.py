@@ -230,6 +230,17 @@ class MGBF:
         """Raise if a bounded device wait ran out since the last check."""
         _abi.check(self._lib.mgbf_status(self._h), "mgbf_status")
 
+    def line_filters(self) -> list:
+        """Procedures 2 and 7's three line filters (colors 1..3): dicts with
+        the generator d, half-span h, formal half-span hs and weights fil[0..h]."""
+        gen = (ctypes.c_int * 6)()
+        hspan = (ctypes.c_int * 3)()
+        hs = (ctypes.c_double * 3)()
+        fil = (ctypes.c_double * 27)()
+        _abi.check(self._lib.mgbf_get_line_filters(self._h, gen, hspan, hs, fil), "mgbf_get_line_filters")
+        return [{"d": (gen[2 * q], gen[2 * q + 1]), "h": hspan[q], "hs": hs[q],
+                 "fil": np.array(fil[9 * q:9 * q + hspan[q] + 1])} for q in range(3)]
+
     def autotune(self, dtype=None) -> None:
         """Choose radial-kernel variants and tile heights by measurement."""
         dt = _dtype_code(dtype if dtype is not None else torch.float32)

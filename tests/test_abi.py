@@ -9,7 +9,8 @@ import numpy as np
 import pytest
 
 from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig, MGBFError, _abi
-from tests.helpers import canonical, canonical_z, small_config
+from oracle import oracle as O
+from tests.helpers import canonical, canonical_z, oracle_cfg, small_config
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -168,6 +169,32 @@ def test_line_filter_procedure_validation(lib):
     with pytest.raises(MGBFError) as e:  # proc 2 is a single-member procedure
         MGBF(small_config(n_ens=2)).filtering_procedure(2, np.zeros(MGBF(small_config(n_ens=2)).field_shape()))
     assert e.value.code == _abi.MGBF_ERR_CONFIG
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+@pytest.mark.parametrize("ampl02", [3.0, 1.2, 0.6, 0.3, 0.15])
+def test_line_filter_setup_matches_oracle(lib, p, ampl02):
+    """The library's own setup of procedure 2's line filters (triad,
+    half-span transform, two-beta weights) equals the oracle's."""
+    # every handle checks the fast filters' line reach and the radial disk's
+    line = int(np.floor(np.sqrt(2 * p + 3) / ampl02 - 1e-12))
+    disk = int(np.floor(np.sqrt((2 * p + 4) * ampl02) - 1e-12))
+    h = max(4, line, disk)
+    c = small_config(p=p, mg_ampl02=ampl02, hx=h, hy=h, nxPE=1, nyPE=1, im_filt=64, jm_filt=64, gm_max=2,
+                     mg_ampl01=canonical_z(2, p), mg_ampl03=0.3)
+    got = MGBF(c).line_filters()
+    ref = O.dibeta_values(oracle_cfg(c, 2))
+    for g, r in zip(got, ref):
+        assert g["d"] == r["d"] and g["h"] == r["h"]
+        assert abs(g["hs"] - r["hs"]) < 1e-13
+        assert np.abs(g["fil"] - r["fil"]).max() < 1e-15
+
+
+def test_line_filter_setup_error_is_reported(lib):
+    op = MGBF(small_config(mg_ampl02=0.035, hx=80, hy=80, im_filt=32, jm_filt=32, gm_max=1))
+    with pytest.raises(MGBFError) as e:
+        op.line_filters()
+    assert e.value.code == _abi.MGBF_ERR_REACH
 
 
 def test_adjoint_of_rad3_is_refused(lib):
