@@ -3,8 +3,8 @@
  *
  * Restates, on one global filter grid, the reference's CPU algorithm for
  * filtering_procedure(1), (6), the fast 1D+1D variants (3) and (8),
- * filtering_rad3 (4) and the line-filter procedures filtering_lin2_bckg (2)
- * and filtering_lin2_ens (7).
+ * filtering_rad3 (4) and the line-filter procedures filtering_lin2_bckg (2),
+ * filtering_lin3 (5) and filtering_lin2_ens (7).
  * Every routine below
  * names the reference routine (file:line, paths inside the reference project)
  * whose loops it follows.  The MPI halo exchange of the reference collapses
@@ -82,10 +82,17 @@ typedef struct {
     int ddx[3], ddy[3], dh[3];
     double dhs[3];
     double dfil[3][ORC_DIB_NFIL + 1];
+    /* filtering_lin3's hexad (proc 5): for colors 1..7 the active slot (or
+     * -1), per slot the generator, half-span and weights */
+    int hslot[8];
+    int hgen[6][3], hh[6];
+    double hhs[6];
+    double hfil[6][ORC_DIB_NFIL + 1];
 } setup_t;
 
 static const double EPS = 1.e-12;
 static int dibeta_setup(const orc_cfg* c, setup_t* s);
+static int hexad_setup(const orc_cfg* c, setup_t* s);
 
 /* mg_parameter.f90:567-572 (rmom2), mg_intstate.f90:360-431 (pasp, cholaspect,
  * getlinesum), jp_pbfil.f90:74-107 (cholaspect1/2), 149-218 (getlinesum1/2). */
@@ -185,6 +192,10 @@ static int setup(const orc_cfg* c, setup_t* s) {
         s->reach3 = gzm;
     }
     if (c->proc == 2 || c->proc == 7) return dibeta_setup(c, s);
+    if (c->proc == 5) {
+        int rc = dibeta_setup(c, s);
+        return rc ? rc : hexad_setup(c, s);
+    }
     return ORC_OK;
 }
 
@@ -206,6 +217,37 @@ static void dib_moments(int p, double* bnorm, double* bsprd) {
         bnorm[h] = 1.0 / s0;
         bsprd[h] = s2 / s0;
     }
+}
+
+/* hstform (jp_pbfil3.f90:1399-1430) of a spread^2 into the formal half-span
+ * hs between two table entries, then blinfil (1463-1501): the weights
+ * fil[0..h] of the two-beta filter of half-spans h = int(hs) and h+1. */
+static int dib_weights(int p, double spread, const double* bnorm, const double* bsprd, int* h_out, double* hs_out,
+                       double* f) {
+    double hs = spread;
+    int found = 0;
+    if (hs >= 0.0)
+        for (int h = 2; h <= ORC_DIB_NH && !found; ++h)
+            if (bsprd[h] >= hs) {
+                hs = h - (bsprd[h] - hs) / (bsprd[h] - bsprd[h - 1]);
+                found = 1;
+            }
+    if (!found) return ORC_ERR_REACH;
+    const int h = (int)hs, hp = h + 1;
+    if (h < 1 || hp > ORC_DIB_NH || hp > ORC_DIB_NFIL) return ORC_ERR_REACH;
+    const double whp = (hs - h) * bnorm[hp], wh = (hp - hs) * bnorm[h];
+    for (int i = 0; i <= ORC_DIB_NFIL; ++i) f[i] = 0.0;
+    for (int i = 0; i <= h; ++i) {
+        double z = (double)i / hp;
+        f[i] = whp * ipow(1.0 - z * z, p);
+    }
+    for (int i = 0; i < h; ++i) {
+        double z = (double)i / h;
+        f[i] += wh * ipow(1.0 - z * z, p);
+    }
+    *h_out = h;
+    *hs_out = hs;
+    return ORC_OK;
 }
 
 /* triad (jp_pbfil3.f90:573-624): resolve the aspect 3-vector (A11, A22, A12)
@@ -261,33 +303,117 @@ static int dibeta_setup(const orc_cfg* c, setup_t* s) {
     double w[3];
     if (orc_triad(asp, lt, w)) return ORC_ERR_ARG;
     for (int q = 0; q < 3; ++q) {
-        double hs = w[q];
-        int found = 0;
-        if (hs >= 0.0)
-            for (int h = 2; h <= ORC_DIB_NH && !found; ++h)
-                if (bsprd[h] >= hs) {
-                    hs = h - (bsprd[h] - hs) / (bsprd[h] - bsprd[h - 1]);
-                    found = 1;
-                }
-        if (!found) return ORC_ERR_REACH;
-        const int h = (int)hs, hp = h + 1;
-        if (h < 1 || hp > ORC_DIB_NH || hp > ORC_DIB_NFIL) return ORC_ERR_REACH;
-        const double whp = (hs - h) * bnorm[hp], wh = (hp - hs) * bnorm[h];
-        double* f = s->dfil[q];
-        for (int i = 0; i <= ORC_DIB_NFIL; ++i) f[i] = 0.0;
-        for (int i = 0; i <= h; ++i) {
-            double z = (double)i / hp;
-            f[i] = whp * ipow(1.0 - z * z, c->p);
-        }
-        for (int i = 0; i < h; ++i) {
-            double z = (double)i / h;
-            f[i] += wh * ipow(1.0 - z * z, c->p);
-        }
+        int rc = dib_weights(c->p, w[q], bnorm, bsprd, &s->dh[q], &s->dhs[q], s->dfil[q]);
+        if (rc) return rc;
         s->ddx[q] = lt[2 * q]; s->ddy[q] = lt[2 * q + 1];
-        s->dh[q] = h; s->dhs[q] = hs;
-        if (h * abs(s->ddx[q]) > c->hx || h * abs(s->ddy[q]) > c->hy) return ORC_ERR_REACH;
+        if (s->dh[q] * abs(s->ddx[q]) > c->hx || s->dh[q] * abs(s->ddy[q]) > c->hy) return ORC_ERR_REACH;
     }
     return ORC_OK;
+}
+
+/* hexad (jp_pbfil3.f90:798-904): resolve the 3D aspect 6-vector
+ * (A11, A22, A33, A23, A31, A12) onto the seven nonnull GF(8) "colors" of a
+ * hexad (one of them, the hexad's own color, null): integer generators
+ * lh[3*(c-1)..] and weights w[c-1], c = 1..7, with A = sum w l l^T.  The
+ * iteration moves only the K-set of three generators (the others follow
+ * from it) and applies a rank-1 update to the projection rows per step;
+ * the default K-set and projections, the six K-set update matrices, the
+ * step offsets, the sign pattern and the output color order are the
+ * reference's tables, restated here. */
+int orc_hexad(const double asp[6], int lh[21], double w7[7]) {
+    static const int deflhex[7][3] = {{0, 0, 0}, {1, -1, 0}, {0, 1, -1}, {0, 0, 1}, {-1, 0, 1}, {0, 1, 0}, {1, 0, 0}};
+    static const int deflui[7][6] = {{0, 0, 0, 0, 0, 0},  {0, 0, 0, 0, 0, -1}, {0, 0, 0, -1, 0, 0}, {0, 0, 1, 1, 1, 0},
+                                     {0, 0, 0, 0, -1, 0}, {0, 1, 0, 1, 0, 1},  {1, 0, 0, 0, 1, 1}};
+    /* M[d-1][c][r]: column c of the K-set update for step d = 1..6 */
+    static const int mm[6][3][3] = {{{1, 1, -1}, {1, 0, 0}, {1, 0, -1}},   {{-1, 1, 0}, {-1, 1, 1}, {0, 1, 0}},
+                                    {{0, -1, 1}, {1, -1, 0}, {1, 0, 0}},   {{0, 0, 1}, {0, -1, 1}, {1, -1, 1}},
+                                    {{-1, 0, 1}, {0, 0, 1}, {-1, 1, 0}},   {{0, 1, 0}, {1, 0, -1}, {0, 1, -1}}};
+    static const int ttriad[7] = {0, 5, 3, 3, 6, 5, 6};                                  /* index 1..6 */
+    static const int sstriad[13] = {-1, -1, 1, -1, 1, 1, 1, -1, -1, 1, -1, 1, 1};        /* index -6..6 */
+    static const int line[3] = {1, 2, 4};
+    static const int jcol[7] = {7, 4, 6, 3, 5, 2, 1};
+#define MOD7(a) ((((a) % 7) + 7) % 7)
+    int lhex[7][3], lui[7][6], K[3][3];
+    double wh[7];
+    memcpy(lhex, deflhex, sizeof(lhex));
+    memcpy(lui, deflui, sizeof(lui));
+    int hcol = 0, kcol = 0;
+    for (int q = 0; q < 7; ++q) {
+        wh[q] = 0.0;
+        for (int r = 0; r < 6; ++r) wh[q] += asp[r] * lui[q][r];
+    }
+    for (int i = 0; i < 3; ++i) memcpy(K[i], lhex[MOD7(hcol - line[i])], sizeof(K[i]));
+    int it;
+    for (it = 1; it <= 200; ++it) {
+        kcol = 0;
+        for (int q = 1; q < 7; ++q)
+            if (wh[q] < wh[kcol]) kcol = q;
+        const double dw = wh[kcol];
+        if (dw >= -1.e-14) break;
+        const int dcol = MOD7(kcol - hcol);
+        hcol = kcol;
+        const int L = MOD7(hcol + ttriad[dcol]);
+        int Kn[3][3];
+        for (int cc = 0; cc < 3; ++cc)
+            for (int e = 0; e < 3; ++e) {
+                int v = 0;
+                for (int r = 0; r < 3; ++r) v += K[r][e] * mm[dcol - 1][cc][r];
+                Kn[cc][e] = v;
+            }
+        memcpy(K, Kn, sizeof(K));
+        int dl[6];
+        for (int r = 0; r < 6; ++r) dl[r] = lui[hcol][r];
+        for (int q = 0; q < 7; ++q) {
+            const int sg = sstriad[q - L + 6];
+            for (int r = 0; r < 6; ++r) lui[q][r] += dl[r] * sg;
+            wh[q] += sg * dw;
+        }
+    }
+    if (it > 200) return ORC_ERR_ARG;
+    for (int i = 0; i < 3; ++i) {
+        const int ip = (i + 1) % 3;
+        for (int e = 0; e < 3; ++e) {
+            lhex[MOD7(hcol - line[i])][e] = K[i][e];
+            lhex[MOD7(hcol + line[i])][e] = K[i][e] - K[ip][e];
+        }
+    }
+    for (int e = 0; e < 3; ++e) lhex[kcol][e] = 0;
+    for (int i = 0; i < 7; ++i) {
+        const int j = jcol[i] - 1;
+        for (int e = 0; e < 3; ++e) lh[3 * j + e] = lhex[i][e];
+        w7[j] = wh[i];
+    }
+#undef MOD7
+    return ORC_OK;
+}
+
+/* init_mg_line's hextform (mg_intstate.f90:471; jp_pbfil3.f90:702-750) for
+ * proc 5: pasp3 = diag(mg_ampl03) after cholaspect3 is diag(c3),
+ * c3 = 1/sqrt(mg_ampl03); the hexad's six active colors in ascending order,
+ * each spread^2 through the half-span transform and the two-beta weights. */
+static int hexad_setup(const orc_cfg* c, setup_t* s) {
+    double bnorm[ORC_DIB_NH + 1], bsprd[ORC_DIB_NH + 1];
+    dib_moments(c->p, bnorm, bsprd);
+    const double c3 = sqrt(1.0 / c->ampl03);
+    const double asp[6] = {c3, c3, c3, 0.0, 0.0, 0.0};
+    int lh[21];
+    double w7[7];
+    if (orc_hexad(asp, lh, w7)) return ORC_ERR_ARG;
+    int slot = 0;
+    for (int col = 0; col < 8; ++col) s->hslot[col] = -1;
+    for (int col = 1; col <= 7; ++col) {
+        const int* g = &lh[3 * (col - 1)];
+        if (g[0] == 0 && g[1] == 0 && g[2] == 0) continue;
+        if (slot == 6) return ORC_ERR_ARG;
+        s->hslot[col] = slot;
+        for (int e = 0; e < 3; ++e) s->hgen[slot][e] = g[e];
+        int rc = dib_weights(c->p, w7[col - 1], bnorm, bsprd, &s->hh[slot], &s->hhs[slot], s->hfil[slot]);
+        if (rc) return rc;
+        const int h = s->hh[slot];
+        if (h * abs(g[0]) > c->hx || h * abs(g[1]) > c->hy || h * abs(g[2]) > c->hz) return ORC_ERR_REACH;
+        ++slot;
+    }
+    return slot == 6 ? ORC_OK : ORC_ERR_ARG;  /* hextform: exactly six active lines */
 }
 
 int orc_dibeta_values(const orc_cfg* c, int gen[6], int h[3], double hs[3], double fil[3 * (ORC_DIB_NFIL + 1)]) {
@@ -581,6 +707,183 @@ static void lin2_forward(const orc_cfg* c, const setup_t* S, arr3 U, arr3 T, int
         fill_h(U, I, J, c->hx, c->hy, k0, k1);
         dibeta_pass(S, q, U, T, I, J, 0, k0, k1);
     }
+}
+
+/* ------------------------- proc 5: filtering_lin3's 3D line filters */
+
+/* The 3D variables of a generation as filtering_lin3 holds them
+ * (mg_filtering.f90:260-557): W(v, i, j, L), v < km3, with x/y halos and a
+ * z halo of hz levels (stack_to_composite, mg_transfer.f90:206-234, puts
+ * VALL((v-1)*lm+L, i, j) at L). */
+typedef struct {
+    double* d;
+    int nv, I, J, lm, hx, hy, hz;
+} w3_t;
+static inline double* w3at(const w3_t* w, int v, int i, int j, int L) {
+    const size_t ni = (size_t)w->I + 2 * w->hx, nj = (size_t)w->J + 2 * w->hy;
+    return w->d + (size_t)v + (size_t)w->nv * ((size_t)(i + w->hx - 1) + ni * ((size_t)(j + w->hy - 1) +
+                                                                              nj * (size_t)(L + w->hz - 1)));
+}
+#define W3(w, v, i, j, L) (*w3at(&(w), (v), (i), (j), (L)))
+
+static void w3_from(w3_t w, arr3 U) {
+    for (int L = 1; L <= w.lm; ++L)
+        for (int j = 1 - w.hy; j <= w.J + w.hy; ++j)
+            for (int i = 1 - w.hx; i <= w.I + w.hx; ++i)
+                for (int v = 0; v < w.nv; ++v) W3(w, v, i, j, L) = A3(U, v * w.lm + L - 1, i, j);
+}
+static void w3_to(w3_t w, arr3 U) {
+    for (int L = 1; L <= w.lm; ++L)
+        for (int j = 1 - w.hy; j <= w.J + w.hy; ++j)
+            for (int i = 1 - w.hx; i <= w.I + w.hx; ++i)
+                for (int v = 0; v < w.nv; ++v) A3(U, v * w.lm + L - 1, i, j) = W3(w, v, i, j, L);
+}
+
+/* W(1-L) = W(1+L), W(lm+L) = W(lm-L), L = 1..hz, on every column */
+static void w3_zmirror(w3_t w) {
+    for (int L = 1; L <= w.hz; ++L)
+        for (int j = 1 - w.hy; j <= w.J + w.hy; ++j)
+            for (int i = 1 - w.hx; i <= w.I + w.hx; ++i)
+                for (int v = 0; v < w.nv; ++v) {
+                    W3(w, v, i, j, 1 - L) = W3(w, v, i, j, 1 + L);
+                    W3(w, v, i, j, w.lm + L) = W3(w, v, i, j, w.lm - L);
+                }
+}
+
+/* boco_3d at the physical edges, levels 1..lm: y on the interior columns
+ * (north, then south), then x on every row (west, then east).  gh = 0 is
+ * boco_3d_g1 (mg_bocos.f90:1425-1774), whose east edge is W(I+i) = W(I-i);
+ * gh = 1 is boco_3d_gh (1777-2170): W(I+i) = W(I+1-i), and the z halo is
+ * mirrored afterwards. */
+static void boco3(w3_t w, int gh) {
+    const int I = w.I, J = w.J;
+    for (int L = 1; L <= w.lm; ++L)
+        for (int j = 1; j <= w.hy; ++j)
+            for (int i = 1; i <= I; ++i)
+                for (int v = 0; v < w.nv; ++v) W3(w, v, i, J + j, L) = W3(w, v, i, J + 1 - j, L);
+    for (int L = 1; L <= w.lm; ++L)
+        for (int j = 1; j <= w.hy; ++j)
+            for (int i = 1; i <= I; ++i)
+                for (int v = 0; v < w.nv; ++v) W3(w, v, i, -w.hy + j, L) = W3(w, v, i, w.hy + 1 - j, L);
+    for (int L = 1; L <= w.lm; ++L)
+        for (int j = 1 - w.hy; j <= J + w.hy; ++j)
+            for (int i = 1; i <= w.hx; ++i)
+                for (int v = 0; v < w.nv; ++v) W3(w, v, -w.hx + i, j, L) = W3(w, v, w.hx + 1 - i, j, L);
+    for (int L = 1; L <= w.lm; ++L)
+        for (int j = 1 - w.hy; j <= J + w.hy; ++j)
+            for (int i = 1; i <= w.hx; ++i)
+                for (int v = 0; v < w.nv; ++v) W3(w, v, I + i, j, L) = W3(w, v, gh ? I + 1 - i : I - i, j, L);
+    if (gh) w3_zmirror(w);
+}
+
+/* bocoT_3d at the physical edges: x on every row (west, then east), levels
+ * 1..lm, then y on the interior columns (south, then north), then the z
+ * halo folded into levels 2..hz+1 and lm-hz..lm-1 on every column.
+ * gh = 0 is bocoT_3d_g1 (mg_bocos.f90:2173-2527), whose east and north
+ * folds read W(I+hx-i) and W(J+hy-j): the edge column and row are added to
+ * themselves and the outermost halo line is not folded.  gh = 1 is
+ * bocoT_3d_gh (2530-2908) with W(I+1+hx-i) and W(J+1+hy-j). */
+static void bocoT3(w3_t w, int gh) {
+    const int I = w.I, J = w.J, hx = w.hx, hy = w.hy, o = gh ? 1 : 0;
+    for (int L = 1; L <= w.lm; ++L)
+        for (int j = 1 - hy; j <= J + hy; ++j)
+            for (int i = 1; i <= hx; ++i)
+                for (int v = 0; v < w.nv; ++v) W3(w, v, i, j, L) += W3(w, v, 1 - i, j, L);
+    for (int L = 1; L <= w.lm; ++L)
+        for (int j = 1 - hy; j <= J + hy; ++j)
+            for (int i = 1; i <= hx; ++i)
+                for (int v = 0; v < w.nv; ++v) W3(w, v, I - hx + i, j, L) += W3(w, v, I + o + hx - i, j, L);
+    for (int L = 1; L <= w.lm; ++L)
+        for (int j = 1; j <= hy; ++j)
+            for (int i = 1; i <= I; ++i)
+                for (int v = 0; v < w.nv; ++v) W3(w, v, i, j, L) += W3(w, v, i, 1 - j, L);
+    for (int L = 1; L <= w.lm; ++L)
+        for (int j = 1; j <= hy; ++j)
+            for (int i = 1; i <= I; ++i)
+                for (int v = 0; v < w.nv; ++v) W3(w, v, i, J - hy + j, L) += W3(w, v, i, J + o + hy - j, L);
+    for (int L = 1; L <= w.hz; ++L) {
+        for (int j = 1 - hy; j <= J + hy; ++j)
+            for (int i = 1 - hx; i <= I + hx; ++i)
+                for (int v = 0; v < w.nv; ++v) W3(w, v, i, j, 1 + L) += W3(w, v, i, j, 1 - L);
+        for (int j = 1 - hy; j <= J + hy; ++j)
+            for (int i = 1 - hx; i <= I + hx; ++i)
+                for (int v = 0; v < w.nv; ++v) W3(w, v, i, j, w.lm - L) += W3(w, v, i, j, w.lm + L);
+    }
+}
+
+/* vdibetax3 / vdibetax3t (jp_pbfil3.f90:1928-1977, 2475-2525) for color col
+ * on the interior: b = 0 (z halo included), then a = b.  Where the point's
+ * hexad has no line of this color, forward copies and adjoint adds the
+ * value.  (The per-point slot counter of the reference is the same at
+ * every point here: the aspect is uniform.) */
+static void dib3(const setup_t* S, w3_t w, w3_t b, int col, int adj) {
+    const size_t n = (size_t)w.nv * (w.I + 2 * w.hx) * (w.J + 2 * w.hy) * (w.lm + 2 * w.hz);
+    memset(b.d, 0, sizeof(double) * n);
+    const int q = S->hslot[col];
+    for (int L = 1; L <= w.lm; ++L)
+        for (int j = 1; j <= w.J; ++j)
+            for (int i = 1; i <= w.I; ++i)
+                for (int v = 0; v < w.nv; ++v) {
+                    if (q < 0) {
+                        W3(b, v, i, j, L) += W3(w, v, i, j, L);
+                        continue;
+                    }
+                    const int dx = S->hgen[q][0], dy = S->hgen[q][1], dz = S->hgen[q][2];
+                    const double* f = S->hfil[q];
+                    if (!adj) {
+                        double acc = f[0] * W3(w, v, i, j, L);
+                        for (int t = 1; t <= S->hh[q]; ++t)
+                            acc += f[t] * (W3(w, v, i + t * dx, j + t * dy, L + t * dz) +
+                                           W3(w, v, i - t * dx, j - t * dy, L - t * dz));
+                        W3(b, v, i, j, L) = acc;
+                    } else {
+                        const double at = W3(w, v, i, j, L);
+                        W3(b, v, i, j, L) += f[0] * at;
+                        for (int t = 1; t <= S->hh[q]; ++t) {
+                            W3(b, v, i + t * dx, j + t * dy, L + t * dz) += f[t] * at;
+                            W3(b, v, i - t * dx, j - t * dy, L - t * dz) += f[t] * at;
+                        }
+                    }
+                }
+    memcpy(w.d, b.d, sizeof(double) * n);
+}
+
+/* One generation of filtering_lin3 (mg_filtering.f90:285-535): the 2D
+ * variables through proc 2's line filters; the 3D variables, adjoint side:
+ * for colors 7..1 the z mirror, dibetat and bocoT_3d; weighting; forward
+ * side: the z mirror once, then for colors 1..7 boco_3d and dibeta.
+ * Generation 1 uses the _g1 halo routines, coarser ones the _gh ones. */
+static void weight_gen(const orc_cfg* c, arr3 V, int I, int J, double a, double b, int k0, int k1);
+static void lin3_generation(const orc_cfg* c, const setup_t* S, arr3 U, arr3 T, int I, int J, double a, double b,
+                            int gh) {
+    const int n3 = c->nzcol * c->lm;
+    const size_t n = (size_t)(c->nzcol > 0 ? c->nzcol : 1) * (I + 2 * c->hx) * (J + 2 * c->hy) * (c->lm + 2 * c->hz);
+    w3_t w = {(double*)calloc(n, sizeof(double)), c->nzcol, I, J, c->lm, c->hx, c->hy, c->hz};
+    w3_t t = w;
+    t.d = (double*)calloc(n, sizeof(double));
+    if (c->nk > n3) lin2_adjoint(c, S, U, T, I, J, n3, c->nk);
+    if (n3 > 0) {
+        w3_from(w, U);
+        for (int col = 7; col >= 1; --col) {
+            w3_zmirror(w);
+            dib3(S, w, t, col, 1);
+            bocoT3(w, gh);
+        }
+        w3_to(w, U);
+    }
+    weight_gen(c, U, I, J, a, b, 0, c->nk);
+    if (c->nk > n3) lin2_forward(c, S, U, T, I, J, n3, c->nk);
+    if (n3 > 0) {
+        w3_from(w, U);
+        w3_zmirror(w);
+        for (int col = 1; col <= 7; ++col) {
+            boco3(w, gh);
+            dib3(S, w, t, col, 0);
+        }
+        w3_to(w, U);
+    }
+    free(w.d);
+    free(t.d);
 }
 
 /* ----------------------------------------------- filtering_rad3: 3D ball */
@@ -917,8 +1220,13 @@ static int check_cfg(const orc_cfg* c) {
     if (!c || c->I <= 0 || c->J <= 0 || c->nk <= 0 || c->gm < 1 || c->gm > ORC_MAX_GEN) return ORC_ERR_ARG;
     if (c->hx < 0 || c->hy < 0 || c->hz < 0 || c->p < 0) return ORC_ERR_ARG;
     if (c->proc != 1 && c->proc != 6 && c->proc != 3 && c->proc != 8 && c->proc != 4 && c->proc != 2 &&
-        c->proc != 7)
+        c->proc != 7 && c->proc != 5)
         return ORC_ERR_ARG;
+    if (c->proc == 5) {
+        if (c->nzcol < 0 || c->lm < 1 || (size_t)c->nzcol * c->lm > (size_t)c->nk) return ORC_ERR_ARG;
+        if (c->nzcol > 0 && c->hz >= c->lm) return ORC_ERR_ARG;
+        if (!(c->ampl03 > 0.0)) return ORC_ERR_ARG;
+    }
     if (c->proc == 4) {
         if (c->nzcol < 0 || c->lm < 1 || (size_t)c->nzcol * c->lm > (size_t)c->nk) return ORC_ERR_ARG;
         if (c->nzcol > 0 && c->hz >= c->lm) return ORC_ERR_ARG;
@@ -1032,7 +1340,8 @@ static void weight_gen(const orc_cfg* c, arr3 V, int I, int J, double a, double 
 
 static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G, int k0, int k1) {
     const int gm = c->gm, hx = c->hx, hy = c->hy;
-    const int filt1 = (c->proc == 1) || (c->proc == 2) || (c->proc == 3) || (c->proc == 4) || c->l_filt_g1;
+    const int filt1 = (c->proc == 1) || (c->proc == 2) || (c->proc == 3) || (c->proc == 4) || (c->proc == 5) ||
+                      c->l_filt_g1;
     const int fast = c->proc == 3 || c->proc == 8;
     double* tb = (double*)malloc(sizeof(double) * (size_t)c->nk);
     /* up: V -> H_2 -> ... -> H_gm */
@@ -1047,6 +1356,10 @@ static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_
         if (g == 0 && !filt1) continue;
         if (c->proc == 4) {  /* whole columns: the caller runs one k-range */
             rad3_generation(c, S, U, G[g].tmp, I, J, c->a[g], c->b[g], tb);
+            continue;
+        }
+        if (c->proc == 5) {  /* whole columns too */
+            lin3_generation(c, S, U, G[g].tmp, I, J, c->a[g], c->b[g], g > 0);
             continue;
         }
         if (fast) {
@@ -1082,7 +1395,8 @@ int orc_filtering_procedure(const orc_cfg* c, double* Vd) {
     rc = setup(c, &S);
     if (rc) return rc;
     arr3 V = {Vd, c->nk, 1 - c->hx, c->I + c->hx, 1 - c->hy, c->J + c->hy};
-    const int zfilt = c->proc != 4 && c->l_vertical_filter && c->nzcol > 0;  /* rad3 has no separate z filter */
+    /* rad3 and lin3 have no separate z filter */
+    const int zfilt = c->proc != 4 && c->proc != 5 && c->l_vertical_filter && c->nzcol > 0;
     if (zfilt) vfilter(c, &S, V, 1);
     gen_t G[ORC_MAX_GEN];
     memset(G, 0, sizeof(G));
@@ -1091,7 +1405,7 @@ int orc_filtering_procedure(const orc_cfg* c, double* Vd) {
 #ifdef _OPENMP
     nth = c->nthreads > 0 ? c->nthreads : omp_get_max_threads();
     if (nth > c->nk) nth = c->nk;
-    if (c->proc == 4) nth = 1;
+    if (c->proc == 4 || c->proc == 5) nth = 1;
 #pragma omp parallel num_threads(nth)
     {
         int t = omp_get_thread_num(), nt = omp_get_num_threads();
@@ -1167,7 +1481,7 @@ int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double
     if (rc) return rc;
     /* proc 4: its adjoint side is not the transpose of its forward side;
      * proc 7: Bz^T M Bz^T, so the gy chain would need Bz, not Bz^T */
-    if (c->proc == 4 || c->proc == 7) return ORC_ERR_ARG;
+    if (c->proc == 4 || c->proc == 5 || c->proc == 7) return ORC_ERR_ARG;
     setup_t S;
     rc = setup(c, &S);
     if (rc) return rc;
@@ -1237,6 +1551,17 @@ int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y) 
         else fast_adjoint(c, &S, a, I, J, 0, nk);
         from_halo(&cc, V, y);
         free(V);
+        return ORC_OK;
+    }
+    if (which == 10) {
+        if (c->proc != 5) return ORC_ERR_ARG;
+        orc_cfg cc = *c; cc.I = I; cc.J = J;
+        double* V = to_halo(&cc, x);
+        arr3 a = {V, nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy};
+        arr3 t = a3_alloc(nk, 1 - c->hx, I + c->hx, 1 - c->hy, J + c->hy);
+        lin3_generation(c, &S, a, t, I, J, c->a[gen - 1], c->b[gen - 1], gen > 1);
+        from_halo(&cc, V, y);
+        a3_free(&t); free(V);
         return ORC_OK;
     }
     if (which == 8 || which == 9) {

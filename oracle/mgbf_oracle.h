@@ -46,7 +46,7 @@ typedef struct orc_cfg {
     double b[ORC_MAX_GEN];  /* Helmholtz Laplacian coefficients (reference: 0) */
     int lhelm;           /* use weighting_helm form                           */
     int proc;            /* 1 rad2_bckg, 6 rad2_ens, 3 fast_bckg, 8 fast_ens, 4 rad3, 2 lin2_bckg,
-                            7 lin2_ens */
+                            7 lin2_ens, 5 lin3 */
     int l_vertical_filter;
     int l_filt_g1;       /* procs 6 and 8 only                                */
     int lquart;          /* quadratic (3-point) interpolation                 */
@@ -84,7 +84,9 @@ int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double
  *        7 = fast-filter horizontal adjoint (rbetaT x, bocoTx, rbetaT y,
  *            bocoTy), on a generation-g grid,
  *        8 = proc 2 line filters forward (boco_2d + dibeta, colors 1..3),
- *        9 = their adjoint (dibetat + bocoT_2d, colors 3..1). */
+ *        9 = their adjoint (dibetat + bocoT_2d, colors 3..1),
+ *       10 = one whole generation of proc 5 (filtering_lin3: adjoint side,
+ *            weight a_gen, forward side; _g1 halo routines at gen 1). */
 int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y);
 
 /* Setup values (for tests): rmom2_1, rmom2_2, exx (1D), exx (2D), ss1, ss2,
@@ -100,6 +102,11 @@ int orc_dibeta_values(const orc_cfg* c, int gen[6], int h[3], double hs[3], doub
 /* The triad decomposition alone: asp = (A11, A22, A12) -> generators
  * lt = (dx0, dy0, dx1, dy1, dx2, dy2) and weights w. */
 int orc_triad(const double asp[3], int lt[6], double w[3]);
+
+/* The hexad decomposition: asp = (A11, A22, A33, A23, A31, A12) ->
+ * generators lh[3*(c-1)..3*(c-1)+2] and weights w[c-1] for colors c = 1..7
+ * (the hexad's own color null). */
+int orc_hexad(const double asp[6], int lh[21], double w[7]);
 
 /* ----------------------------------------------------------------------
  * Transfers between the analysis grid and the filter grid (the new map,

@@ -55,6 +55,8 @@ def _load():
         lib.orc_triad.argtypes = [dp, ip, dp]
         lib.orc_dibeta_values.restype = ctypes.c_int
         lib.orc_triad.restype = ctypes.c_int
+        lib.orc_hexad.argtypes = [dp, ip, dp]
+        lib.orc_hexad.restype = ctypes.c_int
         xp = ctypes.POINTER(_CXfer)
         lib.orc_anal_to_filt.argtypes = [xp, dp, dp]
         lib.orc_filt_to_anal.argtypes = [xp, dp, dp]
@@ -155,7 +157,7 @@ def weight_grads(cfg: OracleConfig, x: np.ndarray, gy: np.ndarray) -> np.ndarray
 
 
 (STAGE_Z_FWD, STAGE_Z_ADJ, STAGE_H_FWD, STAGE_H_ADJ, STAGE_RESTRICT, STAGE_PROLONG, STAGE_FAST_FWD,
- STAGE_FAST_ADJ, STAGE_LIN2_FWD, STAGE_LIN2_ADJ) = range(10)
+ STAGE_FAST_ADJ, STAGE_LIN2_FWD, STAGE_LIN2_ADJ, STAGE_LIN3_GEN) = range(11)
 DIB_NH = 6
 DIB_NFIL = DIB_NH + 2
 
@@ -195,6 +197,16 @@ def dibeta_values(cfg: OracleConfig) -> list:
     _check(_load().orc_dibeta_values(ctypes.byref(c), gen, h, _ptr(hs), _ptr(fil)), "orc_dibeta_values")
     return [{"d": (gen[2 * q], gen[2 * q + 1]), "h": h[q], "hs": float(hs[q]),
              "fil": fil[q * (DIB_NFIL + 1):q * (DIB_NFIL + 1) + h[q] + 1].copy()} for q in range(3)]
+
+
+def hexad(aspect) -> tuple:
+    """The hexad decomposition of (A11, A22, A33, A23, A31, A12): (generators
+    7x3 for colors 1..7, weights 7)."""
+    a = np.ascontiguousarray(aspect, dtype=np.float64)
+    lh = (ctypes.c_int * 21)()
+    w = np.zeros(7)
+    _check(_load().orc_hexad(_ptr(a), lh, _ptr(w)), "orc_hexad")
+    return np.array(list(lh)).reshape(7, 3), w
 
 
 def triad(aspect) -> tuple:

@@ -37,7 +37,7 @@ def oracle_cfg(c: MGBFConfig, proc: int, nthreads: int = 0) -> O.OracleConfig:
         I=c.nxPE * c.im_filt, J=c.nyPE * c.jm_filt, nk=km * c.n_ens,
         hx=c.hx, hy=c.hy, hz=c.hz, p=c.p, ampl01=c.mg_ampl01, ampl02=c.mg_ampl02, gm=gm,
         weights=gen_weights(c, gm), proc=proc, lm=c.lm,
-        nzcol=(c.km3 if proc == 4 else
+        nzcol=(c.km3 if proc in (4, 5) else
                ((c.km3 if proc in (1, 2, 3) else c.km3 * c.n_ens) if (c.l_vertical_filter and c.lm > 1) else 0)),
         l_vertical_filter=bool(c.l_vertical_filter and c.lm > 1), l_filt_g1=bool(c.l_filt_g1),
         lquart=bool(c.lquart), lhelm=bool(c.lhelm), nthreads=nthreads, ampl03=c.mg_ampl03)
