@@ -1,7 +1,7 @@
 """Literal emulation of the reference's MPI-decomposed filtering -- TEST
 INFRASTRUCTURE ONLY.
 
-A second, independent restatement of filtering_procedure(1|6) that keeps the
+A second, independent restatement of filtering_procedure(1|2|6|7) that keeps the
 reference's structure: every rank (nx, my) owns an im x jm tile with halos;
 halos are filled and folded by emulated point-to-point exchange in the
 reference's order; restriction output of 2x2 finer tiles is assembled into the
@@ -22,6 +22,9 @@ Followed routines (reference paths):
   vrbeta2/vrbeta2t   jp_pbfil.f90:888-928, 1011-1050
   sup_vrbeta1[T]_*   mg_filtering.f90:2042-2262
   filtering_rad2_bckg / _ens  mg_filtering.f90:560-680, 1000-1147
+  filtering_lin2_bckg / _ens  mg_filtering.f90:683-822, 1150-1313
+  vdibeta2/vdibeta2t jp_pbfil3.f90:1801-1837, 2345-2382 (as gather/scatter
+                     stencils over each color's generator)
 Arrays are numpy (J_ext, I_ext, nk) per tile: Fortran element (k, i, j) with
 i in 1-h..im+h sits at [j-1+h, i-1+h, k-1].
 """
@@ -247,6 +250,33 @@ def vfilter(V: np.ndarray, lm: int, nzcol: int, zst, adj: bool):
         V[..., c * lm:(c + 1) * lm] = B[..., hz:hz + lm]
 
 
+def line_colors(p: int, ampl02: float, nh: int = 6):
+    """Procs 2/7 (init_mg_line, mg_intstate.f90:436-480): the triad of the
+    Cholesky factor of the inverse aspect, (c, c, 0) with c = 1/sqrt(ampl02),
+    gives generators (1,0), (0,1), (-1,-1) with spreads^2 (c, c, 0); each
+    through hstform and blinfil (jp_pbfil3.f90:1399-1501).  Returned as
+    gather stencils (gx, gy, w) per color."""
+    bnorm, bsprd = np.zeros(nh + 1), np.zeros(nh + 1)
+    for h in range(1, nh + 1):
+        i = np.arange(-h, h + 1)
+        w = (1.0 - (i / h) ** 2) ** p
+        bnorm[h], bsprd[h] = 1.0 / w.sum(), (i * i * w).sum() / w.sum()
+    c = math.sqrt(1.0 / ampl02)
+    out = []
+    for (dx, dy), s2 in (((1, 0), c), ((0, 1), c), ((-1, -1), 0.0)):
+        m = next(m for m in range(2, nh + 1) if bsprd[m] >= s2)
+        hs = m - (bsprd[m] - s2) / (bsprd[m] - bsprd[m - 1])
+        h = int(hs)
+        hp = h + 1
+        fil = np.array([(hs - h) * bnorm[hp] * (1.0 - (t / hp) ** 2) ** p for t in range(h + 1)])
+        fil[:h] += np.array([(hp - hs) * bnorm[h] * (1.0 - (t / h) ** 2) ** p for t in range(h)])
+        st = [(0, 0, fil[0])]
+        for t in range(1, h + 1):
+            st += [(t * dx, t * dy, fil[t]), (-t * dx, -t * dy, fil[t])]
+        out.append(st)
+    return out
+
+
 def filtering(x: np.ndarray, *, nxPE, nyPE, im, jm, hx, p, ampl01, ampl02, weights, gm, proc=1, lm=1,
               nzcol=0, lquart=False, l_filt_g1=True) -> np.ndarray:
     """Apply filtering_procedure(proc) to the global compact field x
@@ -255,7 +285,8 @@ def filtering(x: np.ndarray, *, nxPE, nyPE, im, jm, hx, p, ampl01, ampl02, weigh
     assert I == nxPE * im and J == nyPE * jm
     h = hx
     st = radial_stencil(p, ampl02)
-    filt1 = proc == 1 or l_filt_g1
+    colors = line_colors(p, ampl02) if proc in (2, 7) else None  # filtering_lin2_bckg / _ens
+    filt1 = proc in (1, 2) or l_filt_g1
     hb = 1 if lquart else 2
     V = x.copy()
     if nzcol:
@@ -285,6 +316,20 @@ def filtering(x: np.ndarray, *, nxPE, nyPE, im, jm, hx, p, ampl01, ampl02, weigh
         if g == 0 and not filt1:
             continue
         L = gens[g]
+        if colors is not None:
+            # colors 3, 2, 1: dibetat + bocoT_2d; weighting; colors 1, 2, 3:
+            # boco_2d + dibeta (mg_filtering.f90:725-797, 1180-1290)
+            for cst in reversed(colors):
+                for k in L.keys():
+                    vrbeta2t(L[k], cst)
+                L.fold(h)
+            for k in L.keys():
+                L[k].interior()[...] *= weights[g]
+            for cst in colors:
+                L.fill(h)
+                for k in L.keys():
+                    vrbeta2(L[k], cst)
+            continue
         for k in L.keys():
             vrbeta2t(L[k], st)
         L.fold(h)
@@ -308,5 +353,6 @@ def filtering(x: np.ndarray, *, nxPE, nyPE, im, jm, hx, p, ampl01, ampl02, weigh
     for (tx, ty) in gens[0].keys():
         out[ty * jm:(ty + 1) * jm, tx * im:(tx + 1) * im] = gens[0][(tx, ty)].interior()
     if nzcol:
-        vfilter(out, lm, nzcol, line_stencil(p, ampl01), adj=False)
+        # filtering_lin2_ens (proc 7) ends with the adjoint vertical filter
+        vfilter(out, lm, nzcol, line_stencil(p, ampl01), adj=proc == 7)
     return out

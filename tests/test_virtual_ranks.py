@@ -16,6 +16,11 @@ CASES = [
     (4, 2, 8, 4, 6, False, False),
     (4, 4, 8, 3, 6, True, True),
     (8, 8, 4, 2, 1, False, True),
+    # line filters (procs 2 and 7): half-span 2 along x and y, identity diagonal
+    (2, 2, 8, 3, 2, False, True),
+    (4, 4, 6, 3, 2, True, True),
+    (4, 2, 8, 4, 7, False, False),
+    (4, 4, 8, 3, 7, True, True),
 ]
 
 
