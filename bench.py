@@ -496,7 +496,7 @@ def lin2_forward(torch, dev, dtype):
     (the triad of the Cholesky factor of the inverse aspect)."""
     from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig, _abi
     cfg = MGBFConfig(nxPE=16, nyPE=16, im_filt=48, jm_filt=48, lm=64, km3=1, km2=0, n_ens=1, gm_max=5,
-                     hx=12, hy=12, hz=4, p=2, mg_ampl02=0.3, mg_ampl01=ampl01(4),
+                     hx=12, hy=12, hz=4, p=2, mg_ampl02=0.3, mg_ampl01=ampl01(4), mgbf_line=True,
                      mg_weig1=1.0, mg_weig2=0.5, mg_weig3=0.25, mg_weig4=0.125, mg_weig5=0.0625, layout=1)
     op = MGBF(cfg)
     gen = torch.Generator(device=dev)

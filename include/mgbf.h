@@ -145,7 +145,9 @@ int mgbf_get_line_filters(const mgbf_handle* h, int gen[6], int hspan[3], double
  * three "dibeta" line filters of the triad decomposition, jp_pbfil3.f90,
  * of the Cholesky factor of the inverse aspect that init_mg_line sees;
  * MGBF_ERR_REACH when a line filter's spread is beyond the moment table or
- * its reach beyond the halo), and 7 = filtering_lin2_ens
+ * its reach beyond the halo; with mgbf_line off the reference never sets
+ * the line filters up and every one is a copy, here too), and
+ * 7 = filtering_lin2_ens
  * (mg_filtering.f90:1150-1313: the same line filters over the stacked
  * members, l_filt_g1 and lquart as for 6, ending like the reference with the
  * ADJOINT vertical filter sup_vrbeta1T_ens, so the operator is not

@@ -295,6 +295,16 @@ int orc_triad(const double asp[3], int lt_out[6], double w_out[3]) {
  * table cannot hold, or a reach beyond the halo is an error here; the
  * reference prints and carries on (or reads outside its arrays). */
 static int dibeta_setup(const orc_cfg* c, setup_t* s) {
+    if (!c->mgbf_line) {
+        /* init_mg_line did not run (mg_entrymod.f90:155-157): zero
+         * generators, vdibeta2's copy branch for every color */
+        for (int q = 0; q < 3; ++q) {
+            s->ddx[q] = s->ddy[q] = s->dh[q] = 0;
+            s->dhs[q] = 0.0;
+            for (int i = 0; i <= ORC_DIB_NFIL; ++i) s->dfil[q][i] = i == 0 ? 1.0 : 0.0;
+        }
+        return ORC_OK;
+    }
     double bnorm[ORC_DIB_NH + 1], bsprd[ORC_DIB_NH + 1];
     dib_moments(c->p, bnorm, bsprd);
     const double el = sqrt(1.0 / c->ampl02);
@@ -392,6 +402,8 @@ int orc_hexad(const double asp[6], int lh[21], double w7[7]) {
  * c3 = 1/sqrt(mg_ampl03); the hexad's six active colors in ascending order,
  * each spread^2 through the half-span transform and the two-beta weights. */
 static int hexad_setup(const orc_cfg* c, setup_t* s) {
+    for (int col = 0; col < 8; ++col) s->hslot[col] = -1;
+    if (!c->mgbf_line) return ORC_OK;  /* qcols stay zero: every color copies */
     double bnorm[ORC_DIB_NH + 1], bsprd[ORC_DIB_NH + 1];
     dib_moments(c->p, bnorm, bsprd);
     const double c3 = sqrt(1.0 / c->ampl03);

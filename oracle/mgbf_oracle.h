@@ -54,6 +54,7 @@ typedef struct orc_cfg {
     int nzcol;           /* number of z columns at offsets (k-1)*lm           */
     int nthreads;        /* OpenMP threads (<=0: runtime default)             */
     double ampl03;       /* mg_ampl03: aspect of the 3D filter (proc 4)       */
+    int mgbf_line;       /* init_mg_line ran (procs 2, 5, 7: else identities) */
 } orc_cfg;
 
 /* Error codes (negative), mirroring the library's. */

@@ -31,7 +31,7 @@ class _Cfg(ctypes.Structure):
         ("lhelm", ctypes.c_int), ("proc", ctypes.c_int),
         ("l_vertical_filter", ctypes.c_int), ("l_filt_g1", ctypes.c_int),
         ("lquart", ctypes.c_int), ("lm", ctypes.c_int), ("nzcol", ctypes.c_int),
-        ("nthreads", ctypes.c_int), ("ampl03", ctypes.c_double),
+        ("nthreads", ctypes.c_int), ("ampl03", ctypes.c_double), ("mgbf_line", ctypes.c_int),
     ]
 
 
@@ -95,6 +95,7 @@ class OracleConfig:
     helm_b: Optional[List[float]] = None
     nthreads: int = 0
     ampl03: float = 1.0
+    mgbf_line: bool = True
 
     def to_c(self) -> _Cfg:
         c = _Cfg()
@@ -114,6 +115,7 @@ class OracleConfig:
         c.nzcol = self.nzcol
         c.nthreads = self.nthreads
         c.ampl03 = float(self.ampl03)
+        c.mgbf_line = int(self.mgbf_line)
         return c
 
     def gen_shape(self, g: int):

@@ -242,6 +242,7 @@ struct Group {
     LStencil ls;         // fast filters' line beta (procs 3, 8)
     std::string ls_err;  // why ls is unusable (reach beyond hx/hy), or empty
     double ampl03 = 0;   // filtering_rad3's 3D ball (proc 4)
+    bool line = true;    // mgbf_line: init_mg_line sets the line filters up
     BStencil bs;
     std::string bs_err;
     DStencil ds;         // filtering_lin2_bckg's three line filters (proc 2)
@@ -736,9 +737,19 @@ int build_group(Plan& P, Group& G, bool zneeded) {
     } else {
         G.bs_err = "mg_ampl03 must be positive";
     }
-    // filtering_lin2_bckg's line filters: an error only when proc 2 runs
+    // filtering_lin2_bckg's line filters: an error only when proc 2 runs.
+    // Without mgbf_line the reference never calls init_mg_line: the
+    // generators stay zero (mg_intstate.f90:190-191) and every color is
+    // vdibeta2's copy branch, an identity (half-span 0, weight 1 here).
     G.ds_err.clear();
-    G.ds_rc = build_dstencil(G.p, G.ampl02, G.hx, G.hy, G.ds, err);
+    if (!G.line) {
+        G.ds = DStencil{};
+        for (int q = 0; q < 3; ++q) G.ds.fil[q][0] = 1.0;
+        G.ds.ok = true;
+        G.ds_rc = 0;
+    } else {
+        G.ds_rc = build_dstencil(G.p, G.ampl02, G.hx, G.hy, G.ds, err);
+    }
     if (G.ds_rc) {
         G.ds_err = err;
         G.ds.ok = false;
@@ -1063,6 +1074,7 @@ int mgbf_create(const mgbf_config* cfg, mgbf_handle** out) {
     G.nk = km_all; G.lm = c.lm; G.nzcol = c.km3 * c.n_ens;
     G.hx = c.hx; G.hy = c.hy; G.hz = c.hz; G.p = c.p;
     G.ampl01 = c.mg_ampl01; G.ampl02 = c.mg_ampl02; G.ampl03 = c.mg_ampl03;
+    G.line = c.mgbf_line != 0;
     if ((rc = build_group(P, G, zneeded))) return rc;
     if ((rc = build_interps(P))) return rc;
     h->field_elems = c.layout == MGBF_LAYOUT_HALO

@@ -40,7 +40,8 @@ def oracle_cfg(c: MGBFConfig, proc: int, nthreads: int = 0) -> O.OracleConfig:
         nzcol=(c.km3 if proc in (4, 5) else
                ((c.km3 if proc in (1, 2, 3) else c.km3 * c.n_ens) if (c.l_vertical_filter and c.lm > 1) else 0)),
         l_vertical_filter=bool(c.l_vertical_filter and c.lm > 1), l_filt_g1=bool(c.l_filt_g1),
-        lquart=bool(c.lquart), lhelm=bool(c.lhelm), nthreads=nthreads, ampl03=c.mg_ampl03)
+        lquart=bool(c.lquart), lhelm=bool(c.lhelm), nthreads=nthreads, ampl03=c.mg_ampl03,
+        mgbf_line=bool(c.mgbf_line))
 
 
 def rel_l2(a, b) -> float:

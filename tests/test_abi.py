@@ -162,7 +162,7 @@ def test_line_filter_procedure_validation(lib):
     # spread^2 1/sqrt(0.035) = 5.3 lies beyond the table's largest (half-span
     # 6: 5.14); the fast filters' line reach 75 that every handle checks
     # (def_mg_weights) needs the 80-point halo
-    op = MGBF(small_config(mg_ampl02=0.035, hx=80, hy=80, im_filt=32, jm_filt=32, gm_max=1))
+    op = MGBF(small_config(mg_ampl02=0.035, hx=80, hy=80, im_filt=32, jm_filt=32, gm_max=1, mgbf_line=True))
     with pytest.raises(MGBFError) as e:
         op.filtering_procedure(2, np.zeros(op.field_shape()))
     assert e.value.code == _abi.MGBF_ERR_REACH
@@ -181,7 +181,7 @@ def test_line_filter_setup_matches_oracle(lib, p, ampl02):
     disk = int(np.floor(np.sqrt((2 * p + 4) * ampl02) - 1e-12))
     h = max(4, line, disk)
     c = small_config(p=p, mg_ampl02=ampl02, hx=h, hy=h, nxPE=1, nyPE=1, im_filt=64, jm_filt=64, gm_max=2,
-                     mg_ampl01=canonical_z(2, p), mg_ampl03=0.3)
+                     mg_ampl01=canonical_z(2, p), mg_ampl03=0.3, mgbf_line=True)
     got = MGBF(c).line_filters()
     ref = O.dibeta_values(oracle_cfg(c, 2))
     for g, r in zip(got, ref):
@@ -191,10 +191,18 @@ def test_line_filter_setup_matches_oracle(lib, p, ampl02):
 
 
 def test_line_filter_setup_error_is_reported(lib):
-    op = MGBF(small_config(mg_ampl02=0.035, hx=80, hy=80, im_filt=32, jm_filt=32, gm_max=1))
+    op = MGBF(small_config(mg_ampl02=0.035, hx=80, hy=80, im_filt=32, jm_filt=32, gm_max=1, mgbf_line=True))
     with pytest.raises(MGBFError) as e:
         op.line_filters()
     assert e.value.code == _abi.MGBF_ERR_REACH
+
+
+def test_line_filters_are_identities_without_mgbf_line(lib):
+    """mgbf_line off: init_mg_line does not run (mg_entrymod.f90:155-157),
+    so no table limit applies and every color is a copy."""
+    op = MGBF(small_config(mg_ampl02=0.035, hx=80, hy=80, im_filt=32, jm_filt=32, gm_max=1, mgbf_line=False))
+    for col in op.line_filters():
+        assert col["h"] == 0 and col["fil"].tolist() == [1.0]
 
 
 def test_adjoint_of_rad3_is_refused(lib):

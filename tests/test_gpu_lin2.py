@@ -18,8 +18,9 @@ TOL = {torch.float64: 1e-12, torch.float32: 1e-5, torch.bfloat16: 2e-2}
 
 
 def lin2_config(**kw):
-    # colors along x and y with half-span 2 (spread^2 0.63), identity diagonal
-    d = dict(layout=_abi.MGBF_LAYOUT_COMPACT)
+    # mgbf_line on (init_mg_line runs): colors along x and y with half-span 2
+    # (spread^2 0.63), identity diagonal
+    d = dict(layout=_abi.MGBF_LAYOUT_COMPACT, mgbf_line=True)
     d.update(kw)
     return small_config(**d)
 
@@ -98,6 +99,16 @@ def test_lin2_weight_grads(lib, cuda):
     oc = oracle_cfg(c, 2)
     assert np.allclose(ga, O.weight_grads(oc, x, gy), rtol=1e-10, atol=1e-10)
     assert rel_l2(gx.cpu().numpy(), O.filter_compact(oc, gy)) < 1e-12
+
+
+@pytest.mark.parametrize("proc", [2, 7])
+def test_lin2_without_mgbf_line_is_identity_filtering(lib, cuda, proc):
+    """mgbf_line off: init_mg_line never runs, the generators stay zero and
+    every color copies (vdibeta2's zero-generator branch)."""
+    c = lin2_config(mgbf_line=False, n_ens=2 if proc == 7 else 1)
+    op = MGBF(c)
+    x = np.random.default_rng(57).standard_normal(op.field_shape())
+    assert rel_l2(run(op, x, torch.float64, proc=proc), O.filter_compact(oracle_cfg(c, proc), x)) < 1e-12
 
 
 def test_lin2_host_memory(lib, cuda):

@@ -234,3 +234,13 @@ def test_proc7_weight_grads_refused():
     c = cfg(proc=7)
     with pytest.raises(O.OracleError):
         O.weight_grads(c, np.zeros((c.J, c.I, c.nk)), np.zeros((c.J, c.I, c.nk)))
+
+
+@pytest.mark.parametrize("proc", [2, 7])
+def test_identity_filters_without_mgbf_line(proc):
+    """mgbf_line off: zero generators, every color copies, so one
+    generation without a vertical filter is the weight alone."""
+    c = cfg(proc=proc, mgbf_line=False, weights=[0.7], ampl02=0.02)  # no table limit applies
+    x = rng.standard_normal((c.J, c.I, c.nk))
+    assert np.abs(O.filter_compact(c, x) - 0.7 * x).max() < 1e-15
+    assert all(d["h"] == 0 and d["fil"].tolist() == [1.0] for d in O.dibeta_values(c))

@@ -208,3 +208,18 @@ def test_lin3_setup_errors():
         O.filter_compact(cfg(hz=1, lm=4), np.zeros((12, 16, 9)))
     with pytest.raises(O.OracleError):  # weight gradients: not self-adjoint
         O.weight_grads(cfg(), np.zeros((12, 16, 9)), np.zeros((12, 16, 9)))
+
+
+def test_identity_filters_without_mgbf_line():
+    """mgbf_line off: every color copies, so only the halo routines act.
+    bocoT_3d_g1's east and north folds add the edge column and row to
+    themselves once per adjoint color: seven colors scale the 3D variables'
+    east column and north row by 2^7 and their north-east corner by 4^7,
+    as the reference does; the 2D variables and the rest are the weight."""
+    c = cfg(mgbf_line=False, weights=[0.7])
+    x = rng.standard_normal((c.J, c.I, c.nk))
+    n3 = c.nzcol * c.lm
+    m = np.ones((c.J, c.I, c.nk))
+    m[:, -1, :n3] *= 2.0 ** 7
+    m[-1, :, :n3] *= 2.0 ** 7
+    assert np.abs(O.filter_compact(c, x) - 0.7 * m * x).max() < 1e-12 * np.abs(0.7 * m * x).max()
