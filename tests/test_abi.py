@@ -70,6 +70,19 @@ def test_namelist_parse(lib, tmp_path):
     assert (c.nxPE, c.nyPE, c.im_filt, c.jm_filt) == (20, 20, 64, 32)
 
 
+def test_namelist_mgbf_line_reaches_the_line_filter_setup(lib, tmp_path):
+    """mgbf_line from the namelist decides whether procs 2/5/7 get the triad
+    line filters (init_mg_line) or copies, as mg_entrymod.f90:155-157 does."""
+    text = NML.replace("mgbf_line=.false., mgbf_proc=6, n_ens=20", "mgbf_line=.true., mgbf_proc=2, n_ens=1")
+    c = MGBFConfig.from_namelist(write(tmp_path, text))
+    assert c.mgbf_line and c.mgbf_proc == 2
+    cols = MGBF(c).line_filters()
+    assert [col["d"] for col in cols] == [(1, 0), (0, 1), (-1, -1)]
+    assert cols[0]["h"] >= 1 and abs(cols[0]["fil"][0] + 2 * cols[0]["fil"][1:].sum() - 1.0) < 1e-14
+    c_off = MGBFConfig.from_namelist(write(tmp_path, NML, "off.nml"))
+    assert all(col["h"] == 0 for col in MGBF(c_off).line_filters())
+
+
 def test_namelist_case_and_fortran_exponents(lib, tmp_path):
     text = NML.replace("&PARAMETERS_MGBETA", "&parameters_mgbeta").replace("mg_ampl01=2.0", "MG_AMPL01=2.0D0")
     c = MGBFConfig.from_namelist(write(tmp_path, text))
