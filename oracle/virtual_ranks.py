@@ -1,7 +1,7 @@
 """Literal emulation of the reference's MPI-decomposed filtering -- TEST
 INFRASTRUCTURE ONLY.
 
-A second, independent restatement of filtering_procedure(1|2|6|7) that keeps the
+A second, independent restatement of filtering_procedure(1|2|5|6|7) that keeps the
 reference's structure: every rank (nx, my) owns an im x jm tile with halos;
 halos are filled and folded by emulated point-to-point exchange in the
 reference's order; restriction output of 2x2 finer tiles is assembled into the
@@ -277,19 +277,172 @@ def line_colors(p: int, ampl02: float, nh: int = 6):
     return out
 
 
+def dibeta_weights(p: int, s2: float, nh: int = 6) -> np.ndarray:
+    """hstform + blinfil (jp_pbfil3.f90:1399-1501) of one spread^2."""
+    bnorm, bsprd = np.zeros(nh + 1), np.zeros(nh + 1)
+    for h in range(1, nh + 1):
+        i = np.arange(-h, h + 1)
+        w = (1.0 - (i / h) ** 2) ** p
+        bnorm[h], bsprd[h] = 1.0 / w.sum(), (i * i * w).sum() / w.sum()
+    m = next(m for m in range(2, nh + 1) if bsprd[m] >= s2)
+    hs = m - (bsprd[m] - s2) / (bsprd[m] - bsprd[m - 1])
+    h = int(hs)
+    hp = h + 1
+    fil = np.array([(hs - h) * bnorm[hp] * (1.0 - (t / hp) ** 2) ** p for t in range(h + 1)])
+    fil[:h] += np.array([(hp - hs) * bnorm[h] * (1.0 - (t / h) ** 2) ** p for t in range(h)])
+    return fil
+
+
+class Layout3:
+    """Proc 5's 3D variables on every tile of a generation: arrays
+    (jm+2h, im+2h, (lm+2hz)*nv), last axis (L+hz-1)*nv + v."""
+
+    def __init__(self, L2: "Layout", nv: int, lm: int, hz: int):
+        self.L2, self.nv, self.lm, self.hz = L2, nv, lm, hz
+        self.t = {}
+        for k, T in L2.t.items():
+            a = np.zeros(T.a.shape[:2] + ((lm + 2 * hz) * nv,))
+            for L in range(1, lm + 1):
+                a[..., (L + hz - 1) * nv:(L + hz) * nv] = T.a[..., [v * lm + L - 1 for v in range(nv)]]
+            self.t[k] = a
+
+    def back(self):
+        for k, T in self.L2.t.items():
+            a = self.t[k]
+            for L in range(1, self.lm + 1):
+                T.a[..., [v * self.lm + L - 1 for v in range(self.nv)]] = a[..., (L + self.hz - 1) * self.nv:
+                                                                             (L + self.hz) * self.nv]
+
+    def zl(self, L):
+        return slice((L + self.hz - 1) * self.nv, (L + self.hz) * self.nv)
+
+    def zmirror(self):
+        for a in self.t.values():
+            for L in range(1, self.hz + 1):
+                a[..., self.zl(1 - L)] = a[..., self.zl(1 + L)]
+                a[..., self.zl(self.lm + L)] = a[..., self.zl(self.lm - L)]
+
+    def fill(self, nb, gh):
+        """boco_3d (mg_bocos.f90:1425-2170) on levels 1..lm: N/S rows, then
+        E/W columns; physical east edge W(I+i) = W(I-i) at generation 1
+        (_g1), W(I+1-i) at coarser ones (_gh, which then mirrors z)."""
+        L2, ks = self.L2, slice(self.hz * self.nv, (self.hz + self.lm) * self.nv)
+        ny, nx = L2.nty, L2.ntx
+        snap = {k: a.copy() for k, a in self.t.items()}
+        for (x, y), a in self.t.items():
+            T = L2[(x, y)]
+            h, im, jm = T.h, T.im, T.jm
+            ci = slice(h, h + im)
+            for j in range(1, nb + 1):
+                a[h + jm - 1 + j, ci, ks] = (snap[(x, y)][h + jm - j, ci, ks] if y == ny - 1
+                                             else snap[(x, y + 1)][h + j - 1, ci, ks])
+                a[h - j, ci, ks] = (snap[(x, y)][h + j - 1, ci, ks] if y == 0
+                                    else snap[(x, y - 1)][h + jm - j, ci, ks])
+        snap = {k: a.copy() for k, a in self.t.items()}
+        for (x, y), a in self.t.items():
+            T = L2[(x, y)]
+            h, im, jm = T.h, T.im, T.jm
+            rj = slice(h - nb, h + jm + nb)
+            for i in range(1, nb + 1):
+                a[rj, h - i, ks] = (snap[(x, y)][rj, h + i - 1, ks] if x == 0
+                                    else snap[(x - 1, y)][rj, h + im - i, ks])
+                src = h + im - i if gh else h + im - i - 1
+                a[rj, h + im - 1 + i, ks] = (snap[(x, y)][rj, src, ks] if x == nx - 1
+                                             else snap[(x + 1, y)][rj, h + i - 1, ks])
+        if gh:
+            self.zmirror()
+
+    def fold(self, nb, gh):
+        """bocoT_3d (mg_bocos.f90:2173-2908): E/W columns on every row, N/S
+        rows on the interior columns (levels 1..lm), then the z halo.  At
+        generation 1 the physical east and north folds read one cell
+        inward: W(I+hx-i), W(J+hy-j)."""
+        L2, ks = self.L2, slice(self.hz * self.nv, (self.hz + self.lm) * self.nv)
+        ny, nx = L2.nty, L2.ntx
+        o = 0 if gh else 1
+        snap = {k: a.copy() for k, a in self.t.items()}
+        for (x, y), a in self.t.items():
+            T = L2[(x, y)]
+            h, im, jm = T.h, T.im, T.jm
+            rj = slice(h - nb, h + jm + nb)
+            for i in range(1, nb + 1):
+                a[rj, h + i - 1, ks] += (snap[(x, y)][rj, h - i, ks] if x == 0
+                                         else snap[(x - 1, y)][rj, h + im - 1 + i, ks])
+                a[rj, h + im - i, ks] += (snap[(x, y)][rj, h + im - 1 + i - o, ks] if x == nx - 1
+                                          else snap[(x + 1, y)][rj, h - i, ks])
+        snap = {k: a.copy() for k, a in self.t.items()}
+        for (x, y), a in self.t.items():
+            T = L2[(x, y)]
+            h, im, jm = T.h, T.im, T.jm
+            ci = slice(h, h + im)
+            for j in range(1, nb + 1):
+                a[h + j - 1, ci, ks] += (snap[(x, y)][h - j, ci, ks] if y == 0
+                                         else snap[(x, y - 1)][h + jm - 1 + j, ci, ks])
+                a[h + jm - j, ci, ks] += (snap[(x, y)][h + jm - 1 + j - o, ci, ks] if y == ny - 1
+                                          else snap[(x, y + 1)][h - j, ci, ks])
+        for a in self.t.values():
+            for L in range(1, self.hz + 1):
+                a[..., self.zl(1 + L)] += a[..., self.zl(1 - L)]
+                a[..., self.zl(self.lm - L)] += a[..., self.zl(self.lm + L)]
+
+    def dib(self, color, adj):
+        """vdibetax3 / vdibetax3t of one color on every tile (None: copy)."""
+        nv, hz, lm = self.nv, self.hz, self.lm
+        for k, a in self.t.items():
+            T = self.L2[k]
+            h, im, jm = T.h, T.im, T.jm
+            b = np.zeros_like(a)
+            inner = (slice(h, h + jm), slice(h, h + im), slice(hz * nv, (hz + lm) * nv))
+
+            def sh(t, d):
+                dx, dy, dz = d
+                return (slice(h + t * dy, h + t * dy + jm), slice(h + t * dx, h + t * dx + im),
+                        slice((hz + t * dz) * nv, (hz + t * dz + lm) * nv))
+
+            if color is None:
+                b[inner] = a[inner]
+            else:
+                d, fil = color
+                if not adj:
+                    b[inner] = fil[0] * a[inner]
+                    for t in range(1, len(fil)):
+                        b[inner] += fil[t] * (a[sh(t, d)] + a[sh(-t, d)])
+                else:
+                    b[inner] += fil[0] * a[inner]
+                    for t in range(1, len(fil)):
+                        b[sh(t, d)] += fil[t] * a[inner]
+                        b[sh(-t, d)] += fil[t] * a[inner]
+            self.t[k] = b
+
+
+def sub_layout(L: "Layout", k0: int, k1: int) -> "Layout":
+    """The levels [k0, k1) of every tile as a Layout of copies."""
+    S = Layout(L.ntx, L.nty, k1 - k0, next(iter(L.t.values())).im, next(iter(L.t.values())).jm,
+               next(iter(L.t.values())).h)
+    for k, T in L.t.items():
+        S[k].a = T.a[..., k0:k1].copy()
+    return S
+
+
 def filtering(x: np.ndarray, *, nxPE, nyPE, im, jm, hx, p, ampl01, ampl02, weights, gm, proc=1, lm=1,
-              nzcol=0, lquart=False, l_filt_g1=True) -> np.ndarray:
+              nzcol=0, lquart=False, l_filt_g1=True, ampl03=1.0, hz=1) -> np.ndarray:
     """Apply filtering_procedure(proc) to the global compact field x
     (J, I, nk) through the emulated rank tiles; returns the global result."""
     J, I, nk = x.shape
     assert I == nxPE * im and J == nyPE * jm
     h = hx
     st = radial_stencil(p, ampl02)
-    colors = line_colors(p, ampl02) if proc in (2, 7) else None  # filtering_lin2_bckg / _ens
-    filt1 = proc in (1, 2) or l_filt_g1
+    colors = line_colors(p, ampl02) if proc in (2, 5, 7) else None  # filtering_lin2_* / lin3
+    if proc == 5:  # the hexad of (c3, c3, c3, 0, 0, 0): x, y, z lines, identity diagonals, color 7 null
+        c3 = math.sqrt(1.0 / ampl03)
+        hexcols = {1: ((1, 0, 0), dibeta_weights(p, c3)), 2: ((0, 1, 0), dibeta_weights(p, c3)),
+                   3: ((0, 0, 1), dibeta_weights(p, c3)), 4: ((1, -1, 0), dibeta_weights(p, 0.0)),
+                   5: ((-1, 0, 1), dibeta_weights(p, 0.0)), 6: ((0, 1, -1), dibeta_weights(p, 0.0)), 7: None}
+    filt1 = proc in (1, 2, 5) or l_filt_g1
+    zfilt = nzcol and proc != 5  # filtering_lin3 has no separate vertical filter
     hb = 1 if lquart else 2
     V = x.copy()
-    if nzcol:
+    if zfilt:
         vfilter(V, lm, nzcol, line_stencil(p, ampl01), adj=True)
     # generation layouts: gen g has (nxPE >> (g-1)) x (nyPE >> (g-1)) full tiles
     gens: List[Layout] = []
@@ -316,6 +469,39 @@ def filtering(x: np.ndarray, *, nxPE, nyPE, im, jm, hx, p, ampl01, ampl02, weigh
         if g == 0 and not filt1:
             continue
         L = gens[g]
+        if proc == 5:
+            # filtering_lin3 (mg_filtering.f90:285-535): 2D variables as
+            # proc 2, 3D variables through the seven colors; _g1 halo
+            # routines at generation 1, _gh at coarser ones
+            n3 = nzcol * lm
+            S2 = sub_layout(L, n3, nk)
+            for cst in reversed(colors):
+                for k in S2.keys():
+                    vrbeta2t(S2[k], cst)
+                S2.fold(h)
+            L3 = Layout3(L, nzcol, lm, hz)
+            for col in range(7, 0, -1):
+                L3.zmirror()
+                L3.dib(hexcols[col], True)
+                L3.fold(h, g > 0)
+            L3.back()
+            for k in L.keys():
+                L[k].a[..., n3:] = S2[k].a
+                L[k].interior()[...] *= weights[g]
+            S2 = sub_layout(L, n3, nk)
+            for cst in colors:
+                S2.fill(h)
+                for k in S2.keys():
+                    vrbeta2(S2[k], cst)
+            L3 = Layout3(L, nzcol, lm, hz)
+            L3.zmirror()
+            for col in range(1, 8):
+                L3.fill(h, g > 0)
+                L3.dib(hexcols[col], False)
+            L3.back()
+            for k in L.keys():
+                L[k].a[..., n3:] = S2[k].a
+            continue
         if colors is not None:
             # colors 3, 2, 1: dibetat + bocoT_2d; weighting; colors 1, 2, 3:
             # boco_2d + dibeta (mg_filtering.f90:725-797, 1180-1290)
@@ -352,7 +538,7 @@ def filtering(x: np.ndarray, *, nxPE, nyPE, im, jm, hx, p, ampl01, ampl02, weigh
     out = np.empty_like(V)
     for (tx, ty) in gens[0].keys():
         out[ty * jm:(ty + 1) * jm, tx * im:(tx + 1) * im] = gens[0][(tx, ty)].interior()
-    if nzcol:
+    if zfilt:
         # filtering_lin2_ens (proc 7) ends with the adjoint vertical filter
         vfilter(out, lm, nzcol, line_stencil(p, ampl01), adj=proc == 7)
     return out

@@ -53,3 +53,23 @@ def test_stencil_setup_matches_oracle():
     v = O.setup_values(oc)
     s_vr = [w for g, gy, w in st if g == 0 and gy == 0][0]
     assert s_vr == pytest.approx(v["ss2"], rel=1e-14)
+
+
+@pytest.mark.parametrize("nxPE,nyPE,tile,hx,lquart", [(2, 2, 8, 4, False), (4, 2, 8, 4, True), (4, 4, 8, 3, False)])
+def test_virtual_ranks_match_global_oracle_lin3(nxPE, nyPE, tile, hx, lquart):
+    """Proc 5: the 3D halo routines' generation-1 index forms act at the
+    physical east and north edges only; rank boundaries exchange exactly."""
+    gm = min(VR.def_maxgen(nxPE, nyPE), 3)
+    I, J = nxPE * tile, nyPE * tile
+    lm, nzcol, km2, hz = 4, 2, 1, 3
+    nk = lm * nzcol + km2
+    w = [1.0, 0.5, 0.25][:gm]
+    ampl02 = canonical(hx)
+    x = np.random.default_rng(nxPE * 10 + tile).standard_normal((J, I, nk))
+    y_vr = VR.filtering(x, nxPE=nxPE, nyPE=nyPE, im=tile, jm=tile, hx=hx, p=2, ampl01=1.0, ampl02=ampl02,
+                        weights=w, gm=gm, proc=5, lm=lm, nzcol=nzcol, lquart=lquart, ampl03=0.6, hz=hz)
+    oc = O.OracleConfig(I=I, J=J, nk=nk, hx=hx, hy=hx, hz=hz, p=2, ampl01=1.0, ampl02=ampl02, gm=gm,
+                        weights=w, proc=5, lm=lm, nzcol=nzcol, lquart=lquart, ampl03=0.6,
+                        l_vertical_filter=False)
+    y_or = O.filter_compact(oc, x)
+    assert np.abs(y_vr - y_or).max() <= 1e-12 * np.abs(y_or).max()
