@@ -146,8 +146,9 @@ def numpy_lin2_g1(c, V):
 
 
 @pytest.mark.parametrize("ampl02", [0.5, 1.0])
-def test_one_generation_matches_numpy(ampl02):
-    c = cfg(ampl02=ampl02)
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_one_generation_matches_numpy(ampl02, p):
+    c = cfg(ampl02=ampl02, p=p)
     V = rng.standard_normal((c.J + 2 * c.hy, c.I + 2 * c.hx, c.nk))
     ref = numpy_lin2_g1(c, V)
     got = V.copy()

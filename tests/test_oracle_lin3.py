@@ -176,9 +176,11 @@ def test_hexad_reconstructs_positive_definite_aspects():
 
 
 @pytest.mark.parametrize("gen", [1, 2])
-def test_one_generation_matches_numpy(gen):
-    """Generation 1 uses boco_3d_g1 / bocoT_3d_g1, generation 2 the _gh forms."""
-    c = cfg(gm=2, weights=[0.7, 0.4])
+@pytest.mark.parametrize("p,ampl03,hz", [(2, 0.6, 3), (1, 1.5, 2), (3, 0.35, 4)])
+def test_one_generation_matches_numpy(gen, p, ampl03, hz):
+    """Generation 1 uses boco_3d_g1 / bocoT_3d_g1, generation 2 the _gh forms;
+    z-line half-spans 2 to 4."""
+    c = cfg(gm=2, weights=[0.7, 0.4], p=p, ampl03=ampl03, hz=hz, lm=max(4, hz + 1), nk=2 * max(4, hz + 1) + 1)
     J, I = c.J >> (gen - 1), c.I >> (gen - 1)
     V = np.zeros((J + 2 * c.hy, I + 2 * c.hx, c.nk))
     V[c.hy:c.hy + J, c.hx:c.hx + I] = rng.standard_normal((J, I, c.nk))
