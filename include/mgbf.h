@@ -206,6 +206,15 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
  * Synchronises with the device and clears the status. */
 int mgbf_status(mgbf_handle* h);
 
+/* Polls of a row's mbarrier before a TMA-fed radial kernel gives up
+ * (default 2^20, restored by polls < 0; no reference counterpart: the
+ * reference has no device waits).  A block that gives up records
+ * MGBF_ERR_TIMEOUT for mgbf_status, waits for its own copies still in
+ * flight and returns; its output rows are then incomplete.  polls = 0 makes
+ * every such wait give up at once, which lets a test exercise that path on
+ * a healthy GPU. */
+int mgbf_set_wait_limit(mgbf_handle* h, int polls);
+
 /* Autotuner of tile shapes: times the radial-filter kernel variants (TMA
  * pipelines of one or two rows per barrier, cp.async staging) and output
  * rows per block for every generation and pass of the handle, on the
@@ -297,6 +306,10 @@ int mgbf_batch_set_procedure(mgbf_batch* b, int mg_filt);
 
 /* As mgbf_status, for a batch. */
 int mgbf_batch_status(mgbf_batch* b);
+/* As mgbf_set_weights, for a batch (releases graphs captured before). */
+int mgbf_batch_set_weights(mgbf_batch* b, const double* a, int n);
+/* As mgbf_set_wait_limit, for a batch (releases graphs captured before). */
+int mgbf_batch_set_wait_limit(mgbf_batch* b, int polls);
 /* As mgbf_autotune, for a batch (releases graphs captured before). */
 int mgbf_batch_autotune(mgbf_batch* b, int dtype, void* stream);
 
@@ -318,7 +331,8 @@ int mgbf_batch_autotune(mgbf_batch* b, int dtype, void* stream);
  * support must be the disk of radius reach+1/2 with p = 2 and a compiled
  * reach (4,5,6,8,10,12,16,24), else MGBF_ERR_UNSUPPORTED.  The first call on
  * a device looks up the array's device address and should come before any
- * stream capture.  Calls share the array, so calls that overlap on the GPU
+ * stream capture (a lookup that fails returns MGBF_ERR_CUDA and is retried
+ * by the next call).  Calls share the array, so calls that overlap on the GPU
  * race and must be ordered by the caller.  Asynchronous on `stream`.
  */
 #define MGBF_NOALLOC_MAX_ELEMS ((size_t)8 << 20)

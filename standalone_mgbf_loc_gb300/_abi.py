@@ -104,6 +104,9 @@ SIGNATURES = {
     "mgbf_filt_to_anal": (_I, [_HP, _VP, _VP, _I, _I, _VP]),
     "mgbf_set_tuning": (_I, [_HP, _I, _I, _I]),
     "mgbf_batch_autotune": (_I, [_HP, _I, _VP]),
+    "mgbf_set_wait_limit": (_I, [_HP, _I]),
+    "mgbf_batch_set_wait_limit": (_I, [_HP, _I]),
+    "mgbf_batch_set_weights": (_I, [_HP, ctypes.POINTER(_D), _I]),
     "mgbf_radial_filter_noalloc": (_I, [_VP, _VP, _I, _I, _I, _I, _D, _I, _I, _D, _VP]),
     "mgbf_timers_enable": (_I, [_I]),
     "mgbf_timers_read": (_I, [ctypes.POINTER(MgbfTimerStat), _I, ctypes.POINTER(_I)]),

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "../../include/mgbf.h"
+#include "mgbf_common.cuh"
 #include "mgbf_kernels.cuh"
 #include "mgbf_setup.hpp"
 
@@ -276,6 +277,7 @@ struct Plan {
     DevBuf dot;     // one double per generation
     DevBuf status;  // device status word of bounded waits
     int device = 0;
+    int wait_polls = kDefaultWaitPolls;  // mbarrier polls per row before a TMA-fed kernel gives up
 };
 
 int gen_I(const Plan& P, int g) { return P.I >> g; }
@@ -481,7 +483,7 @@ struct Exec {
         const int I = gen_I(P, g), J = gen_J(P, g);
         const int tx = hmom_tx_for((int)acc_size(t), G.hs.R);
         const long long w0 = (long long)((G.nk + 31) / 32) * ((I + tx - 1) / tx);
-        const long long nz = (152LL * 24 + w0 - 1) / w0;
+        const long long nz = ((long long)device_sm_count() * 24 + w0 - 1) / w0;
         const int rows = (int)((J + nz - 1) / nz);
         return std::max(rows, std::min(J, 4 * G.hs.R));
     }
@@ -492,6 +494,7 @@ struct Exec {
         a.mirror_hx = mirror; a.scale = scale * G.hs.s; a.halo = G.HXP;
         a.tmap = tmap(g, which_in);
         a.status = static_cast<int*>(P.status.p);
+        a.max_polls = P.wait_polls;
         a.variant = variant;
         a.rows = rows;
         LK(launch_hmom(t, G.hs.R, G.hs.p, a, G.hs.mom, stream));
@@ -1638,6 +1641,21 @@ int mgbf_batch_status(mgbf_batch* b) {
     return read_status(b->plan);
 }
 
+int mgbf_set_wait_limit(mgbf_handle* h, int polls) {
+    if (!h) return fail(MGBF_ERR_ARG, "null handle");
+    h->plan.wait_polls = polls < 0 ? kDefaultWaitPolls : polls;
+    return MGBF_OK;
+}
+
+int mgbf_batch_set_wait_limit(mgbf_batch* b, int polls) {
+    if (!b) return fail(MGBF_ERR_ARG, "null handle");
+    DeviceGuard dg(b->plan.device);
+    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);  // captured with the old limit
+    b->graphs.clear();
+    b->plan.wait_polls = polls < 0 ? kDefaultWaitPolls : polls;
+    return MGBF_OK;
+}
+
 int mgbf_autotune(mgbf_handle* h, int dtype, void* stream) {
     if (!h) return fail(MGBF_ERR_ARG, "null handle");
     if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");
@@ -1797,6 +1815,15 @@ int mgbf_batch_apply(mgbf_batch* b, void* const* fields, int dtype, int adjoint,
     if (ec != cudaSuccess) return cuda_fail(ec, "cudaGraphInstantiate");
     b->graphs.push_back(e);
     CU(cudaGraphLaunch(e.exec, s));
+    return MGBF_OK;
+}
+
+int mgbf_batch_set_weights(mgbf_batch* b, const double* a, int n) {
+    if (!b || !a || n < 1 || n > b->plan.gm) return fail(MGBF_ERR_ARG, "bad weights");
+    DeviceGuard dg(b->plan.device);
+    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);  // captured with the old weights
+    b->graphs.clear();
+    for (int g = 0; g < n; ++g) b->plan.a[g] = a[g];
     return MGBF_OK;
 }
 

@@ -96,6 +96,27 @@ __device__ __forceinline__ int reflect_half(int j, int n) {
     return j < 0 ? 0 : (j >= n ? n - 1 : j);
 }
 
+// Streaming multiprocessors of the current device (queried once per device;
+// grid sizing targets whole waves of them).  Falls back to GB300's 152 if
+// the query fails.
+inline int device_sm_count() {
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 152;
+    }
+    if (!cache[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+            cudaGetLastError();
+            n = 152;
+        }
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
+
 // Opts a kernel into more than 48 KB of dynamic shared memory, once per
 // device (the attribute persists, so graph captures later need no API call).
 template <typename K>

@@ -434,9 +434,9 @@ __global__ void __launch_bounds__(128) k_hmom_p2(HMomArgs a, const __grid_consta
 // of the padded generation buffer; out-of-range levels and columns are
 // zero-filled by the copy engine) into a kStages-deep ring of tiles, each
 // guarded by an mbarrier with expect_tx.  Consumers wait on the barrier
-// parity with a bounded number of polls; if the bound runs out the block
-// records the failure in a.status and leaves through a block-uniform exit
-// after a bounded drain of its own copies.
+// parity with a bounded number of polls (a.max_polls); if the bound runs
+// out the block records the failure in a.status and leaves through a
+// block-uniform exit after a bounded drain of its own copies.
 __device__ __forceinline__ void mbar_init(unsigned addr, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(addr), "r"(count) : "memory");
 }
@@ -452,9 +452,8 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned addr, unsigned parity) {
         : "memory");
     return done != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned addr, unsigned parity) {
-    constexpr int kMaxPolls = 1 << 20;
-    for (int it = 0; it < kMaxPolls; ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned addr, unsigned parity, int max_polls = kDefaultWaitPolls) {
+    for (int it = 0; it < max_polls; ++it)
         if (mbar_try_wait(addr, parity)) return true;
     return false;
 }
@@ -583,7 +582,8 @@ __global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_const
             const int r = r0 + u;
             const int st0 = r % kTmaStages, st1 = (r + 1) % kTmaStages;
             const unsigned par = (unsigned)((r / kTmaStages) & 1);  // r even: r, r+1 share a phase
-            const bool ok = mbar_wait_bounded(bbase + 8 * st0, par) && mbar_wait_bounded(bbase + 8 * st1, par);
+            const bool ok = mbar_wait_bounded(bbase + 8 * st0, par, a.max_polls) &&
+                            mbar_wait_bounded(bbase + 8 * st1, par, a.max_polls);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
@@ -727,7 +727,7 @@ __global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_cons
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int r = r0 + u;
-            const bool ok = mbar_wait_bounded(bbase + 8 * u, (unsigned)((r / kStages) & 1));
+            const bool ok = mbar_wait_bounded(bbase + 8 * u, (unsigned)((r / kStages) & 1), a.max_polls);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;

@@ -1047,7 +1047,7 @@ static void zlaunch(const ZArgs& a, cudaStream_t s) {
             const int nt = a.nk / 4;
             const long long blocks_per_col = (long long)((nt + 127) / 128) * a.J;
             int ncol = 32;
-            while (ncol > ZI && blocks_per_col * ((a.I + ncol - 1) / ncol) < 152LL * 8 * 4) ncol /= 2;
+            while (ncol > ZI && blocks_per_col * ((a.I + ncol - 1) / ncol) < (long long)device_sm_count() * 8 * 4) ncol /= 2;
             dim3 block(128), grid((nt + 127) / 128, (a.I + ncol - 1) / ncol, a.J);
             k_zfilter4<T, MZ, ZI><<<grid, block, 0, s>>>(a, ncol);
             return;
@@ -1085,7 +1085,7 @@ int launch_restrict(DType t, const RestrictArgs& a, void* stream) {
         const int cx = t == DType::F64 ? 2 : 4;
         dim3 block(kRsWarps * 32), grid((a.nk + kRsLevels - 1) / kRsLevels, (Ic + kRsWarps * cx - 1) / (kRsWarps * cx), 1);
         const long long tiles = (long long)grid.x * grid.y;
-        const long long nseg = (8LL * 2 * 152 + tiles - 1) / tiles;
+        const long long nseg = (8LL * 2 * device_sm_count() + tiles - 1) / tiles;
         int rows = (int)((Jc + nseg - 1) / nseg);
         rows = std::max(rows, std::min(Jc, 8));
         grid.z = (Jc + rows - 1) / rows;

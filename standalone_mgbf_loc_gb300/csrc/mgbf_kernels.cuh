@@ -170,6 +170,12 @@ struct HMomCoefs {
     A upow[(kMaxReach + 1) * (kMaxMomP + 1)];  // upow[m*(P+1)+q] = C(P,q) (-1)^q (e m)^(2q)
 };
 
+// Polls of an mbarrier before a TMA-fed kernel gives up on a row (the
+// copy engine normally delivers a row within a few hundred polls).  The
+// drain of a block's own copies after such a failure always uses this
+// default, whatever limit the waits ran with.
+constexpr int kDefaultWaitPolls = 1 << 20;
+
 struct HMomArgs {
     View in, out;
     int nk, I, J;
@@ -180,6 +186,7 @@ struct HMomArgs {
     const void* tmap;        // host copy of a 3D TMA tensor map of the input buffer, or null
     int* status;             // device status word: set to 1 when a bounded wait runs out
     int variant = 0;         // FP32 kernels: 0 TMA two-row, 1 TMA one-row, 2 cp.async staged
+    int max_polls = kDefaultWaitPolls;  // polls of a row's barrier before the block gives up
 };
 
 constexpr int kHMomVariants = 3;

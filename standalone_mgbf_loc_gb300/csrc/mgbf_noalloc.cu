@@ -11,9 +11,10 @@
 // of memory obtained from cudaMalloc.  The caller still provides x and y.
 //
 // The array is static: every GPU that loads this library holds its
-// kNoAllocBytes until the process exits.  Its device address is looked up
-// with cudaGetSymbolAddress once per device, by the first call made with that
-// device current; that first call should come before any stream capture.
+// 64 MiB until the process exits.  Its device address is looked up with
+// cudaGetSymbolAddress once per device, by the first call made with that
+// device current; that first call should come before any stream capture
+// (a lookup that fails is retried by the next call).
 // All calls share the array and it keeps the last call's contents (nothing
 // in it has to start at zero: each call overwrites every element it later
 // reads).  Calls that overlap on the GPU (different streams, or different
@@ -25,6 +26,7 @@
 #include <mutex>
 
 #include "../../include/mgbf.h"
+#include "mgbf_common.cuh"
 #include "mgbf_kernels.cuh"
 #include "mgbf_setup.hpp"
 
@@ -36,9 +38,8 @@ constexpr size_t kNoAllocElems = (size_t)2 * MGBF_NOALLOC_MAX_ELEMS;
 static __device__ __align__(256) float g_noalloc_scratch[kNoAllocElems];
 
 constexpr int kMaxDevices = 64;
-float* g_scratch_addr[kMaxDevices];
-cudaError_t g_scratch_err[kMaxDevices];
-std::once_flag g_scratch_once[kMaxDevices];
+float* g_scratch_addr[kMaxDevices];  // set only once a lookup has succeeded
+std::mutex g_scratch_mutex[kMaxDevices];
 
 // Moment coefficients of the canonical radial disk, computed on the stack
 // (the same FP64 formulas as the handle's setup: cholaspect2, getlinesum2).
@@ -103,14 +104,24 @@ extern "C" int mgbf_radial_filter_noalloc(const float* x, float* y, int nk, int 
     if (e != cudaSuccess) return report_error(MGBF_ERR_CUDA, cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return report_error(MGBF_ERR_ARG, "device ordinal out of range");
     // Host code must not use g_noalloc_scratch as an address: look the device
-    // address up once per device, with that device current.
-    std::call_once(g_scratch_once[dev], [dev] {
-        void* p_ = nullptr;
-        g_scratch_err[dev] = cudaGetSymbolAddress(&p_, g_noalloc_scratch);
-        g_scratch_addr[dev] = static_cast<float*>(p_);
-    });
-    if (g_scratch_err[dev] != cudaSuccess) return report_error(MGBF_ERR_CUDA, cudaGetErrorString(g_scratch_err[dev]));
-    float* A = g_scratch_addr[dev];
+    // address up with that device current, and keep it once the lookup has
+    // succeeded.  A failed lookup (for instance one attempted during a stream
+    // capture) is not remembered: the next call tries again.
+    float* A = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_scratch_mutex[dev]);
+        if (!g_scratch_addr[dev]) {
+            void* p_ = nullptr;
+            e = cudaGetSymbolAddress(&p_, g_noalloc_scratch);
+            if (e != cudaSuccess || !p_) {
+                cudaGetLastError();
+                return report_error(MGBF_ERR_CUDA, e != cudaSuccess ? cudaGetErrorString(e)
+                                                                    : "cudaGetSymbolAddress returned no address");
+            }
+            g_scratch_addr[dev] = static_cast<float*>(p_);
+        }
+        A = g_scratch_addr[dev];
+    }
     float* B = A + per;
     mgbf::View vin, vA, vB, vout;
     vin.p = const_cast<float*>(x); vin.si = nk; vin.sj = (long long)nk * im;
@@ -125,7 +136,7 @@ extern "C" int mgbf_radial_filter_noalloc(const float* x, float* y, int nk, int 
     a.mirror_hx = R; a.halo = halo; a.scale = weight * s; a.tmap = nullptr; a.status = nullptr;
     const int tx = mgbf::hmom_tx_for(4, R);
     const long long w0 = (long long)((nk + 31) / 32) * ((im + tx - 1) / tx);
-    const long long nz = (152LL * 24 + w0 - 1) / w0;
+    const long long nz = ((long long)mgbf::device_sm_count() * 24 + w0 - 1) / w0;
     int rows = (int)((jm + nz - 1) / nz);
     a.rows = rows > 4 * R ? rows : (jm < 4 * R ? jm : 4 * R);
     rc = mgbf::launch_hmom(mgbf::DType::F32, R, p, a, coefs, stream);

@@ -230,6 +230,11 @@ class MGBF:
         """Raise if a bounded device wait ran out since the last check."""
         _abi.check(self._lib.mgbf_status(self._h), "mgbf_status")
 
+    def set_wait_limit(self, polls: int) -> None:
+        """mbarrier polls per row before a TMA-fed radial kernel gives up and
+        reports MGBF_ERR_TIMEOUT (polls < 0: the default)."""
+        _abi.check(self._lib.mgbf_set_wait_limit(self._h, int(polls)), "mgbf_set_wait_limit")
+
     def line_filters(self) -> list:
         """Procedures 2 and 7's three line filters (colors 1..3): dicts with
         the generator d, half-span h, formal half-span hs and weights fil[0..h]."""
@@ -371,6 +376,15 @@ class MGBFBatch:
         dt = _dtype_code(dtype if dtype is not None else torch.float32)
         stream = torch.cuda.current_stream().cuda_stream if torch is not None else None
         _abi.check(self._lib.mgbf_batch_autotune(self._h, dt, stream), "mgbf_batch_autotune")
+
+    def set_weights(self, a: Sequence[float]) -> None:
+        """Replace the generation weights a_1..a_n (n <= gm)."""
+        arr = (ctypes.c_double * len(a))(*[float(v) for v in a])
+        _abi.check(self._lib.mgbf_batch_set_weights(self._h, arr, len(a)), "mgbf_batch_set_weights")
+
+    def set_wait_limit(self, polls: int) -> None:
+        """As MGBF.set_wait_limit, for every group of the batch."""
+        _abi.check(self._lib.mgbf_batch_set_wait_limit(self._h, int(polls)), "mgbf_batch_set_wait_limit")
 
     def set_procedure(self, mg_filt: int) -> None:
         """6: radial filters (default); 8: the fast 1D+1D line filters."""

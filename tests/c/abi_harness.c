@@ -2,7 +2,8 @@
  * caller binds it.  Without arguments it runs host-only checks (no GPU
  * needed): namelist parsing, handle creation, derived sizes, error codes.
  * With "gpu" it also filters a field in host memory with
- * filtering_procedure(1) and prints a checksum. */
+ * filtering_procedure(1), prints a checksum and, given a third argument,
+ * writes the filtered VALL there as raw doubles. */
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -48,6 +49,11 @@ int main(int argc, char** argv) {
             if (fabs(v[t]) > m) m = fabs(v[t]);
         }
         printf("impulse response: sum=%.12e max=%.12e\n", s, m);
+        if (argc > 3) {
+            FILE* f = fopen(argv[3], "wb");
+            if (!f || fwrite(v, sizeof(double), d.field_elems, f) != d.field_elems) return 3;
+            fclose(f);
+        }
         free(v);
     }
     CHECK(mgbf_destroy(h));

@@ -44,7 +44,20 @@ def test_c_harness_gpu_impulse(lib, tmp_path):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
+    import numpy as np
+    from oracle import oracle as O
+    from standalone_mgbf_loc_gb300.mgbf import MGBFConfig
+    from tests.helpers import oracle_cfg, rel_l2
     exe = build_harness(lib, tmp_path)
-    r = subprocess.run([str(exe), "gpu", str(tmp_path / "mgbeta.nml")], capture_output=True, text=True)
+    out = tmp_path / "vall.bin"
+    r = subprocess.run([str(exe), "gpu", str(tmp_path / "mgbeta.nml"), str(out)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert "impulse response" in r.stdout
+    # the same impulse (grid centre, level 1) through the oracle's
+    # filtering_procedure(1) on VALL with its halo
+    cfg = oracle_cfg(MGBFConfig.from_namelist(str(tmp_path / "mgbeta.nml")), 1)
+    v = np.zeros((cfg.J + 2 * cfg.hy, cfg.I + 2 * cfg.hx, cfg.nk))
+    v[cfg.J // 2 + cfg.hy, cfg.I // 2 + cfg.hx, 0] = 1.0
+    O.filtering_procedure(cfg, v)
+    got = np.fromfile(out, dtype=np.float64).reshape(v.shape)
+    assert rel_l2(got, v) < 1e-12
