@@ -211,17 +211,30 @@ def run_gpu(args):
     gen = torch.Generator(device=dev)
     gen.manual_seed(1000 + rank)
     fields = [torch.randn((JM, IM, g.nk), generator=gen, device=dev, dtype=torch.float32) for g in gdesc]
-    pristine0 = fields[0][:, :, :VARS[0][0]].double().cpu().numpy() if rank == 0 else None
     pts_op = float(sum(IM * JM * g.nk for g in gdesc))
 
     def step():
         batch.apply(fields, adjoint=False)
         batch.apply(fields, adjoint=True)
 
-    # correctness sample: member 0 of the first variable after one forward
-    batch.apply(fields, adjoint=False)
-    torch.cuda.synchronize()
-    gpu_member0 = fields[0][:, :, :VARS[0][0]].double().cpu().numpy() if rank == 0 else None
+    # correctness sample (checked against the oracle after the timed legs):
+    # member 0 of every variable group through one forward and, from the same
+    # input, one adjoint call
+    sample = {}
+    if rank == 0:
+        lms = [lm for lm, _ in VARS]
+        x0 = [f[:, :, :lm].clone() for f, lm in zip(fields, lms)]
+        batch.apply(fields, adjoint=False)
+        torch.cuda.synchronize()
+        y_fwd = [f[:, :, :lm].double().cpu().numpy() for f, lm in zip(fields, lms)]
+        for f, x, lm in zip(fields, x0, lms):
+            f[:, :, :lm].copy_(x)
+        batch.apply(fields, adjoint=True)
+        torch.cuda.synchronize()
+        y_adj = [f[:, :, :lm].double().cpu().numpy() for f, lm in zip(fields, lms)]
+        sample = {"x": [x.double().cpu().numpy() for x in x0], "fwd": y_fwd, "adj": y_adj}
+        del x0
+    batch.status()
 
     for _ in range(args.warmup):
         step()
@@ -270,11 +283,11 @@ def run_gpu(args):
     # scalar FP operations (adds or multiply-adds) per grid point and pass
     gen_pts = sum((IM >> g) * (JM >> g) for g in range(GM))
     fp_ops = sum(g.nk * gen_pts * (8 * g.hx + 3) for g in gdesc) * 2 * 2 * nstep_t  # 2 passes, fwd+adj
-    fp_peak = 152 * 128 * 2.07e9  # SMs x FP32 lanes x max SM clock (one op per lane per cycle)
-    # DRAM traffic of the radial kernel per grid point and pass, from the ncu
-    # capture summarised in profiles/ (None until measured).
-    traffic_per_pt = HMOM_DRAM_BYTES_PER_POINT
-    traffic = (traffic_per_pt * h_pts / h_launch) if (traffic_per_pt and h_launch) else None
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    clk_sum = clk.summary()
+    sm_hz = (clk_sum.get("sm_mhz") or 2070.0) * 1e6
+    fp_peak = n_sm * 128 * sm_hz  # SMs x FP32 lanes x measured SM clock (one op per lane per cycle)
+    traffic = (HMOM_DRAM_BYTES_PER_POINT * h_pts / h_launch) if h_launch else None
 
     # end to end through the host-streaming pipeline: every step copies the
     # whole field set from pinned host memory, filters it forward and adjoint,
@@ -315,11 +328,18 @@ def run_gpu(args):
     torch.cuda.synchronize()
     copy_gbs = {"h2d": h2d / (c0.elapsed_time(c1) * 1e-3) / 1e9, "d2h": h2d / (c1.elapsed_time(c2) * 1e-3) / 1e9}
     del host, outs, hs
+    batch.close()
+    torch.cuda.empty_cache()
 
-    extras = {}
+    # secondary legs (timed on the GPU; their outputs are kept for the
+    # oracle checks below, which run after every timed region)
+    extras, checks = {}, {}
     if rank == 0 and not args.no_extras:
-        extras["fp64_plain"] = plain_forward(torch, dev, torch.float64)
-        extras["fp32_plain"] = plain_forward(torch, dev, torch.float32)
+        extras["cfg1"], checks["cfg1"] = cfg1_leg(torch, dev)
+        extras["fp64_plain"], checks["cfg2_f64"] = plain_forward(torch, dev, torch.float64, keep=True)
+        extras["fp32_plain"], checks["cfg2_f32"] = plain_forward(torch, dev, torch.float32, keep=True)
+        extras["cfg3_grads_fp32"], checks["cfg3"] = cfg3_leg(torch, dev)
+        extras["cfg5_bf16"], checks["cfg5"] = cfg5_leg(torch, dev, peak, args.cfg5_steps)
         extras["fast_fp32"] = fast_forward(torch, dev, torch.float32, peak)
         extras["transfers_fp32"] = transfers(torch, dev, torch.float32, peak)
         extras["rad3_fp32"] = rad3_forward(torch, dev, torch.float32)
@@ -327,16 +347,18 @@ def run_gpu(args):
     result = None
     if rank == 0:
         cpu = None
-        rel = None
+        parity = None
         if not args.no_extras:
             nthreads = os.cpu_count() or 1
             t0 = time.perf_counter()
-            y, _ = cpu_step(pristine0, nthreads)
+            cpu_step(sample["x"][0], nthreads)
             dt = time.perf_counter() - t0
-            rel = float(np.linalg.norm(gpu_member0 - y) / np.linalg.norm(y))
             cpu = {"value": 2 * IM * JM * VARS[0][0] / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
                    "sample": "one member of the 64-level variable (512x512x64, reach 8), forward+adjoint, "
                              "FP64 CPU restatement with OpenMP"}
+            checks["cfg4"] = sample
+            parity = check_parity(checks, nthreads)
+            extras["cfg5_bf16"]["per_generation_rel_l2"] = parity["cfg5"]["per_generation_rel_l2"]
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -345,15 +367,18 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "members_per_gpu": members, "grid": [IM, JM], "generations": GM,
                        "points_per_op_per_gpu": pts_op, "l2": "no flush: one field set (14.8 GB) >> L2 (129 MB)",
                        "parallelism": f"replicas x{ws} (independent members per GPU, no collective)"},
-            "roofline": {"bound": "hbm", "kernel": "k_hmom (radial beta, moment form)",
+            "roofline": {"bound": "fp32_pipe", "kernel": "k_hmom_tma / k_hmom_tma1 (radial beta, moment form)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "traffic_source": HMOM_TRAFFIC_SOURCE,
                          "peak_source": peak_kind,
                          "algorithmic_bytes": "2 x 4 B per grid point per launch (read + write, FP32)",
-                         "launches": h_launch / nstep_t, "avg_launch_ms": h_ms / h_launch if h_launch else None},
-            "compute_roofline": {"bound": "fp32_pipe", "kernel": "k_hmom_tma",
+                         "launches": h_launch / nstep_t, "avg_launch_ms": h_ms / h_launch if h_launch else None,
+                         "note": "HBM fraction of a kernel limited by the FP32 pipe (see compute_roofline)"},
+            "compute_roofline": {"bound": "fp32_pipe", "kernel": "k_hmom_tma / k_hmom_tma1",
                                  "achieved": fp_ops / (h_ms * 1e-3) if h_ms else None, "peak": fp_peak,
                                  "unit": "FP32 ops/s", "frac": fp_ops / (h_ms * 1e-3) / fp_peak if h_ms else None,
+                                 "peak_from": f"{n_sm} SMs x 128 FP32 lanes x {sm_hz / 1e6:.0f} MHz (measured clock)",
                                  "ops_per_point_pass": "8R+3 (moment form; the direct disk sum costs ~pi R^2)"},
             "step_hbm_frac": (4 * 4 * pts_op) / (ms_step * 1e-3) / (peak * 1e9),
             "stages_ms_per_step": stage_ms,
@@ -363,8 +388,8 @@ def run_gpu(args):
                     "pipeline": "pinned host -> device, fwd+adj, device -> host per step; uploads, filtering "
                                 "and downloads of adjacent steps overlap (two device field sets, three streams)"},
             "gpu_launches": int(round(launches_per_step * args.steps)),
-            "clocks": clk.summary(),
-            "rel_l2_vs_oracle": rel,
+            "clocks": clk_sum,
+            "parity": parity,
         }
         result.update(extras)
         print(json.dumps(result), flush=True)
@@ -375,38 +400,298 @@ def run_gpu(args):
 
 
 # DRAM bytes (read + write) per grid point and pass of the radial moment
-# kernel, from the ncu capture summarised in
-# profiles/k_hmom_tma_reach8_8members_512sq.md (1116.2 MB for 134.2 M points,
-# FP32); traffic grows in proportion to the points a launch processes.
+# kernel, measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on
+# one launch of 134.2 M points (8 members of the 64-level, reach-8 variable,
+# FP32: 1116.2 MB); traffic grows in proportion to the points of a launch.
 HMOM_DRAM_BYTES_PER_POINT = 8.32
+HMOM_TRAFFIC_SOURCE = ("scaled from an ncu capture of one 8-member launch (8.32 B per point); "
+                       "not measured in this run")
 
 
-def plain_forward(torch, dev, dtype):
-    """Plain unbatched forward of one 3D field, 768x768x64, 5 generations,
-    reach 12, vertical reach 4 (filtering_procedure(1))."""
-    from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig
-    cfg = MGBFConfig(nxPE=16, nyPE=16, im_filt=48, jm_filt=48, lm=64, km3=1, km2=0, n_ens=1, gm_max=5,
-                     hx=12, hy=12, hz=4, p=2, mg_ampl02=ampl02(12), mg_ampl01=ampl01(4),
-                     mg_weig1=1.0, mg_weig2=0.5, mg_weig3=0.25, mg_weig4=0.125, mg_weig5=0.0625, layout=1)
-    op = MGBF(cfg)
-    gen = torch.Generator(device=dev)
-    gen.manual_seed(7)
-    x = torch.randn(op.field_shape(), generator=gen, device=dev, dtype=dtype)
-    for _ in range(2):
-        op.filtering_procedure(1, x)
+def timed_calls(torch, fn, n=5, warm=2):
+    """Mean CUDA-event time (ms) of n calls of fn after warm untimed ones."""
+    for _ in range(warm):
+        fn()
     torch.cuda.synchronize()
-    n = 5
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record()
     for _ in range(n):
-        op.filtering_procedure(1, x)
+        fn()
     b.record()
     torch.cuda.synchronize()
-    ms = a.elapsed_time(b) / n
+    return a.elapsed_time(b) / n
+
+
+def plain_cfg(**kw):
+    """One 3D field on 768x768x64 (16x16 ranks of 48x48), 5 generations, h=12, hz=4."""
+    from standalone_mgbf_loc_gb300 import MGBFConfig
+    d = dict(nxPE=16, nyPE=16, im_filt=48, jm_filt=48, lm=64, km3=1, km2=0, n_ens=1, gm_max=5,
+             hx=12, hy=12, hz=4, p=2, mg_ampl02=ampl02(12), mg_ampl01=ampl01(4),
+             mg_weig1=1.0, mg_weig2=0.5, mg_weig3=0.25, mg_weig4=0.125, mg_weig5=0.0625, layout=1)
+    d.update(kw)
+    return MGBFConfig(**d)
+
+
+def plain_forward(torch, dev, dtype, keep=False):
+    """Plain unbatched forward of one 3D field, 768x768x64, 5 generations,
+    reach 12, vertical reach 4 (filtering_procedure(1)); input seeded N(0,1)
+    from numpy (seed 2).  keep: also return (config, input, output) for the
+    oracle check."""
+    from standalone_mgbf_loc_gb300 import MGBF
+    cfg = plain_cfg()
+    op = MGBF(cfg)
+    x_np = np.random.default_rng(2).standard_normal(op.field_shape())
+    x0 = torch.from_numpy(x_np).to(device=dev, dtype=dtype)
+    x = x0.clone()
+    ms = timed_calls(torch, lambda: op.filtering_procedure(1, x))
+    x.copy_(x0)
+    op.filtering_procedure(1, x)
+    torch.cuda.synchronize()
+    op.status()
+    out = x.double().cpu().numpy() if keep else None
     pts = float(np.prod(op.field_shape()))
     op.close()
-    return {"workload": "plain forward, one 3D field 768x768x64, 5 generations, h=12, hz=4",
-            "dtype": str(dtype).replace("torch.", ""), "ms": ms, "value": pts / (ms * 1e-3), "unit": UNIT}
+    res = {"workload": "plain forward, one 3D field 768x768x64, 5 generations, h=12, hz=4",
+           "dtype": str(dtype).replace("torch.", ""), "ms": ms, "value": pts / (ms * 1e-3), "unit": UNIT}
+    if keep:
+        return res, {"cfg": cfg, "proc": 1, "x": x_np, "y": out, "dtype": res["dtype"]}
+    return res
+
+
+def cfg1_leg(torch, dev):
+    """256x256x32 (8x8 ranks of 32x32), 4 generations, h=6, hz=3, weights
+    1, .5, .25, .125; filtering_procedure(1) in FP64 and FP32 on seeded
+    N(0,1) noise (numpy seed 0) and on a unit impulse at Fortran (128,128,16)."""
+    from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig
+    cfg = MGBFConfig(nxPE=8, nyPE=8, im_filt=32, jm_filt=32, lm=32, km3=1, km2=0, n_ens=1, gm_max=4,
+                     hx=6, hy=6, hz=3, p=2, mg_ampl02=ampl02(6), mg_ampl01=ampl01(3),
+                     mg_weig1=1.0, mg_weig2=0.5, mg_weig3=0.25, mg_weig4=0.125, layout=1)
+    op = MGBF(cfg)
+    noise = np.random.default_rng(0).standard_normal(op.field_shape())
+    imp = np.zeros(op.field_shape())
+    imp[127, 127, 15] = 1.0
+    pts = float(np.prod(op.field_shape()))
+    res = {"workload": "plain forward, 256x256x32, 4 generations, h=6, hz=3, weights 1,.5,.25,.125"}
+    outs = {}
+    for dtype in (torch.float64, torch.float32):
+        name = str(dtype).replace("torch.", "")
+        xn = torch.from_numpy(noise).to(device=dev, dtype=dtype)
+        x = xn.clone()
+        ms = timed_calls(torch, lambda: op.filtering_procedure(1, x), n=10)
+        res[name] = {"ms": ms, "value": pts / (ms * 1e-3), "unit": UNIT}
+        for tag, inp in (("noise", noise), ("impulse", imp)):
+            t = torch.from_numpy(inp).to(device=dev, dtype=dtype)
+            op.filtering_procedure(1, t)
+            torch.cuda.synchronize()
+            outs[(name, tag)] = t.double().cpu().numpy()
+    op.status()
+    op.close()
+    return res, {"cfg": cfg, "proc": 1, "inputs": {"noise": noise, "impulse": imp}, "outs": outs}
+
+
+def cfg3_leg(torch, dev):
+    """Differentiation: 512x512x64 (16x16 ranks of 32x32), 5 generations,
+    h=10, hz=4, FP32.  One step = the torch.autograd.Function's forward plus
+    its backward (hand-written adjoint chain; gradients for the field and the
+    five generation weights; coarse generations recomputed in the backward).
+    Kept for the oracle check: y, dL/dx, dL/da, the dot-product residual of
+    forward and adjoint, and central finite differences (step 1e-3) of the
+    weights, each from GPU FP32 calls."""
+    from standalone_mgbf_loc_gb300 import MGBF
+    from standalone_mgbf_loc_gb300.autograd import mgbf_apply
+    cfg = plain_cfg(im_filt=32, jm_filt=32, hx=10, hy=10, mg_ampl02=ampl02(10))
+    op = MGBF(cfg)
+    rng = np.random.default_rng(3)
+    x_np = rng.standard_normal(op.field_shape())
+    r_np = rng.standard_normal(op.field_shape())
+    y2_np = rng.standard_normal(op.field_shape())
+    x = torch.from_numpy(x_np).to(device=dev, dtype=torch.float32)
+    r = torch.from_numpy(r_np).to(device=dev, dtype=torch.float32)
+    w0 = [1.0, 0.5, 0.25, 0.125, 0.0625]
+
+    def step():
+        xg = x.clone().requires_grad_(True)
+        w = torch.tensor(w0, dtype=torch.float64, device=dev, requires_grad=True)
+        loss = (mgbf_apply(op, xg, w, 1) * r).sum()
+        loss.backward()
+        return xg, w
+
+    ms = timed_calls(torch, step, n=5)
+    xg, w = step()
+    y = mgbf_apply(op, x, torch.tensor(w0, dtype=torch.float64, device=dev), 1)
+    out = {"y": y.double().cpu().numpy(), "gx": xg.grad.double().cpu().numpy(),
+           "ga": w.grad.double().cpu().numpy()}
+    # dot-product test of the forward and the adjoint call
+    op.set_weights(w0)
+    ly = torch.from_numpy(y2_np).to(device=dev, dtype=torch.float32)
+    op.filtering_procedure_adjoint(1, ly)
+    lx = y.double()
+    a = float((lx * torch.from_numpy(y2_np).to(dev)).sum())
+    b = float((x.double() * ly.double()).sum())
+    out["dot_residual"] = abs(a - b) / (float(lx.norm()) * float(np.linalg.norm(y2_np)))
+    # central finite differences of <r, L(a) x> in the weights, step 1e-3
+    h = 1e-3
+    fd = []
+    for g in range(5):
+        f = []
+        for sgn in (1, -1):
+            wg = list(w0)
+            wg[g] += sgn * h
+            op.set_weights(wg)
+            t = x.clone()
+            op.filtering_procedure(1, t)
+            f.append(float((t.double() * r.double()).sum()))
+        fd.append((f[0] - f[1]) / (2 * h))
+    out["fd"] = np.array(fd)
+    torch.cuda.synchronize()
+    op.status()
+    pts = float(np.prod(op.field_shape()))
+    op.close()
+    res = {"workload": "autograd forward + backward (field and 5 weight gradients), 512x512x64, 5 generations, "
+                       "h=10, hz=4, FP32",
+           "dtype": "float32", "ms": ms, "value": 2 * pts / (ms * 1e-3), "unit": UNIT,
+           "note": "value counts 2 operator applications per step (forward and adjoint)"}
+    return res, {"cfg": cfg, "proc": 1, "x": x_np, "r": r_np, "w": w0, **out}
+
+
+CFG5 = dict(members=30, n=1536, lm=64, gm=6, h=24, hz=5, weights=[1.0, 0.5, 0.25, 0.125, 0.0625, 0.0625])
+
+
+def cfg5_leg(torch, dev, peak_gbs, steps):
+    """Large batched run: 30 members x one 3D variable on 1536x1536x64,
+    6 generations, h=24, hz=5, BF16 storage with FP32 arithmetic, FP64
+    coefficient setup; seeded N(0,1) inputs (numpy seed 5 for member 0,
+    torch.Generator for the others).  One step = forward + adjoint of the
+    batch (the adjoint recomputes every coarse generation; nothing is stored
+    between the calls).  Kept for the oracle check: member 0's output with
+    every weight and with one generation's weight at a time (the
+    per-generation terms of the operator)."""
+    from standalone_mgbf_loc_gb300 import MGBFBatch, GroupDesc, _abi
+    c = CFG5
+    n, lm, nk = c["n"], c["lm"], c["members"] * c["lm"]
+    gd = [GroupDesc(nk=nk, lm=lm, nzcol=c["members"], hx=c["h"], hy=c["h"], hz=c["hz"], p=P,
+                    mg_ampl01=ampl01(c["hz"]), mg_ampl02=ampl02(c["h"]))]
+    b = MGBFBatch(n, n, c["gm"], c["weights"], gd)
+    b.autotune(torch.bfloat16)
+    b.use_graphs(True)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(55)
+    x0 = torch.randn((n, n, nk), generator=gen, device=dev, dtype=torch.float32).to(torch.bfloat16)
+    m0 = np.random.default_rng(5).standard_normal((n, n, lm))
+    x0[:, :, :lm] = torch.from_numpy(m0).to(device=dev, dtype=torch.bfloat16)
+    f = [x0.clone()]
+
+    def step():
+        b.apply(f, adjoint=False)
+        b.apply(f, adjoint=True)
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    b.status()
+    # radial-kernel launch durations from the stage timers
+    _abi.timers_enable(True)
+    step()
+    torch.cuda.synchronize()
+    st = _abi.timers_read()
+    _abi.timers_enable(False)
+    hb = [st[k] for k in ("hfiltT", "hfilt") if k in st]
+    h_ms, h_pts, h_n = sum(v[1] for v in hb), sum(v[2] for v in hb), sum(v[0] for v in hb)
+    achieved = 2 * 2 * h_pts / (h_ms * 1e-3) / 1e9 if h_ms else None
+    gen_pts = sum((n >> g) * (n >> g) for g in range(c["gm"]))
+    fp_ops = nk * gen_pts * (8 * c["h"] + 3) * 2 * 2  # 2 passes, forward + adjoint
+    # member 0: every weight, then one generation at a time
+    outs = []
+    for g in range(-1, c["gm"]):
+        w = c["weights"] if g < 0 else [c["weights"][q] if q == g else 0.0 for q in range(c["gm"])]
+        b.set_weights(w)
+        f[0].copy_(x0)
+        b.apply(f, adjoint=False)
+        torch.cuda.synchronize()
+        outs.append(f[0][:, :, :lm].float().cpu().numpy())
+    b.status()
+    x_m0 = x0[:, :, :lm].double().cpu().numpy()  # the BF16-rounded input the GPU filtered
+    pts = float(n * n * nk)
+    b.close()
+    del f, x0
+    torch.cuda.empty_cache()
+    res = {"workload": "30 members x 1536x1536x64, 6 generations, h=24, hz=5, BF16 storage, FP32 arithmetic, "
+                       "forward + adjoint",
+           "dtype": "bf16", "ms": ms, "value": 2 * pts / (ms * 1e-3), "unit": UNIT, "steps": steps,
+           "field_gb": pts * 2 / 1e9, "stages_ms_per_step": {k: v[1] for k, v in st.items()},
+           "roofline": {"bound": "fp32_pipe", "kernel": "k_hmom_tma / k_hmom_tma1 (reach 24, BF16)",
+                        "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                        "frac": achieved / peak_gbs if achieved else None,
+                        "algorithmic_bytes": "2 x 2 B per grid point per launch (BF16)",
+                        "launches": h_n, "avg_launch_ms": h_ms / h_n if h_n else None,
+                        "fp32_ops_per_s": fp_ops / (h_ms * 1e-3) if h_ms else None}}
+    return res, {"x": x_m0, "outs": outs}
+
+
+def check_parity(checks, nthreads):
+    """Relative L2 errors of the kept GPU outputs against the FP64 oracle
+    (the oracle is only the checker here; nothing of it is timed above)."""
+    from oracle import oracle as O
+    t_start = time.perf_counter()
+
+    def rel(a, b):
+        d = float(np.linalg.norm(b))
+        return float(np.linalg.norm(np.asarray(a, dtype=np.float64) - b) / (d if d > 0 else 1.0))
+
+    def ocfg(c, proc, **kw):
+        gm = c.gm_max
+        w = [c.mg_weig1, c.mg_weig2, c.mg_weig3, c.mg_weig4, c.mg_weig5][:gm]
+        d = dict(I=c.nxPE * c.im_filt, J=c.nyPE * c.jm_filt, nk=c.lm * c.km3 + c.km2, hx=c.hx, hy=c.hy, hz=c.hz,
+                 p=c.p, ampl01=c.mg_ampl01, ampl02=c.mg_ampl02, gm=gm, weights=w, proc=proc, lm=c.lm,
+                 nzcol=c.km3, l_vertical_filter=True, nthreads=nthreads)
+        d.update(kw)
+        return O.OracleConfig(**d)
+
+    out = {"tolerance": {"f64": 1e-12, "f32": 1e-5, "bf16": "reported (2^-8 storage rounding)",
+                         "dot_residual_f32": 1e-6, "fd_vs_oracle_grad": 1e-3}}
+    c1 = checks["cfg1"]
+    oc = ocfg(c1["cfg"], 1)
+    refs = {tag: O.filter_compact(oc, x) for tag, x in c1["inputs"].items()}
+    out["cfg1"] = {f"{dt}_{tag}": rel(y, refs[tag]) for (dt, tag), y in c1["outs"].items()}
+    c2 = checks["cfg2_f64"]
+    ref2 = O.filter_compact(ocfg(c2["cfg"], 1), c2["x"])
+    out["cfg2"] = {"float64_fwd": rel(c2["y"], ref2), "float32_fwd": rel(checks["cfg2_f32"]["y"], ref2)}
+    c3 = checks["cfg3"]
+    oc3 = ocfg(c3["cfg"], 1)
+    ga = O.weight_grads(oc3, c3["x"], c3["r"])
+    out["cfg3"] = {"float32_fwd": rel(c3["y"], O.filter_compact(oc3, c3["x"])),
+                   "float32_grad_x": rel(c3["gx"], O.filter_compact(oc3, c3["r"])),
+                   "float32_grad_weights": rel(c3["ga"], ga),
+                   "float32_fd_weights_vs_oracle": rel(c3["fd"], ga),
+                   "float32_dot_residual": c3["dot_residual"]}
+    c4 = checks["cfg4"]
+    out["cfg4"] = {}
+    for q, (lm, h) in enumerate(VARS):
+        oc4 = O.OracleConfig(I=IM, J=JM, nk=lm, hx=h, hy=h, hz=HZ, p=P, ampl01=ampl01(HZ), ampl02=ampl02(h), gm=GM,
+                             weights=WEIGHTS, proc=6, lm=lm, nzcol=1 if lm > 1 else 0, l_vertical_filter=lm > 1,
+                             nthreads=nthreads)
+        ref = O.filter_compact(oc4, c4["x"][q])  # L is self-adjoint: the adjoint's reference too
+        out["cfg4"][f"group{q}_lm{lm}_h{h}"] = {"float32_fwd": rel(c4["fwd"][q], ref),
+                                              "float32_adj": rel(c4["adj"][q], ref)}
+    c5 = checks["cfg5"]
+    k = CFG5
+    oc5 = O.OracleConfig(I=k["n"], J=k["n"], nk=k["lm"], hx=k["h"], hy=k["h"], hz=k["hz"], p=P,
+                         ampl01=ampl01(k["hz"]), ampl02=ampl02(k["h"]), gm=k["gm"], weights=k["weights"], proc=6,
+                         lm=k["lm"], nzcol=1, l_vertical_filter=True, nthreads=nthreads)
+    ys = O.contributions(oc5, c5["x"])
+    out["cfg5"] = {"bf16_fwd": rel(c5["outs"][0], sum(ys)),
+                   "per_generation_rel_l2": [rel(c5["outs"][1 + g], ys[g]) for g in range(k["gm"])],
+                   "sample": "member 0 (1536x1536x64); per generation: the operator with only that generation's "
+                             "weight, against the oracle's term of that generation"}
+    out["checker_seconds"] = time.perf_counter() - t_start
+    return out
 
 
 def fast_forward(torch, dev, dtype, peak_gbs):
@@ -575,6 +860,7 @@ def main():
     ap.add_argument("--members", type=int, default=80)
     ap.add_argument("--no-extras", action="store_true", help="skip the plain-forward and CPU-baseline legs")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default radial-kernel tiles")
+    ap.add_argument("--cfg5-steps", type=int, default=5, help="timed steps of the large BF16 leg")
     ap.add_argument("--leg", choices=sorted(LEGS), help="run one secondary leg alone (fp32) and print its JSON line")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -594,6 +880,9 @@ LEGS = {
     "rad3": lambda torch, dev, peak: rad3_forward(torch, dev, torch.float32),
     "lin2": lambda torch, dev, peak: lin2_forward(torch, dev, torch.float32),
     "plain": lambda torch, dev, peak: plain_forward(torch, dev, torch.float32),
+    "cfg1": lambda torch, dev, peak: cfg1_leg(torch, dev)[0],
+    "cfg3": lambda torch, dev, peak: cfg3_leg(torch, dev)[0],
+    "cfg5": lambda torch, dev, peak: cfg5_leg(torch, dev, peak, 5)[0],
 }
 
 

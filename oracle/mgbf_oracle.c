@@ -45,13 +45,37 @@ static arr3 a3_alloc(int nk, int ilo, int ihi, int jlo, int jhi) {
 }
 static void a3_free(arr3* a) { free(a->d); a->d = NULL; }
 
+/* Row parallelism.  Inside the k-split parallel region of
+ * orc_filtering_procedure every thread runs the pipeline on its own level
+ * range and the loops below stay serial.  Called outside any parallel region
+ * (few levels per thread, the stage entry points, the weight gradients) the
+ * loops marked ROWPAR split their rows over g_threads threads instead.  Each
+ * row-parallel loop either writes whole rows of its output from inputs it
+ * does not write, or (the two scatters vrbeta2t and adjoint4) is written in a
+ * target-row form that adds every target's contributions in the order of the
+ * literal loop; either way the results are bit-identical to the serial
+ * literal loops. */
+static int g_threads = 1;
+#ifdef _OPENMP
+#define ROWPAR (!omp_in_parallel() && g_threads > 1)
+#define PRAGMA(x) _Pragma(#x)
+#define ROW_FOR PRAGMA(omp parallel for schedule(static) if(ROWPAR) num_threads(g_threads))
+static void set_threads(int n) { g_threads = n > 0 ? n : omp_get_max_threads(); }
+#else
+#define ROWPAR 0
+#define ROW_FOR
+static void set_threads(int n) { (void)n; g_threads = 1; }
+#endif
+
 /* Zero k-range [k0,k1) of every cell. */
 static void a3_zero(arr3 a, int k0, int k1) {
+    ROW_FOR
     for (int j = a.jlo; j <= a.jhi; ++j)
         for (int i = a.ilo; i <= a.ihi; ++i)
             for (int k = k0; k < k1; ++k) A3(a, k, i, j) = 0.0;
 }
 static void a3_copy(arr3 dst, arr3 src, int k0, int k1) {
+    ROW_FOR
     for (int j = dst.jlo; j <= dst.jhi; ++j)
         for (int i = dst.ilo; i <= dst.ihi; ++i)
             for (int k = k0; k < k1; ++k) A3(dst, k, i, j) = A3(src, k, i, j);
@@ -455,33 +479,85 @@ int orc_setup_values(const orc_cfg* c, double out[11]) {
 
 /* vrbeta2 (jp_pbfil.f90:888-928): gather over the extended domain, output on
  * the interior, halo of the result zeroed; then a = b.  k-range [k0,k1). */
+/* The disk of vrbeta2 / vrbeta2t: for every row gy its column range and
+ * the weights frow = s*(1-rr)^p, computed by the reference's own formulas
+ * (jp_pbfil.f90:909-924).  The stencil is the same at every point (uniform
+ * aspect), so the table is built once per call; the sums below visit the
+ * taps in the reference's order, so the results equal those of evaluating
+ * the formulas at every point. */
+typedef struct {
+    int gyl, gym;
+    int* gxl;     /* per row (index gy - gyl) */
+    int* gxm;
+    double** w;   /* w[row][gx - gxl[row]] */
+} disk_t;
+
+static disk_t disk_table(const setup_t* S, int p) {
+    disk_t d;
+    double exx = S->exx2, eyy = S->eyy2, eyx = S->eyx2, s = S->ss2;
+    double y = 1.0 / eyy;
+    d.gyl = (int)ceil(-y + EPS);
+    d.gym = (int)floor(y - EPS);
+    int n = d.gym - d.gyl + 1;
+    d.gxl = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    d.gxm = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    d.w = (double**)malloc(sizeof(double*) * (size_t)(n > 0 ? n : 1));
+    for (int gy = d.gyl; gy <= d.gym; ++gy) {
+        int r = gy - d.gyl;
+        double yy = gy, xc = -yy * eyx;
+        double rrx = (yy * eyy) * (yy * eyy);
+        double x = sqrt(1.0 - rrx);
+        int gxl = (int)ceil((xc - x) / exx + EPS), gxm = (int)floor((xc + x) / exx - EPS);
+        d.gxl[r] = gxl;
+        d.gxm[r] = gxm;
+        d.w[r] = (double*)malloc(sizeof(double) * (size_t)(gxm >= gxl ? gxm - gxl + 1 : 1));
+        for (int gx = gxl; gx <= gxm; ++gx) {
+            double xx = gx;
+            double rr = rrx + (xx * exx - xc) * (xx * exx - xc);
+            d.w[r][gx - gxl] = s * ipow(1.0 - rr, p);
+        }
+    }
+    return d;
+}
+
+static void disk_free(disk_t* d) {
+    for (int r = 0; r <= d->gym - d->gyl; ++r) free(d->w[r]);
+    free(d->w);
+    free(d->gxl);
+    free(d->gxm);
+}
+
 static void vrbeta2(const setup_t* S, int p, arr3 a, arr3 b, int Lx, int Mx, int Ly, int My,
                     int k0, int k1, double* tb) {
     a3_zero(b, k0, k1);
-    double exx = S->exx2, eyy = S->eyy2, eyx = S->eyx2, s = S->ss2;
-    for (int iy = Ly; iy <= My; ++iy)
-        for (int ix = Lx; ix <= Mx; ++ix) {
-            for (int k = k0; k < k1; ++k) tb[k] = 0.0;
-            double y = 1.0 / eyy;
-            int gyl = (int)ceil(-y + EPS), gym = (int)floor(y - EPS);
-            for (int gy = gyl; gy <= gym; ++gy) {
-                int jy = iy + gy;
-                double yy = gy, xc = -yy * eyx;
-                double rrx = (yy * eyy) * (yy * eyy);
-                double x = sqrt(1.0 - rrx);
-                int gxl = (int)ceil((xc - x) / exx + EPS), gxm = (int)floor((xc + x) / exx - EPS);
-                for (int gx = gxl; gx <= gxm; ++gx) {
-                    int jx = ix + gx;
-                    double xx = gx;
-                    double rr = rrx + (xx * exx - xc) * (xx * exx - xc);
-                    double frow = s * ipow(1.0 - rr, p);
-                    const double* src = &A3(a, 0, jx, jy);
-                    for (int k = k0; k < k1; ++k) tb[k] += frow * src[k];
+    disk_t D = disk_table(S, p);
+    const int par = ROWPAR;
+#ifdef _OPENMP
+#pragma omp parallel if(par) num_threads(g_threads)
+#endif
+    {
+        double* tbl = par ? (double*)malloc(sizeof(double) * (size_t)a.nk) : tb;
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+        for (int iy = Ly; iy <= My; ++iy)
+            for (int ix = Lx; ix <= Mx; ++ix) {
+                for (int k = k0; k < k1; ++k) tbl[k] = 0.0;
+                for (int gy = D.gyl; gy <= D.gym; ++gy) {
+                    int jy = iy + gy, r = gy - D.gyl;
+                    for (int gx = D.gxl[r]; gx <= D.gxm[r]; ++gx) {
+                        int jx = ix + gx;
+                        double frow = D.w[r][gx - D.gxl[r]];
+                        const double* src = &A3(a, 0, jx, jy);
+                        for (int k = k0; k < k1; ++k) tbl[k] += frow * src[k];
+                    }
                 }
+                double* dst = &A3(b, 0, ix, iy);
+                for (int k = k0; k < k1; ++k) dst[k] = tbl[k];
             }
-            double* dst = &A3(b, 0, ix, iy);
-            for (int k = k0; k < k1; ++k) dst[k] = tb[k];
-        }
+        if (par) free(tbl);
+    }
+    disk_free(&D);
     a3_copy(a, b, k0, k1);
 }
 
@@ -490,28 +566,43 @@ static void vrbeta2(const setup_t* S, int p, arr3 a, arr3 b, int Lx, int Mx, int
 static void vrbeta2t(const setup_t* S, int p, arr3 a, arr3 b, int Lx, int Mx, int Ly, int My,
                      int k0, int k1) {
     a3_zero(b, k0, k1);
-    double exx = S->exx2, eyy = S->eyy2, eyx = S->eyx2, s = S->ss2;
-    for (int iy = Ly; iy <= My; ++iy)
-        for (int ix = Lx; ix <= Mx; ++ix) {
-            const double* ta = &A3(a, 0, ix, iy);
-            double y = 1.0 / eyy;
-            int gyl = (int)ceil(-y + EPS), gym = (int)floor(y - EPS);
-            for (int gy = gyl; gy <= gym; ++gy) {
-                int jy = iy + gy;
-                double yy = gy, xc = -yy * eyx;
-                double rrx = (yy * eyy) * (yy * eyy);
-                double x = sqrt(1.0 - rrx);
-                int gxl = (int)ceil((xc - x) / exx + EPS), gxm = (int)floor((xc + x) / exx - EPS);
-                for (int gx = gxl; gx <= gxm; ++gx) {
-                    int jx = ix + gx;
-                    double xx = gx;
-                    double rr = rrx + (xx * exx - xc) * (xx * exx - xc);
-                    double frow = s * ipow(1.0 - rr, p);
-                    double* dst = &A3(b, 0, jx, jy);
-                    for (int k = k0; k < k1; ++k) dst[k] += frow * ta[k];
+    disk_t D = disk_table(S, p);
+    if (!ROWPAR) {
+        for (int iy = Ly; iy <= My; ++iy)
+            for (int ix = Lx; ix <= Mx; ++ix) {
+                const double* ta = &A3(a, 0, ix, iy);
+                for (int gy = D.gyl; gy <= D.gym; ++gy) {
+                    int jy = iy + gy, r = gy - D.gyl;
+                    for (int gx = D.gxl[r]; gx <= D.gxm[r]; ++gx) {
+                        int jx = ix + gx;
+                        double frow = D.w[r][gx - D.gxl[r]];
+                        double* dst = &A3(b, 0, jx, jy);
+                        for (int k = k0; k < k1; ++k) dst[k] += frow * ta[k];
+                    }
+                }
+            }
+    } else {
+        /* target-row form: a thread owns the target rows jy and visits their
+         * source rows iy = jy - gy in increasing order and the source
+         * columns ix in increasing order, the order in which the literal
+         * loop above adds into any one target */
+        ROW_FOR
+        for (int jy = Ly + D.gyl; jy <= My + D.gym; ++jy) {
+            int iylo = jy - D.gym > Ly ? jy - D.gym : Ly, iyhi = jy - D.gyl < My ? jy - D.gyl : My;
+            for (int iy = iylo; iy <= iyhi; ++iy) {
+                int gy = jy - iy, r = gy - D.gyl;
+                for (int ix = Lx; ix <= Mx; ++ix) {
+                    const double* ta = &A3(a, 0, ix, iy);
+                    for (int gx = D.gxl[r]; gx <= D.gxm[r]; ++gx) {
+                        double frow = D.w[r][gx - D.gxl[r]];
+                        double* dst = &A3(b, 0, ix + gx, jy);
+                        for (int k = k0; k < k1; ++k) dst[k] += frow * ta[k];
+                    }
                 }
             }
         }
+    }
+    disk_free(&D);
     a3_copy(a, b, k0, k1);
 }
 
@@ -994,29 +1085,52 @@ static const double BC[3] = {-3.0 / 32.0, 30.0 / 32.0, 5.0 / 32.0};
 static void adjoint4(arr3 F, arr3 W, arr3 aux, int im, int jm, int k0, int k1) {
     int imL = im / 2, jmL = jm / 2;
     a3_zero(aux, k0, k1);
-    for (int j = jm; j >= 2; j -= 2) {
-        int jL = j / 2;
-        for (int i = im; i >= 1; --i)
-            for (int k = k0; k < k1; ++k) {
-                double f = A3(F, k, i, j);
-                A3(aux, k, i, jL + 2) += PC[3] * f;
-                A3(aux, k, i, jL + 1) += PC[2] * f;
-                A3(aux, k, i, jL) += PC[1] * f;
-                A3(aux, k, i, jL - 1) += PC[0] * f;
+    if (!ROWPAR) {
+        for (int j = jm; j >= 2; j -= 2) {
+            int jL = j / 2;
+            for (int i = im; i >= 1; --i)
+                for (int k = k0; k < k1; ++k) {
+                    double f = A3(F, k, i, j);
+                    A3(aux, k, i, jL + 2) += PC[3] * f;
+                    A3(aux, k, i, jL + 1) += PC[2] * f;
+                    A3(aux, k, i, jL) += PC[1] * f;
+                    A3(aux, k, i, jL - 1) += PC[0] * f;
+                }
+        }
+        for (int j = jm - 1; j >= 1; j -= 2) {
+            int jL = j / 2;
+            for (int i = im; i >= 1; --i)
+                for (int k = k0; k < k1; ++k) {
+                    double f = A3(F, k, i, j);
+                    A3(aux, k, i, jL + 2) += QC[3] * f;
+                    A3(aux, k, i, jL + 1) += QC[2] * f;
+                    A3(aux, k, i, jL) += QC[1] * f;
+                    A3(aux, k, i, jL - 1) += QC[0] * f;
+                }
+        }
+    } else {
+        /* target-row form of the two loops above: row r of aux takes the
+         * even fine rows j = 2jL, jL = r+1 .. r-2 (decreasing, as j
+         * decreases above), with weight PC[r-jL+1], then the odd rows
+         * j = 2jL+1 in the same order with QC[r-jL+1] */
+        ROW_FOR
+        for (int r = -1; r <= jmL + 2; ++r) {
+            for (int jL = r + 1; jL >= r - 2; --jL) {
+                if (jL < 1 || jL > jmL) continue;
+                const double c = PC[r - jL + 1];
+                for (int i = im; i >= 1; --i)
+                    for (int k = k0; k < k1; ++k) A3(aux, k, i, r) += c * A3(F, k, i, 2 * jL);
             }
-    }
-    for (int j = jm - 1; j >= 1; j -= 2) {
-        int jL = j / 2;
-        for (int i = im; i >= 1; --i)
-            for (int k = k0; k < k1; ++k) {
-                double f = A3(F, k, i, j);
-                A3(aux, k, i, jL + 2) += QC[3] * f;
-                A3(aux, k, i, jL + 1) += QC[2] * f;
-                A3(aux, k, i, jL) += QC[1] * f;
-                A3(aux, k, i, jL - 1) += QC[0] * f;
+            for (int jL = r + 1; jL >= r - 2; --jL) {
+                if (jL < 0 || jL > jmL - 1) continue;
+                const double c = QC[r - jL + 1];
+                for (int i = im; i >= 1; --i)
+                    for (int k = k0; k < k1; ++k) A3(aux, k, i, r) += c * A3(F, k, i, 2 * jL + 1);
             }
+        }
     }
     a3_zero(W, k0, k1);
+    ROW_FOR
     for (int jL = jmL + 2; jL >= -1; --jL) {
         for (int i = im - 1; i >= 1; i -= 2) {
             int iL = i / 2;
@@ -1045,6 +1159,7 @@ static void adjoint4(arr3 F, arr3 W, arr3 aux, int im, int jm, int k0, int k1) {
  * W(-1:imL+2,-1:jmL+2) to F(1:im,1:jm); aux is (nk, 1:im, -1:jmL+2). */
 static void direct4(arr3 W, arr3 F, arr3 aux, int im, int jm, int k0, int k1) {
     int jmL = jm / 2;
+    ROW_FOR
     for (int jL = -1; jL <= jmL + 2; ++jL) {
         for (int i = 1; i <= im - 1; i += 2) {
             int iL = i / 2;
@@ -1059,6 +1174,7 @@ static void direct4(arr3 W, arr3 F, arr3 aux, int im, int jm, int k0, int k1) {
                                     PC[2] * A3(W, k, iL + 1, jL) + PC[3] * A3(W, k, iL + 2, jL);
         }
     }
+    ROW_FOR
     for (int j = 1; j <= jm - 1; j += 2) {
         int jL = j / 2;
         for (int i = 1; i <= im; ++i)
@@ -1066,6 +1182,7 @@ static void direct4(arr3 W, arr3 F, arr3 aux, int im, int jm, int k0, int k1) {
                 A3(F, k, i, j) = QC[0] * A3(aux, k, i, jL - 1) + QC[1] * A3(aux, k, i, jL) +
                                  QC[2] * A3(aux, k, i, jL + 1) + QC[3] * A3(aux, k, i, jL + 2);
     }
+    ROW_FOR
     for (int j = 2; j <= jm; j += 2) {
         int jL = j / 2;
         for (int i = 1; i <= im; ++i)
@@ -1280,6 +1397,7 @@ static void restrict_gen(const orc_cfg* c, arr3 fine, gen_t* Gf, arr3 coarse, in
     if (!c->lquart) {
         adjoint4(fine, Gf->INT, Gf->aux, I, J, k0, k1);
         fold_h(Gf->INT, IL, JL, 2, 2, k0, k1);
+        ROW_FOR
         for (int j = 1; j <= JL; ++j)
             for (int i = 1; i <= IL; ++i)
                 for (int k = k0; k < k1; ++k) A3(coarse, k, i, j) = A3(Gf->INT, k, i, j);
@@ -1303,6 +1421,7 @@ static void prolong_add(const orc_cfg* c, arr3 coarse, gen_t* Gf, arr3 fine, int
     arr3 W = Gf->INT, aux = Gf->aux;
     int nb = 2;
     if (c->lquart) { W.ilo = 0; W.ihi = IL + 1; W.jlo = 0; W.jhi = JL + 1; aux.jlo = 0; aux.jhi = JL + 1; nb = 1; }
+    ROW_FOR
     for (int j = 1; j <= JL; ++j)
         for (int i = 1; i <= IL; ++i)
             for (int k = k0; k < k1; ++k) A3(W, k, i, j) = A3(coarse, k, i, j);
@@ -1312,6 +1431,7 @@ static void prolong_add(const orc_cfg* c, arr3 coarse, gen_t* Gf, arr3 fine, int
     arr3 Fi = F; /* interior-only view for direct: reuse the full array */
     if (!c->lquart) direct4(W, Fi, aux, I, J, k0, k1);
     else direct3(W, Fi, aux, I, J, k0, k1);
+    ROW_FOR
     for (int j = 1; j <= J; ++j)
         for (int i = 1; i <= I; ++i)
             for (int k = k0; k < k1; ++k) A3(fine, k, i, j) += A3(F, k, i, j);
@@ -1324,6 +1444,7 @@ static void weight_gen(const orc_cfg* c, arr3 V, int I, int J, double a, double 
             /* a*V - 0*(Laplacian): the Laplacian reads halo cells left by the
              * fold; they are finite, so the product is exactly zero. */
         }
+        ROW_FOR
         for (int j = 1; j <= J; ++j)
             for (int i = 1; i <= I; ++i)
                 for (int k = k0; k < k1; ++k) A3(V, k, i, j) *= a;
@@ -1386,6 +1507,13 @@ static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_
             lin2_forward(c, S, U, G[g].tmp, I, J, k0, k1);
             continue;
         }
+        if (c->a[g] == 0.0 && c->b[g] == 0.0) {
+            /* a zero-weighted generation filters to exact zeros (the weight
+             * zeroes the interior, fill_h then every halo cell, and vrbeta2
+             * of zeros is zero): skip its filters */
+            a3_zero(U, k0, k1);
+            continue;
+        }
         vrbeta2t(S, c->p, U, G[g].tmp, 1, I, 1, J, k0, k1);
         fold_h(U, I, J, hx, hy, k0, k1);
         weight_gen(c, U, I, J, c->a[g], c->b[g], k0, k1);
@@ -1403,6 +1531,7 @@ static void horizontal_pipeline(const orc_cfg* c, const setup_t* S, arr3 V, gen_
 int orc_filtering_procedure(const orc_cfg* c, double* Vd) {
     int rc = check_cfg(c);
     if (rc) return rc;
+    set_threads(c->nthreads);
     setup_t S;
     rc = setup(c, &S);
     if (rc) return rc;
@@ -1415,14 +1544,20 @@ int orc_filtering_procedure(const orc_cfg* c, double* Vd) {
     gens_alloc(c, G);
     int nth = 1;
 #ifdef _OPENMP
-    nth = c->nthreads > 0 ? c->nthreads : omp_get_max_threads();
+    nth = g_threads;
     if (nth > c->nk) nth = c->nk;
     if (c->proc == 4 || c->proc == 5) nth = 1;
+    if ((c->proc == 1 || c->proc == 6) && c->nk < 16 * g_threads && g_threads > 1) {
+        /* few levels per thread: the radial pipeline over all levels, its
+         * loops split by rows (ROWPAR) instead of the levels by thread */
+        horizontal_pipeline(c, &S, V, G, 0, c->nk);
+    } else {
 #pragma omp parallel num_threads(nth)
-    {
-        int t = omp_get_thread_num(), nt = omp_get_num_threads();
-        int k0 = (int)((long long)c->nk * t / nt), k1 = (int)((long long)c->nk * (t + 1) / nt);
-        if (k1 > k0) horizontal_pipeline(c, &S, V, G, k0, k1);
+        {
+            int t = omp_get_thread_num(), nt = omp_get_num_threads();
+            int k0 = (int)((long long)c->nk * t / nt), k1 = (int)((long long)c->nk * (t + 1) / nt);
+            if (k1 > k0) horizontal_pipeline(c, &S, V, G, k0, k1);
+        }
     }
 #else
     (void)nth;
@@ -1440,6 +1575,7 @@ static double* to_halo(const orc_cfg* c, const double* x) {
     double* V = (double*)calloc((size_t)c->nk * ni * nj, sizeof(double));
     if (!V) return NULL;
     arr3 a = {V, c->nk, 1 - c->hx, c->I + c->hx, 1 - c->hy, c->J + c->hy};
+    ROW_FOR
     for (int j = 1; j <= c->J; ++j)
         for (int i = 1; i <= c->I; ++i)
             memcpy(&A3(a, 0, i, j), x + (size_t)c->nk * ((size_t)(i - 1) + (size_t)c->I * (j - 1)),
@@ -1448,6 +1584,7 @@ static double* to_halo(const orc_cfg* c, const double* x) {
 }
 static void from_halo(const orc_cfg* c, const double* V, double* y) {
     arr3 a = {(double*)V, c->nk, 1 - c->hx, c->I + c->hx, 1 - c->hy, c->J + c->hy};
+    ROW_FOR
     for (int j = 1; j <= c->J; ++j)
         for (int i = 1; i <= c->I; ++i)
             memcpy(y + (size_t)c->nk * ((size_t)(i - 1) + (size_t)c->I * (j - 1)), &A3(a, 0, i, j),
@@ -1457,6 +1594,7 @@ static void from_halo(const orc_cfg* c, const double* V, double* y) {
 int orc_filter_compact(const orc_cfg* c, const double* x, double* y) {
     int rc = check_cfg(c);
     if (rc) return rc;
+    set_threads(c->nthreads);
     double* V = to_halo(c, x);
     if (!V) return ORC_ERR_ARG;
     rc = orc_filtering_procedure(c, V);
@@ -1491,6 +1629,7 @@ static void half_chain(const orc_cfg* c, const setup_t* S, arr3 V, gen_t* G) {
 int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double* ga) {
     int rc = check_cfg(c);
     if (rc) return rc;
+    set_threads(c->nthreads);
     /* proc 4: its adjoint side is not the transpose of its forward side;
      * proc 7: Bz^T M Bz^T, so the gy chain would need Bz, not Bz^T */
     if (c->proc == 4 || c->proc == 5 || c->proc == 7) return ORC_ERR_ARG;
@@ -1524,6 +1663,7 @@ int orc_weight_grads(const orc_cfg* c, const double* x, const double* gy, double
 int orc_stage(const orc_cfg* c, int which, int gen, const double* x, double* y) {
     int rc = check_cfg(c);
     if (rc) return rc;
+    set_threads(c->nthreads);
     setup_t S;
     rc = setup(c, &S);
     if (rc) return rc;

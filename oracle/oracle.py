@@ -179,6 +179,33 @@ def stage(cfg: OracleConfig, which: int, gen: int, x: np.ndarray) -> np.ndarray:
     return y
 
 
+def contributions(cfg: OracleConfig, x: np.ndarray) -> list:
+    """Per-generation terms of the radial procedures 1 and 6:
+    y_g = Bz P_{1<-g} B_g a_g B_g R_{g<-1} Bz^T x for g = 1..gm, composed from
+    the oracle's stages in the order of orc_filtering_procedure (vertical
+    adjoint, restrictions, per generation vrbeta2t + fold, weight, fill +
+    vrbeta2, prolongations, vertical forward).  Without l_filt_g1 (proc 6)
+    generation 1 is neither filtered nor weighted.  sum_g y_g equals
+    filter_compact(cfg, x) up to rounding."""
+    assert cfg.proc in (1, 6), "radial procedures only"
+    z = bool(cfg.l_vertical_filter and cfg.nzcol > 0)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    h = [stage(cfg, STAGE_Z_ADJ, 1, x) if z else x.copy()]
+    for g in range(1, cfg.gm):
+        h.append(stage(cfg, STAGE_RESTRICT, g, h[-1]))
+    filt1 = cfg.proc == 1 or cfg.l_filt_g1
+    out = []
+    for g in range(cfg.gm):
+        if g == 0 and not filt1:
+            u = h[0]
+        else:
+            u = stage(cfg, STAGE_H_FWD, g + 1, cfg.weights[g] * stage(cfg, STAGE_H_ADJ, g + 1, h[g]))
+        for fine in range(g, 0, -1):  # generation fine+1 -> fine
+            u = stage(cfg, STAGE_PROLONG, fine, u)
+        out.append(stage(cfg, STAGE_Z_FWD, 1, u) if z else u)
+    return out
+
+
 def setup_values(cfg: OracleConfig) -> dict:
     out = np.zeros(11, dtype=np.float64)
     c = cfg.to_c()

@@ -123,3 +123,37 @@ def test_helper_maps_namelist_config():
     c = small_config()
     oc = oracle_cfg(c, 1)
     assert (oc.I, oc.J, oc.nk, oc.gm, oc.nzcol) == (64, 48, 16, 3, 2)
+
+
+@pytest.mark.parametrize("proc,l_filt_g1,lquart", [(1, True, False), (6, True, True), (6, False, False)])
+def test_per_generation_contributions_sum_to_the_operator(proc, l_filt_g1, lquart):
+    """oracle.contributions (the per-generation terms y_g reported against the
+    GPU) adds up to filtering_procedure's output."""
+    c = cfg(I=48, J=32, nk=12, lm=6, nzcol=2, proc=proc, l_filt_g1=l_filt_g1, lquart=lquart, gm=3)
+    x = rng.standard_normal((c.J, c.I, c.nk))
+    ys = O.contributions(c, x)
+    y = O.filter_compact(c, x)
+    assert len(ys) == c.gm
+    assert np.linalg.norm(sum(ys) - y) <= 1e-14 * np.linalg.norm(y)
+    # a generation's term equals the operator with only that weight kept
+    # (without l_filt_g1 the unfiltered generation-1 term stays in every run)
+    for g in range(c.gm):
+        w = [c.weights[q] if q == g else 0.0 for q in range(c.gm)]
+        yg = O.filter_compact(O.OracleConfig(**{**c.__dict__, "weights": w}), x)
+        ref = ys[g] if (l_filt_g1 or proc == 1 or g == 0) else ys[g] + ys[0]
+        assert np.linalg.norm(ref - yg) <= 1e-14 * np.linalg.norm(yg)
+
+
+@pytest.mark.parametrize("proc", [1, 6])
+def test_row_parallel_and_level_split_runs_are_bit_identical(proc):
+    """With few levels per thread the radial pipeline splits rows instead of
+    levels over the threads (and runs the scatters in target-row form); the
+    results must not change by a single bit."""
+    c = cfg(I=64, J=48, nk=32, lm=8, nzcol=4, proc=proc, gm=3, hx=5, hy=5, ampl02=canonical(5))
+    x = rng.standard_normal((c.J, c.I, c.nk))
+    gy = rng.standard_normal((c.J, c.I, c.nk))
+    ys = [O.filter_compact(O.OracleConfig(**{**c.__dict__, "nthreads": n}), x) for n in (1, 2, 4, 8)]
+    gs = [O.weight_grads(O.OracleConfig(**{**c.__dict__, "nthreads": n}), x, gy) for n in (1, 2, 4, 8)]
+    for y, g in zip(ys[1:], gs[1:]):
+        assert np.array_equal(y, ys[0])
+        assert np.array_equal(g, gs[0])
