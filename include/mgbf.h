@@ -151,8 +151,16 @@ int mgbf_get_line_filters(const mgbf_handle* h, int gen[6], int hspan[3], double
  * (mg_filtering.f90:1150-1313: the same line filters over the stacked
  * members, l_filt_g1 and lquart as for 6, ending like the reference with the
  * ADJOINT vertical filter sup_vrbeta1T_ens, so the operator is not
- * symmetric).  5 returns MGBF_ERR_UNSUPPORTED; any other value is a no-op
- * returning MGBF_OK, as the reference's select has no default case.
+ * symmetric), and
+ * 5 = filtering_lin3 (mg_filtering.f90:260-557: the 2D variables through the
+ * line filters of 2, the 3D variables through the seven colors of the hexad
+ * decomposition, jp_pbfil3.f90:798-904, of the Cholesky factor of the
+ * inverse 3D aspect mg_ampl03, each color a dibeta line along its 3D
+ * generator between the reference's 3D halo routines, whose generation-1
+ * forms mirror the east edge about the last column and fold the east column
+ * and north row onto themselves, so the operator is not symmetric; no
+ * separate vertical filter).  Any other value is a no-op returning MGBF_OK,
+ * as the reference's select has no default case.
  *   vall:   field pointer (device or host, per mem), laid out per the
  *           handle's layout, element type per dtype.
  *   stream: cudaStream_t (NULL = legacy default stream).  Device calls are
@@ -184,8 +192,8 @@ int mgbf_filt_to_anal(mgbf_handle* h, void* vall, void* worka, int dtype, int me
 /* Adjoint of filtering_procedure(mg_filt), run through the explicit
  * transposed chain (no reference counterpart: the reference's adjoint test
  * is an empty stub, RBETA_TEST.f90:64-69).  Procedures 1, 2, 3, 6 and 8 are
- * self-adjoint, so the result equals the forward up to rounding; 4 and 7
- * are not and return MGBF_ERR_UNSUPPORTED. */
+ * self-adjoint, so the result equals the forward up to rounding; 4, 5 and
+ * 7 are not and return MGBF_ERR_UNSUPPORTED. */
 int mgbf_filtering_procedure_adjoint(mgbf_handle* h, int mg_filt, void* vall, int dtype, int mem,
                                      void* stream);
 
@@ -195,8 +203,8 @@ int mgbf_filtering_procedure_adjoint(mgbf_handle* h, int mg_filt, void* vall, in
  *   u_g = B_g R_g Bz^T x, v_g = B_g R_g Bz^T gy, for g = 1..gm.
  * x, gy, gx: fields in the handle's layout (gx may alias gy).  ga: host
  * array of gm doubles.  Coarse generations are recomputed from x.
- * Returns after ga is on the host.  Procedures 4 and 7 (not self-adjoint)
- * return MGBF_ERR_UNSUPPORTED.
+ * Returns after ga is on the host.  Procedures 4, 5 and 7 (not
+ * self-adjoint) return MGBF_ERR_UNSUPPORTED.
  */
 int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, const void* gy,
                                  void* gx, double* ga, int dtype, int mem, void* stream);

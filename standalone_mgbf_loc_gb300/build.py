@@ -25,12 +25,15 @@ SOURCES = [
     "mgbf_setup.cpp",
     "mgbf_kernels.cu",
     "mgbf_hbeta_f32.cu",
+    "mgbf_hbeta_f32_b.cu",
     "mgbf_hbeta_f64.cu",
     "mgbf_hbeta_bf16.cu",
+    "mgbf_hbeta_bf16_b.cu",
     "mgbf_noalloc.cu",
     "mgbf_xfer.cu",
     "mgbf_rad3.cu",
     "mgbf_dibeta.cu",
+    "mgbf_lin3.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -249,6 +249,10 @@ struct Group {
     DStencil ds;         // filtering_lin2_bckg's three line filters (proc 2)
     std::string ds_err;
     int ds_rc = 0;
+    XStencil xs;         // filtering_lin3's hexad of 3D line filters (proc 5)
+    std::string xs_err;
+    int xs_rc = 0;
+    int n3 = 0;          // leading levels held by the 3D variables (km3*lm of one member)
     DevBuf btaps, bw[2];  // ball taps (int4) and weights per accumulation type
     DevBuf brows, brw[2];  // the ball's rows along x (int2) and their weights
     int HXP = 0;  // x padding of internal generation buffers
@@ -257,6 +261,11 @@ struct Group {
     // internal buffers per storage type and generation: A, B, C
     struct Set {
         std::vector<std::unique_ptr<DevBuf>> A, B, C, D;  // D: between the fast filters' two line passes
+        // proc 5: the two 3D work arrays of each generation, and which of
+        // them holds the current state (it carries the halo values the
+        // adjoint side leaves over to the forward side, as in the reference)
+        std::vector<std::unique_ptr<DevBuf>> E, F;
+        int l3cur[MGBF_MAX_GEN] = {0};
     } bufs[3];
     // TMA maps of the A/B buffers: key = dtype*64 + gen*2 + (0: A, 1: B),
     // each with the base address it was encoded for
@@ -331,6 +340,29 @@ View gen_view(const Plan& P, const Group& G, void* base, DType t, int g) {
     return v;
 }
 
+// proc 5's work arrays: n3/lm columns x (I_g+2hx) x (J_g+2hy) x (lm+2hz),
+// zeroed when first allocated
+int ensure_lin3_bufs(Plan& P, Group& G, DType t) {
+    auto& S = G.bufs[(int)t];
+    const int nv = G.n3 / G.lm;
+    auto grow = [&](std::vector<std::unique_ptr<DevBuf>>& v) -> int {
+        if ((int)v.size() < P.gm) v.resize(P.gm);
+        for (int g = 0; g < P.gm; ++g) {
+            if (!v[g]) v[g].reset(new DevBuf);
+            const size_t n = (size_t)nv * (size_t)(gen_I(P, g) + 2 * G.hx) * (size_t)(gen_J(P, g) + 2 * G.hy) *
+                             (size_t)(G.lm + 2 * G.hz) * elem_size(t);
+            if (v[g]->bytes >= n && v[g]->p) continue;
+            int rc = v[g]->ensure(n);
+            if (rc) return rc;
+            CU(cudaMemset(v[g]->p, 0, n));
+        }
+        return 0;
+    };
+    int rc;
+    if ((rc = grow(S.E))) return rc;
+    return grow(S.F);
+}
+
 int ensure_bufs(Plan& P, Group& G, DType t, bool needC, bool needD = false) {
     auto& S = G.bufs[(int)t];
     auto grow = [&](std::vector<std::unique_ptr<DevBuf>>& v) -> int {
@@ -364,6 +396,7 @@ struct Exec {
     View D(int g) { return gen_view(P, G, G.bufs[(int)t].D[g]->p, t, g); }
     bool fast = false;  // procs 3 and 8: separable line filters instead of the radial disk
     bool lin2 = false;  // procs 2, 7: three line filters along the triad's generators
+    bool lin3 = false;  // proc 5: the hexad's 3D line filters on the 3D variables, proc 2's on the 2D ones
     bool zadj_out = false;  // proc 7: ends with the adjoint vertical filter (mg_filtering.f90:1304)
     int n3 = -1;        // proc 4: levels of the 3D variables (ball); the rest take the 2D radial filter
     bool has_prev = false;  // proc 4, generation 1: the caller's halo, folded by the adjoint side
@@ -524,10 +557,92 @@ struct Exec {
         return 0;
     }
 
+    // One color q of proc 2's line filters on the levels k0..nk-1.
+    int dib_from(int g, View in, View out, int q, bool adjoint, double scale, int k0) {
+        DibArgs a;
+        a.in = in; a.out = out;
+        a.in.p = static_cast<char*>(in.p) + elem_size(t) * (size_t)k0;
+        a.out.p = static_cast<char*>(out.p) + elem_size(t) * (size_t)k0;
+        a.nk = G.nk - k0; a.I = gen_I(P, g); a.J = gen_J(P, g);
+        a.dx = G.ds.dx[q]; a.dy = G.ds.dy[q]; a.h = G.ds.h[q];
+        a.hx = G.hx; a.hy = G.hy; a.adjoint = adjoint ? 1 : 0;
+        for (int i = 0; i < 9; ++i) a.fil[i] = G.ds.fil[q][i];
+        a.scale = scale;
+        LK(launch_dibeta(t, a, stream));
+        return 0;
+    }
+
+    // filtering_lin3 (mg_filtering.f90:260-557), one side of generation g.
+    // 2D variables (levels n3..nk-1): proc 2's colors 3, 2, 1 (adjoint side)
+    // or 1, 2, 3 (forward side).  3D variables: the adjoint side runs colors
+    // 7..1 as vdibetax3t + bocoT_3d (the z mirror the reference applies
+    // before each of them is overwritten by the scatter, which reads the
+    // interior only) and the weight; the forward side mirrors the z halo
+    // once, then runs colors 1..7 as boco_3d (+ the z mirror at coarser
+    // generations) + vdibetax3.
+    int lin3_pass(int g, View in, View out, double scale, bool adj) {
+        int rc;
+        const int n3 = G.n3;
+        if (G.nk > n3) {
+            const int q0 = adj ? 2 : 0, dq = adj ? -1 : 1;
+            if ((rc = dib_from(g, in, out, q0, adj, 1.0, n3))) return rc;
+            if ((rc = dib_from(g, out, D(g), q0 + dq, adj, 1.0, n3))) return rc;
+            if ((rc = dib_from(g, D(g), out, q0 + 2 * dq, adj, scale, n3))) return rc;
+        }
+        if (n3 <= 0) return 0;
+        auto& S = G.bufs[(int)t];
+        void* buf[2] = {S.E[g]->p, S.F[g]->p};
+        int cur = S.l3cur[g];
+        Lin3Args a{};
+        a.in = in; a.out = out;
+        a.nv = n3 / G.lm; a.lm = G.lm; a.I = gen_I(P, g); a.J = gen_J(P, g);
+        a.hx = G.hx; a.hy = G.hy; a.hz = G.hz; a.gh = g > 0 ? 1 : 0;
+        auto run = [&](int op) -> int {
+            a.w = buf[cur];
+            a.t = buf[1 - cur];
+            LK(launch_lin3(t, a, op, stream));
+            return 0;
+        };
+        auto color = [&](int col) {
+            const int q = G.xs.slot[col];
+            for (int i = 0; i <= kMaxL3Span; ++i) a.fil[i] = 0.0;
+            if (q < 0) {  // no line of this color: the value is copied
+                a.dx = a.dy = a.dz = 0; a.h = 0; a.fil[0] = 1.0;
+            } else {
+                a.dx = G.xs.g[q][0]; a.dy = G.xs.g[q][1]; a.dz = G.xs.g[q][2]; a.h = G.xs.h[q];
+                for (int i = 0; i <= a.h && i <= kMaxL3Span; ++i) a.fil[i] = G.xs.fil[q][i];
+            }
+        };
+        if ((rc = run(kL3From))) return rc;
+        if (adj) {
+            for (int col = 7; col >= 1; --col) {
+                color(col);
+                if ((rc = run(kL3DibAdj))) return rc;
+                cur = 1 - cur;
+                if ((rc = run(kL3FoldX)) || (rc = run(kL3FoldY)) || (rc = run(kL3FoldZ))) return rc;
+            }
+            a.scale = scale;
+        } else {
+            if ((rc = run(kL3ZMirror))) return rc;
+            for (int col = 1; col <= 7; ++col) {
+                if ((rc = run(kL3FillY)) || (rc = run(kL3FillX))) return rc;
+                if (a.gh && (rc = run(kL3ZMirror))) return rc;
+                color(col);
+                if ((rc = run(kL3DibFwd))) return rc;
+                cur = 1 - cur;
+            }
+            a.scale = 1.0;
+        }
+        if ((rc = run(kL3To))) return rc;
+        S.l3cur[g] = cur;
+        return 0;
+    }
+
     int hpass(int g, View in, View out, double scale, int mirror, int stage, int which_in) {
         const int I = gen_I(P, g), J = gen_J(P, g);
         StageTimer tm(stage, stream, pts(g));
         if (n3 >= 0) return rad3_pass(g, in, out, scale, mirror, which_in);
+        if (lin3) return lin3_pass(g, in, out, scale, which_in == 0);
         if (lin2) {
             // adjoint side: colors 3, 2, 1; forward side: colors 1, 2, 3;
             // in -> out -> D -> out, the generation weight on the last pass
@@ -654,8 +769,14 @@ struct mgbf_batch {
     };
     std::vector<GraphEntry> graphs;
     cudaStream_t cap_stream = nullptr;
+    // the graph runs the variable groups' pipelines as concurrent branches:
+    // one capture stream per group, forked from and joined into cap_stream
+    std::vector<cudaStream_t> branch;
+    std::vector<cudaEvent_t> branch_ev;  // [0]: fork, [1 + q]: group q done
     ~mgbf_batch() {
         for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
+        for (auto st : branch) cudaStreamDestroy(st);
+        for (auto e : branch_ev) cudaEventDestroy(e);
         if (cap_stream) cudaStreamDestroy(cap_stream);
     }
 };
@@ -739,6 +860,13 @@ int build_group(Plan& P, Group& G, bool zneeded) {
         }
     } else {
         G.bs_err = "mg_ampl03 must be positive";
+    }
+    // filtering_lin3's hexad: an error only when proc 5 runs
+    G.xs_err.clear();
+    G.xs_rc = build_xstencil(G.p, G.ampl03, G.hx, G.hy, G.hz, G.line, G.xs, err);
+    if (G.xs_rc) {
+        G.xs_err = err;
+        G.xs.ok = false;
     }
     // filtering_lin2_bckg's line filters: an error only when proc 2 runs.
     // Without mgbf_line the reference never calls init_mg_line: the
@@ -1075,6 +1203,7 @@ int mgbf_create(const mgbf_config* cfg, mgbf_handle** out) {
     P.groups.resize(1);
     Group& G = P.groups[0];
     G.nk = km_all; G.lm = c.lm; G.nzcol = c.km3 * c.n_ens;
+    G.n3 = c.km3 * c.lm;
     G.hx = c.hx; G.hy = c.hy; G.hz = c.hz; G.p = c.p;
     G.ampl01 = c.mg_ampl01; G.ampl02 = c.mg_ampl02; G.ampl03 = c.mg_ampl03;
     G.line = c.mgbf_line != 0;
@@ -1134,15 +1263,27 @@ int mgbf_set_weights(mgbf_handle* h, const double* a, int n) {
 }
 
 static bool is_fast(int mg_filt) { return mg_filt == 3 || mg_filt == 8; }
-static bool is_bckg(int mg_filt) { return mg_filt == 1 || mg_filt == 2 || mg_filt == 3 || mg_filt == 4; }
+static bool is_bckg(int mg_filt) {
+    return mg_filt == 1 || mg_filt == 2 || mg_filt == 3 || mg_filt == 4 || mg_filt == 5;
+}
 static bool is_lin2(int mg_filt) { return mg_filt == 2 || mg_filt == 7; }
-static bool needs_d(int mg_filt) { return is_fast(mg_filt) || is_lin2(mg_filt); }
+static bool needs_d(int mg_filt) { return is_fast(mg_filt) || is_lin2(mg_filt) || mg_filt == 5; }
 
 static int check_proc(mgbf_handle* h, int mg_filt, bool& noop) {
     noop = false;
-    if (mg_filt == 1 || mg_filt == 2 || mg_filt == 6 || mg_filt == 7 || mg_filt == 3 || mg_filt == 8 || mg_filt == 4) {
+    if (mg_filt >= 1 && mg_filt <= 8) {
         if (is_bckg(mg_filt) && h->cfg.n_ens != 1)
-            return fail(MGBF_ERR_CONFIG, "filtering_rad2_bckg / filtering_lin2_bckg / filtering_fast_bckg / filtering_rad3 (procs 1, 2, 3, 4) need n_ens = 1: their arrays are dimensioned km, not km_all");
+            return fail(MGBF_ERR_CONFIG, "filtering_rad2_bckg / filtering_lin2_bckg / filtering_fast_bckg / filtering_rad3 / filtering_lin3 (procs 1-5) need n_ens = 1: their arrays are dimensioned km, not km_all");
+        if (mg_filt == 5) {
+            const Group& G = h->plan.groups[0];
+            if (h->cfg.km3 > 0 && !G.xs.ok)
+                return fail(G.xs_rc ? G.xs_rc : MGBF_ERR_CONFIG, "filtering_lin3: " + G.xs_err);
+            if (h->cfg.km2 > 0 && !G.ds.ok)
+                return fail(G.ds_rc ? G.ds_rc : MGBF_ERR_CONFIG, "filtering_lin3: " + G.ds_err);
+            if (h->cfg.km3 > 0 && h->cfg.hz >= h->cfg.lm)
+                return fail(MGBF_ERR_CONFIG, "filtering_lin3: the z halo mirror needs hz < lm");
+            return MGBF_OK;
+        }
         if (is_lin2(mg_filt) && !h->plan.groups[0].ds.ok)
             return fail(h->plan.groups[0].ds_rc ? h->plan.groups[0].ds_rc : MGBF_ERR_CONFIG,
                         (mg_filt == 2 ? "filtering_lin2_bckg: " : "filtering_lin2_ens: ") + h->plan.groups[0].ds_err);
@@ -1161,8 +1302,6 @@ static int check_proc(mgbf_handle* h, int mg_filt, bool& noop) {
             return fail(MGBF_ERR_DIVISIBILITY, h->plan.groups[0].ls_err);
         return MGBF_OK;
     }
-    if (mg_filt >= 2 && mg_filt <= 8)
-        return fail(MGBF_ERR_UNSUPPORTED, "filtering procedure " + std::to_string(mg_filt) + " is not implemented (supported: 1, 2, 3, 4, 6, 7, 8)");
     noop = true;  // no case default in the reference's select
     return MGBF_OK;
 }
@@ -1183,13 +1322,16 @@ static int run_proc(mgbf_handle* h, int mg_filt, const void* xin, void* yout, DT
     int rc;
     if ((rc = ensure_tables(P, G, t))) return rc;
     if ((rc = ensure_bufs(P, G, t, false, needs_d(mg_filt)))) return rc;
-    const bool rad3 = mg_filt == 4;
-    const int nzcol = (!rad3 && h->cfg.l_vertical_filter && h->cfg.lm > 1)
-                          ? (is_bckg(mg_filt) ? h->nzcol_proc1 : h->nzcol_proc6) : 0;  // rad3: no separate z filter
+    const bool rad3 = mg_filt == 4, lin3 = mg_filt == 5;
+    if (lin3 && G.n3 > 0 && (rc = ensure_lin3_bufs(P, G, t))) return rc;
+    // rad3 and lin3: no separate z filter
+    const int nzcol = (!rad3 && !lin3 && h->cfg.l_vertical_filter && h->cfg.lm > 1)
+                          ? (is_bckg(mg_filt) ? h->nzcol_proc1 : h->nzcol_proc6) : 0;
     const bool filt1 = is_bckg(mg_filt) || h->cfg.l_filt_g1;
     Exec ex{P, G, t, stream};
     ex.fast = is_fast(mg_filt);
     ex.lin2 = is_lin2(mg_filt);
+    ex.lin3 = lin3;
     ex.zadj_out = mg_filt == 7;
     View x = field_view(h, const_cast<void*>(xin), t);
     View y = field_view(h, yout, t);
@@ -1251,9 +1393,10 @@ int mgbf_filtering_procedure_adjoint(mgbf_handle* h, int mg_filt, void* vall, in
     // transposing each stage in reverse order reproduces the same launch
     // sequence (Bz^T first, restriction = P^T, B^T = B, a_g, B, P, Bz).
     // filtering_rad3's adjoint side is not the transpose of its forward side.
-    if (mg_filt == 4 || mg_filt == 7)
+    if (mg_filt == 4 || mg_filt == 5 || mg_filt == 7)
         return fail(MGBF_ERR_UNSUPPORTED, std::string("adjoint of ") +
-                                              (mg_filt == 4 ? "filtering_rad3" : "filtering_lin2_ens") +
+                                              (mg_filt == 4 ? "filtering_rad3"
+                                                            : mg_filt == 5 ? "filtering_lin3" : "filtering_lin2_ens") +
                                               ": the operator is not self-adjoint");
     return with_field(h, mg_filt, vall, dtype, mem, stream);
 }
@@ -1273,6 +1416,9 @@ int mgbf_apply_with_weight_grads(mgbf_handle* h, int mg_filt, const void* x, con
     if (mg_filt == 7)
         return fail(MGBF_ERR_UNSUPPORTED,
                     "weight gradients of filtering_lin2_ens: it ends with the adjoint vertical filter, so it is not self-adjoint");
+    if (mg_filt == 5)
+        return fail(MGBF_ERR_UNSUPPORTED,
+                    "weight gradients of filtering_lin3: its generation-1 halo routines make it not self-adjoint");
     DeviceGuard dg(h->plan.device);
     const DType t = (DType)dtype;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1755,17 +1901,38 @@ int mgbf_batch_create(int im, int jm, int gm, const double* weights, int lquart,
     return MGBF_OK;
 }
 
-static int batch_launch(mgbf_batch* b, void* const* fields, DType t, void* stream) {
+static int batch_group(mgbf_batch* b, void* const* fields, DType t, size_t q, void* stream) {
     Plan& P = b->plan;
+    Group& G = P.groups[q];
+    View v;
+    v.p = fields[q]; v.si = G.nk; v.sj = (long long)G.nk * P.I;
+    Exec ex{P, G, t, stream};
+    ex.fast = b->proc == 8;
+    const int nzcol = (G.lm > 1) ? G.nzcol : 0;
+    return ex.forward(v, v, nzcol, b->filt1);
+}
+
+static int batch_launch(mgbf_batch* b, void* const* fields, DType t, void* stream) {
     int rc;
-    for (size_t q = 0; q < P.groups.size(); ++q) {
-        Group& G = P.groups[q];
-        View v;
-        v.p = fields[q]; v.si = G.nk; v.sj = (long long)G.nk * P.I;
-        Exec ex{P, G, t, stream};
-        ex.fast = b->proc == 8;
-        const int nzcol = (G.lm > 1) ? G.nzcol : 0;
-        if ((rc = ex.forward(v, v, nzcol, b->filt1))) return rc;
+    for (size_t q = 0; q < b->plan.groups.size(); ++q)
+        if ((rc = batch_group(b, fields, t, q, stream))) return rc;
+    return MGBF_OK;
+}
+
+// The groups' pipelines as branches that fork from `stream` and join back
+// into it (while `stream` is being captured, the branch streams join the
+// capture through the fork event), so that a graph may run the groups'
+// kernels side by side; the small coarse-generation launches of one group
+// then overlap the work of the others.
+static int batch_launch_branches(mgbf_batch* b, void* const* fields, DType t, cudaStream_t stream) {
+    const size_t ng = b->plan.groups.size();
+    CU(cudaEventRecord(b->branch_ev[0], stream));
+    int rc;
+    for (size_t q = 0; q < ng; ++q) {
+        CU(cudaStreamWaitEvent(b->branch[q], b->branch_ev[0], 0));
+        if ((rc = batch_group(b, fields, t, q, b->branch[q]))) return rc;
+        CU(cudaEventRecord(b->branch_ev[1 + q], b->branch[q]));
+        CU(cudaStreamWaitEvent(stream, b->branch_ev[1 + q], 0));
     }
     return MGBF_OK;
 }
@@ -1797,8 +1964,18 @@ int mgbf_batch_apply(mgbf_batch* b, void* const* fields, int dtype, int adjoint,
             return MGBF_OK;
         }
     if (!b->cap_stream) CU(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
+    while (b->branch.size() < ng) {
+        cudaStream_t bs = nullptr;
+        CU(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+        b->branch.push_back(bs);
+    }
+    while (b->branch_ev.size() < ng + 1) {
+        cudaEvent_t ev = nullptr;
+        CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        b->branch_ev.push_back(ev);
+    }
     CU(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
-    rc = batch_launch(b, fields, t, b->cap_stream);
+    rc = batch_launch_branches(b, fields, t, b->cap_stream);
     cudaGraph_t graph = nullptr;
     cudaError_t ec = cudaStreamEndCapture(b->cap_stream, &graph);
     if (rc) {

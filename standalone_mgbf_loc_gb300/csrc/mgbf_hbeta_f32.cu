@@ -1,18 +1,21 @@
-// Moment-form radial beta kernels instantiated for float storage (one
-// translation unit per storage type so the build compiles them in parallel).
+// Moment-form radial beta kernels for float storage, reaches 4-8; reaches
+// 10-24 are in mgbf_hbeta_f32_b.cu (separate translation units compile in
+// parallel).
 #include "mgbf_hbeta.cuh"
 
 namespace mgbf {
+
+int hmom_dispatch_f32_b(int R, const HMomArgs& a, const HMomCoefs<double>& c, cudaStream_t s);
 
 int hmom_dispatch_f32(int R, const HMomArgs& a, const HMomCoefs<double>& c, cudaStream_t s) {
     switch (R) {
 #define MGBF_CASE(r) \
     case r:          \
         return run_hmom<r, 2, float>(a, c, s);
-        MGBF_HMOM_REACHES(MGBF_CASE)
+        MGBF_HMOM_REACHES_A(MGBF_CASE)
 #undef MGBF_CASE
         default:
-            return -1;
+            return hmom_dispatch_f32_b(R, a, c, s);
     }
 }
 

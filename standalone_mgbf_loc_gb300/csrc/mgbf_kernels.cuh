@@ -127,6 +127,24 @@ struct DibArgs {
     float scalef;       // set by launch_dibeta
 };
 
+// filtering_lin3's 3D part on one generation (mgbf_lin3.cu).  w, t: work
+// arrays W(v, i, j, L) with halos hx, hy, hz, level index fastest,
+// element (v, i, j, L) at (L+hz) + (lm+2hz)*(v + nv*((i+hx) + (I+2hx)*(j+hy))).
+constexpr int kMaxL3Span = 8;  // dibeta half-span limit (nfil)
+enum Lin3Op : int { kL3From = 0, kL3To, kL3DibFwd, kL3DibAdj, kL3FoldX, kL3FoldY, kL3FoldZ, kL3FillY, kL3FillX,
+                    kL3ZMirror };
+struct Lin3Args {
+    View in, out;            // generation buffers (k = v*lm + L, i, j): kL3From reads in, kL3To writes out
+    void* w;                 // the array a stage works on
+    void* t;                 // dibeta output
+    int nv, lm, I, J, hx, hy, hz;
+    int gh;                  // 0: generation 1 halo forms (boco_3d_g1, bocoT_3d_g1), 1: coarser
+    int dx, dy, dz, h;       // dibeta generator and half-span
+    double fil[kMaxL3Span + 1];
+    float filf[kMaxL3Span + 1];  // set by launch_lin3
+    double scale;            // kL3To: multiplies the output
+};
+
 struct RestrictArgs {
     View fine, coarse;
     int nk, If, Jf;     // fine interior sizes; coarse = If/2, Jf/2
@@ -198,6 +216,9 @@ constexpr int hmom_tma_cols(int R) { return 4 * hmom_tma_tx(R) + 2 * R; }
 
 // Reaches with a compiled moment kernel (p = 2).
 #define MGBF_HMOM_REACHES(X) X(4) X(5) X(6) X(8) X(10) X(12) X(16) X(24)
+// the same list in two halves, instantiated by separate translation units
+#define MGBF_HMOM_REACHES_A(X) X(4) X(5) X(6) X(8)
+#define MGBF_HMOM_REACHES_B(X) X(10) X(12) X(16) X(24)
 
 // Columns per thread of the moment kernel for reach R, chosen to keep the
 // ring of output rows and the input row segment in registers.
@@ -224,6 +245,7 @@ int launch_copy(DType t, View in, View out, int nk, int I, int J, int mirror_hx,
 int launch_line(DType t, const LineArgs& a, void* stream);
 int launch_ball(DType t, const BallArgs& a, void* stream);
 int launch_dibeta(DType t, const DibArgs& a, void* stream);
+int launch_lin3(DType t, const Lin3Args& a, int op, void* stream);
 int launch_rad3_halo(DType t, View out, View src, int nk, int n3, int I, int J, int hx, int hy, void* stream);
 int launch_xfer_direct(DType t, const XferDirectArgs& a, void* stream);
 int launch_xfer_gather(DType t, const XferGatherArgs& a, void* stream);

@@ -1,0 +1,247 @@
+// filtering_lin3 (procedure 5, mg_filtering.f90:260-557): the 3D line
+// filters of the hexad on the 3D variables of one generation (sm_103a).
+//
+// The reference copies the 3D variables of a generation into a work array
+// W(km3, 1-hx:im+hx, 1-hy:jm+hy, 1-hz:lm+hz) and runs, per color, its 3D
+// halo routines and the dibeta line filter along the color's generator
+// (jp_pbfil3.f90:1928-1977 vdibetax3, 2475-2525 vdibetax3t;
+// mg_bocos.f90:1425-2908 boco_3d / bocoT_3d).  Here the work array lives in
+// HBM with the level index fastest, W[(j+hy)][(i+hx)][v][L+hz], so that a
+// warp reads 32 consecutive levels of one column whichever direction a
+// generator points.  Each stage is its own launch over whole rows, columns
+// or cells; the stages keep the reference's order (x before y before z in
+// the folds, y before x in the fills), so every element goes through the
+// same sequence of additions as in the reference.
+#include "mgbf_common.cuh"
+#include "mgbf_kernels.cuh"
+
+namespace mgbf {
+namespace {
+
+struct W3 {
+    long long LX, NV, NI;  // extended levels, variables, extended columns
+    int lm, I, J, hx, hy, hz;
+    __device__ __forceinline__ long long at(int v, int i, int j, int L) const {
+        return (long long)(L + hz) + LX * ((long long)v + NV * ((long long)(i + hx) + NI * (long long)(j + hy)));
+    }
+    __device__ __forceinline__ bool interior(int i, int j, int L) const {
+        return i >= 0 && i < I && j >= 0 && j < J && L >= 0 && L < lm;
+    }
+};
+
+W3 make_w3(const Lin3Args& a) {
+    W3 w;
+    w.LX = a.lm + 2 * a.hz;
+    w.NV = a.nv;
+    w.NI = a.I + 2 * a.hx;
+    w.lm = a.lm; w.I = a.I; w.J = a.J; w.hx = a.hx; w.hy = a.hy; w.hz = a.hz;
+    return w;
+}
+
+// generation buffer (k = v*lm + L, i, j) <-> work array interior; `to`
+// multiplies by scale (the generation weight on the adjoint side)
+template <typename T>
+__global__ void __launch_bounds__(256) k_l3_copy(Lin3Args a, W3 w, int to) {
+    using A = typename AccOf<T>::type;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.nv * a.lm) return;
+    const int i = blockIdx.y, j = blockIdx.z;
+    const int v = k / a.lm, L = k - v * a.lm;
+    T* W = static_cast<T*>(a.w);
+    if (to) {
+        T* out = static_cast<T*>(a.out.p) + k + a.out.si * i + a.out.sj * j;
+        stv(out, static_cast<A>(ldc(W + w.at(v, i, j, L))) * static_cast<A>(a.scale));
+    } else {
+        const T* in = static_cast<const T*>(a.in.p) + k + a.in.si * i + a.in.sj * j;
+        W[w.at(v, i, j, L)] = *in;
+    }
+}
+
+// One color's dibeta over every cell of the extended array, into t.
+// Forward (vdibetax3): interior cells gather fil[0] W(p) + sum_s fil[s]
+// (W(p + s d) + W(p - s d)), halo cells are zero.  Adjoint (vdibetax3t,
+// the scatter from the interior, written as a gather): cell q collects
+// fil[0] W(q) if q is interior and fil[s] W(q -+ s d) from each interior
+// q -+ s d.  A color without a line (h = 0, fil[0] = 1) copies the interior.
+template <typename T>
+__global__ void __launch_bounds__(256) k_l3_dib(Lin3Args a, W3 w, int adj) {
+    using A = typename AccOf<T>::type;
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= w.LX * w.NV) return;
+    const int v = (int)(x / w.LX), L = (int)(x - (long long)v * w.LX) - a.hz;
+    const int i = (int)blockIdx.y - a.hx, j = (int)blockIdx.z - a.hy;
+    const T* W = static_cast<const T*>(a.w);
+    T* Tb = static_cast<T*>(a.t);
+    A fil[kMaxL3Span + 1];
+#pragma unroll
+    for (int s = 0; s <= kMaxL3Span; ++s) fil[s] = sizeof(A) == 8 ? (A)a.fil[s] : (A)a.filf[s];
+    const bool in_p = w.interior(i, j, L);
+    A acc = A(0);
+    if (!adj) {
+        if (in_p) {
+            acc = fil[0] * static_cast<A>(ldc(W + w.at(v, i, j, L)));
+#pragma unroll
+            for (int s = 1; s <= kMaxL3Span; ++s) {
+                if (s > a.h) break;
+                acc += fil[s] * (static_cast<A>(ldc(W + w.at(v, i + s * a.dx, j + s * a.dy, L + s * a.dz))) +
+                                 static_cast<A>(ldc(W + w.at(v, i - s * a.dx, j - s * a.dy, L - s * a.dz))));
+            }
+        }
+    } else {
+        if (in_p) acc = fil[0] * static_cast<A>(ldc(W + w.at(v, i, j, L)));
+#pragma unroll
+        for (int s = 1; s <= kMaxL3Span; ++s) {
+            if (s > a.h) break;
+            const int im = i - s * a.dx, jm = j - s * a.dy, Lm = L - s * a.dz;
+            const int ip = i + s * a.dx, jp = j + s * a.dy, Lp = L + s * a.dz;
+            if (w.interior(im, jm, Lm)) acc += fil[s] * static_cast<A>(ldc(W + w.at(v, im, jm, Lm)));
+            if (w.interior(ip, jp, Lp)) acc += fil[s] * static_cast<A>(ldc(W + w.at(v, ip, jp, Lp)));
+        }
+    }
+    stv(Tb + w.at(v, i, j, L), acc);
+}
+
+// bocoT_3d x part (mg_bocos.f90:2173-2527, 2530-2908): on every row of the
+// extended y range and every level 1..lm, west then east; o = 0 for the
+// generation-1 form (the east fold reads W(I+hx-i): the edge column is
+// added to itself), 1 for coarser generations.
+template <typename T>
+__global__ void __launch_bounds__(256) k_l3_foldx(Lin3Args a, W3 w, int o) {
+    using A = typename AccOf<T>::type;
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= (long long)a.lm * a.nv) return;
+    const int v = (int)(x / a.lm), L = (int)(x - (long long)v * a.lm);
+    const int j = (int)blockIdx.y - a.hy;
+    T* W = static_cast<T*>(a.w);
+    for (int s = 1; s <= a.hx; ++s) {
+        T* d = W + w.at(v, s - 1, j, L);
+        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(W + w.at(v, -s, j, L))));
+    }
+    for (int s = 1; s <= a.hx; ++s) {
+        T* d = W + w.at(v, a.I - a.hx + s - 1, j, L);
+        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(W + w.at(v, a.I + o + a.hx - s - 1, j, L))));
+    }
+}
+
+// bocoT_3d y part: interior columns, levels 1..lm, south then north.
+template <typename T>
+__global__ void __launch_bounds__(256) k_l3_foldy(Lin3Args a, W3 w, int o) {
+    using A = typename AccOf<T>::type;
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= (long long)a.lm * a.nv) return;
+    const int v = (int)(x / a.lm), L = (int)(x - (long long)v * a.lm);
+    const int i = blockIdx.y;
+    T* W = static_cast<T*>(a.w);
+    for (int s = 1; s <= a.hy; ++s) {
+        T* d = W + w.at(v, i, s - 1, L);
+        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(W + w.at(v, i, -s, L))));
+    }
+    for (int s = 1; s <= a.hy; ++s) {
+        T* d = W + w.at(v, i, a.J - a.hy + s - 1, L);
+        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(W + w.at(v, i, a.J + o + a.hy - s - 1, L))));
+    }
+}
+
+// bocoT_3d z part: on every column of the extended plane, for L = 1..hz the
+// lower halo level into level 1+L, then the upper one into lm-L.
+template <typename T>
+__global__ void __launch_bounds__(256) k_l3_foldz(Lin3Args a, W3 w) {
+    using A = typename AccOf<T>::type;
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= w.NV * w.NI) return;
+    const int v = (int)(x % w.NV), i = (int)(x / w.NV) - a.hx;
+    const int j = (int)blockIdx.y - a.hy;
+    T* W = static_cast<T*>(a.w);
+    for (int s = 1; s <= a.hz; ++s) {
+        T* lo = W + w.at(v, i, j, s);
+        stv(lo, static_cast<A>(ldc(lo)) + static_cast<A>(ldc(W + w.at(v, i, j, -s))));
+        T* hi = W + w.at(v, i, j, a.lm - s - 1);
+        stv(hi, static_cast<A>(ldc(hi)) + static_cast<A>(ldc(W + w.at(v, i, j, a.lm + s - 1))));
+    }
+}
+
+// boco_3d y part (interior columns, levels 1..lm): north, then south, as
+// half-sample mirrors W(J+j) = W(J+1-j), W(-hy+j) = W(hy+1-j).
+template <typename T>
+__global__ void __launch_bounds__(256) k_l3_filly(Lin3Args a, W3 w) {
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= (long long)a.lm * a.nv) return;
+    const int v = (int)(x / a.lm), L = (int)(x - (long long)v * a.lm);
+    const int i = blockIdx.y;
+    T* W = static_cast<T*>(a.w);
+    for (int s = 1; s <= a.hy; ++s) W[w.at(v, i, a.J + s - 1, L)] = W[w.at(v, i, a.J - s, L)];
+    for (int s = 1; s <= a.hy; ++s) W[w.at(v, i, -a.hy + s - 1, L)] = W[w.at(v, i, a.hy - s, L)];
+}
+
+// boco_3d x part (every row of the extended y range, levels 1..lm): west
+// W(-hx+i) = W(hx+1-i), then east W(I+i) = W(I-i) at generation 1
+// (boco_3d_g1) or W(I+1-i) (boco_3d_gh, o = 1).
+template <typename T>
+__global__ void __launch_bounds__(256) k_l3_fillx(Lin3Args a, W3 w, int o) {
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= (long long)a.lm * a.nv) return;
+    const int v = (int)(x / a.lm), L = (int)(x - (long long)v * a.lm);
+    const int j = (int)blockIdx.y - a.hy;
+    T* W = static_cast<T*>(a.w);
+    for (int s = 1; s <= a.hx; ++s) W[w.at(v, -a.hx + s - 1, j, L)] = W[w.at(v, a.hx - s, j, L)];
+    for (int s = 1; s <= a.hx; ++s) W[w.at(v, a.I + s - 1, j, L)] = W[w.at(v, a.I - s - 1 + o, j, L)];
+}
+
+// Whole-sample mirror of the z halo on every column of the extended plane:
+// W(1-L) = W(1+L), W(lm+L) = W(lm-L), L = 1..hz.
+template <typename T>
+__global__ void __launch_bounds__(256) k_l3_zmirror(Lin3Args a, W3 w) {
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= w.NV * w.NI) return;
+    const int v = (int)(x % w.NV), i = (int)(x / w.NV) - a.hx;
+    const int j = (int)blockIdx.y - a.hy;
+    T* W = static_cast<T*>(a.w);
+    for (int s = 1; s <= a.hz; ++s) {
+        W[w.at(v, i, j, -s)] = W[w.at(v, i, j, s)];
+        W[w.at(v, i, j, a.lm + s - 1)] = W[w.at(v, i, j, a.lm - s - 1)];
+    }
+}
+
+template <typename T>
+int launch_lin3_t(const Lin3Args& a0, int op, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Lin3Args a = a0;
+    for (int q = 0; q <= kMaxL3Span; ++q) a.filf[q] = (float)a.fil[q];
+    const W3 w = make_w3(a);
+    const int NI = a.I + 2 * a.hx, NJ = a.J + 2 * a.hy;
+    const long long nlv = (long long)a.lm * a.nv;
+    const long long ncol = (long long)a.nv * NI;
+    auto blocks = [](long long n) { return (unsigned)((n + 255) / 256); };
+    switch (op) {
+        case kL3From:
+        case kL3To:
+            k_l3_copy<T><<<dim3(blocks(nlv), a.I, a.J), 256, 0, s>>>(a, w, op == kL3To);
+            break;
+        case kL3DibFwd:
+        case kL3DibAdj:
+            k_l3_dib<T><<<dim3(blocks(w.LX * w.NV), NI, NJ), 256, 0, s>>>(a, w, op == kL3DibAdj);
+            break;
+        case kL3FoldX: k_l3_foldx<T><<<dim3(blocks(nlv), NJ), 256, 0, s>>>(a, w, a.gh); break;
+        case kL3FoldY: k_l3_foldy<T><<<dim3(blocks(nlv), a.I), 256, 0, s>>>(a, w, a.gh); break;
+        case kL3FoldZ: k_l3_foldz<T><<<dim3(blocks(ncol), NJ), 256, 0, s>>>(a, w); break;
+        case kL3FillY: k_l3_filly<T><<<dim3(blocks(nlv), a.I), 256, 0, s>>>(a, w); break;
+        case kL3FillX: k_l3_fillx<T><<<dim3(blocks(nlv), NJ), 256, 0, s>>>(a, w, a.gh); break;
+        case kL3ZMirror: k_l3_zmirror<T><<<dim3(blocks(ncol), NJ), 256, 0, s>>>(a, w); break;
+        default: return (int)cudaErrorInvalidValue;
+    }
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : (int)e;
+}
+
+}  // namespace
+
+int launch_lin3(DType t, const Lin3Args& a, int op, void* stream) {
+    switch (t) {
+        case DType::F64: return launch_lin3_t<double>(a, op, stream);
+        case DType::F32: return launch_lin3_t<float>(a, op, stream);
+        case DType::BF16: return launch_lin3_t<__nv_bfloat16>(a, op, stream);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+}  // namespace mgbf

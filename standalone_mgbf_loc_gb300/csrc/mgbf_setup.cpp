@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <cstdlib>
 #include <cstdio>
 
@@ -246,15 +247,10 @@ int build_interp(int nf, bool quart, Interp1D& T, std::string& err) {
 
 // getlinesum1 (jp_pbfil.f90:149-180) and the vrbeta1 weights
 // (jp_pbfil.f90:856-885) for el = paspx = paspy = pasp02.
-int build_dstencil(int p, double ampl02, int hx, int hy, DStencil& out, std::string& err) {
-    out = DStencil{};
-    if (!(ampl02 > 0.0) || p < 1) {
-        err = "line filters need mg_ampl02 > 0 and p >= 1";
-        return MGBF_ERR_CONFIG;
-    }
-    // beta filters of integer half-span m: normalisation and spread^2 (the
-    // corrected moments of inimomtab are these exact sums)
-    double norm[kDibNH + 1], spread[kDibNH + 1];
+// Beta filters of integer half-span m = 1..nh: normalisation and spread^2
+// (the corrected moments of inimomtab, jp_pbfil3.f90:378-457, are these
+// exact sums).
+static void dib_table(int p, double* norm, double* spread) {
     for (int m = 1; m <= kDibNH; ++m) {
         double s0 = 0.0, s2 = 0.0;
         for (int i = -m; i <= m; ++i) {
@@ -266,6 +262,46 @@ int build_dstencil(int p, double ampl02, int hx, int hy, DStencil& out, std::str
         norm[m] = 1.0 / s0;
         spread[m] = s2 / s0;
     }
+}
+
+// hstform (jp_pbfil3.f90:1399-1430): spread^2 -> formal half-span hs between
+// the table entries around it; blinfil (1463-1501): the weights fil[0..h] of
+// the two-beta filter of half-spans h = int(hs) and h + 1.  False when the
+// spread is beyond the table.
+static bool dib_weights(int p, double s2, const double* norm, const double* spread, int& h_out, double& hs_out,
+                        double* fil) {
+    double hs = -1.0;
+    if (s2 >= 0.0)
+        for (int m = 2; m <= kDibNH; ++m)
+            if (spread[m] >= s2) {
+                hs = m - (spread[m] - s2) / (spread[m] - spread[m - 1]);
+                break;
+            }
+    const int h = hs < 0.0 ? 0 : int(hs), hp = h + 1;
+    if (hs < 0.0 || h < 1 || hp > kDibNH || hp > kDibNFil) return false;
+    const double whp = (hs - h) * norm[hp], wh = (hp - hs) * norm[h];
+    for (int i = 0; i <= kDibNFil; ++i) fil[i] = 0.0;
+    for (int i = 0; i <= h; ++i) {
+        const double u = 1.0 - (double(i) / hp) * (double(i) / hp);
+        fil[i] = whp * std::pow(u, p);
+    }
+    for (int i = 0; i < h; ++i) {
+        const double u = 1.0 - (double(i) / h) * (double(i) / h);
+        fil[i] += wh * std::pow(u, p);
+    }
+    h_out = h;
+    hs_out = hs;
+    return true;
+}
+
+int build_dstencil(int p, double ampl02, int hx, int hy, DStencil& out, std::string& err) {
+    out = DStencil{};
+    if (!(ampl02 > 0.0) || p < 1) {
+        err = "line filters need mg_ampl02 > 0 and p >= 1";
+        return MGBF_ERR_CONFIG;
+    }
+    double norm[kDibNH + 1], spread[kDibNH + 1];
+    dib_table(p, norm, spread);
     // triad of (A11, A22, A12): generators g[q], projections lu[q] (rows of
     // the inverse basis), weights w[q] = A . lu[q]
     const double c = std::sqrt(1.0 / ampl02);
@@ -302,28 +338,12 @@ int build_dstencil(int p, double ampl02, int hx, int hy, DStencil& out, std::str
         return MGBF_ERR_CONFIG;
     }
     for (int q = 0; q < 3; ++q) {
-        // spread^2 -> formal half-span between the table entries around it
-        double hs = -1.0;
-        if (w[q] >= 0.0)
-            for (int m = 2; m <= kDibNH; ++m)
-                if (spread[m] >= w[q]) {
-                    hs = m - (spread[m] - w[q]) / (spread[m] - spread[m - 1]);
-                    break;
-                }
-        const int h = hs < 0.0 ? 0 : int(hs), hp = h + 1;
-        if (hs < 0.0 || h < 1 || hp > kDibNH || hp > kDibNFil) {
+        int h = 0;
+        double hs = 0.0;
+        if (!dib_weights(p, w[q], norm, spread, h, hs, out.fil[q])) {
             err = "line filter spread^2 " + std::to_string(w[q]) + " (mg_ampl02) is beyond the moment table (nh = " +
                   std::to_string(kDibNH) + ")";
             return MGBF_ERR_REACH;
-        }
-        const double whp = (hs - h) * norm[hp], wh = (hp - hs) * norm[h];
-        for (int i = 0; i <= h; ++i) {
-            const double u = 1.0 - (double(i) / hp) * (double(i) / hp);
-            out.fil[q][i] = whp * std::pow(u, p);
-        }
-        for (int i = 0; i < h; ++i) {
-            const double u = 1.0 - (double(i) / h) * (double(i) / h);
-            out.fil[q][i] += wh * std::pow(u, p);
         }
         out.dx[q] = g[q][0]; out.dy[q] = g[q][1]; out.h[q] = h; out.hs[q] = hs;
         if (h * std::abs(g[q][0]) > hx || h * std::abs(g[q][1]) > hy) {
@@ -332,6 +352,137 @@ int build_dstencil(int p, double ampl02, int hx, int hy, DStencil& out, std::str
                   std::to_string(hx) + ", hy=" + std::to_string(hy);
             return MGBF_ERR_REACH;
         }
+    }
+    out.ok = true;
+    return MGBF_OK;
+}
+
+// The hexad of a 3D aspect (jp_pbfil3.f90:798-904).  The seven nonzero
+// elements of GF(8) index the colors; a hexad is a set of six of them whose
+// generators span the aspect with non-negative weights, the seventh (its
+// own color, hcol) being null.  The iteration keeps three K-set generators
+// (the colors hcol - 1, hcol - 2, hcol - 4), derives the other three as
+// differences of consecutive ones, and while a weight is negative moves the
+// null color there, transforms the K-set by one of six unimodular matrices
+// (chosen by the step hcol_new - hcol_old) and applies a rank-one update
+// with the sign pattern of the new color's lines to the projection rows.
+// The starting generators and projections, the six matrices, the step
+// offsets, the sign pattern and the output color order are the reference's
+// tables (they decide which generators the filters use and in what order,
+// which changes the result).  Returns false if 200 steps do not settle.
+static bool hexad(const double A[6], int gen[7][3], double wgt[7]) {
+    static const int l0[7][3] = {{0, 0, 0}, {1, -1, 0}, {0, 1, -1}, {0, 0, 1}, {-1, 0, 1}, {0, 1, 0}, {1, 0, 0}};
+    static const int u0[7][6] = {{0, 0, 0, 0, 0, 0},  {0, 0, 0, 0, 0, -1}, {0, 0, 0, -1, 0, 0}, {0, 0, 1, 1, 1, 0},
+                                 {0, 0, 0, 0, -1, 0}, {0, 1, 0, 1, 0, 1},  {1, 0, 0, 0, 1, 1}};
+    static const int mk[6][3][3] = {{{1, 1, -1}, {1, 0, 0}, {1, 0, -1}},  {{-1, 1, 0}, {-1, 1, 1}, {0, 1, 0}},
+                                    {{0, -1, 1}, {1, -1, 0}, {1, 0, 0}},  {{0, 0, 1}, {0, -1, 1}, {1, -1, 1}},
+                                    {{-1, 0, 1}, {0, 0, 1}, {-1, 1, 0}},  {{0, 1, 0}, {1, 0, -1}, {0, 1, -1}}};
+    static const int step_off[7] = {0, 5, 3, 3, 6, 5, 6};
+    static const int sign[13] = {-1, -1, 1, -1, 1, 1, 1, -1, -1, 1, -1, 1, 1};  // offset -6..6
+    static const int lines[3] = {1, 2, 4};
+    static const int out_color[7] = {7, 4, 6, 3, 5, 2, 1};
+    auto md7 = [](int a) { return ((a % 7) + 7) % 7; };
+    int L[7][3], U[7][6], K[3][3];
+    std::memcpy(L, l0, sizeof(L));
+    std::memcpy(U, u0, sizeof(U));
+    double w[7];
+    for (int q = 0; q < 7; ++q) {
+        w[q] = 0.0;
+        for (int r = 0; r < 6; ++r) w[q] += A[r] * U[q][r];
+    }
+    int hcol = 0, kcol = 0;
+    for (int i = 0; i < 3; ++i) std::memcpy(K[i], L[md7(hcol - lines[i])], sizeof(K[i]));
+    bool done = false;
+    for (int it = 0; it < 200; ++it) {
+        kcol = 0;
+        for (int q = 1; q < 7; ++q)
+            if (w[q] < w[kcol]) kcol = q;
+        const double dw = w[kcol];
+        if (dw >= -1e-14) {
+            done = true;
+            break;
+        }
+        const int d = md7(kcol - hcol);
+        hcol = kcol;
+        const int lc = md7(hcol + step_off[d]);
+        int Kn[3][3];
+        for (int c = 0; c < 3; ++c)
+            for (int e = 0; e < 3; ++e) {
+                int v = 0;
+                for (int r = 0; r < 3; ++r) v += K[r][e] * mk[d - 1][c][r];
+                Kn[c][e] = v;
+            }
+        std::memcpy(K, Kn, sizeof(K));
+        int du[6];
+        for (int r = 0; r < 6; ++r) du[r] = U[hcol][r];
+        for (int q = 0; q < 7; ++q) {
+            const int sg = sign[q - lc + 6];
+            for (int r = 0; r < 6; ++r) U[q][r] += sg * du[r];
+            w[q] += sg * dw;
+        }
+    }
+    if (!done) return false;
+    for (int i = 0; i < 3; ++i)
+        for (int e = 0; e < 3; ++e) {
+            L[md7(hcol - lines[i])][e] = K[i][e];
+            L[md7(hcol + lines[i])][e] = K[i][e] - K[(i + 1) % 3][e];
+        }
+    for (int e = 0; e < 3; ++e) L[kcol][e] = 0;
+    for (int i = 0; i < 7; ++i) {
+        const int c = out_color[i] - 1;
+        for (int e = 0; e < 3; ++e) gen[c][e] = L[i][e];
+        wgt[c] = w[i];
+    }
+    return true;
+}
+
+int build_xstencil(int p, double ampl03, int hx, int hy, int hz, bool line, XStencil& out, std::string& err) {
+    out = XStencil{};
+    if (!line) {  // init_mg_line did not run: the colors' slots stay empty, every color copies
+        out.ok = true;
+        return MGBF_OK;
+    }
+    if (!(ampl03 > 0.0) || p < 1) {
+        err = "3D line filters need mg_ampl03 > 0 and p >= 1";
+        return MGBF_ERR_CONFIG;
+    }
+    double norm[kDibNH + 1], spread[kDibNH + 1];
+    dib_table(p, norm, spread);
+    const double c3 = std::sqrt(1.0 / ampl03);  // cholaspect3 of diag(mg_ampl03)
+    const double A[6] = {c3, c3, c3, 0.0, 0.0, 0.0};
+    int gen[7][3];
+    double w[7];
+    if (!hexad(A, gen, w)) {
+        err = "hexad: the 3D aspect did not resolve into six line filters";
+        return MGBF_ERR_CONFIG;
+    }
+    int slot = 0;
+    for (int col = 1; col <= 7; ++col) {
+        const int* g = gen[col - 1];
+        if (g[0] == 0 && g[1] == 0 && g[2] == 0) continue;
+        if (slot == 6) {
+            err = "hexad: more than six active colors";
+            return MGBF_ERR_CONFIG;
+        }
+        out.slot[col] = slot;
+        for (int e = 0; e < 3; ++e) out.g[slot][e] = g[e];
+        if (!dib_weights(p, w[col - 1], norm, spread, out.h[slot], out.hs[slot], out.fil[slot])) {
+            err = "3D line filter spread^2 " + std::to_string(w[col - 1]) +
+                  " (mg_ampl03) is beyond the moment table (nh = " + std::to_string(kDibNH) + ")";
+            return MGBF_ERR_REACH;
+        }
+        const int h = out.h[slot];
+        if (h * std::abs(g[0]) > hx || h * std::abs(g[1]) > hy || h * std::abs(g[2]) > hz) {
+            err = "3D line filter of color " + std::to_string(col) + " reaches " + std::to_string(h) + " steps of (" +
+                  std::to_string(g[0]) + "," + std::to_string(g[1]) + "," + std::to_string(g[2]) +
+                  "), beyond the halo (hx, hy, hz)";
+            return MGBF_ERR_REACH;
+        }
+        ++slot;
+    }
+    if (slot != 6) {  // hextform wants exactly six active lines
+        err = "hexad: " + std::to_string(slot) + " active colors instead of six";
+        return MGBF_ERR_CONFIG;
     }
     out.ok = true;
     return MGBF_OK;

@@ -57,6 +57,21 @@ struct DStencil {
     double fil[3][kDibNFil + 1] = {};
 };
 
+// filtering_lin3's 3D line filters (procedure 5) as init_mg_line sets them
+// up (mg_intstate.f90:465-477; jp_pbfil3.f90:657-934): the hexad
+// decomposition of the Cholesky factor of the inverse 3D aspect, (c3, c3, c3,
+// 0, 0, 0) with c3 = 1/sqrt(mg_ampl03), into seven colors; per color the
+// active slot (or -1: the color copies), and per slot the generator
+// (dx, dy, dz), half-span h and dibeta weights fil[0..h].
+struct XStencil {
+    bool ok = false;
+    int slot[8] = {-1, -1, -1, -1, -1, -1, -1, -1};  // by color 1..7 (index 0 unused)
+    int g[6][3] = {};
+    int h[6] = {};
+    double hs[6] = {};
+    double fil[6][kDibNFil + 1] = {};
+};
+
 // filtering_rad3's 3D ball: vrbeta3 (jp_pbfil.f90:930-977) with el from
 // cholaspect3 of pasp3 = diag(mg_ampl03) (jp_pbfil.f90:109-126), normalised
 // by getlinesum3 (jp_pbfil.f90:220-268); taps in the reference's gz, gy, gx
@@ -111,6 +126,8 @@ int build_interp(int nf, bool quart, Interp1D& out, std::string& err);
 int build_lstencil(int p, double ampl02, int hx, int hy, LStencil& out, std::string& err);
 int build_dstencil(int p, double ampl02, int hx, int hy, DStencil& out, std::string& err);
 int build_bstencil(int p, double ampl03, int hx, int hy, int hz, BStencil& out, std::string& err);
+// line = mgbf_line: without it init_mg_line never runs and every color copies.
+int build_xstencil(int p, double ampl03, int hx, int hy, int hz, bool line, XStencil& out, std::string& err);
 
 // Reach checks def_mg_weights performs for the other filters of the
 // reference (getlinesum on paspx/paspy, mg_intstate.f90:427-428, which skip

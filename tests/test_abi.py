@@ -158,10 +158,17 @@ def test_reach_larger_than_coarsest_generation(lib):
 def test_unsupported_and_unknown_procedures(lib):
     op = MGBF(small_config())
     x = np.zeros(op.field_shape())
-    for proc in (5,):
-        with pytest.raises(MGBFError) as e:
-            op.filtering_procedure(proc, x)
-        assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
+    # filtering_lin3 (5) is not self-adjoint: adjoint and weight gradients are refused
+    with pytest.raises(MGBFError) as e:
+        op.filtering_procedure_adjoint(5, x)
+    assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
+    with pytest.raises(MGBFError) as e:
+        op.apply_with_weight_grads(5, x, x.copy())
+    assert e.value.code == _abi.MGBF_ERR_UNSUPPORTED
+    # proc 5 with several members is refused like the other background procedures
+    with pytest.raises(MGBFError) as e:
+        MGBF(small_config(n_ens=2)).filtering_procedure(5, np.zeros(MGBF(small_config(n_ens=2)).field_shape()))
+    assert e.value.code == _abi.MGBF_ERR_CONFIG
     # no case default in the reference's select: other values do nothing
     x[...] = 1.0
     op.filtering_procedure(0, x)
