@@ -401,10 +401,11 @@ def run_gpu(args):
 
 # DRAM bytes (read + write) per grid point and pass of the radial moment
 # kernel, measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on
-# one launch of 134.2 M points (8 members of the 64-level, reach-8 variable,
-# FP32: 1116.2 MB); traffic grows in proportion to the points of a launch.
-HMOM_DRAM_BYTES_PER_POINT = 8.32
-HMOM_TRAFFIC_SOURCE = ("scaled from an ncu capture of one 8-member launch (8.32 B per point); "
+# one k_hmom_tma1 launch of 134.2 M points (8 members of the 64-level,
+# reach-8 variable, FP32: 1093.0 MB); traffic grows in proportion to the
+# points of a launch.
+HMOM_DRAM_BYTES_PER_POINT = 8.15
+HMOM_TRAFFIC_SOURCE = ("scaled from an ncu capture of one 8-member launch (8.15 B per point); "
                        "not measured in this run")
 
 

@@ -232,7 +232,8 @@ int mgbf_set_wait_limit(mgbf_handle* h, int polls);
 int mgbf_autotune(mgbf_handle* h, int dtype, void* stream);
 
 /* Pins the radial-filter kernel variant (0: TMA, two rows per barrier;
- * 1: TMA, one row per barrier; 2: cp.async staging) and output rows per block
+ * 1: TMA, one row per barrier; 2: cp.async staging; 3: TMA, two rows per
+ * barrier filtered one after the other) and output rows per block
  * (<= 0: the default) for every generation and pass; variant < 0 returns
  * to the defaults.  FP64 always uses its one kernel.  For tests and manual
  * tuning; mgbf_autotune chooses by measurement. */

@@ -164,9 +164,9 @@ bool make_tmap(CUtensorMap* m, void* base, DType t, int nk, int ncols, int nrows
 // ------------------------------------------------------------ stage timers
 
 enum Stage { ST_VFILTT, ST_UPSEND, ST_HFILTT, ST_HFILT, ST_DNSEND, ST_VFILT, ST_DNSEND_VFILT, ST_COPY, ST_HALO, ST_WGRAD,
-             ST_AN2FILT, ST_FILT2AN, ST_N };
+             ST_AN2FILT, ST_FILT2AN, ST_VFILTT_UPSEND, ST_N };
 const char* kStageNames[ST_N] = {"vfiltT", "upsend", "hfiltT", "hfilt", "dnsend", "vfilt", "dnsend+vfilt", "copy", "halo", "wgrad",
-                                 "an2filt", "filt2an"};
+                                 "an2filt", "filt2an", "vfiltT+upsend"};
 
 struct TimerEvent {
     cudaEvent_t a, b;
@@ -218,6 +218,11 @@ struct StageTimer {
         ev.stage = stage;
         ev.points = points;
         active = cudaEventRecord(ev.a, static_cast<cudaStream_t>(stream)) == cudaSuccess;
+    }
+    // the bracketed launch did not happen: give the events back unrecorded
+    void cancel() {
+        if (active) g_timers.pool.emplace_back(ev.a, ev.b);
+        active = false;
     }
     ~StageTimer() {
         if (!active) return;
@@ -678,13 +683,44 @@ struct Exec {
         return 0;
     }
 
+    // Bz^T x (or, without z columns, the copy of x) into A(0) and its
+    // restriction into A(1) in one pass over x; -1 when the fused kernel does
+    // not cover the shape.
+    int zrestrict(View x, int nzcol) {
+        if (P.gm < 2) return -1;
+        const bool z_on = nzcol > 0 && !G.zs.fwd.empty();
+        ZRestrictArgs z;
+        RestrictArgs& a = z.r;
+        a.fine = x; a.coarse = A(1); a.nk = G.nk; a.If = P.I; a.Jf = P.J;
+        a.wx = G.tab[ai()].rwx[0]->p; a.wy = G.tab[ai()].rwy[0]->p;
+        a.mirror_hx = G.hs.R;
+        z.zout = A(0); z.mirror_z = G.hs.R;
+        z.band = z_on ? G.tab[ai()].zadj.p : nullptr;
+        z.lm = z_on ? G.lm : 1; z.nzk = z_on ? nzcol * G.lm : 0; z.mz = z_on ? G.zs.mz : 0;
+        StageTimer tm(ST_VFILTT_UPSEND, stream, pts(0));
+        const int r = launch_zrestrict(t, z, stream);
+        if (r == -1) {
+            tm.cancel();
+            return -1;
+        }
+        LK(r);
+        return 0;
+    }
+
     // Steps 1-2 and the first radial pass: leaves B_g R_g Bz^T x in `dst(g)`
     // (with mirror halo when mirror_out) and R_g Bz^T x in A(g).
     template <typename DstF>
     int half_chain(View x, int nzcol, bool filt1, DstF dst, bool mirror_out, const double* scales) {
         int rc;
-        if ((rc = zstage(x, A(0), true, nzcol, G.hs.R))) return rc;
-        for (int g = 0; g + 1 < P.gm; ++g)
+        int g0 = 0;  // first restriction still to run
+        const int fused = zrestrict(x, nzcol);
+        if (fused == -1) {
+            if ((rc = zstage(x, A(0), true, nzcol, G.hs.R))) return rc;
+        } else {
+            if (fused) return fused;
+            g0 = 1;
+        }
+        for (int g = g0; g + 1 < P.gm; ++g)
             if ((rc = restrict_(g, A(g), A(g + 1)))) return rc;
         for (int g = 0; g < P.gm; ++g) {
             if (g == 0 && !filt1) continue;

@@ -471,8 +471,11 @@ constexpr size_t hmom_tma_stage_bytes() {
     return (size_t)kTmaStages * (kStageWarps * TX + 2 * R) * 64 * sizeof(T);
 }
 
-template <int R, int P, int TX, typename T>
-__global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
+// SEQ: the two rows of a barrier are filtered one after the other (the
+// registers of one row, as k_hmom_tma1, with half its block barriers);
+// otherwise both rows' chains run interleaved for more work in flight.
+template <int R, int P, int TX, typename T, bool SEQ>
+__global__ void __launch_bounds__(128, SEQ ? 4 : 1) k_hmom_tma(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
                                                   const __grid_constant__ HMomCoefs2 c) {
     constexpr int U = 4;                           // rows per ring shift
     constexpr int NS = TX + 2 * R;
@@ -519,6 +522,39 @@ __global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_const
     for (int r = 0; r < NR; ++r)
 #pragma unroll
         for (int q = 0; q < TX; ++q) acc[r][q] = make_float2(0.f, 0.f);
+
+    auto row1 = [&](const int st, const int u) {
+        const T* tp = tiles + st * TILE + warp * TX * 64 + 2 * lane;
+        float2 seg[NS];
+#pragma unroll
+        for (int s2 = 0; s2 < NS; ++s2) seg[s2] = P2<T>::lds(tp + s2 * 64);
+#pragma unroll
+        for (int q = 0; q < TX; ++q) {
+            float2 t[PQ];
+            t[0] = seg[R + q];
+#pragma unroll
+            for (int e = 1; e < PQ; ++e) t[e] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int m = 0; m <= R; ++m) {
+                if (m > 0) {
+                    const float2 pr = __fadd2_rn(seg[R + q + m], seg[R + q - m]);
+                    t[0] = __fadd2_rn(t[0], pr);
+#pragma unroll
+                    for (int e = 1; e < PQ; ++e) t[e] = __ffma2_rn(c.upow[m * PQ + e], pr, t[e]);
+                }
+#pragma unroll
+                for (int gy = 0; gy <= R; ++gy) {
+                    if (mcanon<R>(gy) == m) {
+                        float2 v = t[0];
+#pragma unroll
+                        for (int e = 1; e < PQ; ++e) v = __ffma2_rn(v, c.coef[gy], t[e]);
+                        acc[R + u - gy][q] = __fadd2_rn(acc[R + u - gy][q], v);
+                        if (gy) acc[R + u + gy][q] = __fadd2_rn(acc[R + u + gy][q], v);
+                    }
+                }
+            }
+        }
+    };
 
     // Two input rows (ring slots u and u+1) at once: their moment chains are
     // independent, which doubles the work in flight per warp.
@@ -592,7 +628,12 @@ __global__ void __launch_bounds__(128) k_hmom_tma(HMomArgs a, const __grid_const
             // the previous pair's stages are free now
             issue(r + kTmaStages - 2);
             issue(r + kTmaStages - 1);
-            row2(st0, st1, u);
+            if constexpr (SEQ) {
+                row1(st0, u);
+                row1(st1, u + 1);
+            } else {
+                row2(st0, st1, u);
+            }
         }
         if (failed) break;
         const int jin0 = jb - R + r0;
@@ -818,15 +859,23 @@ static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t
                         if (ea != cudaSuccess) return (int)ea;
                     }
                     k_hmom_tma1<R, P, TX2, T><<<grid2, block, smt, s>>>(b, tm, c2);
-                } else {  // two rows per barrier
+                } else if (a.variant == 3) {  // two rows per barrier, filtered one after the other
+                    constexpr size_t smt = hmom_tma_stage_bytes<R, TX2, T>();
+                    if (smt + 1024 > 48 * 1024) {
+                        static unsigned long long done = 0;  // per instantiation
+                        cudaError_t ea = smem_optin(k_hmom_tma<R, P, TX2, T, true>, smt, done);
+                        if (ea != cudaSuccess) return (int)ea;
+                    }
+                    k_hmom_tma<R, P, TX2, T, true><<<grid2, block, smt, s>>>(b, tm, c2);
+                } else {  // two rows per barrier, interleaved
                     constexpr size_t smt = hmom_tma_stage_bytes<R, TX2, T>();
                     // opt in above the default 48 KB (dynamic + the static mbarriers)
                     if (smt + 1024 > 48 * 1024) {
                         static unsigned long long done = 0;  // per instantiation
-                        cudaError_t ea = smem_optin(k_hmom_tma<R, P, TX2, T>, smt, done);
+                        cudaError_t ea = smem_optin(k_hmom_tma<R, P, TX2, T, false>, smt, done);
                         if (ea != cudaSuccess) return (int)ea;
                     }
-                    k_hmom_tma<R, P, TX2, T><<<grid2, block, smt, s>>>(b, tm, c2);
+                    k_hmom_tma<R, P, TX2, T, false><<<grid2, block, smt, s>>>(b, tm, c2);
                 }
                 cudaError_t e = cudaGetLastError();
                 return e == cudaSuccess ? 0 : (int)e;

@@ -353,6 +353,208 @@ __global__ void __launch_bounds__(kRsWarps * 32) k_restrict_p(RestrictArgs a, in
     cp_async_wait<0>();
 }
 
+// Generation 1's vertical adjoint filter fused into its restriction: the
+// same block and row pipeline as k_restrict_p, but the staged fine rows come
+// from the caller's field x.  Once a pair of rows is in shared memory, each
+// warp applies Bz^T (the band matrix with the whole-sample mirror and fold of
+// sup_vrbeta1T, mg_filtering.f90:2094-2262) in place to whole columns of
+// levels it owns (columns w, w+4, ...; lane = 4 levels, band rows in
+// registers), writes the columns the block owns to generation 1 (zout, with
+// the mirrored x halo), and the restriction then reads the filtered rows.
+// x is read from HBM once instead of once by each kernel.  A block covers
+// LV levels, whole z columns (lm divides LV).
+// Levels l0-4 .. l0+7 of a staged column; window parts outside the levels
+// the block holds (lmax + 4 of them) are clamped into it (their band weights
+// are zero).
+template <typename T>
+__device__ __forceinline__ void zr_window(const T* col, int l0, int lmax, typename AccOf<T>::type (&x)[12]) {
+    using A = typename AccOf<T>::type;
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        const int o = min(max(l0 + 4 * (v - 1), 0), lmax);
+        A t[4];
+        V4<T>::ldc(col + o, t);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) x[4 * v + e] = t[e];
+    }
+}
+
+template <typename T, int CX, int S, int LV, int MZ>
+__global__ void __launch_bounds__(kRsWarps * 32) k_zrestrict_p(ZRestrictArgs z, int seg_rows) {
+    using A = typename AccOf<T>::type;
+    static_assert(S % 2 == 0 && S >= 4, "stages come in pairs of fine rows");
+    static_assert(MZ <= 4 && LV % 4 == 0 && LV <= 128, "window of 12 levels, 4 levels per lane");
+    const RestrictArgs& a = z.r;
+    constexpr int NF = rs_cols<T, CX>();
+    constexpr int EPC = 16 / (int)sizeof(T);
+    constexpr int CH = LV / EPC;
+    constexpr int P2 = S / 2;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* stg = reinterpret_cast<T*>(smem_raw);          // [S][NF][LV]
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const int Ic = a.If / 2, Jc = a.Jf / 2;
+    const int kb = blockIdx.x * LV;
+    const int chunks = (min(LV, a.nk - kb)) / EPC;
+    const int cs = blockIdx.y * (kRsWarps * CX);
+    const int d0 = blockIdx.z * seg_rows;
+    const int d1 = min(d0 + seg_rows, Jc);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c0 = cs + warp * CX;
+    const T* fine = static_cast<const T*>(a.fine.p) + kb;
+
+    auto issue = [&](int fr, int stage) {
+        const int fj = min(max(fr, 0), a.Jf - 1);
+        const T* row = fine + a.fine.sj * fj;
+        for (int t = threadIdx.x; t < NF * CH; t += kRsWarps * 32) {
+            const int col = t / CH, ch = t - col * CH;
+            if (ch < chunks) {
+                const int fc = min(max(2 * cs - 3 + col, 0), a.If - 1);
+                cp_async16(sbase + (unsigned)(((stage * NF + col) * LV + ch * EPC) * (int)sizeof(T)),
+                           row + a.fine.si * fc + ch * EPC, 16);
+            }
+        }
+    };
+
+    // band rows of this lane's four levels (identity past the z columns)
+    const bool lv = 4 * lane < chunks * EPC;
+    A wz[4][2 * MZ + 1];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int kq = kb + 4 * lane + q;
+        const bool zc = lv && kq < z.nzk;
+        const int L = zc ? kq % z.lm : 0;
+        const A* b = static_cast<const A*>(z.band) + (size_t)L * (2 * z.mz + 1) + z.mz;
+#pragma unroll
+        for (int d = -MZ; d <= MZ; ++d) {
+            const bool ok = zc && d >= -z.mz && d <= z.mz && L + d >= 0 && L + d < z.lm;
+            wz[q][d + MZ] = ok ? b[d] : ((!zc && d == 0) ? A(1) : A(0));
+        }
+    }
+
+    const A* wyp = static_cast<const A*>(a.wy);
+    A wx[CX][8];
+#pragma unroll
+    for (int c = 0; c < CX; ++c) {
+        const int cc = min(c0 + c, Ic - 1);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) wx[c][q] = static_cast<const A*>(a.wx)[cc * 8 + q];
+    }
+    A acc[4][CX][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < CX; ++c)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[r][c][e] = A(0);
+
+    const int niter = d1 - d0 + 3;
+#pragma unroll
+    for (int q = 0; q < P2; ++q) {
+        if (q < niter) {
+            issue(2 * d0 - 3 + 2 * q, 2 * q);
+            issue(2 * d0 - 2 + 2 * q, 2 * q + 1);
+        }
+        cp_async_commit();
+    }
+    const bool kv = 4 * lane < chunks * EPC;
+    for (int it = 0; it < niter; ++it) {
+        const int d = d0 - 3 + it;
+        const int sp = it % P2;
+        cp_async_wait<P2 - 1>();
+        __syncthreads();
+        // Bz^T on the staged pair, column by column within each warp
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int fr = 2 * d0 - 3 + 2 * it + h;  // fine row in this stage
+            const bool own_row = fr >= 2 * d0 && fr < 2 * d1;
+            T* srow = stg + (size_t)(2 * sp + h) * NF * LV;
+            T* zrow = static_cast<T*>(z.zout.p) + z.zout.sj * (long long)fr + kb + 4 * lane;
+            for (int col = warp; col < NF; col += kRsWarps) {
+                T* cp = srow + (size_t)col * LV;
+                A x[12];
+                if (lv) zr_window<T>(cp, 4 * lane, chunks * EPC - 4, x);
+                __syncwarp();
+                if (lv) {
+                    A y[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        A s2 = A(0);
+#pragma unroll
+                        for (int dd = -MZ; dd <= MZ; ++dd) s2 = fma(wz[q][dd + MZ], x[4 + q + dd], s2);
+                        y[q] = s2;
+                    }
+                    V4<T>::st(cp + 4 * lane, y);
+                    const int gc = 2 * cs - 3 + col;
+                    if (own_row && col >= 3 && col < 3 + 2 * kRsWarps * CX && gc < a.If) {
+                        V4<T>::st(zrow + z.zout.si * gc, y);
+                        if (gc < z.mirror_z) V4<T>::st(zrow + z.zout.si * (-1 - gc), y);
+                        if (gc >= a.If - z.mirror_z) V4<T>::st(zrow + z.zout.si * (2 * a.If - 1 - gc), y);
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();  // the filtered pair is complete for every warp
+        // lanes past the block's levels read nothing: with LV < 128 their
+        // four levels would lie past the column (and, for the last column
+        // of the last stage, past the shared allocation)
+#pragma unroll
+        for (int h = 0; h < 2 && kv; ++h) {
+            const T* srow = stg + (size_t)(2 * sp + h) * NF * LV + 4 * lane + 2 * warp * CX * LV;
+            A wy[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int dd = min(max(d + r, 0), Jc - 1);
+                wy[r] = __ldg(wyp + dd * 8 + 6 + h - 2 * r);
+            }
+#pragma unroll
+            for (int c = 0; c < CX; ++c) {
+                A xr[4] = {A(0), A(0), A(0), A(0)};
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    A v[4];
+                    V4<T>::ldc(srow + (2 * c + q) * LV, v);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) xr[e] = fma(wx[c][q], v[e], xr[e]);
+                }
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) acc[r][c][e] = fma(wy[r], xr[e], acc[r][c][e]);
+            }
+        }
+        __syncthreads();  // every warp is done with stage pair sp
+        if (it + P2 < niter) {
+            issue(2 * d0 - 3 + 2 * (it + P2), 2 * sp);
+            issue(2 * d0 - 2 + 2 * (it + P2), 2 * sp + 1);
+        }
+        cp_async_commit();
+        if (d >= d0 && kv) {
+            T* out = static_cast<T*>(a.coarse.p) + a.coarse.sj * d + kb + 4 * lane;
+#pragma unroll
+            for (int c = 0; c < CX; ++c) {
+                const int cc = c0 + c;
+                if (cc < Ic) {
+                    V4<T>::st(out + a.coarse.si * cc, acc[0][c]);
+                    if (cc < a.mirror_hx) V4<T>::st(out + a.coarse.si * (-1 - cc), acc[0][c]);
+                    if (cc >= Ic - a.mirror_hx) V4<T>::st(out + a.coarse.si * (2 * Ic - 1 - cc), acc[0][c]);
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < CX; ++c)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[r][c][e] = acc[r + 1][c][e];
+#pragma unroll
+        for (int c = 0; c < CX; ++c)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[3][c][e] = A(0);
+    }
+    cp_async_wait<0>();
+}
+
 // -------------------------------------------------------- prolongation
 // out(i,j) = base(i,j) + (P o fill2) coarse: downsend + boco_2d(...,2,2) +
 // direct1 + add (mg_generations.f90:210-267, 1190-1250), or the quadratic
@@ -1068,6 +1270,50 @@ int launch_zfilter(DType t, const ZArgs& a, void* stream) {
                       : mz <= 8 ? zlaunch<T, 8>(a, s)
                       : zlaunch<T, kMaxZReach>(a, s)));
     return last_err();
+}
+
+
+// Rows per block of the restriction kernels: about 8 waves of blocks (2
+// resident per SM), at least 8 coarse rows.
+static int rs_rows(long long tiles, int Jc) {
+    const long long nseg = (8LL * 2 * device_sm_count() + tiles - 1) / tiles;
+    int rows = (int)((Jc + nseg - 1) / nseg);
+    return std::max(rows, std::min(Jc, 8));
+}
+
+template <typename T, int CX, int LV>
+static int zrlaunch(const ZRestrictArgs& z, cudaStream_t s) {
+    const RestrictArgs& a = z.r;
+    const int Ic = a.If / 2, Jc = a.Jf / 2;
+    dim3 block(kRsWarps * 32), grid((a.nk + LV - 1) / LV, (Ic + kRsWarps * CX - 1) / (kRsWarps * CX), 1);
+    const int rows = rs_rows((long long)grid.x * grid.y, Jc);
+    grid.z = (Jc + rows - 1) / rows;
+    constexpr size_t sm = (size_t)4 * rs_cols<T, CX>() * LV * sizeof(T);
+    static unsigned long long done = 0;  // per instantiation
+    cudaError_t e = smem_optin(k_zrestrict_p<T, CX, 4, LV, 4>, sm, done);
+    if (e != cudaSuccess) return (int)e;
+    k_zrestrict_p<T, CX, 4, LV, 4><<<grid, block, sm, s>>>(z, rows);
+    return last_err();
+}
+
+int launch_zrestrict(DType t, const ZRestrictArgs& z, void* stream) {
+    const RestrictArgs& a = z.r;
+    if (a.nk % 4 || (a.nk * elem_size(t)) % 16 || !aligned16(a.fine.p) || !aligned16(a.coarse.p) ||
+        !aligned16(z.zout.p) || z.mz > 4 || z.lm < 1 || (a.fine.si * elem_size(t)) % 16 ||
+        (a.fine.sj * elem_size(t)) % 16 || (z.zout.sj * elem_size(t)) % 16 || a.If < 2 || a.Jf < 2)
+        return -1;
+    const int LV = (z.nzk == 0 || 128 % z.lm == 0) ? 128 : (96 % z.lm == 0 ? 96 : 0);
+    if (!LV) return -1;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // two coarse columns per warp: the band rows of the z filter share the
+    // registers with the restriction's accumulators
+    int rc = 0;
+    if (LV == 128) {
+        MGBF_DISPATCH(t, (rc = zrlaunch<T, 2, 128>(z, s)));
+    } else {
+        MGBF_DISPATCH(t, (rc = zrlaunch<T, 2, 96>(z, s)));
+    }
+    return rc;
 }
 
 int launch_restrict(DType t, const RestrictArgs& a, void* stream) {

@@ -153,6 +153,18 @@ struct RestrictArgs {
     int mirror_hx;      // x halo width to mirror into the coarse view
 };
 
+// Generation 1's vertical adjoint filter fused with its restriction:
+// zout = Bz^T fine (with a mirrored x halo of mirror_z columns), coarse =
+// R zout.  band: lm x (2mz+1) adjoint band (accumulation type); levels past
+// nzk are copied.
+struct ZRestrictArgs {
+    RestrictArgs r;      // fine = the caller's field, coarse = generation 2
+    View zout;           // generation 1
+    int mirror_z;
+    const void* band;
+    int lm, nzk, mz;
+};
+
 struct ProlongArgs {
     View coarse, base, out;  // out = base + P(coarse); out may equal base
     int nk, If, Jf;          // fine interior sizes
@@ -203,11 +215,12 @@ struct HMomArgs {
     double scale;            // multiplies every output (normalisation s x generation weight)
     const void* tmap;        // host copy of a 3D TMA tensor map of the input buffer, or null
     int* status;             // device status word: set to 1 when a bounded wait runs out
-    int variant = 0;         // FP32 kernels: 0 TMA two-row, 1 TMA one-row, 2 cp.async staged
+    int variant = 0;         // FP32 kernels: 0 TMA two-row, 1 TMA one-row, 2 cp.async staged,
+                             // 3 TMA two rows per barrier filtered one after the other
     int max_polls = kDefaultWaitPolls;  // polls of a row's barrier before the block gives up
 };
 
-constexpr int kHMomVariants = 3;
+constexpr int kHMomVariants = 4;
 
 // Tile columns of the TMA moment kernel for reach R (box = 64 levels x this
 // many columns x 1 row); the host encodes tensor maps with this box.
@@ -235,6 +248,11 @@ struct DotArgs {
 // Launchers; return 0 or a cudaError_t value.
 int launch_zfilter(DType t, const ZArgs& a, void* stream);
 int launch_restrict(DType t, const RestrictArgs& a, void* stream);
+// Returns -1 (nothing launched) when the shape does not fit: levels not a
+// multiple of 4, unaligned views, vertical reach above 4, or z columns of lm
+// levels that divide neither 128 nor 96; the caller then runs Bz^T and the
+// restriction apart.
+int launch_zrestrict(DType t, const ZRestrictArgs& a, void* stream);
 int launch_prolong(DType t, const ProlongArgs& a, void* stream);
 // Returns -1 when the shape is outside the fused kernel's limits (lm > 256 or
 // vertical reach > 8); the caller then runs prolongation and z filter apart.

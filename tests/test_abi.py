@@ -281,7 +281,7 @@ def test_set_tuning_validation(lib):
     op.set_tuning(2, 5)
     op.set_tuning(-1)
     with pytest.raises(MGBFError):
-        op.set_tuning(3)
+        op.set_tuning(4)
     assert lib.mgbf_set_tuning(None, 1, 0, 0) == _abi.MGBF_ERR_ARG
     assert lib.mgbf_set_tuning(op._h, 7, 0, 0) == _abi.MGBF_ERR_ARG
 

@@ -255,7 +255,7 @@ def test_autotuned_choice_keeps_parity(lib, cuda, dtype):
 
 
 @pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("rows", [0, 7])
 @pytest.mark.parametrize("h", [5, 8, 12, 16])
 def test_parity_each_radial_variant(lib, cuda, dtype, variant, rows, h):
@@ -285,5 +285,18 @@ def test_level_counts_not_multiple_of_four(lib, cuda, dtype, nk_levels):
     c = small_config(lm=lm, km3=km3, gm_max=3, hz=2)
     op = MGBF(c)
     x = compact_input(op, 60 + lm)
+    y = run_gpu(op, 1, x, dtype, cuda)
+    assert rel_l2(y, O.filter_compact(oracle_cfg(c, 1), x)) < TOL[dtype]
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("lm,km3,km2", [(8, 2, 0), (12, 2, 0), (48, 2, 0), (40, 1, 0), (16, 1, 4)])
+def test_fused_vertical_adjoint_and_restriction(lib, cuda, dtype, lm, km3, km2):
+    """Generation 1's Bz^T and restriction run as one kernel when the z
+    columns fit its 128- or 96-level blocks (lm 8, 12, 48, 16 with 2D levels
+    after them) and apart otherwise (lm 40): both against the oracle."""
+    c = small_config(lm=lm, km3=km3, km2=km2, n_ens=1, hz=3, mg_ampl01=canonical_z(3))
+    op = MGBF(c)
+    x = compact_input(op, 300 + lm)
     y = run_gpu(op, 1, x, dtype, cuda)
     assert rel_l2(y, O.filter_compact(oracle_cfg(c, 1), x)) < TOL[dtype]

@@ -19,7 +19,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("variant", [0, 1])  # TMA two rows per barrier, one row per barrier
+@pytest.mark.parametrize("variant", [0, 1, 3])  # the TMA variants
 def test_wait_runs_out_and_recovers(lib, cuda, variant):
     c = small_config()
     op = MGBF(c)
