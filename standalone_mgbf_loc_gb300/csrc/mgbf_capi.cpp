@@ -23,6 +23,7 @@
 #include <cstring>
 #include <fstream>
 #include <map>
+#include <tuple>
 #include <memory>
 #include <sstream>
 #include <string>
@@ -161,6 +162,25 @@ bool make_tmap(CUtensorMap* m, void* base, DType t, int nk, int ncols, int nrows
     return r == CUDA_SUCCESS;
 }
 
+// 3D map of a field view (levels x ncols x nrows, column and row strides of
+// the view) with a box of box_levels x box_cols x 1 row.  False if the view
+// does not meet TMA's rules (16-byte aligned base and strides).
+bool make_tmap_view(CUtensorMap* m, const View& v, DType t, int nk, int ncols, int nrows, int box_levels, int box_cols) {
+    if (t == DType::F64) return false;
+    const size_t es = t == DType::F32 ? 4 : 2;
+    if (((uintptr_t)v.p & 15u) || (v.si * es) % 16 || (v.sj * es) % 16 || v.si < nk || v.sj < v.si * ncols) return false;
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)nk, (cuuint64_t)ncols, (cuuint64_t)nrows};
+    cuuint64_t strides[2] = {(cuuint64_t)v.si * es, (cuuint64_t)v.sj * es};
+    cuuint32_t box[3] = {(cuuint32_t)box_levels, (cuuint32_t)box_cols, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(m, t == DType::F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, v.p, dims,
+                    strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 // ------------------------------------------------------------ stage timers
 
 enum Stage { ST_VFILTT, ST_UPSEND, ST_HFILTT, ST_HFILT, ST_DNSEND, ST_VFILT, ST_DNSEND_VFILT, ST_COPY, ST_HALO, ST_WGRAD,
@@ -276,6 +296,10 @@ struct Group {
     // each with the base address it was encoded for
     std::map<int, std::pair<void*, std::unique_ptr<CUtensorMap>>> tmaps;
     std::map<int, void*> tmap_failed;
+    // TMA maps of callers' fields for the fused generation-1 restriction,
+    // keyed by (dtype, base, column stride, row stride); a null map records
+    // a view TMA cannot describe
+    std::map<std::tuple<int, void*, long long, long long>, std::unique_ptr<CUtensorMap>> xmaps;
     // autotuned radial-kernel choice per (dtype, generation, pass):
     // key = dtype*1024 + g*2 + pass -> (kernel variant, output rows per block)
     std::map<int, std::pair<int, int>> tune;
@@ -683,6 +707,22 @@ struct Exec {
         return 0;
     }
 
+    // TMA map of the caller's field x for the fused restriction, made at
+    // first use of each view; null when the kernel or TMA cannot take it.
+    const CUtensorMap* xmap(const View& x, int lm, int nzk) {
+        const ZrBox b = zrestrict_box(t, lm, nzk);
+        if (!b.lv) return nullptr;
+        auto key = std::make_tuple((int)t, x.p, x.si, x.sj);
+        auto it = G.xmaps.find(key);
+        if (it != G.xmaps.end()) return it->second.get();
+        if (G.xmaps.size() >= 16) G.xmaps.clear();  // callers cycle through a few fields
+        std::unique_ptr<CUtensorMap> m(new CUtensorMap);
+        if (!make_tmap_view(m.get(), x, t, G.nk, P.I, P.J, b.levels, b.cols)) m.reset();
+        const CUtensorMap* r = m.get();
+        G.xmaps[key] = std::move(m);
+        return r;
+    }
+
     // Bz^T x (or, without z columns, the copy of x) into A(0) and its
     // restriction into A(1) in one pass over x; -1 when the fused kernel does
     // not cover the shape.
@@ -697,6 +737,10 @@ struct Exec {
         z.zout = A(0); z.mirror_z = G.hs.R;
         z.band = z_on ? G.tab[ai()].zadj.p : nullptr;
         z.lm = z_on ? G.lm : 1; z.nzk = z_on ? nzcol * G.lm : 0; z.mz = z_on ? G.zs.mz : 0;
+        z.status = static_cast<int*>(P.status.p);
+        z.max_polls = P.wait_polls;
+        z.tmap = xmap(x, z.lm, z.nzk);
+        if (!z.tmap) return -1;
         StageTimer tm(ST_VFILTT_UPSEND, stream, pts(0));
         const int r = launch_zrestrict(t, z, stream);
         if (r == -1) {

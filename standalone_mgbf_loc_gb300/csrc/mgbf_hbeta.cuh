@@ -437,33 +437,6 @@ __global__ void __launch_bounds__(128) k_hmom_p2(HMomArgs a, const __grid_consta
 // parity with a bounded number of polls (a.max_polls); if the bound runs
 // out the block records the failure in a.status and leaves through a
 // block-uniform exit after a bounded drain of its own copies.
-__device__ __forceinline__ void mbar_init(unsigned addr, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(addr), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned addr, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(addr), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned addr, unsigned parity) {
-    unsigned done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    return done != 0;
-}
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned addr, unsigned parity, int max_polls = kDefaultWaitPolls) {
-    for (int it = 0; it < max_polls; ++it)
-        if (mbar_try_wait(addr, parity)) return true;
-    return false;
-}
-__device__ __forceinline__ void tma_load_3d(unsigned dst, const void* tmap, int c0, int c1, int c2, unsigned bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(dst),
-        "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
-        : "memory");
-}
-
 constexpr int kTmaStages = 8;  // rows in flight: kTmaStages - 2
 
 template <int R, int TX, typename T>
@@ -669,7 +642,7 @@ __global__ void __launch_bounds__(128, SEQ ? 4 : 1) k_hmom_tma(HMomArgs a, const
             atomicExch(a.status, 1);
             const int issued = min(nrp, waited + kTmaStages - 2);
             for (int r = waited; r < issued; ++r)
-                mbar_wait_bounded(bbase + 8 * (r % kTmaStages), (unsigned)((r / kTmaStages) & 1));
+                mbar_wait_bounded(bbase + 8 * (r % kTmaStages), (unsigned)((r / kTmaStages) & 1), kDefaultWaitPolls);
         }
         __syncthreads();
     }
@@ -810,7 +783,8 @@ __global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_cons
         if (tid == 0) {
             atomicExch(a.status, 1);
             const int issued = min(nrp, waited + kStages - 1);
-            for (int r = waited; r < issued; ++r) mbar_wait_bounded(bbase + 8 * (r % kStages), (unsigned)((r / kStages) & 1));
+            for (int r = waited; r < issued; ++r)
+                mbar_wait_bounded(bbase + 8 * (r % kStages), (unsigned)((r / kStages) & 1), kDefaultWaitPolls);
         }
         __syncthreads();
     }

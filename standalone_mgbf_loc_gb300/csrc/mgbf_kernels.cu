@@ -8,6 +8,8 @@
 // consecutive lanes take consecutive k and every warp access is one
 // contiguous 128-byte (FP32) segment.  MPI halo exchange of the reference
 // becomes index reflection at the global edges.
+#include <cuda.h>
+
 #include "mgbf_common.cuh"
 #include "mgbf_kernels.cuh"
 
@@ -353,155 +355,149 @@ __global__ void __launch_bounds__(kRsWarps * 32) k_restrict_p(RestrictArgs a, in
     cp_async_wait<0>();
 }
 
-// Generation 1's vertical adjoint filter fused into its restriction: the
-// same block and row pipeline as k_restrict_p, but the staged fine rows come
-// from the caller's field x.  Once a pair of rows is in shared memory, each
-// warp applies Bz^T (the band matrix with the whole-sample mirror and fold of
-// sup_vrbeta1T, mg_filtering.f90:2094-2262) in place to whole columns of
-// levels it owns (columns w, w+4, ...; lane = 4 levels, band rows in
-// registers), writes the columns the block owns to generation 1 (zout, with
-// the mirrored x halo), and the restriction then reads the filtered rows.
-// x is read from HBM once instead of once by each kernel.  A block covers
-// LV levels, whole z columns (lm divides LV).
-// Levels l0-4 .. l0+7 of a staged column; window parts outside the levels
-// the block holds (lmax + 4 of them) are clamped into it (their band weights
-// are zero).
+// Generation 1's vertical adjoint filter fused into its restriction, fed by
+// TMA.  A block takes LV levels (whole z columns: lm divides LV) x 4*CX
+// coarse columns x a segment of coarse rows and walks down the rows in pairs
+// of fine rows.  One elected thread loads each fine row with
+// cp.async.bulk.tensor (box: LV + 2*PAD levels x NF columns x 1 row of the
+// caller's field; levels, columns and rows outside the field arrive as zeros,
+// and the restriction gives them zero weight) into a ring of kZrPairs pairs,
+// one mbarrier per pair.  Phase `it` z-filters pair it+1 in place and
+// restricts pair it, then one block barrier frees pair it's slot for the
+// load of pair it+kZrPairs.  The z filter (Bz^T: the band matrix with the
+// whole-sample mirror and fold of sup_vrbeta1T, mg_filtering.f90:2094-2262)
+// runs per staged column: lane = 4 levels, a 12-level window from the padded
+// column (the band gives levels outside the lane's z column zero weight),
+// band rows in registers; the columns the block owns go to generation 1
+// (zout, with the mirrored x halo).  The restriction is k_restrict_p's: the
+// x pass once per fine row, then the ring of the four coarse rows it feeds.
+// x is read from HBM once.
+constexpr int kZrPairs = 3;
 template <typename T>
-__device__ __forceinline__ void zr_window(const T* col, int l0, int lmax, typename AccOf<T>::type (&x)[12]) {
-    using A = typename AccOf<T>::type;
-#pragma unroll
-    for (int v = 0; v < 3; ++v) {
-        const int o = min(max(l0 + 4 * (v - 1), 0), lmax);
-        A t[4];
-        V4<T>::ldc(col + o, t);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) x[4 * v + e] = t[e];
-    }
+__host__ __device__ constexpr int zr_pad() { return sizeof(T) == 2 ? 8 : 4; }  // 16 bytes of levels
+template <typename T, int CX, int LV>
+__host__ __device__ constexpr size_t zr_row_bytes() {
+    return ((size_t)rs_cols<T, CX>() * (LV + 2 * zr_pad<T>()) * sizeof(T) + 127) / 128 * 128;
 }
+template <typename T, int CX, int LV>
+constexpr size_t zr_smem() { return 2 * kZrPairs * zr_row_bytes<T, CX, LV>(); }
 
-template <typename T, int CX, int S, int LV, int MZ>
-__global__ void __launch_bounds__(kRsWarps * 32) k_zrestrict_p(ZRestrictArgs z, int seg_rows) {
-    using A = typename AccOf<T>::type;
-    static_assert(S % 2 == 0 && S >= 4, "stages come in pairs of fine rows");
-    static_assert(MZ <= 4 && LV % 4 == 0 && LV <= 128, "window of 12 levels, 4 levels per lane");
+template <typename T, int CX, int LV, int MZ>
+__global__ void __launch_bounds__(kRsWarps * 32, 3)
+    k_zrestrict_tma(ZRestrictArgs z, const __grid_constant__ CUtensorMap xmap, int seg_rows) {
+    static_assert(sizeof(T) <= 4, "FP32 accumulation: float or bfloat16 storage");
+    static_assert(MZ <= 4 && LV % 4 == 0 && LV + 2 * zr_pad<T>() <= 256, "12-level window, 4 levels per lane, TMA box");
+    constexpr int PAD = zr_pad<T>();
+    constexpr int COL = LV + 2 * PAD;                 // staged levels per column
+    constexpr int NF = rs_cols<T, CX>();              // staged fine columns: 2*4*CX owned + 6 shared
+    constexpr unsigned ROWB = (unsigned)zr_row_bytes<T, CX, LV>();
+    constexpr unsigned BOXB = (unsigned)(NF * COL * sizeof(T));
     const RestrictArgs& a = z.r;
-    constexpr int NF = rs_cols<T, CX>();
-    constexpr int EPC = 16 / (int)sizeof(T);
-    constexpr int CH = LV / EPC;
-    constexpr int P2 = S / 2;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    T* stg = reinterpret_cast<T*>(smem_raw);          // [S][NF][LV]
+    __shared__ __align__(8) unsigned long long bars[kZrPairs];
     const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const unsigned bbase = (unsigned)__cvta_generic_to_shared(bars);
     const int Ic = a.If / 2, Jc = a.Jf / 2;
     const int kb = blockIdx.x * LV;
-    const int chunks = (min(LV, a.nk - kb)) / EPC;
     const int cs = blockIdx.y * (kRsWarps * CX);
     const int d0 = blockIdx.z * seg_rows;
     const int d1 = min(d0 + seg_rows, Jc);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int c0 = cs + warp * CX;
-    const T* fine = static_cast<const T*>(a.fine.p) + kb;
-
-    auto issue = [&](int fr, int stage) {
-        const int fj = min(max(fr, 0), a.Jf - 1);
-        const T* row = fine + a.fine.sj * fj;
-        for (int t = threadIdx.x; t < NF * CH; t += kRsWarps * 32) {
-            const int col = t / CH, ch = t - col * CH;
-            if (ch < chunks) {
-                const int fc = min(max(2 * cs - 3 + col, 0), a.If - 1);
-                cp_async16(sbase + (unsigned)(((stage * NF + col) * LV + ch * EPC) * (int)sizeof(T)),
-                           row + a.fine.si * fc + ch * EPC, 16);
-            }
-        }
+    const int niter = d1 - d0 + 3;  // coarse rows d0-3 .. d1-1; pair it = fine rows 2d0-3+2it, 2d0-2+2it
+    if (tid == 0) {
+#pragma unroll
+        for (int s = 0; s < kZrPairs; ++s) mbar_init(bbase + 8 * s, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int it) {  // thread 0: pair it into slot it % kZrPairs
+        const int sl = it % kZrPairs;
+        const int fr = 2 * d0 - 3 + 2 * it;
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        mbar_expect_tx(bbase + 8 * sl, 2 * BOXB);
+        tma_load_3d(sbase + 2 * sl * ROWB, &xmap, kb - PAD, 2 * cs - 3, fr, bbase + 8 * sl);
+        tma_load_3d(sbase + (2 * sl + 1) * ROWB, &xmap, kb - PAD, 2 * cs - 3, fr + 1, bbase + 8 * sl);
     };
+    if (tid == 0)
+        for (int it = 0; it < kZrPairs && it < niter; ++it) issue(it);
 
+    // lanes past LV (LV = 96) take no part: their window would reach into
+    // the next staged column
+    constexpr unsigned kLanes = LV / 4 >= 32 ? 0xffffffffu : (1u << (LV / 4)) - 1u;
+    const bool lin = lane < LV / 4;
     // band rows of this lane's four levels (identity past the z columns)
-    const bool lv = 4 * lane < chunks * EPC;
-    A wz[4][2 * MZ + 1];
+    const bool lv = lin && kb + 4 * lane < a.nk;  // nk % 4 == 0: all four levels exist
+    float wz[4][2 * MZ + 1];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int kq = kb + 4 * lane + q;
         const bool zc = lv && kq < z.nzk;
         const int L = zc ? kq % z.lm : 0;
-        const A* b = static_cast<const A*>(z.band) + (size_t)L * (2 * z.mz + 1) + z.mz;
+        const float* b = static_cast<const float*>(z.band) + (size_t)L * (2 * z.mz + 1) + z.mz;
 #pragma unroll
         for (int d = -MZ; d <= MZ; ++d) {
             const bool ok = zc && d >= -z.mz && d <= z.mz && L + d >= 0 && L + d < z.lm;
-            wz[q][d + MZ] = ok ? b[d] : ((!zc && d == 0) ? A(1) : A(0));
+            wz[q][d + MZ] = ok ? b[d] : ((!zc && d == 0) ? 1.f : 0.f);
         }
     }
-
-    const A* wyp = static_cast<const A*>(a.wy);
-    A wx[CX][8];
+    const float* wyp = static_cast<const float*>(a.wy);
+    float wx[CX][8];
 #pragma unroll
     for (int c = 0; c < CX; ++c) {
         const int cc = min(c0 + c, Ic - 1);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) wx[c][q] = static_cast<const A*>(a.wx)[cc * 8 + q];
+        for (int q = 0; q < 8; ++q) wx[c][q] = static_cast<const float*>(a.wx)[cc * 8 + q];
     }
-    A acc[4][CX][4];
+    float acc[4][CX][4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
         for (int c = 0; c < CX; ++c)
 #pragma unroll
-            for (int e = 0; e < 4; ++e) acc[r][c][e] = A(0);
+            for (int e = 0; e < 4; ++e) acc[r][c][e] = 0.f;
 
-    const int niter = d1 - d0 + 3;
+    T* const stg = reinterpret_cast<T*>(smem_raw);
+    // Bz^T in place on staged row sr (fine row fr); owned columns to zout
+    auto zfilter_row = [&](int sr, int fr) {
+        T* srow = stg + (size_t)sr * (ROWB / sizeof(T)) + PAD + 4 * lane;
+        const bool own_row = lv && fr >= 2 * d0 && fr < 2 * d1;
+        T* zrow = static_cast<T*>(z.zout.p) + z.zout.sj * (long long)fr + kb + 4 * lane;
 #pragma unroll
-    for (int q = 0; q < P2; ++q) {
-        if (q < niter) {
-            issue(2 * d0 - 3 + 2 * q, 2 * q);
-            issue(2 * d0 - 2 + 2 * q, 2 * q + 1);
-        }
-        cp_async_commit();
-    }
-    const bool kv = 4 * lane < chunks * EPC;
-    for (int it = 0; it < niter; ++it) {
-        const int d = d0 - 3 + it;
-        const int sp = it % P2;
-        cp_async_wait<P2 - 1>();
-        __syncthreads();
-        // Bz^T on the staged pair, column by column within each warp
+        for (int t = 0; t < (NF + kRsWarps - 1) / kRsWarps; ++t) {
+            const int col = warp + kRsWarps * t;
+            if (col < NF && lin) {  // col is warp-uniform
+                T* cp = srow + col * COL;
+                float x[3][4];  // levels 4*lane-4 .. 4*lane+7
+                V4<T>::ldc(cp - 4, x[0]);
+                V4<T>::ldc(cp, x[1]);
+                V4<T>::ldc(cp + 4, x[2]);
+                __syncwarp(kLanes);  // every lane has its window before any lane overwrites
+                float y[4];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int fr = 2 * d0 - 3 + 2 * it + h;  // fine row in this stage
-            const bool own_row = fr >= 2 * d0 && fr < 2 * d1;
-            T* srow = stg + (size_t)(2 * sp + h) * NF * LV;
-            T* zrow = static_cast<T*>(z.zout.p) + z.zout.sj * (long long)fr + kb + 4 * lane;
-            for (int col = warp; col < NF; col += kRsWarps) {
-                T* cp = srow + (size_t)col * LV;
-                A x[12];
-                if (lv) zr_window<T>(cp, 4 * lane, chunks * EPC - 4, x);
-                __syncwarp();
-                if (lv) {
-                    A y[4];
+                for (int q = 0; q < 4; ++q) {
+                    float s2 = 0.f;
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        A s2 = A(0);
-#pragma unroll
-                        for (int dd = -MZ; dd <= MZ; ++dd) s2 = fma(wz[q][dd + MZ], x[4 + q + dd], s2);
-                        y[q] = s2;
-                    }
-                    V4<T>::st(cp + 4 * lane, y);
-                    const int gc = 2 * cs - 3 + col;
-                    if (own_row && col >= 3 && col < 3 + 2 * kRsWarps * CX && gc < a.If) {
-                        V4<T>::st(zrow + z.zout.si * gc, y);
-                        if (gc < z.mirror_z) V4<T>::st(zrow + z.zout.si * (-1 - gc), y);
-                        if (gc >= a.If - z.mirror_z) V4<T>::st(zrow + z.zout.si * (2 * a.If - 1 - gc), y);
-                    }
+                    for (int dd = -MZ; dd <= MZ; ++dd) s2 = fmaf(wz[q][dd + MZ], x[(4 + q + dd) / 4][(4 + q + dd) % 4], s2);
+                    y[q] = s2;
                 }
-                __syncwarp();
+                V4<T>::st(cp, y);
+                const int gc = 2 * cs - 3 + col;
+                if (own_row && col >= 3 && col < 3 + 2 * kRsWarps * CX && gc < a.If) {
+                    V4<T>::st(zrow + z.zout.si * gc, y);
+                    if (gc < z.mirror_z) V4<T>::st(zrow + z.zout.si * (-1 - gc), y);
+                    if (gc >= a.If - z.mirror_z) V4<T>::st(zrow + z.zout.si * (2 * a.If - 1 - gc), y);
+                }
             }
         }
-        __syncthreads();  // the filtered pair is complete for every warp
-        // lanes past the block's levels read nothing: with LV < 128 their
-        // four levels would lie past the column (and, for the last column
-        // of the last stage, past the shared allocation)
+    };
+    // R on the filtered pair in slot sl: its rows feed coarse rows d..d+3
+    auto restrict_pair = [&](int sl, int d) {
+        if (!lin) return;
 #pragma unroll
-        for (int h = 0; h < 2 && kv; ++h) {
-            const T* srow = stg + (size_t)(2 * sp + h) * NF * LV + 4 * lane + 2 * warp * CX * LV;
-            A wy[4];
+        for (int h = 0; h < 2; ++h) {
+            const T* srow = stg + (size_t)(2 * sl + h) * (ROWB / sizeof(T)) + PAD + 4 * lane + 2 * warp * CX * COL;
+            float wy[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
                 const int dd = min(max(d + r, 0), Jc - 1);
@@ -509,27 +505,51 @@ __global__ void __launch_bounds__(kRsWarps * 32) k_zrestrict_p(ZRestrictArgs z, 
             }
 #pragma unroll
             for (int c = 0; c < CX; ++c) {
-                A xr[4] = {A(0), A(0), A(0), A(0)};
+                float xr[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
-                    A v[4];
-                    V4<T>::ldc(srow + (2 * c + q) * LV, v);
+                    float v[4];
+                    V4<T>::ldc(srow + (2 * c + q) * COL, v);
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) xr[e] = fma(wx[c][q], v[e], xr[e]);
+                    for (int e = 0; e < 4; ++e) xr[e] = fmaf(wx[c][q], v[e], xr[e]);
                 }
 #pragma unroll
                 for (int r = 0; r < 4; ++r)
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[r][c][e] = fma(wy[r], xr[e], acc[r][c][e]);
+                    for (int e = 0; e < 4; ++e) acc[r][c][e] = fmaf(wy[r], xr[e], acc[r][c][e]);
             }
         }
-        __syncthreads();  // every warp is done with stage pair sp
-        if (it + P2 < niter) {
-            issue(2 * d0 - 3 + 2 * (it + P2), 2 * sp);
-            issue(2 * d0 - 2 + 2 * (it + P2), 2 * sp + 1);
+    };
+
+    // pipeline fill: pair 0 filtered before the first restriction
+    int waited = 0;                          // pairs whose barrier every thread has passed
+    int issued = min(niter, kZrPairs);       // pairs whose loads thread 0 has issued
+    bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(bbase, 0u, z.max_polls));
+    if (ok) {
+        zfilter_row(0, 2 * d0 - 3);
+        zfilter_row(1, 2 * d0 - 2);
+    }
+    bool failed = __syncthreads_or(!ok);
+    if (!failed) waited = 1;
+    for (int it = 0; it < niter && !failed; ++it) {
+        const int d = d0 - 3 + it;
+        if (it + 1 < niter) {
+            const int sl1 = (it + 1) % kZrPairs;
+            ok = __all_sync(0xffffffffu, mbar_wait_bounded(bbase + 8 * sl1, (unsigned)(((it + 1) / kZrPairs) & 1), z.max_polls));
+            if (ok) {
+                zfilter_row(2 * sl1, 2 * d0 - 1 + 2 * it);
+                zfilter_row(2 * sl1 + 1, 2 * d0 + 2 * it);
+            }
         }
-        cp_async_commit();
-        if (d >= d0 && kv) {
+        restrict_pair(it % kZrPairs, d);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        waited = min(niter, it + 2);
+        if (tid == 0 && it + kZrPairs < niter) issue(it + kZrPairs);  // into the slot pair it has left
+        issued = min(niter, it + 1 + kZrPairs);
+        if (d >= d0 && lv) {
             T* out = static_cast<T*>(a.coarse.p) + a.coarse.sj * d + kb + 4 * lane;
 #pragma unroll
             for (int c = 0; c < CX; ++c) {
@@ -550,9 +570,17 @@ __global__ void __launch_bounds__(kRsWarps * 32) k_zrestrict_p(ZRestrictArgs z, 
 #pragma unroll
         for (int c = 0; c < CX; ++c)
 #pragma unroll
-            for (int e = 0; e < 4; ++e) acc[3][c][e] = A(0);
+            for (int e = 0; e < 4; ++e) acc[3][c][e] = 0.f;
     }
-    cp_async_wait<0>();
+    if (failed) {
+        // record, then drain this block's outstanding copies (bounded) before exit
+        if (tid == 0) {
+            atomicExch(z.status, 1);
+            for (int p = waited; p < issued; ++p)
+                mbar_wait_bounded(bbase + 8 * (p % kZrPairs), (unsigned)((p / kZrPairs) & 1), kDefaultWaitPolls);
+        }
+        __syncthreads();
+    }
 }
 
 // -------------------------------------------------------- prolongation
@@ -1281,39 +1309,46 @@ static int rs_rows(long long tiles, int Jc) {
     return std::max(rows, std::min(Jc, 8));
 }
 
-template <typename T, int CX, int LV>
+ZrBox zrestrict_box(DType t, int lm, int nzk) {
+    ZrBox b;
+    if (t == DType::F64 || lm < 1) return b;
+    const int lv = (nzk == 0 || 128 % lm == 0) ? 128 : (96 % lm == 0 ? 96 : 0);
+    if (!lv) return b;
+    b.lv = lv;
+    b.levels = lv + 2 * (t == DType::BF16 ? zr_pad<__nv_bfloat16>() : zr_pad<float>());
+    b.cols = rs_cols<float, 2>();
+    return b;
+}
+
+template <typename T, int LV>
 static int zrlaunch(const ZRestrictArgs& z, cudaStream_t s) {
+    constexpr int CX = 2;
     const RestrictArgs& a = z.r;
     const int Ic = a.If / 2, Jc = a.Jf / 2;
     dim3 block(kRsWarps * 32), grid((a.nk + LV - 1) / LV, (Ic + kRsWarps * CX - 1) / (kRsWarps * CX), 1);
     const int rows = rs_rows((long long)grid.x * grid.y, Jc);
     grid.z = (Jc + rows - 1) / rows;
-    constexpr size_t sm = (size_t)4 * rs_cols<T, CX>() * LV * sizeof(T);
+    constexpr size_t sm = zr_smem<T, CX, LV>();
     static unsigned long long done = 0;  // per instantiation
-    cudaError_t e = smem_optin(k_zrestrict_p<T, CX, 4, LV, 4>, sm, done);
+    cudaError_t e = smem_optin(k_zrestrict_tma<T, CX, LV, 4>, sm, done);
     if (e != cudaSuccess) return (int)e;
-    k_zrestrict_p<T, CX, 4, LV, 4><<<grid, block, sm, s>>>(z, rows);
+    k_zrestrict_tma<T, CX, LV, 4><<<grid, block, sm, s>>>(z, *static_cast<const CUtensorMap*>(z.tmap), rows);
     return last_err();
 }
 
 int launch_zrestrict(DType t, const ZRestrictArgs& z, void* stream) {
     const RestrictArgs& a = z.r;
-    if (a.nk % 4 || (a.nk * elem_size(t)) % 16 || !aligned16(a.fine.p) || !aligned16(a.coarse.p) ||
-        !aligned16(z.zout.p) || z.mz > 4 || z.lm < 1 || (a.fine.si * elem_size(t)) % 16 ||
-        (a.fine.sj * elem_size(t)) % 16 || (z.zout.sj * elem_size(t)) % 16 || a.If < 2 || a.Jf < 2)
+    const ZrBox b = zrestrict_box(t, z.lm, z.nzk);
+    const long long es = (long long)elem_size(t);
+    // the tensor map covers the fine field; V4 stores need 16-byte (FP32) or
+    // 8-byte (BF16) aligned columns in zout and coarse
+    if (!b.lv || !z.tmap || !z.status || a.nk % 4 || z.mz > 4 || a.If < 2 || a.Jf < 2 || !aligned16(z.zout.p) ||
+        !aligned16(a.coarse.p) || (z.zout.si * es) % 16 || (z.zout.sj * es) % 16 || (a.coarse.si * es) % 16 ||
+        (a.coarse.sj * es) % 16)
         return -1;
-    const int LV = (z.nzk == 0 || 128 % z.lm == 0) ? 128 : (96 % z.lm == 0 ? 96 : 0);
-    if (!LV) return -1;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    // two coarse columns per warp: the band rows of the z filter share the
-    // registers with the restriction's accumulators
-    int rc = 0;
-    if (LV == 128) {
-        MGBF_DISPATCH(t, (rc = zrlaunch<T, 2, 128>(z, s)));
-    } else {
-        MGBF_DISPATCH(t, (rc = zrlaunch<T, 2, 96>(z, s)));
-    }
-    return rc;
+    if (t == DType::F32) return b.lv == 128 ? zrlaunch<float, 128>(z, s) : zrlaunch<float, 96>(z, s);
+    return b.lv == 128 ? zrlaunch<__nv_bfloat16, 128>(z, s) : zrlaunch<__nv_bfloat16, 96>(z, s);
 }
 
 int launch_restrict(DType t, const RestrictArgs& a, void* stream) {

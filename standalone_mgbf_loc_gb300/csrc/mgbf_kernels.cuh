@@ -23,6 +23,12 @@ constexpr int kMaxReach = 32;
 constexpr int kMaxMomP = 4;
 constexpr int kMaxZReach = 16;  // vertical reach handled by the z kernel
 
+// Polls of an mbarrier before a TMA-fed kernel gives up on a row (the
+// copy engine normally delivers a row within a few hundred polls).  The
+// drain of a block's own copies after such a failure always uses this
+// default, whatever limit the waits ran with.
+constexpr int kDefaultWaitPolls = 1 << 20;
+
 struct ZArgs {
     View in, out;
     int nk, I, J;
@@ -163,6 +169,9 @@ struct ZRestrictArgs {
     int mirror_z;
     const void* band;
     int lm, nzk, mz;
+    const void* tmap = nullptr;  // host CUtensorMap of the fine field: levels x If x Jf (box: see zrestrict_box)
+    int* status = nullptr;       // device status word: set to 1 when a bounded wait runs out
+    int max_polls = kDefaultWaitPolls;
 };
 
 struct ProlongArgs {
@@ -199,12 +208,6 @@ struct HMomCoefs {
     A coef[(kMaxReach + 1) * (kMaxMomP + 1)];  // coef[gy*(P+1)] = A(gy) = 1 - (e gy)^2
     A upow[(kMaxReach + 1) * (kMaxMomP + 1)];  // upow[m*(P+1)+q] = C(P,q) (-1)^q (e m)^(2q)
 };
-
-// Polls of an mbarrier before a TMA-fed kernel gives up on a row (the
-// copy engine normally delivers a row within a few hundred polls).  The
-// drain of a block's own copies after such a failure always uses this
-// default, whatever limit the waits ran with.
-constexpr int kDefaultWaitPolls = 1 << 20;
 
 struct HMomArgs {
     View in, out;
@@ -248,10 +251,17 @@ struct DotArgs {
 // Launchers; return 0 or a cudaError_t value.
 int launch_zfilter(DType t, const ZArgs& a, void* stream);
 int launch_restrict(DType t, const RestrictArgs& a, void* stream);
-// Returns -1 (nothing launched) when the shape does not fit: levels not a
-// multiple of 4, unaligned views, vertical reach above 4, or z columns of lm
-// levels that divide neither 128 nor 96; the caller then runs Bz^T and the
-// restriction apart.
+// TMA box of the fused generation-1 restriction for a group: lv levels per
+// block (0: the fused kernel does not cover the group -- FP64, or z columns
+// of lm levels that divide neither 128 nor 96), and the box the tensor map of
+// the fine field must be encoded with: `levels` x `cols` x 1 row.
+struct ZrBox {
+    int lv = 0, levels = 0, cols = 0;
+};
+ZrBox zrestrict_box(DType t, int lm, int nzk);
+// Returns -1 (nothing launched) when the shape does not fit: no box, no
+// tensor map or status word, levels not a multiple of 4, unaligned views or
+// vertical reach above 4; the caller then runs Bz^T and the restriction apart.
 int launch_zrestrict(DType t, const ZRestrictArgs& a, void* stream);
 int launch_prolong(DType t, const ProlongArgs& a, void* stream);
 // Returns -1 when the shape is outside the fused kernel's limits (lm > 256 or
