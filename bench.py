@@ -205,8 +205,12 @@ def run_gpu(args):
     members = args.members
     gdesc = groups(members)
     batch = MGBFBatch(IM, JM, GM, WEIGHTS, gdesc)
+    tuned = None
     if not args.no_autotune:
         batch.autotune(torch.float32)  # radial-kernel variant and tile height per generation and pass
+        variant_names = {-1: "default", 0: "tma2", 1: "tma1", 2: "cp.async", 3: "tma2seq"}
+        tuned = {f"lm{lm}_h{h}": [[f"{variant_names.get(v, v)}/{r}" for v, r in gen_pair] for gen_pair in per_group]
+                 for (lm, h), per_group in zip(VARS, batch.tuning(torch.float32))}
     batch.use_graphs(True)  # each repeated fwd / adj call replays one captured CUDA graph
     gen = torch.Generator(device=dev)
     gen.manual_seed(1000 + rank)
@@ -291,17 +295,17 @@ def run_gpu(args):
 
     # end to end through the host-streaming pipeline: every step copies the
     # whole field set from pinned host memory, filters it forward and adjoint,
-    # and copies the result back; two device sets and three streams let the
+    # and copies the result back; three device sets and three streams let the
     # copies of neighbouring steps overlap the filtering
     from standalone_mgbf_loc_gb300.pipeline import HostStream
     host = [f.to("cpu").pin_memory() for f in fields]
     outs = [torch.empty(h.shape, dtype=h.dtype).pin_memory() for h in host]
     del fields
     torch.cuda.empty_cache()
-    hs = HostStream(batch, torch.float32, dev, ops=("fwd", "adj"))
+    hs = HostStream(batch, torch.float32, dev, ops=("fwd", "adj"), nsets=3)
     h2d = hs.bytes_per_step()
     e2e_steps = max(2, args.steps)
-    for _ in range(2):
+    for _ in range(hs.nsets):  # every device set once (graph capture per set)
         hs.submit(host, outs)
     hs.finish()
     torch.cuda.synchronize()
@@ -386,8 +390,10 @@ def run_gpu(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "steps": e2e_steps, "ms_per_step": ms_e2e / e2e_steps, "copy_gbs": copy_gbs,
                     "pipeline": "pinned host -> device, fwd+adj, device -> host per step; uploads, filtering "
-                                "and downloads of adjacent steps overlap (two device field sets, three streams)"},
+                                "and downloads of adjacent steps overlap (three device field sets, three streams)"},
             "gpu_launches": int(round(launches_per_step * args.steps)),
+            "autotune": {"radial_kernel_per_generation": tuned,
+                         "key": "variant/output rows per block, [pass after restriction, pass before prolongation]"},
             "clocks": clk_sum,
             "parity": parity,
         }

@@ -321,6 +321,14 @@ int mgbf_batch_set_weights(mgbf_batch* b, const double* a, int n);
 int mgbf_batch_set_wait_limit(mgbf_batch* b, int polls);
 /* As mgbf_autotune, for a batch (releases graphs captured before). */
 int mgbf_batch_autotune(mgbf_batch* b, int dtype, void* stream);
+/* The radial-filter kernel a batch runs for variable group `group`,
+ * generation `gen` (0-based) and pass (0: the pass after the restriction,
+ * 1: the pass before the prolongation) in storage type dtype: *variant as
+ * in mgbf_set_tuning (-1: no moment kernel for this group, or not tuned:
+ * the default) and *rows, the output rows per block (0: the default).
+ * Extension for reporting what the autotuner chose; the reference has no
+ * counterpart. */
+int mgbf_batch_get_tuning(const mgbf_batch* b, int dtype, int group, int gen, int pass, int* variant, int* rows);
 
 /* ------------------------------------------------------------------------
  * Allocation-free radial filtering (no counterpart in the reference).

@@ -1909,6 +1909,19 @@ int mgbf_set_tuning(mgbf_handle* h, int dtype, int variant, int rows) {
     return MGBF_OK;
 }
 
+int mgbf_batch_get_tuning(const mgbf_batch* b, int dtype, int group, int gen, int pass, int* variant, int* rows) {
+    if (!b || !variant || !rows) return fail(MGBF_ERR_ARG, "null argument");
+    if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");
+    const Plan& P = b->plan;
+    if (group < 0 || group >= (int)P.groups.size() || gen < 0 || gen >= P.gm || pass < 0 || pass > 1)
+        return fail(MGBF_ERR_ARG, "group, generation or pass out of range");
+    const auto& tune = P.groups[group].tune;
+    auto it = tune.find(dtype * 1024 + gen * 2 + pass);
+    *variant = it == tune.end() ? -1 : it->second.first;
+    *rows = it == tune.end() ? 0 : it->second.second;
+    return MGBF_OK;
+}
+
 int mgbf_batch_autotune(mgbf_batch* b, int dtype, void* stream) {
     if (!b) return fail(MGBF_ERR_ARG, "null handle");
     if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");

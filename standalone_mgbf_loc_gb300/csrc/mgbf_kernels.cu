@@ -503,21 +503,32 @@ __global__ void __launch_bounds__(kRsWarps * 32, 3)
                 const int dd = min(max(d + r, 0), Jc - 1);
                 wy[r] = __ldg(wyp + dd * 8 + 6 + h - 2 * r);
             }
+            // x pass: the warp's 2*CX+6 staged columns are each read once
+            // and feed every coarse column whose 8 taps cover them
+            float xr[CX][4];
 #pragma unroll
-            for (int c = 0; c < CX; ++c) {
-                float xr[4] = {0.f, 0.f, 0.f, 0.f};
+            for (int c = 0; c < CX; ++c)
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    float v[4];
-                    V4<T>::ldc(srow + (2 * c + q) * COL, v);
+                for (int e = 0; e < 4; ++e) xr[c][e] = 0.f;
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) xr[e] = fmaf(wx[c][q], v[e], xr[e]);
+            for (int j = 0; j < 2 * CX + 6; ++j) {
+                float v[4];
+                V4<T>::ldc(srow + j * COL, v);
+#pragma unroll
+                for (int c = 0; c < CX; ++c) {
+                    const int q = j - 2 * c;
+                    if (q >= 0 && q < 8) {
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) xr[c][e] = fmaf(wx[c][q], v[e], xr[c][e]);
+                    }
                 }
+            }
+#pragma unroll
+            for (int c = 0; c < CX; ++c)
 #pragma unroll
                 for (int r = 0; r < 4; ++r)
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[r][c][e] = fmaf(wy[r], xr[e], acc[r][c][e]);
-            }
+                    for (int e = 0; e < 4; ++e) acc[r][c][e] = fmaf(wy[r], xr[c][e], acc[r][c][e]);
         }
     };
 

@@ -377,6 +377,25 @@ class MGBFBatch:
         stream = torch.cuda.current_stream().cuda_stream if torch is not None else None
         _abi.check(self._lib.mgbf_batch_autotune(self._h, dt, stream), "mgbf_batch_autotune")
 
+    def tuning(self, dtype=None):
+        """The radial-kernel choice per group, generation and pass: a list
+        (one entry per group) of lists (per generation) of two
+        (variant, rows) pairs; variant -1 means the default."""
+        dt = _dtype_code(dtype if dtype is not None else torch.float32)
+        v, r = ctypes.c_int(), ctypes.c_int()
+        out = []
+        for q in range(len(self.groups)):
+            gens = []
+            for g in range(self.gm):
+                pair = []
+                for ps in range(2):
+                    _abi.check(self._lib.mgbf_batch_get_tuning(self._h, dt, q, g, ps, ctypes.byref(v), ctypes.byref(r)),
+                               "mgbf_batch_get_tuning")
+                    pair.append((v.value, r.value))
+                gens.append(pair)
+            out.append(gens)
+        return out
+
     def set_weights(self, a: Sequence[float]) -> None:
         """Replace the generation weights a_1..a_n (n <= gm)."""
         arr = (ctypes.c_double * len(a))(*[float(v) for v in a])

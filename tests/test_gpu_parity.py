@@ -257,7 +257,7 @@ def test_autotuned_choice_keeps_parity(lib, cuda, dtype):
 @pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
 @pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("rows", [0, 7])
-@pytest.mark.parametrize("h", [5, 8, 12, 16])
+@pytest.mark.parametrize("h", [5, 8, 10, 12, 16])
 def test_parity_each_radial_variant(lib, cuda, dtype, variant, rows, h):
     """Every kernel variant the autotuner may choose, with the default row
     blocking and with short, uneven row blocks."""
