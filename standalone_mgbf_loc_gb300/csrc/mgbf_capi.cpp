@@ -299,7 +299,7 @@ struct Group {
     // TMA maps of callers' fields for the fused generation-1 restriction,
     // keyed by (dtype, base, column stride, row stride); a null map records
     // a view TMA cannot describe
-    std::map<std::tuple<int, void*, long long, long long>, std::unique_ptr<CUtensorMap>> xmaps;
+    std::map<std::tuple<int, void*, long long, long long, int, int>, std::unique_ptr<CUtensorMap>> xmaps;
     // autotuned radial-kernel choice per (dtype, generation, pass):
     // key = dtype*1024 + g*2 + pass -> (kernel variant, output rows per block)
     std::map<int, std::pair<int, int>> tune;
@@ -532,6 +532,12 @@ struct Exec {
         a.has_base = 1;
         z.band = G.tab[ai()].zfwd.p; z.lm = G.lm; z.nzk = nzcol * G.lm; z.mz = G.zs.mz;
         if (z.lm < 2 || z.lm > 256 || z.mz > 8) return -1;  // the fused kernel's limits
+        const PzBox pb = prolongz_box(t, z.lm, a.ntap);
+        if (pb.lv) {
+            z.tmap = view_map(coarse, gen_I(P, 1), gen_J(P, 1), pb.lv, pb.cols);
+            z.status = static_cast<int*>(P.status.p);
+            z.max_polls = P.wait_polls;
+        }
         StageTimer tm(ST_DNSEND_VFILT, stream, pts(0));
         LK(launch_prolong_z(t, z, stream));
         return 0;
@@ -707,20 +713,26 @@ struct Exec {
         return 0;
     }
 
-    // TMA map of the caller's field x for the fused restriction, made at
-    // first use of each view; null when the kernel or TMA cannot take it.
-    const CUtensorMap* xmap(const View& x, int lm, int nzk) {
-        const ZrBox b = zrestrict_box(t, lm, nzk);
-        if (!b.lv) return nullptr;
-        auto key = std::make_tuple((int)t, x.p, x.si, x.sj);
+    // TMA map of a field view (ncols x nrows interior points, a box of
+    // box_levels x box_cols x 1 row), made at first use of each view and box;
+    // null when TMA cannot describe the view.
+    const CUtensorMap* view_map(const View& v, int ncols, int nrows, int box_levels, int box_cols) {
+        auto key = std::make_tuple((int)t, v.p, v.si, v.sj, box_levels, box_cols);
         auto it = G.xmaps.find(key);
         if (it != G.xmaps.end()) return it->second.get();
-        if (G.xmaps.size() >= 16) G.xmaps.clear();  // callers cycle through a few fields
+        if (G.xmaps.size() >= 32) G.xmaps.clear();  // callers cycle through a few fields
         std::unique_ptr<CUtensorMap> m(new CUtensorMap);
-        if (!make_tmap_view(m.get(), x, t, G.nk, P.I, P.J, b.levels, b.cols)) m.reset();
+        if (!make_tmap_view(m.get(), v, t, G.nk, ncols, nrows, box_levels, box_cols)) m.reset();
         const CUtensorMap* r = m.get();
         G.xmaps[key] = std::move(m);
         return r;
+    }
+    // TMA map of the caller's field x for the fused restriction; null when
+    // the kernel or TMA cannot take it.
+    const CUtensorMap* xmap(const View& x, int lm, int nzk) {
+        const ZrBox b = zrestrict_box(t, lm, nzk);
+        if (!b.lv) return nullptr;
+        return view_map(x, P.I, P.J, b.levels, b.cols);
     }
 
     // Bz^T x (or, without z columns, the copy of x) into A(0) and its

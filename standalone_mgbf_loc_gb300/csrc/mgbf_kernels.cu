@@ -861,6 +861,243 @@ __global__ void __launch_bounds__(256) k_prolong_z(ProlongZArgs z) {
     }
 }
 
+// Last prolongation fused with the forward vertical filter, fed by TMA:
+// y = Bz (base + P coarse) for generation 1 (downsending + direct1/direct2
+// then sup_vrbeta1_ens, mg_generations.f90:1190-1374, mg_filtering.f90:2042-2092).
+// A block takes LV levels (whole z columns: lm divides LV) x 4*PW column
+// pairs x a run of row pairs and walks down the coarse rows.  One elected
+// thread loads each coarse row (box: LV levels x 4*PW+NT-1 coarse columns x
+// 1 row, the row index mirrored half-sample) into a ring of kPzStages
+// stages, one mbarrier each.  Each warp owns PW column pairs: it
+// x-interpolates every coarse row once as it arrives (the NT taps of each
+// pair, column indices mirrored at the grid's edges within the staged
+// window) into a register ring of the NT rows a row pair reads, combines
+// them along y on top of the base values of its 2 x 2*PW fine points, stores
+// those columns into its own padded staging columns in shared memory and
+// applies the band rows of its lane's four levels (a 12-level window) before
+// writing y.  One block barrier per row pair frees the coarse row's stage.
+constexpr int kPzStages = 6;
+constexpr int kPzPairsPerWarp = 2;
+constexpr int kPzPad = 4;  // staged levels below and above each column (zero)
+template <typename T, int NT>
+__host__ __device__ constexpr int pz_cols() { return 4 * kPzPairsPerWarp + NT - 1; }  // staged coarse columns
+template <typename T, int NT, int LV>
+__host__ __device__ constexpr size_t pz_stage_bytes() { return ((size_t)pz_cols<T, NT>() * LV * sizeof(T) + 127) / 128 * 128; }
+template <typename T, int NT, int LV>
+constexpr size_t pz_smem() {
+    // coarse ring + per warp 2 rows x 2*PW fine columns of LV + 2*pad floats
+    return kPzStages * pz_stage_bytes<T, NT, LV>() + (size_t)4 * 4 * kPzPairsPerWarp * (LV + 2 * kPzPad) * sizeof(float);
+}
+
+template <typename T, int NT, int LV, int MZ>
+__global__ void __launch_bounds__(128, 3) k_prolong_z_tma(ProlongZArgs z, const __grid_constant__ CUtensorMap cmap,
+                                                        int seg_steps) {
+    static_assert(sizeof(T) <= 4 && MZ <= 4 && LV % 4 == 0 && LV <= 128, "FP32 arithmetic, 12-level window, 4 levels per lane");
+    constexpr int O = NT == 4 ? 1 : 0;       // fine column of pair m is 2m - O
+    constexpr int S = NT == 4 ? 2 : 1;       // first coarse tap of pair m is m - S
+    constexpr int PW = kPzPairsPerWarp;
+    constexpr int FC = 2 * PW;               // fine columns per warp
+    constexpr int CW = pz_cols<T, NT>();
+    constexpr unsigned STB = (unsigned)pz_stage_bytes<T, NT, LV>();
+    constexpr unsigned BOXB = (unsigned)(CW * LV * sizeof(T));
+    constexpr int ZC = LV + 2 * kPzPad;      // staged levels per fine column
+    constexpr unsigned kLanes = LV / 4 >= 32 ? 0xffffffffu : (1u << (LV / 4)) - 1u;
+    const ProlongArgs& a = z.p;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long bars[kPzStages];
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const unsigned bbase = (unsigned)__cvta_generic_to_shared(bars);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int Ic = a.If / 2, Jc = a.Jf / 2;
+    const int npy = Jc + O;
+    const int kb = blockIdx.x * LV;
+    const int m0 = blockIdx.y * (4 * PW);     // first column pair of the block
+    const int n0 = blockIdx.z * seg_steps;
+    const int n1 = min(n0 + seg_steps, npy);
+    const int nsteps = n1 - n0;
+    const int nq = nsteps + NT - 1;           // coarse rows n0-S .. n1-1-S+NT-1
+    if (tid == 0) {
+#pragma unroll
+        for (int st = 0; st < kPzStages; ++st) mbar_init(bbase + 8 * st, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    const bool lin = lane < LV / 4;
+    const bool lv = lin && kb + 4 * lane < a.nk;
+    // this warp's staging columns, zero pads
+    float* zst = reinterpret_cast<float*>(smem_raw + kPzStages * STB) + (size_t)warp * 2 * FC * ZC;
+    for (int i = lane; i < 2 * FC * 2 * kPzPad; i += 32) {
+        const int col = i / (2 * kPzPad), e = i % (2 * kPzPad);
+        zst[col * ZC + (e < kPzPad ? e : LV + e)] = 0.f;
+    }
+    __syncthreads();
+    auto issue = [&](int q) {  // thread 0: coarse row n0-S+q into stage q % kPzStages
+        const int st = q % kPzStages;
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        mbar_expect_tx(bbase + 8 * st, BOXB);
+        tma_load_3d(sbase + st * STB, &cmap, kb, m0 - S, reflect_half(n0 - S + q, Jc), bbase + 8 * st);
+    };
+    if (tid == 0)
+        for (int q = 0; q < kPzStages && q < nq; ++q) issue(q);
+
+    // staged-window column of tap u of this warp's pair p (mirrored at the
+    // edges).  Pairs past the last one (npx - 1) write nothing; they read the
+    // last pair's taps, which lie inside the window like every real pair's.
+    const int npx = Ic + O;
+    int tcol[PW][NT];
+#pragma unroll
+    for (int p = 0; p < PW; ++p)
+#pragma unroll
+        for (int u = 0; u < NT; ++u)
+            tcol[p][u] = reflect_half(min(m0 + PW * warp + p, npx - 1) - S + u, Ic) - (m0 - S);
+    // band rows of this lane's four levels (identity past the z columns)
+    float wz[4][2 * MZ + 1];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int kq = kb + 4 * lane + q;
+        const bool zc = lv && kq < z.nzk;
+        const int L = zc ? kq % z.lm : 0;
+        const float* b = static_cast<const float*>(z.band) + (size_t)L * (2 * z.mz + 1) + z.mz;
+#pragma unroll
+        for (int d = -MZ; d <= MZ; ++d) {
+            const bool ok = zc && d >= -z.mz && d <= z.mz && L + d >= 0 && L + d < z.lm;
+            wz[q][d + MZ] = ok ? b[d] : ((!zc && d == 0) ? 1.f : 0.f);
+        }
+    }
+    const T* const ring = reinterpret_cast<const T*>(smem_raw) + 4 * lane;
+    float xr[NT][FC][4];  // x-interpolated coarse rows, oldest first
+#pragma unroll
+    for (int t = 0; t < NT; ++t)
+#pragma unroll
+        for (int f = 0; f < FC; ++f)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) xr[t][f][e] = 0.f;
+    int waited = 0, issued = min(nq, kPzStages);
+    bool failed = false;
+    // x pass of coarse row q into xr[NT-1]; false if its wait ran out
+    auto xpass = [&](int q) -> bool {
+        const int st = q % kPzStages;
+        const bool ok = mbar_wait_bounded(bbase + 8 * st, (unsigned)((q / kPzStages) & 1), z.max_polls);
+        if (ok && lin) {
+            const T* row = ring + (size_t)st * (STB / sizeof(T));
+#pragma unroll
+            for (int f = 0; f < FC; ++f)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) xr[NT - 1][f][e] = 0.f;
+#pragma unroll
+            for (int p = 0; p < PW; ++p)
+#pragma unroll
+                for (int u = 0; u < NT; ++u) {
+                    float v[4];
+                    V4<T>::ldc(row + tcol[p][u] * LV, v);
+                    const float c0 = (float)PCoef<NT>::c0(u), c1 = (float)PCoef<NT>::c1(u);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        xr[NT - 1][2 * p][e] = fmaf(c0, v[e], xr[NT - 1][2 * p][e]);
+                        xr[NT - 1][2 * p + 1][e] = fmaf(c1, v[e], xr[NT - 1][2 * p + 1][e]);
+                    }
+                }
+        }
+        // every warp is done with the stage: load the row kPzStages ahead into it
+        if (__syncthreads_or(!ok)) return false;
+        waited = q + 1;
+        if (tid == 0 && q + kPzStages < nq) issue(q + kPzStages);
+        issued = min(nq, q + 1 + kPzStages);
+        return true;
+    };
+    // ring fill: coarse rows 0 .. NT-2
+    for (int q = 0; q < NT - 1 && !failed; ++q) {
+#pragma unroll
+        for (int t = 0; t < NT - 1; ++t)
+#pragma unroll
+            for (int f = 0; f < FC; ++f)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) xr[t][f][e] = xr[t + 1][f][e];
+        failed = !xpass(q);
+    }
+    const T* base = static_cast<const T*>(a.base.p) + kb + 4 * lane;
+    T* out = static_cast<T*>(a.out.p) + kb + 4 * lane;
+    for (int s = 0; s < nsteps && !failed; ++s) {
+        const int n = n0 + s;
+        // base values of the row pair (fine rows 2n-O, 2n-O+1)
+        float acc[2][FC][4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int fj = 2 * n - O + h;
+#pragma unroll
+            for (int f = 0; f < FC; ++f) {
+                const int fi = 2 * (m0 + PW * warp + f / 2) - O + (f & 1);
+                if (lv && fj >= 0 && fj < a.Jf && fi >= 0 && fi < a.If)
+                    V4<T>::ld(base + a.base.sj * (long long)fj + a.base.si * (long long)fi, acc[h][f]);
+                else
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) acc[h][f][e] = 0.f;
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < NT - 1; ++t)
+#pragma unroll
+            for (int f = 0; f < FC; ++f)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) xr[t][f][e] = xr[t + 1][f][e];
+        if (!xpass(s + NT - 1)) {
+            failed = true;
+            break;
+        }
+        if (!lin) continue;
+        // y pass on top of the base values
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            const float w0 = (float)PCoef<NT>::c0(t), w1 = (float)PCoef<NT>::c1(t);
+#pragma unroll
+            for (int f = 0; f < FC; ++f)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    acc[0][f][e] = fmaf(w0, xr[t][f][e], acc[0][f][e]);
+                    acc[1][f][e] = fmaf(w1, xr[t][f][e], acc[1][f][e]);
+                }
+        }
+        // the warp's columns into its staging area, then Bz per column
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int f = 0; f < FC; ++f) V4<float>::st(zst + (h * FC + f) * ZC + kPzPad + 4 * lane, acc[h][f]);
+        __syncwarp(kLanes);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int fj = 2 * n - O + h;
+#pragma unroll
+            for (int f = 0; f < FC; ++f) {
+                const float* cp = zst + (h * FC + f) * ZC + kPzPad + 4 * lane;
+                float x[3][4];
+                V4<float>::ldc(cp - 4, x[0]);
+                V4<float>::ldc(cp, x[1]);
+                V4<float>::ldc(cp + 4, x[2]);
+                float y[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float s2 = 0.f;
+#pragma unroll
+                    for (int dd = -MZ; dd <= MZ; ++dd) s2 = fmaf(wz[q][dd + MZ], x[(4 + q + dd) / 4][(4 + q + dd) % 4], s2);
+                    y[q] = s2;
+                }
+                const int fi = 2 * (m0 + PW * warp + f / 2) - O + (f & 1);
+                if (lv && fj >= 0 && fj < a.Jf && fi >= 0 && fi < a.If)
+                    V4<T>::st(out + a.out.sj * (long long)fj + a.out.si * (long long)fi, y);
+            }
+        }
+        __syncwarp(kLanes);  // the staging columns are rewritten by the next row pair
+    }
+    if (failed) {
+        // record, then drain this block's outstanding copies (bounded) before exit
+        if (tid == 0) {
+            atomicExch(z.status, 1);
+            for (int q = waited; q < issued; ++q)
+                mbar_wait_bounded(bbase + 8 * (q % kPzStages), (unsigned)((q / kPzStages) & 1), kDefaultWaitPolls);
+        }
+        __syncthreads();
+    }
+}
+
 // Vectorised fused prolongation + z forward: each lane owns 4 consecutive
 // levels (one 16-byte access), the block a tile of KT = blockDim.x * 4
 // levels (whole z columns).  Base values are fetched first, the prolonged
@@ -1446,12 +1683,58 @@ static void pzlaunch4(const ProlongZArgs& z, int KT, dim3 grid, cudaStream_t s) 
     else k_prolong_z4<T, 3, MZ><<<grid, KT / 4, sm, s>>>(z);
 }
 
+PzBox prolongz_box(DType t, int lm, int ntap) {
+    PzBox b;
+    if (t == DType::F64 || lm < 1 || (ntap != 3 && ntap != 4)) return b;
+    b.lv = 128 % lm == 0 ? 128 : (96 % lm == 0 ? 96 : 0);
+    b.cols = b.lv ? (ntap == 4 ? pz_cols<float, 4>() : pz_cols<float, 3>()) : 0;
+    return b;
+}
+
+template <typename T, int NT, int LV>
+static int pzlaunch_tma(const ProlongZArgs& z, cudaStream_t s) {
+    const ProlongArgs& a = z.p;
+    constexpr int O = NT == 4 ? 1 : 0;
+    const int npx = a.If / 2 + O, npy = a.Jf / 2 + O;
+    dim3 block(128), grid((a.nk + LV - 1) / LV, (npx + 4 * kPzPairsPerWarp - 1) / (4 * kPzPairsPerWarp), 1);
+    // row runs: about 8 waves of blocks (3 resident per SM), at least 4*NT
+    // row pairs so that the NT-1 rows of ring fill stay cheap
+    const long long tiles = (long long)grid.x * grid.y;
+    const long long nseg = (8LL * 3 * device_sm_count() + tiles - 1) / tiles;
+    int seg = (int)((npy + nseg - 1) / nseg);
+    seg = std::max(seg, std::min(npy, 4 * NT));
+    grid.z = (npy + seg - 1) / seg;
+    constexpr size_t sm = pz_smem<T, NT, LV>();
+    static unsigned long long done = 0;  // per instantiation
+    cudaError_t e = smem_optin(k_prolong_z_tma<T, NT, LV, 4>, sm, done);
+    if (e != cudaSuccess) return (int)e;
+    k_prolong_z_tma<T, NT, LV, 4><<<grid, block, sm, s>>>(z, *static_cast<const CUtensorMap*>(z.tmap), seg);
+    return last_err();
+}
+
+template <typename T>
+static int pzdispatch_tma(const ProlongZArgs& z, int lv, cudaStream_t s) {
+    if (z.p.ntap == 4) return lv == 128 ? pzlaunch_tma<T, 4, 128>(z, s) : pzlaunch_tma<T, 4, 96>(z, s);
+    return lv == 128 ? pzlaunch_tma<T, 3, 128>(z, s) : pzlaunch_tma<T, 3, 96>(z, s);
+}
+
 int launch_prolong_z(DType t, const ProlongZArgs& z, void* stream) {
     const ProlongArgs& a = z.p;
     if (z.lm < 2 || z.lm > 256 || z.mz > 8 || !a.has_base) return -1;
     const int O = a.ntap == 4 ? 1 : 0;
     const int npx = a.If / 2 + O, npy = a.Jf / 2 + O;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // TMA-fed form: whole z columns in 128- or 96-level blocks, 16-byte
+    // aligned columns, vertical reach <= 4, coarse grids of at least NT
+    // points per direction (edge mirroring stays inside the staged window)
+    const PzBox b = prolongz_box(t, z.lm, a.ntap);
+    const long long es = (long long)elem_size(t);
+    if (b.lv && z.tmap && z.status && z.mz <= 4 && a.nk % 4 == 0 && a.If / 2 >= a.ntap && a.Jf / 2 >= a.ntap &&
+        aligned16(a.base.p) && aligned16(a.out.p) && (a.base.si * es) % 16 == 0 && (a.base.sj * es) % 16 == 0 &&
+        (a.out.si * es) % 16 == 0 && (a.out.sj * es) % 16 == 0) {
+        if (t == DType::F32) return pzdispatch_tma<float>(z, b.lv, s);
+        return pzdispatch_tma<__nv_bfloat16>(z, b.lv, s);
+    }
     // vector form: whole columns in tiles of a multiple of 4 levels (<= 512)
     if (a.nk % 4 == 0 && aligned16(a.coarse.p) && aligned16(a.base.p) && aligned16(a.out.p)) {
         int c = 512 / z.lm;

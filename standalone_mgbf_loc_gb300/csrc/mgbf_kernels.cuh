@@ -191,6 +191,9 @@ struct ProlongZArgs {
     ProlongArgs p;      // coarse = generation 2, base = generation 1, out = y
     const void* band;   // lm x (2mz+1) forward band
     int lm, nzk, mz;
+    const void* tmap = nullptr;  // host CUtensorMap of the coarse field (box: see prolongz_box), or null
+    int* status = nullptr;       // device status word: set to 1 when a bounded wait runs out
+    int max_polls = kDefaultWaitPolls;
 };
 
 struct HDirectArgs {
@@ -264,8 +267,18 @@ ZrBox zrestrict_box(DType t, int lm, int nzk);
 // vertical reach above 4; the caller then runs Bz^T and the restriction apart.
 int launch_zrestrict(DType t, const ZRestrictArgs& a, void* stream);
 int launch_prolong(DType t, const ProlongArgs& a, void* stream);
-// Returns -1 when the shape is outside the fused kernel's limits (lm > 256 or
+// Coarse-field TMA box of the fused last prolongation for a group: lv
+// levels per block (0: no TMA form -- FP64, or z columns of lm levels that
+// divide neither 128 nor 96) and the staged coarse columns; the tensor map of
+// the coarse field is encoded with a box of lv x cols x 1 row.
+struct PzBox {
+    int lv = 0, cols = 0;
+};
+PzBox prolongz_box(DType t, int lm, int ntap);
+// Returns -1 when the shape is outside the fused kernels' limits (lm > 256 or
 // vertical reach > 8); the caller then runs prolongation and z filter apart.
+// The TMA-fed kernel runs when a tensor map and status word are given and the
+// shape fits it; otherwise the shared-memory kernels.
 int launch_prolong_z(DType t, const ProlongZArgs& a, void* stream);
 int launch_hdirect(DType t, const HDirectArgs& a, void* stream);
 int launch_mirror_x(DType t, View v, int nk, int I, int J, int hx, void* stream);
