@@ -321,6 +321,16 @@ int mgbf_batch_set_weights(mgbf_batch* b, const double* a, int n);
 int mgbf_batch_set_wait_limit(mgbf_batch* b, int polls);
 /* As mgbf_autotune, for a batch (releases graphs captured before). */
 int mgbf_batch_autotune(mgbf_batch* b, int dtype, void* stream);
+/* With blocks_per_sm > 0, runs each radial side (the pass after the
+ * restriction, and the pass before the prolongation) of every variable
+ * group as one persistent launch over all its generations: blocks_per_sm
+ * resident blocks per SM (at most as many as fit) take tiles from a device
+ * counter, instead of one launch per generation (FP32/BF16 storage with the
+ * moment kernel; otherwise per generation).  0 (the default) launches per
+ * generation.  Releases graphs captured before.  The reference has no
+ * counterpart: its generations are filtered one after another on each
+ * rank. */
+int mgbf_batch_use_persistent(mgbf_batch* b, int blocks_per_sm);
 /* The radial-filter kernel a batch runs for variable group `group`,
  * generation `gen` (0-based) and pass (0: the pass after the restriction,
  * 1: the pass before the prolongation) in storage type dtype: *variant as

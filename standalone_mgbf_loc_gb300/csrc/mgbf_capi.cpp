@@ -300,6 +300,7 @@ struct Group {
     // keyed by (dtype, base, column stride, row stride); a null map records
     // a view TMA cannot describe
     std::map<std::tuple<int, void*, long long, long long, int, int>, std::unique_ptr<CUtensorMap>> xmaps;
+    DevBuf queue;  // tile counters of the persistent radial sides (one int per side)
     // autotuned radial-kernel choice per (dtype, generation, pass):
     // key = dtype*1024 + g*2 + pass -> (kernel variant, output rows per block)
     std::map<int, std::pair<int, int>> tune;
@@ -316,6 +317,7 @@ struct Plan {
     DevBuf status;  // device status word of bounded waits
     int device = 0;
     int wait_polls = kDefaultWaitPolls;  // mbarrier polls per row before a TMA-fed kernel gives up
+    int persistent = 0;  // radial sides as one persistent launch per group: resident blocks per SM (0: off; mgbf_batch_use_persistent)
 };
 
 int gen_I(const Plan& P, int g) { return P.I >> g; }
@@ -408,7 +410,9 @@ int ensure_bufs(Plan& P, Group& G, DType t, bool needC, bool needD = false) {
     if ((rc = grow(S.B))) return rc;
     if (needC && (rc = grow(S.C))) return rc;
     if (needD && (rc = grow(S.D))) return rc;
-    return 0;
+    // tile counters of the persistent radial sides (allocated before any
+    // graph capture)
+    return G.queue.ensure(2 * sizeof(int));
 }
 
 // ------------------------------------------------------------ kernel calls
@@ -566,6 +570,52 @@ struct Exec {
         a.variant = variant;
         a.rows = rows;
         LK(launch_hmom(t, G.hs.R, G.hs.p, a, G.hs.mom, stream));
+        return 0;
+    }
+
+    // One radial side of generations g0 .. gm-1 as one persistent launch
+    // (k_hmom_persist): side 0 reads A(g) and writes B(g) (weighted by
+    // scales, mirrored x halo when mirror_out), side 1 reads B(g) and writes
+    // A(g).  -1 when it does not apply (persistent mode off, FP64, no moment
+    // kernel, a generation without a TMA map, more generations than one
+    // launch holds); the caller then launches per generation.
+    int hside(int g0, int side, const double* scales, bool mirror_out) {
+        if (!P.persistent || t == DType::F64 || !moment_path() || g0 >= P.gm || P.gm - g0 > kMaxPersistSegs ||
+            !G.queue.p || !P.status.p)
+            return -1;
+        HMomPersistArgs pa;
+        HMomMaps maps;
+        double pts_all = 0;
+        for (int g = g0; g < P.gm; ++g) {
+            const CUtensorMap* m = tmap(g, side);
+            if (!m) return -1;
+            HMomSeg& sg = pa.seg[pa.nseg];
+            HMomArgs& a = sg.a;
+            a.in = side ? B(g) : A(g);
+            a.out = side ? A(g) : B(g);
+            a.nk = G.nk; a.I = gen_I(P, g); a.J = gen_J(P, g);
+            a.mirror_hx = (side == 0 && mirror_out) ? G.hs.R : 0;
+            a.scale = (scales ? scales[g] : 1.0) * G.hs.s;
+            a.halo = G.HXP;
+            a.tmap = nullptr;
+            a.status = static_cast<int*>(P.status.p);
+            a.max_polls = P.wait_polls;
+            a.variant = 1;
+            auto it = G.tune.find((int)t * 1024 + g * 2 + side);
+            a.rows = it != G.tune.end() ? it->second.second : default_rows(g);
+            maps.m[pa.nseg] = *m;
+            ++pa.nseg;
+            pts_all += pts(g);
+        }
+        pa.queue = static_cast<int*>(G.queue.p) + side;
+        pa.blocks_per_sm = P.persistent;
+        StageTimer tm(side ? ST_HFILT : ST_HFILTT, stream, pts_all);
+        const int r = launch_hmom_persist(t, G.hs.R, G.hs.p, pa, maps, G.hs.mom, stream);
+        if (r == -1) {
+            tm.cancel();
+            return -1;
+        }
+        LK(r);
         return 0;
     }
 
@@ -778,6 +828,11 @@ struct Exec {
         }
         for (int g = g0; g + 1 < P.gm; ++g)
             if ((rc = restrict_(g, A(g), A(g + 1)))) return rc;
+        const int gf = filt1 ? 0 : 1;  // first filtered generation
+        if (gf < P.gm && dst(gf).p == B(gf).p) {
+            const int r = hside(gf, 0, scales, mirror_out);
+            if (r != -1) return r;
+        }
         for (int g = 0; g < P.gm; ++g) {
             if (g == 0 && !filt1) continue;
             if ((rc = hpass(g, A(g), dst(g), scales ? scales[g] : 1.0, mirror_out ? G.hs.R : 0, ST_HFILTT, 0))) return rc;
@@ -789,7 +844,9 @@ struct Exec {
     // by a_g unless scales are given; finishes into y.
     int second_half(View y, int nzcol, bool filt1, const double* scales) {
         int rc;
-        for (int g = 0; g < P.gm; ++g) {
+        const int side = hside(filt1 ? 0 : 1, 1, scales, false);  // 0: done, -1: per generation
+        if (side != 0 && side != -1) return side;
+        for (int g = 0; g < P.gm && side == -1; ++g) {
             if (g == 0 && !filt1) continue;
             if ((rc = hpass(g, B(g), A(g), scales ? scales[g] : 1.0, 0, ST_HFILT, 1))) return rc;
         }
@@ -2121,6 +2178,16 @@ int mgbf_batch_set_procedure(mgbf_batch* b, int mg_filt) {
     for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);  // captured for the other procedure
     b->graphs.clear();
     b->proc = mg_filt;
+    return MGBF_OK;
+}
+
+int mgbf_batch_use_persistent(mgbf_batch* b, int blocks_per_sm) {
+    if (!b) return fail(MGBF_ERR_ARG, "null handle");
+    if (blocks_per_sm < 0) return fail(MGBF_ERR_ARG, "negative blocks per SM");
+    DeviceGuard dg(b->plan.device);
+    b->plan.persistent = blocks_per_sm;
+    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);  // captured with the old launch sequence
+    b->graphs.clear();
     return MGBF_OK;
 }
 

@@ -32,6 +32,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 namespace mgbf {
@@ -648,12 +649,22 @@ __global__ void __launch_bounds__(128, SEQ ? 4 : 1) k_hmom_tma(HMomArgs a, const
     }
 }
 
-// Single-row variant of the TMA kernel (4-deep ring, one input row per
-// barrier): fewer registers, more blocks per SM; the autotuner picks
-// between the two.
+// One tile of the single-row TMA pipeline (4-deep ring, one input row per
+// barrier): levels k0 .. k0+63, the column strip from ib, output rows
+// jb .. min(jb + a.rows, a.J) - 1.  The tile reads nrp rows, a multiple of
+// kStages; its row r uses ring stage r % kStages and the phase parity of
+// row rbase + r, so a persistent block that runs tile after tile continues
+// the barriers' phases (rbase is the rows its earlier tiles read).  Returns
+// false when a bounded wait ran out, after recording it in a.status and
+// draining this block's own copies.
+template <int R, int TX>
+__host__ __device__ constexpr int hmom_tma1_rows(int out_rows) {
+    return ((out_rows + 2 * R + kStages - 1) / kStages) * kStages;
+}
+
 template <int R, int P, int TX, typename T>
-__global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
-                                                  const __grid_constant__ HMomCoefs2 c) {
+__device__ __forceinline__ bool hmom_tma1_tile(const HMomArgs& a, const CUtensorMap* tmap, const HMomCoefs2& c,
+                                               int k0, int ib, int jb, unsigned sbase, unsigned bbase, int rbase) {
     constexpr int U = kStages;
     constexpr int NS = TX + 2 * R;
     constexpr int NR = 2 * R + U;
@@ -662,30 +673,17 @@ __global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_cons
     constexpr int TILE = NC * 64;
     constexpr unsigned TILE_BYTES = TILE * sizeof(T);
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) unsigned long long bars[kStages];
-    T* tiles = reinterpret_cast<T*>(smem_raw);
-    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
-    const unsigned bbase = (unsigned)__cvta_generic_to_shared(bars);
+    const T* tiles = reinterpret_cast<const T*>(smem_raw);
     const int lane = threadIdx.x, warp = threadIdx.y, tid = warp * 32 + lane;
-    const int k0 = blockIdx.x * 64;
-    const int ib = blockIdx.y * (kStageWarps * TX);
-    const int jb = blockIdx.z * a.rows;
     const int je = min(jb + a.rows, a.J);
-    const int nrows = je - jb + 2 * R;
-    const int nrp = ((nrows + U - 1) / U) * U;  // rows read by the unrolled loop
-    if (tid == 0) {
-#pragma unroll
-        for (int s2 = 0; s2 < kStages; ++s2) mbar_init(bbase + 8 * s2, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    __syncthreads();
+    const int nrp = hmom_tma1_rows<R, TX>(je - jb);  // rows read by the unrolled loop
     auto issue = [&](int r) {
         if (tid == 0 && r < nrp) {
             const int st = r % kStages;
             const int jr = reflect_half(jb - R + r, a.J);
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_expect_tx(bbase + 8 * st, TILE_BYTES);
-            tma_load_3d(sbase + st * TILE_BYTES, &tmap, k0, ib - R + a.halo, jr, bbase + 8 * st);
+            tma_load_3d(sbase + st * TILE_BYTES, tmap, k0, ib - R + a.halo, jr, bbase + 8 * st);
         }
     };
 
@@ -741,7 +739,7 @@ __global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_cons
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int r = r0 + u;
-            const bool ok = mbar_wait_bounded(bbase + 8 * u, (unsigned)((r / kStages) & 1), a.max_polls);
+            const bool ok = mbar_wait_bounded(bbase + 8 * u, (unsigned)(((rbase + r) / kStages) & 1), a.max_polls);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
@@ -784,9 +782,73 @@ __global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_cons
             atomicExch(a.status, 1);
             const int issued = min(nrp, waited + kStages - 1);
             for (int r = waited; r < issued; ++r)
-                mbar_wait_bounded(bbase + 8 * (r % kStages), (unsigned)((r / kStages) & 1), kDefaultWaitPolls);
+                mbar_wait_bounded(bbase + 8 * (r % kStages), (unsigned)(((rbase + r) / kStages) & 1), kDefaultWaitPolls);
         }
         __syncthreads();
+    }
+    return !failed;
+}
+
+// Single-row variant of the TMA kernel: one tile per block; fewer registers
+// than the two-row kernel, more blocks per SM; the autotuner picks between
+// them.
+template <int R, int P, int TX, typename T>
+__global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
+                                                  const __grid_constant__ HMomCoefs2 c) {
+    __shared__ __align__(8) unsigned long long bars[kStages];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const unsigned bbase = (unsigned)__cvta_generic_to_shared(bars);
+    if (threadIdx.y == 0 && threadIdx.x == 0) {
+#pragma unroll
+        for (int s2 = 0; s2 < kStages; ++s2) mbar_init(bbase + 8 * s2, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    hmom_tma1_tile<R, P, TX, T>(a, &tmap, c, blockIdx.x * 64, blockIdx.y * (kStageWarps * TX), blockIdx.z * a.rows, sbase,
+                                bbase, 0);
+}
+
+// Persistent form of one radial side: every generation's tiles of one
+// variable group in one launch.  Blocks (as many as fit on the device at
+// once) take tiles from a device counter in order -- the finest
+// generation's first -- and run each with hmom_tma1_tile; the generations
+// of a side are independent, so any order is correct.  The counter must be
+// zero at launch.
+template <int R, int P, int TX, typename T>
+__global__ void __launch_bounds__(128) k_hmom_persist(const __grid_constant__ HMomPersistArgs pa,
+                                                     const __grid_constant__ HMomMaps maps,
+                                                     const __grid_constant__ HMomCoefs2 c) {
+    __shared__ __align__(8) unsigned long long bars[kStages];
+    __shared__ int next_tile;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const unsigned bbase = (unsigned)__cvta_generic_to_shared(bars);
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    if (tid == 0) {
+#pragma unroll
+        for (int s2 = 0; s2 < kStages; ++s2) mbar_init(bbase + 8 * s2, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    int rbase = 0;  // rows read by this block's earlier tiles
+    for (;;) {
+        if (tid == 0) next_tile = atomicAdd(pa.queue, 1);
+        __syncthreads();
+        const int t = next_tile;
+        __syncthreads();  // every thread has read next_tile before thread 0 writes it again
+        if (t >= pa.ntiles) break;
+        int sg = 0;
+        while (sg + 1 < pa.nseg && t >= pa.seg[sg + 1].first) ++sg;
+        const HMomSeg& g = pa.seg[sg];
+        int lt = t - g.first;
+        const int kx = lt % g.nkb;
+        lt /= g.nkb;
+        const int iy = lt % g.nstrip;
+        const int jz = lt / g.nstrip;
+        const int jb = jz * g.a.rows;
+        if (!hmom_tma1_tile<R, P, TX, T>(g.a, &maps.m[sg], c, kx * 64, iy * (kStageWarps * TX), jb, sbase, bbase, rbase))
+            break;
+        rbase += hmom_tma1_rows<R, TX>(min(jb + g.a.rows, g.a.J) - jb);
     }
 }
 
@@ -879,6 +941,54 @@ static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t
     }
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? 0 : (int)e;
+}
+
+template <int R, int P, typename T>
+static int run_hmom_persist(HMomPersistArgs pa, const HMomMaps& maps, const HMomCoefs<double>& cd, cudaStream_t s) {
+    if constexpr (sizeof(T) == 8) {
+        return -1;
+    } else {
+        constexpr int TX2 = hmom_p2_tx(R);
+        if (pa.nseg <= 0 || pa.nseg > kMaxPersistSegs || !pa.queue) return -1;
+        int ntiles = 0;
+        for (int i = 0; i < pa.nseg; ++i) {
+            HMomSeg& g = pa.seg[i];
+            const HMomArgs& a = g.a;
+            // the packed TMA pipeline's conditions (as run_hmom)
+            if (!a.status || a.rows <= 0 || a.nk % 2 || (a.nk * (int)sizeof(T)) % 16 || a.halo < R ||
+                ((uintptr_t)a.in.p & 15u) || ((uintptr_t)a.out.p & 7u))
+                return -1;
+            g.nkb = (a.nk + 63) / 64;
+            g.nstrip = ((a.I + TX2 - 1) / TX2 + kStageWarps - 1) / kStageWarps;
+            g.nrowb = (a.J + a.rows - 1) / a.rows;
+            g.first = ntiles;
+            ntiles += g.nkb * g.nstrip * g.nrowb;
+        }
+        pa.ntiles = ntiles;
+        if (ntiles == 0) return 0;
+        HMomCoefs2 c2;
+        for (int g = 0; g <= kMaxReach; ++g) c2.coef[g] = make_float2((float)cd.coef[g * (P + 1)], (float)cd.coef[g * (P + 1)]);
+        for (int t = 0; t < (kMaxReach + 1) * (kMaxMomP + 1); ++t) c2.upow[t] = make_float2((float)cd.upow[t], (float)cd.upow[t]);
+        constexpr size_t smt = (size_t)kStages * (kStageWarps * TX2 + 2 * R) * 64 * sizeof(T);
+        static unsigned long long done = 0;  // per instantiation
+        if (smt + 1024 > 48 * 1024) {
+            cudaError_t ea = smem_optin(k_hmom_persist<R, P, TX2, T>, smt, done);
+            if (ea != cudaSuccess) return (int)ea;
+        }
+        // blocks_per_sm per SM, at most as many as fit on the device at once
+        int per_sm = 0;
+        cudaError_t eo = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hmom_persist<R, P, TX2, T>,
+                                                                     32 * kStageWarps, smt);
+        if (eo != cudaSuccess) return (int)eo;
+        per_sm = std::max(per_sm, 1);
+        if (pa.blocks_per_sm > 0) per_sm = std::min(per_sm, pa.blocks_per_sm);
+        const int grid = std::max(1, std::min(ntiles, per_sm * device_sm_count()));
+        cudaError_t em = cudaMemsetAsync(pa.queue, 0, sizeof(int), s);
+        if (em != cudaSuccess) return (int)em;
+        k_hmom_persist<R, P, TX2, T><<<grid, dim3(32, kStageWarps), smt, s>>>(pa, maps, c2);
+        cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? 0 : (int)e;
+    }
 }
 
 }  // namespace mgbf

@@ -17,4 +17,17 @@ int hmom_dispatch_bf16_b(int R, const HMomArgs& a, const HMomCoefs<double>& c, c
     }
 }
 
+int hmom_persist_dispatch_bf16_b(int R, const HMomPersistArgs& pa, const HMomMaps& maps, const HMomCoefs<double>& c,
+                                cudaStream_t s) {
+    switch (R) {
+#define MGBF_CASE(r) \
+    case r:          \
+        return run_hmom_persist<r, 2, __nv_bfloat16>(pa, maps, c, s);
+        MGBF_HMOM_REACHES_B(MGBF_CASE)
+#undef MGBF_CASE
+        default:
+            return -1;
+    }
+}
+
 }  // namespace mgbf

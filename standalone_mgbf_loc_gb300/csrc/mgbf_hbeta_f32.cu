@@ -6,6 +6,8 @@
 namespace mgbf {
 
 int hmom_dispatch_f32_b(int R, const HMomArgs& a, const HMomCoefs<double>& c, cudaStream_t s);
+int hmom_persist_dispatch_f32_b(int R, const HMomPersistArgs& pa, const HMomMaps& maps, const HMomCoefs<double>& c,
+                                cudaStream_t s);
 
 int hmom_dispatch_f32(int R, const HMomArgs& a, const HMomCoefs<double>& c, cudaStream_t s) {
     switch (R) {
@@ -16,6 +18,19 @@ int hmom_dispatch_f32(int R, const HMomArgs& a, const HMomCoefs<double>& c, cuda
 #undef MGBF_CASE
         default:
             return hmom_dispatch_f32_b(R, a, c, s);
+    }
+}
+
+int hmom_persist_dispatch_f32(int R, const HMomPersistArgs& pa, const HMomMaps& maps, const HMomCoefs<double>& c,
+                              cudaStream_t s) {
+    switch (R) {
+#define MGBF_CASE(r) \
+    case r:          \
+        return run_hmom_persist<r, 2, float>(pa, maps, c, s);
+        MGBF_HMOM_REACHES_A(MGBF_CASE)
+#undef MGBF_CASE
+        default:
+            return hmom_persist_dispatch_f32_b(R, pa, maps, c, s);
     }
 }
 

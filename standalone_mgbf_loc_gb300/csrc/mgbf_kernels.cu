@@ -1783,6 +1783,18 @@ int launch_hmom(DType t, int R, int p, const HMomArgs& a, const HMomCoefs<double
     return -1;
 }
 
+int hmom_persist_dispatch_f32(int R, const HMomPersistArgs& pa, const HMomMaps& maps, const HMomCoefs<double>& c,
+                              cudaStream_t s);
+int hmom_persist_dispatch_bf16(int R, const HMomPersistArgs& pa, const HMomMaps& maps, const HMomCoefs<double>& c,
+                               cudaStream_t s);
+
+int launch_hmom_persist(DType t, int R, int p, const HMomPersistArgs& pa, const HMomMaps& maps,
+                        const HMomCoefs<double>& c, void* stream) {
+    if (t == DType::F64 || !hmom_available(t, R, p)) return -1;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    return t == DType::F32 ? hmom_persist_dispatch_f32(R, pa, maps, c, s) : hmom_persist_dispatch_bf16(R, pa, maps, c, s);
+}
+
 int launch_hdirect(DType t, const HDirectArgs& a, void* stream) {
     constexpr int TX = 4, NW = 4;
     const int W = 2 * a.R + 1;

@@ -6,6 +6,8 @@
 // Views produced for a horizontal filter carry an x halo of `hx` mirrored
 // columns on each side (columns -hx..-1 and I..I+hx-1 are readable).
 #pragma once
+#include <cuda.h>
+
 #include <cstdint>
 
 namespace mgbf {
@@ -305,5 +307,31 @@ int launch_dot(DType t, const DotArgs& a, void* stream);
 bool hmom_available(DType t, int R, int p);
 int launch_hmom(DType t, int R, int p, const HMomArgs& a, const HMomCoefs<double>& c,
                 void* stream);
+
+// Persistent radial side: the generations of one variable group in one
+// launch of k_hmom_persist (the single-row TMA pipeline, tile after tile).
+// Each segment is one generation: its HMomArgs (views, sizes, rows per
+// block, scale, mirror, status, poll limit; tmap and variant unused) and,
+// filled in by the launcher, its tile grid and first tile.  queue: one int
+// of device memory the launcher zeroes before the launch.
+constexpr int kMaxPersistSegs = 8;
+struct HMomSeg {
+    HMomArgs a;
+    int nkb = 0, nstrip = 0, nrowb = 0, first = 0;
+};
+struct HMomPersistArgs {
+    HMomSeg seg[kMaxPersistSegs];
+    int nseg = 0, ntiles = 0;
+    int* queue = nullptr;
+    int blocks_per_sm = 0;  // resident blocks per SM the launch asks for (capped by occupancy; <= 0: all that fit)
+};
+struct HMomMaps {
+    CUtensorMap m[kMaxPersistSegs];  // TMA map of each segment's input buffer (box as k_hmom_tma)
+};
+// Returns -1 (nothing launched) for FP64, reaches without a moment kernel,
+// or views the TMA pipeline cannot take; the caller then launches per
+// generation.
+int launch_hmom_persist(DType t, int R, int p, const HMomPersistArgs& pa, const HMomMaps& maps,
+                        const HMomCoefs<double>& c, void* stream);
 
 }  // namespace mgbf

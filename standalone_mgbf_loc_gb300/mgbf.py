@@ -377,6 +377,12 @@ class MGBFBatch:
         stream = torch.cuda.current_stream().cuda_stream if torch is not None else None
         _abi.check(self._lib.mgbf_batch_autotune(self._h, dt, stream), "mgbf_batch_autotune")
 
+    def use_persistent(self, blocks_per_sm: int = 8) -> None:
+        """Run each radial side of every group as one persistent launch over
+        all generations (FP32/BF16), with up to blocks_per_sm resident
+        blocks per SM; 0 (or False) returns to one launch per generation."""
+        _abi.check(self._lib.mgbf_batch_use_persistent(self._h, int(blocks_per_sm)), "mgbf_batch_use_persistent")
+
     def tuning(self, dtype=None):
         """The radial-kernel choice per group, generation and pass: a list
         (one entry per group) of lists (per generation) of two
