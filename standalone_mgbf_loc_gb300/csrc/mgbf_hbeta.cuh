@@ -816,7 +816,7 @@ __global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_cons
 // of a side are independent, so any order is correct.  The counter must be
 // zero at launch.
 template <int R, int P, int TX, typename T>
-__global__ void __launch_bounds__(128) k_hmom_persist(const __grid_constant__ HMomPersistArgs pa,
+__global__ void __launch_bounds__(128, R <= 8 ? 4 : 3) k_hmom_persist(const __grid_constant__ HMomPersistArgs pa,
                                                      const __grid_constant__ HMomMaps maps,
                                                      const __grid_constant__ HMomCoefs2 c) {
     __shared__ __align__(8) unsigned long long bars[kStages];
@@ -845,10 +845,13 @@ __global__ void __launch_bounds__(128) k_hmom_persist(const __grid_constant__ HM
         lt /= g.nkb;
         const int iy = lt % g.nstrip;
         const int jz = lt / g.nstrip;
-        const int jb = jz * g.a.rows;
-        if (!hmom_tma1_tile<R, P, TX, T>(g.a, &maps.m[sg], c, kx * 64, iy * (kStageWarps * TX), jb, sbase, bbase, rbase))
+        // the segment's arguments, read once per tile (a dynamic index into
+        // the parameter space would reload them at every use)
+        const HMomArgs a = g.a;
+        const int jb = jz * a.rows;
+        if (!hmom_tma1_tile<R, P, TX, T>(a, &maps.m[sg], c, kx * 64, iy * (kStageWarps * TX), jb, sbase, bbase, rbase))
             break;
-        rbase += hmom_tma1_rows<R, TX>(min(jb + g.a.rows, g.a.J) - jb);
+        rbase += hmom_tma1_rows<R, TX>(min(jb + a.rows, a.J) - jb);
     }
 }
 
