@@ -371,6 +371,8 @@ def run_gpu(args):
         extras["fast_fp32"] = fast_forward(torch, dev, torch.float32, peak)
         extras["transfers_fp32"] = transfers(torch, dev, torch.float32, peak)
         extras["rad3_fp32"] = rad3_forward(torch, dev, torch.float32)
+        extras["lin2_fp32"] = lin2_forward(torch, dev, torch.float32)
+        extras["lin3_fp32"] = lin3_forward(torch, dev, torch.float32)
 
     result = None
     if rank == 0:
@@ -842,6 +844,45 @@ def lin2_forward(torch, dev, dtype):
             "stages_ms": {k: v[1] for k, v in st.items()}}
 
 
+def lin3_forward(torch, dev, dtype):
+    """filtering_procedure(5) (filtering_lin3) on one 768x768x64 field, 5
+    generations: per generation the seven colors of the hexad's 3D line
+    filters (x, y and z lines of half-span 2 at mg_ampl03 = 0.6, three
+    identity diagonals, color 7 null) on both sides, restriction and
+    prolongation as procedure 1."""
+    from standalone_mgbf_loc_gb300 import MGBF, MGBFConfig, _abi
+    cfg = MGBFConfig(nxPE=16, nyPE=16, im_filt=48, jm_filt=48, lm=64, km3=1, km2=0, n_ens=1, gm_max=5,
+                     hx=12, hy=12, hz=3, p=2, mg_ampl02=0.3, mg_ampl01=ampl01(3), mg_ampl03=0.6, mgbf_line=True,
+                     mg_weig1=1.0, mg_weig2=0.5, mg_weig3=0.25, mg_weig4=0.125, mg_weig5=0.0625,
+                     layout=_abi.MGBF_LAYOUT_COMPACT)
+    op = MGBF(cfg)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(12)
+    x = torch.randn(op.field_shape(), generator=gen, device=dev, dtype=dtype)
+    for _ in range(2):
+        op.filtering_procedure(5, x)
+    torch.cuda.synchronize()
+    n = 5
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(n):
+        op.filtering_procedure(5, x)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / n
+    _abi.timers_enable(True)
+    op.filtering_procedure(5, x)
+    torch.cuda.synchronize()
+    st = _abi.timers_read()
+    _abi.timers_enable(False)
+    op.status()
+    pts = float(np.prod(op.field_shape()))
+    op.close()
+    return {"workload": "filtering_lin3 (proc 5), one 3D field 768x768x64, 5 generations, 3D line half-span 2",
+            "dtype": str(dtype).replace("torch.", ""), "ms": ms, "value": pts / (ms * 1e-3), "unit": UNIT,
+            "stages_ms": {k: v[1] for k, v in st.items()}}
+
+
 def transfers(torch, dev, dtype, peak_gbs, half=False):
     """anal_to_filt_all2 / filt_to_anal_all2 on the shipped namelist's grids:
     analysis 1440x960, filter 20x20 ranks of 64x32 (1280x640), 4 3D
@@ -911,6 +952,7 @@ LEGS = {
     "transfers_half": lambda torch, dev, peak: transfers(torch, dev, torch.float32, peak, half=True),
     "rad3": lambda torch, dev, peak: rad3_forward(torch, dev, torch.float32),
     "lin2": lambda torch, dev, peak: lin2_forward(torch, dev, torch.float32),
+    "lin3": lambda torch, dev, peak: lin3_forward(torch, dev, torch.float32),
     "plain": lambda torch, dev, peak: plain_forward(torch, dev, torch.float32),
     "cfg1": lambda torch, dev, peak: cfg1_leg(torch, dev)[0],
     "cfg3": lambda torch, dev, peak: cfg3_leg(torch, dev)[0],
