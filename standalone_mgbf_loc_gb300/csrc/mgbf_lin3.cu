@@ -43,9 +43,10 @@ W3 make_w3(const Lin3Args& a) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_copy(Lin3Args a, W3 w, int to) {
     using A = typename AccOf<T>::type;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.nv * a.lm) return;
-    const int i = blockIdx.y, j = blockIdx.z;
+    const int nlv = a.nv * a.lm;
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (k, i) of row j, k fastest
+    if (x >= (long long)nlv * a.I) return;
+    const int i = (int)(x / nlv), k = (int)(x - (long long)i * nlv), j = blockIdx.y;
     const int v = k / a.lm, L = k - v * a.lm;
     T* W = static_cast<T*>(a.w);
     if (to) {
@@ -66,10 +67,12 @@ __global__ void __launch_bounds__(256) k_l3_copy(Lin3Args a, W3 w, int to) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_dib(Lin3Args a, W3 w, int adj) {
     using A = typename AccOf<T>::type;
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= w.LX * w.NV) return;
-    const int v = (int)(x / w.LX), L = (int)(x - (long long)v * w.LX) - a.hz;
-    const int i = (int)blockIdx.y - a.hx, j = (int)blockIdx.z - a.hy;
+    const long long cell = w.LX * w.NV;  // extended levels of one column
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (L, v, i) of row j, L fastest
+    if (x >= cell * w.NI) return;
+    const long long ic = x / cell, r = x - ic * cell;
+    const int v = (int)(r / w.LX), L = (int)(r - (long long)v * w.LX) - a.hz;
+    const int i = (int)ic - a.hx, j = (int)blockIdx.y - a.hy;
     const T* W = static_cast<const T*>(a.w);
     T* Tb = static_cast<T*>(a.t);
     A fil[kMaxL3Span + 1];
@@ -108,10 +111,12 @@ __global__ void __launch_bounds__(256) k_l3_dib(Lin3Args a, W3 w, int adj) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_foldx(Lin3Args a, W3 w, int o) {
     using A = typename AccOf<T>::type;
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= (long long)a.lm * a.nv) return;
-    const int v = (int)(x / a.lm), L = (int)(x - (long long)v * a.lm);
-    const int j = (int)blockIdx.y - a.hy;
+    const long long nlv = (long long)a.lm * a.nv;
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), j), L fastest
+    if (x >= nlv * (a.J + 2 * a.hy)) return;
+    const long long jr = x / nlv, r = x - jr * nlv;
+    const int v = (int)(r / a.lm), L = (int)(r - (long long)v * a.lm);
+    const int j = (int)jr - a.hy;
     T* W = static_cast<T*>(a.w);
     for (int s = 1; s <= a.hx; ++s) {
         T* d = W + w.at(v, s - 1, j, L);
@@ -127,10 +132,12 @@ __global__ void __launch_bounds__(256) k_l3_foldx(Lin3Args a, W3 w, int o) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_foldy(Lin3Args a, W3 w, int o) {
     using A = typename AccOf<T>::type;
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= (long long)a.lm * a.nv) return;
-    const int v = (int)(x / a.lm), L = (int)(x - (long long)v * a.lm);
-    const int i = blockIdx.y;
+    const long long nlv = (long long)a.lm * a.nv;
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), i), L fastest
+    if (x >= nlv * a.I) return;
+    const long long ir = x / nlv, r = x - ir * nlv;
+    const int v = (int)(r / a.lm), L = (int)(r - (long long)v * a.lm);
+    const int i = (int)ir;
     T* W = static_cast<T*>(a.w);
     for (int s = 1; s <= a.hy; ++s) {
         T* d = W + w.at(v, i, s - 1, L);
@@ -164,10 +171,12 @@ __global__ void __launch_bounds__(256) k_l3_foldz(Lin3Args a, W3 w) {
 // half-sample mirrors W(J+j) = W(J+1-j), W(-hy+j) = W(hy+1-j).
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_filly(Lin3Args a, W3 w) {
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= (long long)a.lm * a.nv) return;
-    const int v = (int)(x / a.lm), L = (int)(x - (long long)v * a.lm);
-    const int i = blockIdx.y;
+    const long long nlv = (long long)a.lm * a.nv;
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), i), L fastest
+    if (x >= nlv * a.I) return;
+    const long long ir = x / nlv, r = x - ir * nlv;
+    const int v = (int)(r / a.lm), L = (int)(r - (long long)v * a.lm);
+    const int i = (int)ir;
     T* W = static_cast<T*>(a.w);
     for (int s = 1; s <= a.hy; ++s) W[w.at(v, i, a.J + s - 1, L)] = W[w.at(v, i, a.J - s, L)];
     for (int s = 1; s <= a.hy; ++s) W[w.at(v, i, -a.hy + s - 1, L)] = W[w.at(v, i, a.hy - s, L)];
@@ -178,10 +187,12 @@ __global__ void __launch_bounds__(256) k_l3_filly(Lin3Args a, W3 w) {
 // (boco_3d_g1) or W(I+1-i) (boco_3d_gh, o = 1).
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_fillx(Lin3Args a, W3 w, int o) {
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= (long long)a.lm * a.nv) return;
-    const int v = (int)(x / a.lm), L = (int)(x - (long long)v * a.lm);
-    const int j = (int)blockIdx.y - a.hy;
+    const long long nlv = (long long)a.lm * a.nv;
+    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), j), L fastest
+    if (x >= nlv * (a.J + 2 * a.hy)) return;
+    const long long jr = x / nlv, r = x - jr * nlv;
+    const int v = (int)(r / a.lm), L = (int)(r - (long long)v * a.lm);
+    const int j = (int)jr - a.hy;
     T* W = static_cast<T*>(a.w);
     for (int s = 1; s <= a.hx; ++s) W[w.at(v, -a.hx + s - 1, j, L)] = W[w.at(v, a.hx - s, j, L)];
     for (int s = 1; s <= a.hx; ++s) W[w.at(v, a.I + s - 1, j, L)] = W[w.at(v, a.I - s - 1 + o, j, L)];
@@ -215,17 +226,17 @@ int launch_lin3_t(const Lin3Args& a0, int op, void* stream) {
     switch (op) {
         case kL3From:
         case kL3To:
-            k_l3_copy<T><<<dim3(blocks(nlv), a.I, a.J), 256, 0, s>>>(a, w, op == kL3To);
+            k_l3_copy<T><<<dim3(blocks(nlv * a.I), a.J), 256, 0, s>>>(a, w, op == kL3To);
             break;
         case kL3DibFwd:
         case kL3DibAdj:
-            k_l3_dib<T><<<dim3(blocks(w.LX * w.NV), NI, NJ), 256, 0, s>>>(a, w, op == kL3DibAdj);
+            k_l3_dib<T><<<dim3(blocks(w.LX * w.NV * NI), NJ), 256, 0, s>>>(a, w, op == kL3DibAdj);
             break;
-        case kL3FoldX: k_l3_foldx<T><<<dim3(blocks(nlv), NJ), 256, 0, s>>>(a, w, a.gh); break;
-        case kL3FoldY: k_l3_foldy<T><<<dim3(blocks(nlv), a.I), 256, 0, s>>>(a, w, a.gh); break;
+        case kL3FoldX: k_l3_foldx<T><<<blocks(nlv * NJ), 256, 0, s>>>(a, w, a.gh); break;
+        case kL3FoldY: k_l3_foldy<T><<<blocks(nlv * a.I), 256, 0, s>>>(a, w, a.gh); break;
         case kL3FoldZ: k_l3_foldz<T><<<dim3(blocks(ncol), NJ), 256, 0, s>>>(a, w); break;
-        case kL3FillY: k_l3_filly<T><<<dim3(blocks(nlv), a.I), 256, 0, s>>>(a, w); break;
-        case kL3FillX: k_l3_fillx<T><<<dim3(blocks(nlv), NJ), 256, 0, s>>>(a, w, a.gh); break;
+        case kL3FillY: k_l3_filly<T><<<blocks(nlv * a.I), 256, 0, s>>>(a, w); break;
+        case kL3FillX: k_l3_fillx<T><<<blocks(nlv * NJ), 256, 0, s>>>(a, w, a.gh); break;
         case kL3ZMirror: k_l3_zmirror<T><<<dim3(blocks(ncol), NJ), 256, 0, s>>>(a, w); break;
         default: return (int)cudaErrorInvalidValue;
     }
