@@ -43,10 +43,12 @@ W3 make_w3(const Lin3Args& a) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_copy(Lin3Args a, W3 w, int to) {
     using A = typename AccOf<T>::type;
-    const int nlv = a.nv * a.lm;
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (k, i) of row j, k fastest
-    if (x >= (long long)nlv * a.I) return;
-    const int i = (int)(x / nlv), k = (int)(x - (long long)i * nlv), j = blockIdx.y;
+    // 32-bit decode: one row's index space is small, and a 64-bit division
+    // by a runtime value costs far more than the copy itself
+    const unsigned nlv = (unsigned)(a.nv * a.lm);
+    const unsigned x = blockIdx.x * blockDim.x + threadIdx.x;  // (k, i) of row j, k fastest
+    if (x >= nlv * (unsigned)a.I) return;
+    const int i = (int)(x / nlv), k = (int)(x - (unsigned)i * nlv), j = blockIdx.y;
     const int v = k / a.lm, L = k - v * a.lm;
     T* W = static_cast<T*>(a.w);
     if (to) {
@@ -67,11 +69,11 @@ __global__ void __launch_bounds__(256) k_l3_copy(Lin3Args a, W3 w, int to) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_dib(Lin3Args a, W3 w, int adj) {
     using A = typename AccOf<T>::type;
-    const long long cell = w.LX * w.NV;  // extended levels of one column
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (L, v, i) of row j, L fastest
-    if (x >= cell * w.NI) return;
-    const long long ic = x / cell, r = x - ic * cell;
-    const int v = (int)(r / w.LX), L = (int)(r - (long long)v * w.LX) - a.hz;
+    const unsigned lx = (unsigned)w.LX, cell = (unsigned)(w.LX * w.NV);  // extended levels of one column
+    const unsigned x = blockIdx.x * blockDim.x + threadIdx.x;  // (L, v, i) of row j, L fastest (32-bit decode)
+    if (x >= cell * (unsigned)w.NI) return;
+    const unsigned ic = x / cell, r = x - ic * cell;
+    const int v = (int)(r / lx), L = (int)(r - (unsigned)v * lx) - a.hz;
     const int i = (int)ic - a.hx, j = (int)blockIdx.y - a.hy;
     const T* W = static_cast<const T*>(a.w);
     T* Tb = static_cast<T*>(a.t);
@@ -111,11 +113,11 @@ __global__ void __launch_bounds__(256) k_l3_dib(Lin3Args a, W3 w, int adj) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_foldx(Lin3Args a, W3 w, int o) {
     using A = typename AccOf<T>::type;
-    const long long nlv = (long long)a.lm * a.nv;
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), j), L fastest
-    if (x >= nlv * (a.J + 2 * a.hy)) return;
-    const long long jr = x / nlv, r = x - jr * nlv;
-    const int v = (int)(r / a.lm), L = (int)(r - (long long)v * a.lm);
+    const unsigned nlv = (unsigned)(a.lm * a.nv), lm = (unsigned)a.lm;
+    const unsigned x = blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), j), L fastest (32-bit decode)
+    if (x >= nlv * (unsigned)(a.J + 2 * a.hy)) return;
+    const unsigned jr = x / nlv, r = x - jr * nlv;
+    const int v = (int)(r / lm), L = (int)(r - (unsigned)v * lm);
     const int j = (int)jr - a.hy;
     T* W = static_cast<T*>(a.w);
     for (int s = 1; s <= a.hx; ++s) {
@@ -132,11 +134,11 @@ __global__ void __launch_bounds__(256) k_l3_foldx(Lin3Args a, W3 w, int o) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_foldy(Lin3Args a, W3 w, int o) {
     using A = typename AccOf<T>::type;
-    const long long nlv = (long long)a.lm * a.nv;
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), i), L fastest
-    if (x >= nlv * a.I) return;
-    const long long ir = x / nlv, r = x - ir * nlv;
-    const int v = (int)(r / a.lm), L = (int)(r - (long long)v * a.lm);
+    const unsigned nlv = (unsigned)(a.lm * a.nv), lm = (unsigned)a.lm;
+    const unsigned x = blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), i), L fastest (32-bit decode)
+    if (x >= nlv * (unsigned)a.I) return;
+    const unsigned ir = x / nlv, r = x - ir * nlv;
+    const int v = (int)(r / lm), L = (int)(r - (unsigned)v * lm);
     const int i = (int)ir;
     T* W = static_cast<T*>(a.w);
     for (int s = 1; s <= a.hy; ++s) {
@@ -154,9 +156,10 @@ __global__ void __launch_bounds__(256) k_l3_foldy(Lin3Args a, W3 w, int o) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_foldz(Lin3Args a, W3 w) {
     using A = typename AccOf<T>::type;
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= w.NV * w.NI) return;
-    const int v = (int)(x % w.NV), i = (int)(x / w.NV) - a.hx;
+    const unsigned nv = (unsigned)w.NV;
+    const unsigned x = blockIdx.x * blockDim.x + threadIdx.x;  // (v, i), v fastest (32-bit decode)
+    if (x >= nv * (unsigned)w.NI) return;
+    const int v = (int)(x % nv), i = (int)(x / nv) - a.hx;
     const int j = (int)blockIdx.y - a.hy;
     T* W = static_cast<T*>(a.w);
     for (int s = 1; s <= a.hz; ++s) {
@@ -171,11 +174,11 @@ __global__ void __launch_bounds__(256) k_l3_foldz(Lin3Args a, W3 w) {
 // half-sample mirrors W(J+j) = W(J+1-j), W(-hy+j) = W(hy+1-j).
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_filly(Lin3Args a, W3 w) {
-    const long long nlv = (long long)a.lm * a.nv;
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), i), L fastest
-    if (x >= nlv * a.I) return;
-    const long long ir = x / nlv, r = x - ir * nlv;
-    const int v = (int)(r / a.lm), L = (int)(r - (long long)v * a.lm);
+    const unsigned nlv = (unsigned)(a.lm * a.nv), lm = (unsigned)a.lm;
+    const unsigned x = blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), i), L fastest (32-bit decode)
+    if (x >= nlv * (unsigned)a.I) return;
+    const unsigned ir = x / nlv, r = x - ir * nlv;
+    const int v = (int)(r / lm), L = (int)(r - (unsigned)v * lm);
     const int i = (int)ir;
     T* W = static_cast<T*>(a.w);
     for (int s = 1; s <= a.hy; ++s) W[w.at(v, i, a.J + s - 1, L)] = W[w.at(v, i, a.J - s, L)];
@@ -187,11 +190,11 @@ __global__ void __launch_bounds__(256) k_l3_filly(Lin3Args a, W3 w) {
 // (boco_3d_g1) or W(I+1-i) (boco_3d_gh, o = 1).
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_fillx(Lin3Args a, W3 w, int o) {
-    const long long nlv = (long long)a.lm * a.nv;
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), j), L fastest
-    if (x >= nlv * (a.J + 2 * a.hy)) return;
-    const long long jr = x / nlv, r = x - jr * nlv;
-    const int v = (int)(r / a.lm), L = (int)(r - (long long)v * a.lm);
+    const unsigned nlv = (unsigned)(a.lm * a.nv), lm = (unsigned)a.lm;
+    const unsigned x = blockIdx.x * blockDim.x + threadIdx.x;  // ((v, L), j), L fastest (32-bit decode)
+    if (x >= nlv * (unsigned)(a.J + 2 * a.hy)) return;
+    const unsigned jr = x / nlv, r = x - jr * nlv;
+    const int v = (int)(r / lm), L = (int)(r - (unsigned)v * lm);
     const int j = (int)jr - a.hy;
     T* W = static_cast<T*>(a.w);
     for (int s = 1; s <= a.hx; ++s) W[w.at(v, -a.hx + s - 1, j, L)] = W[w.at(v, a.hx - s, j, L)];
@@ -202,9 +205,10 @@ __global__ void __launch_bounds__(256) k_l3_fillx(Lin3Args a, W3 w, int o) {
 // W(1-L) = W(1+L), W(lm+L) = W(lm-L), L = 1..hz.
 template <typename T>
 __global__ void __launch_bounds__(256) k_l3_zmirror(Lin3Args a, W3 w) {
-    const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= w.NV * w.NI) return;
-    const int v = (int)(x % w.NV), i = (int)(x / w.NV) - a.hx;
+    const unsigned nv = (unsigned)w.NV;
+    const unsigned x = blockIdx.x * blockDim.x + threadIdx.x;  // (v, i), v fastest (32-bit decode)
+    if (x >= nv * (unsigned)w.NI) return;
+    const int v = (int)(x % nv), i = (int)(x / nv) - a.hx;
     const int j = (int)blockIdx.y - a.hy;
     T* W = static_cast<T*>(a.w);
     for (int s = 1; s <= a.hz; ++s) {
