@@ -698,10 +698,24 @@ struct Exec {
                 for (int i = 0; i <= a.h && i <= kMaxL3Span; ++i) a.fil[i] = G.xs.fil[q][i];
             }
         };
+        // A color without a line (h = 0, weight 1) copies the interior exactly
+        // and leaves zeros in every halo cell: in place, that is zeroing the
+        // halo.  On the forward side the fills before it write only halo
+        // cells it then zeroes, so they do not run.  On the adjoint side the
+        // folds after it add those zeros into the interior at coarser
+        // generations and are skipped there; at generation 1 they run, since
+        // bocoT_3d_g1's east and north folds also add the edge column and row
+        // (interior cells) to themselves.
+        auto is_copy = [&]() { return a.h == 0 && a.fil[0] == 1.0; };
         if ((rc = run(kL3From))) return rc;
         if (adj) {
             for (int col = 7; col >= 1; --col) {
                 color(col);
+                if (is_copy()) {
+                    if ((rc = run(kL3HaloZero))) return rc;
+                    if (!a.gh && ((rc = run(kL3FoldX)) || (rc = run(kL3FoldY)) || (rc = run(kL3FoldZ)))) return rc;
+                    continue;
+                }
                 if ((rc = run(kL3DibAdj))) return rc;
                 cur = 1 - cur;
                 if ((rc = run(kL3FoldX)) || (rc = run(kL3FoldY)) || (rc = run(kL3FoldZ))) return rc;
@@ -710,9 +724,13 @@ struct Exec {
         } else {
             if ((rc = run(kL3ZMirror))) return rc;
             for (int col = 1; col <= 7; ++col) {
+                color(col);
+                if (is_copy()) {
+                    if ((rc = run(kL3HaloZero))) return rc;
+                    continue;
+                }
                 if ((rc = run(kL3FillY)) || (rc = run(kL3FillX))) return rc;
                 if (a.gh && (rc = run(kL3ZMirror))) return rc;
-                color(col);
                 if ((rc = run(kL3DibFwd))) return rc;
                 cur = 1 - cur;
             }

@@ -140,7 +140,7 @@ struct DibArgs {
 // element (v, i, j, L) at (L+hz) + (lm+2hz)*(v + nv*((i+hx) + (I+2hx)*(j+hy))).
 constexpr int kMaxL3Span = 8;  // dibeta half-span limit (nfil)
 enum Lin3Op : int { kL3From = 0, kL3To, kL3DibFwd, kL3DibAdj, kL3FoldX, kL3FoldY, kL3FoldZ, kL3FillY, kL3FillX,
-                    kL3ZMirror };
+                    kL3ZMirror, kL3HaloZero };
 struct Lin3Args {
     View in, out;            // generation buffers (k = v*lm + L, i, j): kL3From reads in, kL3To writes out
     void* w;                 // the array a stage works on

@@ -81,29 +81,33 @@ __global__ void __launch_bounds__(256) k_l3_dib(Lin3Args a, W3 w, int adj) {
 #pragma unroll
     for (int s = 0; s <= kMaxL3Span; ++s) fil[s] = sizeof(A) == 8 ? (A)a.fil[s] : (A)a.filf[s];
     const bool in_p = w.interior(i, j, L);
+    // the cell's index once, and one step along the generator (its
+    // neighbours are base +- s * step: no index arithmetic per tap)
+    const long long base = w.at(v, i, j, L);
+    const long long step = (long long)a.dz + w.LX * (w.NV * ((long long)a.dx + w.NI * (long long)a.dy));
+    const T* Wc = W + base;
     A acc = A(0);
     if (!adj) {
         if (in_p) {
-            acc = fil[0] * static_cast<A>(ldc(W + w.at(v, i, j, L)));
+            acc = fil[0] * static_cast<A>(ldc(Wc));
 #pragma unroll
             for (int s = 1; s <= kMaxL3Span; ++s) {
                 if (s > a.h) break;
-                acc += fil[s] * (static_cast<A>(ldc(W + w.at(v, i + s * a.dx, j + s * a.dy, L + s * a.dz))) +
-                                 static_cast<A>(ldc(W + w.at(v, i - s * a.dx, j - s * a.dy, L - s * a.dz))));
+                acc += fil[s] * (static_cast<A>(ldc(Wc + s * step)) + static_cast<A>(ldc(Wc - s * step)));
             }
         }
     } else {
-        if (in_p) acc = fil[0] * static_cast<A>(ldc(W + w.at(v, i, j, L)));
+        if (in_p) acc = fil[0] * static_cast<A>(ldc(Wc));
 #pragma unroll
         for (int s = 1; s <= kMaxL3Span; ++s) {
             if (s > a.h) break;
             const int im = i - s * a.dx, jm = j - s * a.dy, Lm = L - s * a.dz;
             const int ip = i + s * a.dx, jp = j + s * a.dy, Lp = L + s * a.dz;
-            if (w.interior(im, jm, Lm)) acc += fil[s] * static_cast<A>(ldc(W + w.at(v, im, jm, Lm)));
-            if (w.interior(ip, jp, Lp)) acc += fil[s] * static_cast<A>(ldc(W + w.at(v, ip, jp, Lp)));
+            if (w.interior(im, jm, Lm)) acc += fil[s] * static_cast<A>(ldc(Wc - s * step));
+            if (w.interior(ip, jp, Lp)) acc += fil[s] * static_cast<A>(ldc(Wc + s * step));
         }
     }
-    stv(Tb + w.at(v, i, j, L), acc);
+    stv(Tb + base, acc);
 }
 
 // bocoT_3d x part (mg_bocos.f90:2173-2527, 2530-2908): on every row of the
@@ -119,14 +123,15 @@ __global__ void __launch_bounds__(256) k_l3_foldx(Lin3Args a, W3 w, int o) {
     const unsigned jr = x / nlv, r = x - jr * nlv;
     const int v = (int)(r / lm), L = (int)(r - (unsigned)v * lm);
     const int j = (int)jr - a.hy;
-    T* W = static_cast<T*>(a.w);
+    T* const row = static_cast<T*>(a.w) + w.at(v, 0, j, L);  // column c at row + c * cs
+    const long long cs = w.LX * w.NV;
     for (int s = 1; s <= a.hx; ++s) {
-        T* d = W + w.at(v, s - 1, j, L);
-        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(W + w.at(v, -s, j, L))));
+        T* d = row + (s - 1) * cs;
+        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(row - s * cs)));
     }
     for (int s = 1; s <= a.hx; ++s) {
-        T* d = W + w.at(v, a.I - a.hx + s - 1, j, L);
-        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(W + w.at(v, a.I + o + a.hx - s - 1, j, L))));
+        T* d = row + (a.I - a.hx + s - 1) * cs;
+        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(row + (a.I + o + a.hx - s - 1) * cs)));
     }
 }
 
@@ -140,14 +145,15 @@ __global__ void __launch_bounds__(256) k_l3_foldy(Lin3Args a, W3 w, int o) {
     const unsigned ir = x / nlv, r = x - ir * nlv;
     const int v = (int)(r / lm), L = (int)(r - (unsigned)v * lm);
     const int i = (int)ir;
-    T* W = static_cast<T*>(a.w);
+    T* const col = static_cast<T*>(a.w) + w.at(v, i, 0, L);  // row r at col + r * rs
+    const long long rs = w.LX * w.NV * w.NI;
     for (int s = 1; s <= a.hy; ++s) {
-        T* d = W + w.at(v, i, s - 1, L);
-        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(W + w.at(v, i, -s, L))));
+        T* d = col + (s - 1) * rs;
+        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(col - s * rs)));
     }
     for (int s = 1; s <= a.hy; ++s) {
-        T* d = W + w.at(v, i, a.J - a.hy + s - 1, L);
-        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(W + w.at(v, i, a.J + o + a.hy - s - 1, L))));
+        T* d = col + (a.J - a.hy + s - 1) * rs;
+        stv(d, static_cast<A>(ldc(d)) + static_cast<A>(ldc(col + (a.J + o + a.hy - s - 1) * rs)));
     }
 }
 
@@ -161,12 +167,12 @@ __global__ void __launch_bounds__(256) k_l3_foldz(Lin3Args a, W3 w) {
     if (x >= nv * (unsigned)w.NI) return;
     const int v = (int)(x % nv), i = (int)(x / nv) - a.hx;
     const int j = (int)blockIdx.y - a.hy;
-    T* W = static_cast<T*>(a.w);
+    T* const c0 = static_cast<T*>(a.w) + w.at(v, i, j, 0);  // level L at c0 + L
     for (int s = 1; s <= a.hz; ++s) {
-        T* lo = W + w.at(v, i, j, s);
-        stv(lo, static_cast<A>(ldc(lo)) + static_cast<A>(ldc(W + w.at(v, i, j, -s))));
-        T* hi = W + w.at(v, i, j, a.lm - s - 1);
-        stv(hi, static_cast<A>(ldc(hi)) + static_cast<A>(ldc(W + w.at(v, i, j, a.lm + s - 1))));
+        T* lo = c0 + s;
+        stv(lo, static_cast<A>(ldc(lo)) + static_cast<A>(ldc(c0 - s)));
+        T* hi = c0 + (a.lm - s - 1);
+        stv(hi, static_cast<A>(ldc(hi)) + static_cast<A>(ldc(c0 + (a.lm + s - 1))));
     }
 }
 
@@ -180,9 +186,10 @@ __global__ void __launch_bounds__(256) k_l3_filly(Lin3Args a, W3 w) {
     const unsigned ir = x / nlv, r = x - ir * nlv;
     const int v = (int)(r / lm), L = (int)(r - (unsigned)v * lm);
     const int i = (int)ir;
-    T* W = static_cast<T*>(a.w);
-    for (int s = 1; s <= a.hy; ++s) W[w.at(v, i, a.J + s - 1, L)] = W[w.at(v, i, a.J - s, L)];
-    for (int s = 1; s <= a.hy; ++s) W[w.at(v, i, -a.hy + s - 1, L)] = W[w.at(v, i, a.hy - s, L)];
+    T* const col = static_cast<T*>(a.w) + w.at(v, i, 0, L);  // row r at col + r * rs
+    const long long rs = w.LX * w.NV * w.NI;
+    for (int s = 1; s <= a.hy; ++s) col[(a.J + s - 1) * rs] = col[(a.J - s) * rs];
+    for (int s = 1; s <= a.hy; ++s) col[(-a.hy + s - 1) * rs] = col[(a.hy - s) * rs];
 }
 
 // boco_3d x part (every row of the extended y range, levels 1..lm): west
@@ -196,9 +203,10 @@ __global__ void __launch_bounds__(256) k_l3_fillx(Lin3Args a, W3 w, int o) {
     const unsigned jr = x / nlv, r = x - jr * nlv;
     const int v = (int)(r / lm), L = (int)(r - (unsigned)v * lm);
     const int j = (int)jr - a.hy;
-    T* W = static_cast<T*>(a.w);
-    for (int s = 1; s <= a.hx; ++s) W[w.at(v, -a.hx + s - 1, j, L)] = W[w.at(v, a.hx - s, j, L)];
-    for (int s = 1; s <= a.hx; ++s) W[w.at(v, a.I + s - 1, j, L)] = W[w.at(v, a.I - s - 1 + o, j, L)];
+    T* const row = static_cast<T*>(a.w) + w.at(v, 0, j, L);  // column c at row + c * cs
+    const long long cs = w.LX * w.NV;
+    for (int s = 1; s <= a.hx; ++s) row[(-a.hx + s - 1) * cs] = row[(a.hx - s) * cs];
+    for (int s = 1; s <= a.hx; ++s) row[(a.I + s - 1) * cs] = row[(a.I - s - 1 + o) * cs];
 }
 
 // Whole-sample mirror of the z halo on every column of the extended plane:
@@ -210,11 +218,25 @@ __global__ void __launch_bounds__(256) k_l3_zmirror(Lin3Args a, W3 w) {
     if (x >= nv * (unsigned)w.NI) return;
     const int v = (int)(x % nv), i = (int)(x / nv) - a.hx;
     const int j = (int)blockIdx.y - a.hy;
-    T* W = static_cast<T*>(a.w);
+    T* const c0 = static_cast<T*>(a.w) + w.at(v, i, j, 0);  // level L at c0 + L
     for (int s = 1; s <= a.hz; ++s) {
-        W[w.at(v, i, j, -s)] = W[w.at(v, i, j, s)];
-        W[w.at(v, i, j, a.lm + s - 1)] = W[w.at(v, i, j, a.lm - s - 1)];
+        c0[-s] = c0[s];
+        c0[a.lm + s - 1] = c0[a.lm - s - 1];
     }
+}
+
+// Zero every halo cell of the extended array (x, y and z halos) in place:
+// what the dibeta of a color without a line (h = 0, fil[0] = 1) leaves,
+// since it copies the interior exactly and writes zero elsewhere.
+template <typename T>
+__global__ void __launch_bounds__(256) k_l3_halo_zero(Lin3Args a, W3 w) {
+    const unsigned lx = (unsigned)w.LX, cell = (unsigned)(w.LX * w.NV);
+    const unsigned x = blockIdx.x * blockDim.x + threadIdx.x;  // (L, v, i) of row j, L fastest (32-bit decode)
+    if (x >= cell * (unsigned)w.NI) return;
+    const unsigned ic = x / cell, r = x - ic * cell;
+    const int v = (int)(r / lx), L = (int)(r - (unsigned)v * lx) - a.hz;
+    const int i = (int)ic - a.hx, j = (int)blockIdx.y - a.hy;
+    if (!w.interior(i, j, L)) static_cast<T*>(a.w)[w.at(v, i, j, L)] = T(0.0f);
 }
 
 template <typename T>
@@ -242,6 +264,7 @@ int launch_lin3_t(const Lin3Args& a0, int op, void* stream) {
         case kL3FillY: k_l3_filly<T><<<blocks(nlv * a.I), 256, 0, s>>>(a, w); break;
         case kL3FillX: k_l3_fillx<T><<<blocks(nlv * NJ), 256, 0, s>>>(a, w, a.gh); break;
         case kL3ZMirror: k_l3_zmirror<T><<<dim3(blocks(ncol), NJ), 256, 0, s>>>(a, w); break;
+        case kL3HaloZero: k_l3_halo_zero<T><<<dim3(blocks(w.LX * w.NV * NI), NJ), 256, 0, s>>>(a, w); break;
         default: return (int)cudaErrorInvalidValue;
     }
     const cudaError_t e = cudaGetLastError();
