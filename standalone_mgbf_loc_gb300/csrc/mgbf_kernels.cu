@@ -1237,13 +1237,24 @@ struct LinePos {
     bool ok;
 };
 __device__ __forceinline__ LinePos line_pos(int nq, int n, int m, int TL) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int nstrip = (n + TL - 1) / TL;
     LinePos r;
-    r.q = (int)(idx % nq);
-    const long long rest = idx / nq;
-    r.t0 = (int)(rest % nstrip) * TL;
-    r.line = (int)(rest / nstrip);
+    if ((unsigned long long)gridDim.x * blockDim.x <= 0xffffffffull) {
+        // 32-bit decode (every launch of realistic size): a 64-bit division
+        // by a runtime value costs more than a thread's share of the filter
+        const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
+        const unsigned rest = idx / (unsigned)nq;
+        r.q = (int)(idx - rest * (unsigned)nq);
+        const unsigned ln = rest / (unsigned)nstrip;
+        r.t0 = (int)(rest - ln * (unsigned)nstrip) * TL;
+        r.line = (int)ln;
+    } else {
+        const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        r.q = (int)(idx % nq);
+        const long long rest = idx / nq;
+        r.t0 = (int)(rest % nstrip) * TL;
+        r.line = (int)(rest / nstrip);
+    }
     r.ok = r.line < m;
     return r;
 }
