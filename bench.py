@@ -224,10 +224,8 @@ def run_gpu(args):
     # radial sides per generation or as one persistent launch per group: a
     # short timing of each (after a capturing call), the faster one is kept
     # for the timed region and the correctness sample
-    trials = {}
-    for blocks_per_sm in (0, 1, 2, 8):  # 0: per generation; else persistent with up to that many blocks per SM
-        batch.use_persistent(blocks_per_sm)
-        step()
+    def trial_ms():
+        step()  # captures the graph of this launch sequence
         torch.cuda.synchronize()
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a0.record()
@@ -235,12 +233,28 @@ def run_gpu(args):
             step()
         a1.record()
         torch.cuda.synchronize()
-        trials[blocks_per_sm] = a0.elapsed_time(a1) / 2
+        return a0.elapsed_time(a1) / 2
+
+    trials = {}
+    for blocks_per_sm in (0, 1, 2, 8):  # 0: per generation; else persistent with up to that many blocks per SM
+        batch.use_persistent(blocks_per_sm)
+        trials[blocks_per_sm] = trial_ms()
     best = min(trials, key=trials.get)
     batch.use_persistent(best)
     radial_launch = {"ms_per_step": {("per generation" if k == 0 else f"persistent, <= {k} blocks/SM"): v
                                      for k, v in trials.items()},
                      "chosen": "per generation" if best == 0 else f"persistent, <= {best} blocks/SM"}
+    # graph-node priorities of the concurrent group branches (0 none, 1
+    # memory-bound kernels first, 2 radial kernels first)
+    prio_names = {0: "none", 1: "memory-bound kernels first", 2: "radial kernels first"}
+    prio_trials = {0: trials[best]}
+    for mode in (1, 2):
+        batch.set_priorities(mode)
+        prio_trials[mode] = trial_ms()
+    best_prio = min(prio_trials, key=prio_trials.get)
+    batch.set_priorities(best_prio)
+    graph_priorities = {"ms_per_step": {prio_names[k]: v for k, v in prio_trials.items()},
+                        "chosen": prio_names[best_prio]}
     # fresh N(0,1) inputs: the trial steps above filtered the fields in place
     for f in fields:
         f.normal_(generator=gen)
@@ -419,6 +433,7 @@ def run_gpu(args):
                                 "and downloads of adjacent steps overlap (three device field sets, three streams)"},
             "gpu_launches": int(round(launches_per_step * args.steps)),
             "radial_launch": radial_launch,
+            "graph_priorities": graph_priorities,
             "autotune": {"radial_kernel_per_generation": tuned,
                          "key": "variant/output rows per block, [pass after restriction, pass before prolongation]"},
             "clocks": clk_sum,

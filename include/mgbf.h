@@ -331,6 +331,16 @@ int mgbf_batch_autotune(mgbf_batch* b, int dtype, void* stream);
  * counterpart: its generations are filtered one after another on each
  * rank. */
 int mgbf_batch_use_persistent(mgbf_batch* b, int blocks_per_sm);
+/* Scheduling priority of the kernels in a batch's CUDA graphs (with
+ * mgbf_batch_use_graphs): 0 (the default) leaves every kernel at the launch
+ * stream's priority; 1 gives the memory-bound kernels (vertical filter,
+ * restriction, prolongation) the device's highest priority and the radial
+ * kernels its lowest; 2 the reverse.  The variable groups run as concurrent
+ * graph branches, so the priority decides whose blocks the SMs take first
+ * when one group's radial pass and another's restriction or prolongation
+ * are both waiting.  Releases graphs captured before.  The reference has no
+ * counterpart. */
+int mgbf_batch_set_priorities(mgbf_batch* b, int mode);
 /* The radial-filter kernel a batch runs for variable group `group`,
  * generation `gen` (0-based) and pass (0: the pass after the restriction,
  * 1: the pass before the prolongation) in storage type dtype: *variant as

@@ -106,6 +106,7 @@ SIGNATURES = {
     "mgbf_batch_autotune": (_I, [_HP, _I, _VP]),
     "mgbf_batch_get_tuning": (_I, [_HP, _I, _I, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "mgbf_batch_use_persistent": (_I, [_HP, _I]),
+    "mgbf_batch_set_priorities": (_I, [_HP, _I]),
     "mgbf_set_wait_limit": (_I, [_HP, _I]),
     "mgbf_batch_set_wait_limit": (_I, [_HP, _I]),
     "mgbf_batch_set_weights": (_I, [_HP, ctypes.POINTER(_D), _I]),

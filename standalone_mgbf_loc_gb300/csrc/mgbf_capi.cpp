@@ -797,8 +797,8 @@ struct Exec {
     }
     // TMA map of the caller's field x for the fused restriction; null when
     // the kernel or TMA cannot take it.
-    const CUtensorMap* xmap(const View& x, int lm, int nzk) {
-        const ZrBox b = zrestrict_box(t, lm, nzk);
+    const CUtensorMap* xmap(const View& x, int lm, int nzk, int mz) {
+        const ZrBox b = zrestrict_box(t, lm, nzk, mz);
         if (!b.lv) return nullptr;
         return view_map(x, P.I, P.J, b.levels, b.cols);
     }
@@ -819,7 +819,7 @@ struct Exec {
         z.lm = z_on ? G.lm : 1; z.nzk = z_on ? nzcol * G.lm : 0; z.mz = z_on ? G.zs.mz : 0;
         z.status = static_cast<int*>(P.status.p);
         z.max_polls = P.wait_polls;
-        z.tmap = xmap(x, z.lm, z.nzk);
+        z.tmap = xmap(x, z.lm, z.nzk, z.mz);
         if (!z.tmap) return -1;
         StageTimer tm(ST_VFILTT_UPSEND, stream, pts(0));
         const int r = launch_zrestrict(t, z, stream);
@@ -929,6 +929,7 @@ struct mgbf_batch {
     int proc = 6;  // 6: radial (filtering_rad2_ens), 8: fast 1D+1D (filtering_fast_ens)
     // CUDA-graph replay of the launch sequence (mgbf_batch_use_graphs)
     bool use_graphs = false;
+    int priorities = 0;  // mgbf_batch_set_priorities: 0 off, 1 memory-bound kernels first, 2 radial first
     struct GraphEntry {
         int dtype, adjoint;
         std::vector<void*> fields;
@@ -2117,6 +2118,34 @@ static int batch_launch_branches(mgbf_batch* b, void* const* fields, DType t, cu
     return MGBF_OK;
 }
 
+// Tags every kernel node of a captured batch graph with a scheduling
+// priority by its kind: the radial kernels (k_hmom*, k_hdirect*) are bound
+// by the FP32 pipe, everything else by HBM.  mode 1 puts the HBM-bound
+// kernels first, mode 2 the radial ones.  Takes effect when the graph is
+// instantiated with cudaGraphInstantiateFlagUseNodePriority.
+static int set_node_priorities(cudaGraph_t graph, int mode) {
+    int least = 0, greatest = 0;
+    CU(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    size_t n = 0;
+    CU(cudaGraphGetNodes(graph, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) CU(cudaGraphGetNodes(graph, nodes.data(), &n));
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType ty;
+        CU(cudaGraphNodeGetType(nodes[i], &ty));
+        if (ty != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams kp{};
+        CU(cudaGraphKernelNodeGetParams(nodes[i], &kp));
+        const char* name = nullptr;
+        CU(cudaFuncGetName(&name, kp.func));
+        const bool radial = name && (std::strstr(name, "k_hmom") || std::strstr(name, "k_hdirect"));
+        cudaKernelNodeAttrValue v{};
+        v.priority = (radial == (mode == 2)) ? greatest : least;
+        CU(cudaGraphKernelNodeSetAttribute(nodes[i], cudaKernelNodeAttributePriority, &v));
+    }
+    return MGBF_OK;
+}
+
 int mgbf_batch_apply(mgbf_batch* b, void* const* fields, int dtype, int adjoint, void* stream) {
     // the transposed chain issues the same launches (see mgbf_filtering_procedure_adjoint)
     if (!b || !fields) return fail(MGBF_ERR_ARG, "null argument");
@@ -2167,7 +2196,15 @@ int mgbf_batch_apply(mgbf_batch* b, void* const* fields, int dtype, int adjoint,
     e.dtype = dtype;
     e.adjoint = adjoint != 0;
     e.fields.assign(fields, fields + ng);
-    ec = cudaGraphInstantiate(&e.exec, graph, 0);
+    unsigned long long iflags = 0;
+    if (b->priorities) {
+        if ((rc = set_node_priorities(graph, b->priorities))) {
+            cudaGraphDestroy(graph);
+            return rc;
+        }
+        iflags = cudaGraphInstantiateFlagUseNodePriority;
+    }
+    ec = cudaGraphInstantiate(&e.exec, graph, iflags);
     cudaGraphDestroy(graph);
     if (ec != cudaSuccess) return cuda_fail(ec, "cudaGraphInstantiate");
     b->graphs.push_back(e);
@@ -2205,6 +2242,16 @@ int mgbf_batch_use_persistent(mgbf_batch* b, int blocks_per_sm) {
     DeviceGuard dg(b->plan.device);
     b->plan.persistent = blocks_per_sm;
     for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);  // captured with the old launch sequence
+    b->graphs.clear();
+    return MGBF_OK;
+}
+
+int mgbf_batch_set_priorities(mgbf_batch* b, int mode) {
+    if (!b) return fail(MGBF_ERR_ARG, "null handle");
+    if (mode < 0 || mode > 2) return fail(MGBF_ERR_ARG, "priority mode must be 0, 1 or 2");
+    DeviceGuard dg(b->plan.device);
+    b->priorities = mode;
+    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);  // instantiated with the old priorities
     b->graphs.clear();
     return MGBF_OK;
 }

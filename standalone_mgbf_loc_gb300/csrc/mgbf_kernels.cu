@@ -366,31 +366,36 @@ __global__ void __launch_bounds__(kRsWarps * 32) k_restrict_p(RestrictArgs a, in
 // restricts pair it, then one block barrier frees pair it's slot for the
 // load of pair it+kZrPairs.  The z filter (Bz^T: the band matrix with the
 // whole-sample mirror and fold of sup_vrbeta1T, mg_filtering.f90:2094-2262)
-// runs per staged column: lane = 4 levels, a 12-level window from the padded
-// column (the band gives levels outside the lane's z column zero weight),
-// band rows in registers; the columns the block owns go to generation 1
+// runs per staged column: lane = 4 levels, a window of 12 levels (vertical
+// reach MZ = 4) or 20 (MZ = 8) from the padded column (the band gives levels
+// outside the lane's z column zero weight), band rows in registers; the columns the block owns go to generation 1
 // (zout, with the mirrored x halo).  The restriction is k_restrict_p's: the
 // x pass once per fine row, then the ring of the four coarse rows it feeds.
 // x is read from HBM once.
 constexpr int kZrPairs = 3;
-template <typename T>
-__host__ __device__ constexpr int zr_pad() { return sizeof(T) == 2 ? 8 : 4; }  // 16 bytes of levels
-template <typename T, int CX, int LV>
-__host__ __device__ constexpr size_t zr_row_bytes() {
-    return ((size_t)rs_cols<T, CX>() * (LV + 2 * zr_pad<T>()) * sizeof(T) + 127) / 128 * 128;
+// Levels staged below and above each column: the z window of a lane reaches
+// 4*ceil(MZ/4) levels past its own four, and a TMA row starts on 16 bytes.
+template <typename T, int MZ>
+__host__ __device__ constexpr int zr_pad() {
+    return 4 * ((MZ + 3) / 4) > 16 / (int)sizeof(T) ? 4 * ((MZ + 3) / 4) : 16 / (int)sizeof(T);
 }
-template <typename T, int CX, int LV>
-constexpr size_t zr_smem() { return 2 * kZrPairs * zr_row_bytes<T, CX, LV>(); }
+template <typename T, int CX, int LV, int MZ>
+__host__ __device__ constexpr size_t zr_row_bytes() {
+    return ((size_t)rs_cols<T, CX>() * (LV + 2 * zr_pad<T, MZ>()) * sizeof(T) + 127) / 128 * 128;
+}
+template <typename T, int CX, int LV, int MZ>
+constexpr size_t zr_smem() { return 2 * kZrPairs * zr_row_bytes<T, CX, LV, MZ>(); }
 
 template <typename T, int CX, int LV, int MZ>
 __global__ void __launch_bounds__(kRsWarps * 32, 3)
     k_zrestrict_tma(ZRestrictArgs z, const __grid_constant__ CUtensorMap xmap, int seg_rows) {
     static_assert(sizeof(T) <= 4, "FP32 accumulation: float or bfloat16 storage");
-    static_assert(MZ <= 4 && LV % 4 == 0 && LV + 2 * zr_pad<T>() <= 256, "12-level window, 4 levels per lane, TMA box");
-    constexpr int PAD = zr_pad<T>();
+    static_assert(MZ <= 8 && LV % 4 == 0 && LV + 2 * zr_pad<T, MZ>() <= 256, "z window, 4 levels per lane, TMA box");
+    constexpr int PAD = zr_pad<T, MZ>();
+    constexpr int NB = (MZ + 3) / 4;                  // window: NB vectors of 4 levels on each side
     constexpr int COL = LV + 2 * PAD;                 // staged levels per column
     constexpr int NF = rs_cols<T, CX>();              // staged fine columns: 2*4*CX owned + 6 shared
-    constexpr unsigned ROWB = (unsigned)zr_row_bytes<T, CX, LV>();
+    constexpr unsigned ROWB = (unsigned)zr_row_bytes<T, CX, LV, MZ>();
     constexpr unsigned BOXB = (unsigned)(NF * COL * sizeof(T));
     const RestrictArgs& a = z.r;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -468,17 +473,17 @@ __global__ void __launch_bounds__(kRsWarps * 32, 3)
             const int col = warp + kRsWarps * t;
             if (col < NF && lin) {  // col is warp-uniform
                 T* cp = srow + col * COL;
-                float x[3][4];  // levels 4*lane-4 .. 4*lane+7
-                V4<T>::ldc(cp - 4, x[0]);
-                V4<T>::ldc(cp, x[1]);
-                V4<T>::ldc(cp + 4, x[2]);
+                float x[2 * NB + 1][4];  // levels 4*lane-4*NB .. 4*lane+3+4*NB
+#pragma unroll
+                for (int v = 0; v <= 2 * NB; ++v) V4<T>::ldc(cp + 4 * (v - NB), x[v]);
                 __syncwarp(kLanes);  // every lane has its window before any lane overwrites
                 float y[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     float s2 = 0.f;
 #pragma unroll
-                    for (int dd = -MZ; dd <= MZ; ++dd) s2 = fmaf(wz[q][dd + MZ], x[(4 + q + dd) / 4][(4 + q + dd) % 4], s2);
+                    for (int dd = -MZ; dd <= MZ; ++dd)
+                        s2 = fmaf(wz[q][dd + MZ], x[(4 * NB + q + dd) / 4][(4 * NB + q + dd) % 4], s2);
                     y[q] = s2;
                 }
                 V4<T>::st(cp, y);
@@ -874,25 +879,31 @@ __global__ void __launch_bounds__(256) k_prolong_z(ProlongZArgs z) {
 // window) into a register ring of the NT rows a row pair reads, combines
 // them along y on top of the base values of its 2 x 2*PW fine points, stores
 // those columns into its own padded staging columns in shared memory and
-// applies the band rows of its lane's four levels (a 12-level window) before
-// writing y.  One block barrier per row pair frees the coarse row's stage.
+// applies the band rows of its lane's four levels (a window of 12 levels for
+// vertical reach MZ = 4, 20 for MZ = 8) before writing y.  One block barrier per row pair frees the coarse row's stage.
 constexpr int kPzStages = 6;
 constexpr int kPzPairsPerWarp = 2;
-constexpr int kPzPad = 4;  // staged levels below and above each column (zero)
+// staged levels below and above each fine column (zero): the reach of a
+// lane's z window, 4*ceil(MZ/4) levels past its own four
+template <int MZ>
+__host__ __device__ constexpr int pz_pad() { return 4 * ((MZ + 3) / 4); }
 template <typename T, int NT>
 __host__ __device__ constexpr int pz_cols() { return 4 * kPzPairsPerWarp + NT - 1; }  // staged coarse columns
 template <typename T, int NT, int LV>
 __host__ __device__ constexpr size_t pz_stage_bytes() { return ((size_t)pz_cols<T, NT>() * LV * sizeof(T) + 127) / 128 * 128; }
-template <typename T, int NT, int LV>
+template <typename T, int NT, int LV, int MZ>
 constexpr size_t pz_smem() {
     // coarse ring + per warp 2 rows x 2*PW fine columns of LV + 2*pad floats
-    return kPzStages * pz_stage_bytes<T, NT, LV>() + (size_t)4 * 4 * kPzPairsPerWarp * (LV + 2 * kPzPad) * sizeof(float);
+    return kPzStages * pz_stage_bytes<T, NT, LV>() +
+           (size_t)4 * 4 * kPzPairsPerWarp * (LV + 2 * pz_pad<MZ>()) * sizeof(float);
 }
 
 template <typename T, int NT, int LV, int MZ>
-__global__ void __launch_bounds__(128, 3) k_prolong_z_tma(ProlongZArgs z, const __grid_constant__ CUtensorMap cmap,
-                                                        int seg_steps) {
-    static_assert(sizeof(T) <= 4 && MZ <= 4 && LV % 4 == 0 && LV <= 128, "FP32 arithmetic, 12-level window, 4 levels per lane");
+__global__ void __launch_bounds__(128, MZ <= 4 ? 3 : 2)
+    k_prolong_z_tma(ProlongZArgs z, const __grid_constant__ CUtensorMap cmap, int seg_steps) {
+    static_assert(sizeof(T) <= 4 && MZ <= 8 && LV % 4 == 0 && LV <= 128, "FP32 arithmetic, z window, 4 levels per lane");
+    constexpr int PAD = pz_pad<MZ>();
+    constexpr int NB = PAD / 4;              // window: NB vectors of 4 levels on each side
     constexpr int O = NT == 4 ? 1 : 0;       // fine column of pair m is 2m - O
     constexpr int S = NT == 4 ? 2 : 1;       // first coarse tap of pair m is m - S
     constexpr int PW = kPzPairsPerWarp;
@@ -900,7 +911,7 @@ __global__ void __launch_bounds__(128, 3) k_prolong_z_tma(ProlongZArgs z, const 
     constexpr int CW = pz_cols<T, NT>();
     constexpr unsigned STB = (unsigned)pz_stage_bytes<T, NT, LV>();
     constexpr unsigned BOXB = (unsigned)(CW * LV * sizeof(T));
-    constexpr int ZC = LV + 2 * kPzPad;      // staged levels per fine column
+    constexpr int ZC = LV + 2 * PAD;         // staged levels per fine column
     constexpr unsigned kLanes = LV / 4 >= 32 ? 0xffffffffu : (1u << (LV / 4)) - 1u;
     const ProlongArgs& a = z.p;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -925,9 +936,9 @@ __global__ void __launch_bounds__(128, 3) k_prolong_z_tma(ProlongZArgs z, const 
     const bool lv = lin && kb + 4 * lane < a.nk;
     // this warp's staging columns, zero pads
     float* zst = reinterpret_cast<float*>(smem_raw + kPzStages * STB) + (size_t)warp * 2 * FC * ZC;
-    for (int i = lane; i < 2 * FC * 2 * kPzPad; i += 32) {
-        const int col = i / (2 * kPzPad), e = i % (2 * kPzPad);
-        zst[col * ZC + (e < kPzPad ? e : LV + e)] = 0.f;
+    for (int i = lane; i < 2 * FC * 2 * PAD; i += 32) {
+        const int col = i / (2 * PAD), e = i % (2 * PAD);
+        zst[col * ZC + (e < PAD ? e : LV + e)] = 0.f;
     }
     __syncthreads();
     auto issue = [&](int q) {  // thread 0: coarse row n0-S+q into stage q % kPzStages
@@ -1060,24 +1071,24 @@ __global__ void __launch_bounds__(128, 3) k_prolong_z_tma(ProlongZArgs z, const 
 #pragma unroll
         for (int h = 0; h < 2; ++h)
 #pragma unroll
-            for (int f = 0; f < FC; ++f) V4<float>::st(zst + (h * FC + f) * ZC + kPzPad + 4 * lane, acc[h][f]);
+            for (int f = 0; f < FC; ++f) V4<float>::st(zst + (h * FC + f) * ZC + PAD + 4 * lane, acc[h][f]);
         __syncwarp(kLanes);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int fj = 2 * n - O + h;
 #pragma unroll
             for (int f = 0; f < FC; ++f) {
-                const float* cp = zst + (h * FC + f) * ZC + kPzPad + 4 * lane;
-                float x[3][4];
-                V4<float>::ldc(cp - 4, x[0]);
-                V4<float>::ldc(cp, x[1]);
-                V4<float>::ldc(cp + 4, x[2]);
+                const float* cp = zst + (h * FC + f) * ZC + PAD + 4 * lane;
+                float x[2 * NB + 1][4];  // levels 4*lane-PAD .. 4*lane+3+PAD
+#pragma unroll
+                for (int v = 0; v <= 2 * NB; ++v) V4<float>::ldc(cp + 4 * (v - NB), x[v]);
                 float y[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     float s2 = 0.f;
 #pragma unroll
-                    for (int dd = -MZ; dd <= MZ; ++dd) s2 = fmaf(wz[q][dd + MZ], x[(4 + q + dd) / 4][(4 + q + dd) % 4], s2);
+                    for (int dd = -MZ; dd <= MZ; ++dd)
+                        s2 = fmaf(wz[q][dd + MZ], x[(4 * NB + q + dd) / 4][(4 * NB + q + dd) % 4], s2);
                     y[q] = s2;
                 }
                 const int fi = 2 * (m0 + PW * warp + f / 2) - O + (f & 1);
@@ -1568,18 +1579,20 @@ static int rs_rows(long long tiles, int Jc) {
     return std::max(rows, std::min(Jc, 8));
 }
 
-ZrBox zrestrict_box(DType t, int lm, int nzk) {
+ZrBox zrestrict_box(DType t, int lm, int nzk, int mz) {
     ZrBox b;
-    if (t == DType::F64 || lm < 1) return b;
+    if (t == DType::F64 || lm < 1 || mz > 8) return b;
     const int lv = (nzk == 0 || 128 % lm == 0) ? 128 : (96 % lm == 0 ? 96 : 0);
     if (!lv) return b;
     b.lv = lv;
-    b.levels = lv + 2 * (t == DType::BF16 ? zr_pad<__nv_bfloat16>() : zr_pad<float>());
+    const int pad = t == DType::BF16 ? (mz <= 4 ? zr_pad<__nv_bfloat16, 4>() : zr_pad<__nv_bfloat16, 8>())
+                                     : (mz <= 4 ? zr_pad<float, 4>() : zr_pad<float, 8>());
+    b.levels = lv + 2 * pad;
     b.cols = rs_cols<float, 2>();
     return b;
 }
 
-template <typename T, int LV>
+template <typename T, int LV, int MZ>
 static int zrlaunch(const ZRestrictArgs& z, cudaStream_t s) {
     constexpr int CX = 2;
     const RestrictArgs& a = z.r;
@@ -1587,27 +1600,37 @@ static int zrlaunch(const ZRestrictArgs& z, cudaStream_t s) {
     dim3 block(kRsWarps * 32), grid((a.nk + LV - 1) / LV, (Ic + kRsWarps * CX - 1) / (kRsWarps * CX), 1);
     const int rows = rs_rows((long long)grid.x * grid.y, Jc);
     grid.z = (Jc + rows - 1) / rows;
-    constexpr size_t sm = zr_smem<T, CX, LV>();
+    constexpr size_t sm = zr_smem<T, CX, LV, MZ>();
     static unsigned long long done = 0;  // per instantiation
-    cudaError_t e = smem_optin(k_zrestrict_tma<T, CX, LV, 4>, sm, done);
+    cudaError_t e = smem_optin(k_zrestrict_tma<T, CX, LV, MZ>, sm, done);
     if (e != cudaSuccess) return (int)e;
-    k_zrestrict_tma<T, CX, LV, 4><<<grid, block, sm, s>>>(z, *static_cast<const CUtensorMap*>(z.tmap), rows);
+    k_zrestrict_tma<T, CX, LV, MZ><<<grid, block, sm, s>>>(z, *static_cast<const CUtensorMap*>(z.tmap), rows);
     return last_err();
+}
+
+// compiled z reaches: 4, 5, 6 and 8 (7 runs as 8); the band's own reach
+// z.mz <= MZ, taps past it have zero weight
+template <typename T, int LV>
+static int zrdispatch(const ZRestrictArgs& z, cudaStream_t s) {
+    if (z.mz <= 4) return zrlaunch<T, LV, 4>(z, s);
+    if (z.mz == 5) return zrlaunch<T, LV, 5>(z, s);
+    if (z.mz == 6) return zrlaunch<T, LV, 6>(z, s);
+    return zrlaunch<T, LV, 8>(z, s);
 }
 
 int launch_zrestrict(DType t, const ZRestrictArgs& z, void* stream) {
     const RestrictArgs& a = z.r;
-    const ZrBox b = zrestrict_box(t, z.lm, z.nzk);
+    const ZrBox b = zrestrict_box(t, z.lm, z.nzk, z.mz);
     const long long es = (long long)elem_size(t);
     // the tensor map covers the fine field; V4 stores need 16-byte (FP32) or
     // 8-byte (BF16) aligned columns in zout and coarse
-    if (!b.lv || !z.tmap || !z.status || a.nk % 4 || z.mz > 4 || a.If < 2 || a.Jf < 2 || !aligned16(z.zout.p) ||
+    if (!b.lv || !z.tmap || !z.status || a.nk % 4 || z.mz > 8 || a.If < 2 || a.Jf < 2 || !aligned16(z.zout.p) ||
         !aligned16(a.coarse.p) || (z.zout.si * es) % 16 || (z.zout.sj * es) % 16 || (a.coarse.si * es) % 16 ||
         (a.coarse.sj * es) % 16)
         return -1;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (t == DType::F32) return b.lv == 128 ? zrlaunch<float, 128>(z, s) : zrlaunch<float, 96>(z, s);
-    return b.lv == 128 ? zrlaunch<__nv_bfloat16, 128>(z, s) : zrlaunch<__nv_bfloat16, 96>(z, s);
+    if (t == DType::F32) return b.lv == 128 ? zrdispatch<float, 128>(z, s) : zrdispatch<float, 96>(z, s);
+    return b.lv == 128 ? zrdispatch<__nv_bfloat16, 128>(z, s) : zrdispatch<__nv_bfloat16, 96>(z, s);
 }
 
 int launch_restrict(DType t, const RestrictArgs& a, void* stream) {
@@ -1702,31 +1725,34 @@ PzBox prolongz_box(DType t, int lm, int ntap) {
     return b;
 }
 
-template <typename T, int NT, int LV>
+// MZ: the compiled z reach (the band's own reach z.mz <= MZ; taps past it
+// have zero weight)
+template <typename T, int NT, int LV, int MZ>
 static int pzlaunch_tma(const ProlongZArgs& z, cudaStream_t s) {
     const ProlongArgs& a = z.p;
     constexpr int O = NT == 4 ? 1 : 0;
+    constexpr int kResident = MZ <= 4 ? 3 : 2;  // blocks per SM (launch bounds)
     const int npx = a.If / 2 + O, npy = a.Jf / 2 + O;
     dim3 block(128), grid((a.nk + LV - 1) / LV, (npx + 4 * kPzPairsPerWarp - 1) / (4 * kPzPairsPerWarp), 1);
-    // row runs: about 8 waves of blocks (3 resident per SM), at least 4*NT
-    // row pairs so that the NT-1 rows of ring fill stay cheap
+    // row runs: about 8 waves of blocks, at least 4*NT row pairs so that the
+    // NT-1 rows of ring fill stay cheap
     const long long tiles = (long long)grid.x * grid.y;
-    const long long nseg = (8LL * 3 * device_sm_count() + tiles - 1) / tiles;
+    const long long nseg = (8LL * kResident * device_sm_count() + tiles - 1) / tiles;
     int seg = (int)((npy + nseg - 1) / nseg);
     seg = std::max(seg, std::min(npy, 4 * NT));
     grid.z = (npy + seg - 1) / seg;
-    constexpr size_t sm = pz_smem<T, NT, LV>();
+    constexpr size_t sm = pz_smem<T, NT, LV, MZ>();
     static unsigned long long done = 0;  // per instantiation
-    cudaError_t e = smem_optin(k_prolong_z_tma<T, NT, LV, 4>, sm, done);
+    cudaError_t e = smem_optin(k_prolong_z_tma<T, NT, LV, MZ>, sm, done);
     if (e != cudaSuccess) return (int)e;
-    k_prolong_z_tma<T, NT, LV, 4><<<grid, block, sm, s>>>(z, *static_cast<const CUtensorMap*>(z.tmap), seg);
+    k_prolong_z_tma<T, NT, LV, MZ><<<grid, block, sm, s>>>(z, *static_cast<const CUtensorMap*>(z.tmap), seg);
     return last_err();
 }
 
-template <typename T>
+template <typename T, int MZ>
 static int pzdispatch_tma(const ProlongZArgs& z, int lv, cudaStream_t s) {
-    if (z.p.ntap == 4) return lv == 128 ? pzlaunch_tma<T, 4, 128>(z, s) : pzlaunch_tma<T, 4, 96>(z, s);
-    return lv == 128 ? pzlaunch_tma<T, 3, 128>(z, s) : pzlaunch_tma<T, 3, 96>(z, s);
+    if (z.p.ntap == 4) return lv == 128 ? pzlaunch_tma<T, 4, 128, MZ>(z, s) : pzlaunch_tma<T, 4, 96, MZ>(z, s);
+    return lv == 128 ? pzlaunch_tma<T, 3, 128, MZ>(z, s) : pzlaunch_tma<T, 3, 96, MZ>(z, s);
 }
 
 int launch_prolong_z(DType t, const ProlongZArgs& z, void* stream) {
@@ -1736,15 +1762,21 @@ int launch_prolong_z(DType t, const ProlongZArgs& z, void* stream) {
     const int npx = a.If / 2 + O, npy = a.Jf / 2 + O;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     // TMA-fed form: whole z columns in 128- or 96-level blocks, 16-byte
-    // aligned columns, vertical reach <= 4, coarse grids of at least NT
+    // aligned columns, vertical reach <= 8, coarse grids of at least NT
     // points per direction (edge mirroring stays inside the staged window)
     const PzBox b = prolongz_box(t, z.lm, a.ntap);
     const long long es = (long long)elem_size(t);
-    if (b.lv && z.tmap && z.status && z.mz <= 4 && a.nk % 4 == 0 && a.If / 2 >= a.ntap && a.Jf / 2 >= a.ntap &&
+    if (b.lv && z.tmap && z.status && a.nk % 4 == 0 && a.If / 2 >= a.ntap && a.Jf / 2 >= a.ntap &&
         aligned16(a.base.p) && aligned16(a.out.p) && (a.base.si * es) % 16 == 0 && (a.base.sj * es) % 16 == 0 &&
         (a.out.si * es) % 16 == 0 && (a.out.sj * es) % 16 == 0) {
-        if (t == DType::F32) return pzdispatch_tma<float>(z, b.lv, s);
-        return pzdispatch_tma<__nv_bfloat16>(z, b.lv, s);
+        // compiled z reaches: 4, 5, 6 and 8 (7 runs as 8)
+        const int mzc = z.mz <= 4 ? 4 : z.mz <= 6 ? z.mz : 8;
+        if (t == DType::F32)
+            return mzc == 4 ? pzdispatch_tma<float, 4>(z, b.lv, s) : mzc == 5 ? pzdispatch_tma<float, 5>(z, b.lv, s)
+                 : mzc == 6 ? pzdispatch_tma<float, 6>(z, b.lv, s) : pzdispatch_tma<float, 8>(z, b.lv, s);
+        return mzc == 4 ? pzdispatch_tma<__nv_bfloat16, 4>(z, b.lv, s)
+             : mzc == 5 ? pzdispatch_tma<__nv_bfloat16, 5>(z, b.lv, s)
+             : mzc == 6 ? pzdispatch_tma<__nv_bfloat16, 6>(z, b.lv, s) : pzdispatch_tma<__nv_bfloat16, 8>(z, b.lv, s);
     }
     // vector form: whole columns in tiles of a multiple of 4 levels (<= 512)
     if (a.nk % 4 == 0 && aligned16(a.coarse.p) && aligned16(a.base.p) && aligned16(a.out.p)) {

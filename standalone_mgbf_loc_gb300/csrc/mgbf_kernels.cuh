@@ -258,15 +258,16 @@ int launch_zfilter(DType t, const ZArgs& a, void* stream);
 int launch_restrict(DType t, const RestrictArgs& a, void* stream);
 // TMA box of the fused generation-1 restriction for a group: lv levels per
 // block (0: the fused kernel does not cover the group -- FP64, or z columns
-// of lm levels that divide neither 128 nor 96), and the box the tensor map of
-// the fine field must be encoded with: `levels` x `cols` x 1 row.
+// of lm levels that divide neither 128 nor 96, or a vertical reach mz above
+// 8), and the box the tensor map of the fine field must be encoded with:
+// `levels` x `cols` x 1 row (the levels padding grows with mz).
 struct ZrBox {
     int lv = 0, levels = 0, cols = 0;
 };
-ZrBox zrestrict_box(DType t, int lm, int nzk);
+ZrBox zrestrict_box(DType t, int lm, int nzk, int mz);
 // Returns -1 (nothing launched) when the shape does not fit: no box, no
 // tensor map or status word, levels not a multiple of 4, unaligned views or
-// vertical reach above 4; the caller then runs Bz^T and the restriction apart.
+// vertical reach above 8; the caller then runs Bz^T and the restriction apart.
 int launch_zrestrict(DType t, const ZRestrictArgs& a, void* stream);
 int launch_prolong(DType t, const ProlongArgs& a, void* stream);
 // Coarse-field TMA box of the fused last prolongation for a group: lv

@@ -383,6 +383,11 @@ class MGBFBatch:
         blocks per SM; 0 (or False) returns to one launch per generation."""
         _abi.check(self._lib.mgbf_batch_use_persistent(self._h, int(blocks_per_sm)), "mgbf_batch_use_persistent")
 
+    def set_priorities(self, mode: int) -> None:
+        """Graph-node scheduling priorities: 0 none (the default), 1 the
+        memory-bound kernels first, 2 the radial kernels first."""
+        _abi.check(self._lib.mgbf_batch_set_priorities(self._h, int(mode)), "mgbf_batch_set_priorities")
+
     def tuning(self, dtype=None):
         """The radial-kernel choice per group, generation and pass: a list
         (one entry per group) of lists (per generation) of two

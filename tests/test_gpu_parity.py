@@ -222,6 +222,40 @@ def test_batched_groups(lib, cuda):
         assert rel_l2(t.double().cpu().numpy(), O.filter_compact(oc, x)) < 1e-5
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+def test_batch_graph_node_priorities(lib, cuda, mode):
+    """Graph-node priorities change only the order in which the SMs take
+    blocks of the concurrent group branches: results equal the graph
+    without priorities bit for bit."""
+    I = J = 64
+    groups = [GroupDesc(nk=2 * 8, lm=8, nzcol=2, hx=4, hy=4, hz=2, p=2, mg_ampl01=canonical_z(2),
+                        mg_ampl02=canonical(4)),
+              GroupDesc(nk=6, lm=1, nzcol=0, hx=6, hy=6, hz=2, p=2, mg_ampl01=canonical_z(2),
+                        mg_ampl02=canonical(6))]
+    rng = np.random.default_rng(12)
+    xs = [torch.from_numpy(rng.standard_normal((J, I, g.nk))).to(cuda, torch.float32) for g in groups]
+    plain = MGBFBatch(I, J, 3, [1.0, 0.5, 0.25], groups)
+    prio = MGBFBatch(I, J, 3, [1.0, 0.5, 0.25], groups)
+    for b in (plain, prio):
+        b.use_graphs(True)
+    prio.set_priorities(mode)
+    a = [x.clone() for x in xs]
+    p = [x.clone() for x in xs]
+    for _ in range(3):  # first call direct, second captures, third replays
+        plain.apply(a)
+        plain.apply(a, adjoint=True)
+        prio.apply(p)
+        prio.apply(p, adjoint=True)
+    torch.cuda.synchronize()
+    prio.status()
+    for u, v in zip(a, p):
+        assert torch.equal(u, v)
+    with pytest.raises(_abi.MGBFError):
+        prio.set_priorities(3)
+    plain.close()
+    prio.close()
+
+
 def test_batch_graph_replay_matches_direct(lib, cuda):
     """Graph replay (captured launch sequence) gives bit-identical results."""
     I = J = 64
@@ -300,3 +334,29 @@ def test_fused_vertical_adjoint_and_restriction(lib, cuda, dtype, lm, km3, km2):
     x = compact_input(op, 300 + lm)
     y = run_gpu(op, 1, x, dtype, cuda)
     assert rel_l2(y, O.filter_compact(oracle_cfg(c, 1), x)) < TOL[dtype]
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("lm", [16, 48])
+@pytest.mark.parametrize("hz", [5, 6, 7, 8])
+def test_fused_z_kernels_vertical_reach_above_four(lib, cuda, dtype, lm, hz):
+    """Vertical reach 5..8: generation 1's fused Bz^T + restriction and the
+    fused last prolongation + Bz run their wide-window form (20-level
+    window, 8 padding levels; reaches 5, 6 and 8 compiled, 7 runs as 8;
+    128-level blocks for lm 16, 96 for lm 48).
+    Stage timers show the fused stages ran; forward against the oracle and
+    the adjoint by the dot-product test."""
+    c = small_config(lm=lm, km3=2, n_ens=1, hz=hz, mg_ampl01=canonical_z(hz))
+    op = MGBF(c)
+    rng = np.random.default_rng(400 + lm + hz)
+    x, yv = rng.standard_normal(op.field_shape()), rng.standard_normal(op.field_shape())
+    _abi.timers_enable(True)
+    lx = run_gpu(op, 1, x, dtype, cuda)
+    stages = _abi.timers_read()
+    _abi.timers_enable(False)
+    assert "vfiltT+upsend" in stages and "dnsend+vfilt" in stages and "vfiltT" not in stages
+    assert rel_l2(lx, O.filter_compact(oracle_cfg(c, 1), x)) < TOL[dtype]
+    if dtype == torch.float32:
+        lty = run_gpu(op, 1, yv, dtype, cuda, adjoint=True)
+        a, b = (lx * yv).sum(), (x * lty).sum()
+        assert abs(a - b) / (np.linalg.norm(lx) * np.linalg.norm(yv)) < 1e-6
