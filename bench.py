@@ -606,8 +606,9 @@ def cfg3_leg(torch, dev):
 CFG5 = dict(members=30, n=1536, lm=64, gm=6, h=24, hz=5, weights=[1.0, 0.5, 0.25, 0.125, 0.0625, 0.0625])
 
 
-def cfg5_leg(torch, dev, peak_gbs, steps):
-    """Large batched run: 30 members x one 3D variable on 1536x1536x64,
+def cfg5_leg(torch, dev, peak_gbs, steps, members=None):
+    """Large batched run: 30 members (or `members`, for small profiling
+    cases) x one 3D variable on 1536x1536x64,
     6 generations, h=24, hz=5, BF16 storage with FP32 arithmetic, FP64
     coefficient setup; seeded N(0,1) inputs (numpy seed 5 for member 0,
     torch.Generator for the others).  One step = forward + adjoint of the
@@ -616,7 +617,7 @@ def cfg5_leg(torch, dev, peak_gbs, steps):
     every weight and with one generation's weight at a time (the
     per-generation terms of the operator)."""
     from standalone_mgbf_loc_gb300 import MGBFBatch, GroupDesc, _abi
-    c = CFG5
+    c = dict(CFG5, members=members or CFG5["members"])
     n, lm, nk = c["n"], c["lm"], c["members"] * c["lm"]
     gd = [GroupDesc(nk=nk, lm=lm, nzcol=c["members"], hx=c["h"], hy=c["h"], hz=c["hz"], p=P,
                     mg_ampl01=ampl01(c["hz"]), mg_ampl02=ampl02(c["h"]))]
@@ -671,8 +672,8 @@ def cfg5_leg(torch, dev, peak_gbs, steps):
     b.close()
     del f, x0
     torch.cuda.empty_cache()
-    res = {"workload": "30 members x 1536x1536x64, 6 generations, h=24, hz=5, BF16 storage, FP32 arithmetic, "
-                       "forward + adjoint",
+    res = {"workload": f"{c['members']} members x 1536x1536x64, 6 generations, h=24, hz=5, BF16 storage, "
+                       "FP32 arithmetic, forward + adjoint",
            "dtype": "bf16", "ms": ms, "value": 2 * pts / (ms * 1e-3), "unit": UNIT, "steps": steps,
            "field_gb": pts * 2 / 1e9, "stages_ms_per_step": {k: v[1] for k, v in st.items()},
            "roofline": {"bound": "fp32_pipe", "kernel": "k_hmom_tma / k_hmom_tma1 (reach 24, BF16)",
@@ -949,12 +950,14 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the plain-forward and CPU-baseline legs")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default radial-kernel tiles")
     ap.add_argument("--cfg5-steps", type=int, default=5, help="timed steps of the large BF16 leg")
+    ap.add_argument("--cfg5-members", type=int, default=None,
+                    help="members of the large BF16 leg run alone with --leg cfg5 (default 30; fewer for profiles)")
     ap.add_argument("--leg", choices=sorted(LEGS), help="run one secondary leg alone (fp32) and print its JSON line")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.leg:
-        return run_leg(args.leg)
+        return run_leg(args.leg, args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
@@ -971,15 +974,18 @@ LEGS = {
     "plain": lambda torch, dev, peak: plain_forward(torch, dev, torch.float32),
     "cfg1": lambda torch, dev, peak: cfg1_leg(torch, dev)[0],
     "cfg3": lambda torch, dev, peak: cfg3_leg(torch, dev)[0],
-    "cfg5": lambda torch, dev, peak: cfg5_leg(torch, dev, peak, 5)[0],
+    "cfg5": lambda torch, dev, peak: cfg5_leg(torch, dev, peak, 5, LEG_ARGS.get("cfg5_members"))[0],
 }
+LEG_ARGS = {}
 
 
-def run_leg(name):
+def run_leg(name, args=None):
     import torch
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     peak, _ = measured_peaks()
+    if args is not None:
+        LEG_ARGS["cfg5_members"] = args.cfg5_members
     print(json.dumps({"leg": name, **LEGS[name](torch, dev, peak)}), flush=True)
     return 0
 

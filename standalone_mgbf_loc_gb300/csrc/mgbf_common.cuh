@@ -83,6 +83,10 @@ template <> struct V4<__nv_bfloat16> {
 __device__ __forceinline__ void cp_async16(unsigned saddr, const void* g, int bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(g), "r"(bytes) : "memory");
 }
+// 8-byte form (cp.async.ca); bytes < 8 zero-fills the rest
+__device__ __forceinline__ void cp_async8(unsigned saddr, const void* g, int bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(saddr), "l"(g), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }

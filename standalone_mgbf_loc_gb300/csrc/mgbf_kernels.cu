@@ -891,11 +891,16 @@ template <typename T, int NT>
 __host__ __device__ constexpr int pz_cols() { return 4 * kPzPairsPerWarp + NT - 1; }  // staged coarse columns
 template <typename T, int NT, int LV>
 __host__ __device__ constexpr size_t pz_stage_bytes() { return ((size_t)pz_cols<T, NT>() * LV * sizeof(T) + 127) / 128 * 128; }
+template <int LV, int MZ>
+__host__ __device__ constexpr size_t pz_zst_bytes() {  // z staging: per warp 2 rows x 2*PW columns of LV + 2*pad floats
+    return (size_t)4 * 4 * kPzPairsPerWarp * (LV + 2 * pz_pad<MZ>()) * sizeof(float);
+}
 template <typename T, int NT, int LV, int MZ>
 constexpr size_t pz_smem() {
-    // coarse ring + per warp 2 rows x 2*PW fine columns of LV + 2*pad floats
-    return kPzStages * pz_stage_bytes<T, NT, LV>() +
-           (size_t)4 * 4 * kPzPairsPerWarp * (LV + 2 * pz_pad<MZ>()) * sizeof(float);
+    // coarse ring + z staging + the base values of the next row pair (per
+    // warp 2 rows x 2*PW columns of LV levels, in storage type)
+    return kPzStages * pz_stage_bytes<T, NT, LV>() + pz_zst_bytes<LV, MZ>() +
+           (size_t)4 * 4 * kPzPairsPerWarp * LV * sizeof(T);
 }
 
 template <typename T, int NT, int LV, int MZ>
@@ -936,6 +941,10 @@ __global__ void __launch_bounds__(128, MZ <= 4 ? 3 : 2)
     const bool lv = lin && kb + 4 * lane < a.nk;
     // this warp's staging columns, zero pads
     float* zst = reinterpret_cast<float*>(smem_raw + kPzStages * STB) + (size_t)warp * 2 * FC * ZC;
+    // this warp's base values of the next row pair ([h][f][LV]), fetched by
+    // cp.async one row pair ahead; each lane reads back only what it copied
+    const unsigned bst = sbase + kPzStages * STB + (unsigned)pz_zst_bytes<LV, MZ>() +
+                         (unsigned)((warp * 2 * FC * LV + 4 * lane) * sizeof(T));
     for (int i = lane; i < 2 * FC * 2 * PAD; i += 32) {
         const int col = i / (2 * PAD), e = i % (2 * PAD);
         zst[col * ZC + (e < PAD ? e : LV + e)] = 0.f;
@@ -1027,23 +1036,30 @@ __global__ void __launch_bounds__(128, MZ <= 4 ? 3 : 2)
     }
     const T* base = static_cast<const T*>(a.base.p) + kb + 4 * lane;
     T* out = static_cast<T*>(a.out.p) + kb + 4 * lane;
-    for (int s = 0; s < nsteps && !failed; ++s) {
+    // base values of row pair s (fine rows 2n-O, 2n-O+1) into this lane's
+    // slots of bst; points outside the field (or levels past nk) are zero
+    auto prefetch = [&](int s) {
+        if (!lin) return;
         const int n = n0 + s;
-        // base values of the row pair (fine rows 2n-O, 2n-O+1)
-        float acc[2][FC][4];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int fj = 2 * n - O + h;
 #pragma unroll
             for (int f = 0; f < FC; ++f) {
                 const int fi = 2 * (m0 + PW * warp + f / 2) - O + (f & 1);
-                if (lv && fj >= 0 && fj < a.Jf && fi >= 0 && fi < a.If)
-                    V4<T>::ld(base + a.base.sj * (long long)fj + a.base.si * (long long)fi, acc[h][f]);
-                else
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[h][f][e] = 0.f;
+                const bool in = lv && fj >= 0 && fj < a.Jf && fi >= 0 && fi < a.If;
+                const T* src = in ? base + a.base.sj * (long long)fj + a.base.si * (long long)fi
+                                  : static_cast<const T*>(a.base.p);
+                const unsigned dst = bst + (unsigned)((h * FC + f) * LV * sizeof(T));
+                if constexpr (sizeof(T) == 4) cp_async16(dst, src, in ? 16 : 0);
+                else cp_async8(dst, src, in ? 8 : 0);
             }
         }
+        cp_async_commit();
+    };
+    if (nsteps > 0 && !failed) prefetch(0);
+    for (int s = 0; s < nsteps && !failed; ++s) {
+        const int n = n0 + s;
 #pragma unroll
         for (int t = 0; t < NT - 1; ++t)
 #pragma unroll
@@ -1055,6 +1071,15 @@ __global__ void __launch_bounds__(128, MZ <= 4 ? 3 : 2)
             break;
         }
         if (!lin) continue;
+        // base values of the row pair, fetched one row pair ahead
+        float acc[2][FC][4];
+        cp_async_wait<0>();
+        const T* bsp = reinterpret_cast<const T*>(smem_raw + kPzStages * STB + pz_zst_bytes<LV, MZ>()) +
+                       warp * 2 * FC * LV + 4 * lane;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int f = 0; f < FC; ++f) V4<T>::ldc(bsp + (h * FC + f) * LV, acc[h][f]);
         // y pass on top of the base values
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
@@ -1067,6 +1092,10 @@ __global__ void __launch_bounds__(128, MZ <= 4 ? 3 : 2)
                     acc[1][f][e] = fmaf(w1, xr[t][f][e], acc[1][f][e]);
                 }
         }
+        // the slots are read (the y pass used every value): fetch the next
+        // row pair's base values behind this one's z filter and the next
+        // coarse row's x pass
+        if (s + 1 < nsteps) prefetch(s + 1);
         // the warp's columns into its staging area, then Bz per column
 #pragma unroll
         for (int h = 0; h < 2; ++h)
@@ -1098,6 +1127,7 @@ __global__ void __launch_bounds__(128, MZ <= 4 ? 3 : 2)
         }
         __syncwarp(kLanes);  // the staging columns are rewritten by the next row pair
     }
+    cp_async_wait<0>();  // a prefetch left behind by a failed wait lands before the block exits
     if (failed) {
         // record, then drain this block's outstanding copies (bounded) before exit
         if (tid == 0) {
