@@ -18,6 +18,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -429,6 +430,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "steps": e2e_steps, "ms_per_step": ms_e2e / e2e_steps, "copy_gbs": copy_gbs,
+                    "numa_nodes": numa_nodes(),
                     "pipeline": "pinned host -> device, fwd+adj, device -> host per step; uploads, filtering "
                                 "and downloads of adjacent steps overlap (three device field sets, three streams)"},
             "gpu_launches": int(round(launches_per_step * args.steps)),
@@ -604,6 +606,14 @@ def cfg3_leg(torch, dev):
 
 
 CFG5 = dict(members=30, n=1536, lm=64, gm=6, h=24, hz=5, weights=[1.0, 0.5, 0.25, 0.125, 0.0625, 0.0625])
+
+
+def numa_nodes():
+    """NUMA nodes the host exposes (pinned buffers land on one of them)."""
+    try:
+        return sum(1 for d in os.listdir("/sys/devices/system/node") if re.fullmatch(r"node\d+", d))
+    except OSError:
+        return None
 
 
 def cfg5_leg(torch, dev, peak_gbs, steps, members=None):
