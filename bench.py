@@ -225,16 +225,16 @@ def run_gpu(args):
     # radial sides per generation or as one persistent launch per group: a
     # short timing of each (after a capturing call), the faster one is kept
     # for the timed region and the correctness sample
-    def trial_ms():
+    def trial_ms(n=2):
         step()  # captures the graph of this launch sequence
         torch.cuda.synchronize()
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a0.record()
-        for _ in range(2):
+        for _ in range(n):
             step()
         a1.record()
         torch.cuda.synchronize()
-        return a0.elapsed_time(a1) / 2
+        return a0.elapsed_time(a1) / n
 
     trials = {}
     for blocks_per_sm in (0, 1, 2, 8):  # 0: per generation; else persistent with up to that many blocks per SM
@@ -246,16 +246,24 @@ def run_gpu(args):
                                      for k, v in trials.items()},
                      "chosen": "per generation" if best == 0 else f"persistent, <= {best} blocks/SM"}
     # graph-node priorities of the concurrent group branches (0 none, 1
-    # memory-bound kernels first, 2 radial kernels first)
+    # memory-bound kernels first, 2 radial kernels first) and the vertical
+    # filter passes (2 as the reference: Bz^T first, Bz last; 1: M = Bz Bz^T
+    # once, in the last prolongation -- the same operator).  They interact
+    # (how the groups' stages overlap depends on both), so every pair is
+    # timed and the fastest kept.
     prio_names = {0: "none", 1: "memory-bound kernels first", 2: "radial kernels first"}
-    prio_trials = {0: trials[best]}
-    for mode in (1, 2):
-        batch.set_priorities(mode)
-        prio_trials[mode] = trial_ms()
-    best_prio = min(prio_trials, key=prio_trials.get)
-    batch.set_priorities(best_prio)
-    graph_priorities = {"ms_per_step": {prio_names[k]: v for k, v in prio_trials.items()},
-                        "chosen": prio_names[best_prio]}
+    grid = {}
+    for passes in (2, 1):
+        batch.set_vertical_passes(passes)
+        for mode in (0, 1, 2):
+            batch.set_priorities(mode)
+            grid[(mode, passes)] = trial_ms(3)
+    best_mode, best_vp = min(grid, key=grid.get)
+    batch.set_priorities(best_mode)
+    batch.set_vertical_passes(best_vp)
+    graph_priorities = {"ms_per_step": {prio_names[m]: grid[(m, best_vp)] for m in (0, 1, 2)},
+                        "chosen": prio_names[best_mode]}
+    vertical_passes = {"ms_per_step": {str(v): grid[(best_mode, v)] for v in (2, 1)}, "chosen": best_vp}
     # fresh N(0,1) inputs: the trial steps above filtered the fields in place
     for f in fields:
         f.normal_(generator=gen)
@@ -436,6 +444,7 @@ def run_gpu(args):
             "gpu_launches": int(round(launches_per_step * args.steps)),
             "radial_launch": radial_launch,
             "graph_priorities": graph_priorities,
+            "vertical_passes": vertical_passes,
             "autotune": {"radial_kernel_per_generation": tuned,
                          "key": "variant/output rows per block, [pass after restriction, pass before prolongation]"},
             "clocks": clk_sum,

@@ -223,6 +223,20 @@ int mgbf_status(mgbf_handle* h);
  * a healthy GPU. */
 int mgbf_set_wait_limit(mgbf_handle* h, int polls);
 
+/* Vertical filter passes of the radial procedures (1, 6): 2 (the default)
+ * runs them as the reference does, Bz^T first (sup_vrbeta1T_bck / _ens,
+ * mg_filtering.f90:583, 1026) and Bz last (sup_vrbeta1_bck / _ens, :674,
+ * 1140); 1 applies M = Bz Bz^T once, in the last prolongation.  Both give the same operator: the vertical filter acts on
+ * every column alike and the rest of the chain on every level alike, so
+ * Bz H Bz^T = H Bz Bz^T; results differ by rounding.  With 1 the
+ * restriction writes no generation-1 copy of the field and generation 1's
+ * first radial pass reads the caller's field itself, one write of the field
+ * less per call.  Used where it applies (FP32/BF16, the radial moment
+ * kernel at reach <= 16, vertical reach <= 4, generation 1 filtered, no
+ * persistent sides); elsewhere the two passes run.  No reference
+ * counterpart. */
+int mgbf_set_vertical_passes(mgbf_handle* h, int passes);
+
 /* Autotuner of tile shapes: times the radial-filter kernel variants (TMA
  * pipelines of one or two rows per barrier, cp.async staging) and output
  * rows per block for every generation and pass of the handle, on the
@@ -319,6 +333,8 @@ int mgbf_batch_status(mgbf_batch* b);
 int mgbf_batch_set_weights(mgbf_batch* b, const double* a, int n);
 /* As mgbf_set_wait_limit, for a batch (releases graphs captured before). */
 int mgbf_batch_set_wait_limit(mgbf_batch* b, int polls);
+/* As mgbf_set_vertical_passes, for a batch (releases graphs captured before). */
+int mgbf_batch_set_vertical_passes(mgbf_batch* b, int passes);
 /* As mgbf_autotune, for a batch (releases graphs captured before). */
 int mgbf_batch_autotune(mgbf_batch* b, int dtype, void* stream);
 /* With blocks_per_sm > 0, runs each radial side (the pass after the

@@ -256,7 +256,7 @@ struct StageTimer {
 // Tables converted to one accumulation type (float or double).
 struct AccTables {
     bool ready = false;
-    DevBuf zfwd, zadj, hw;
+    DevBuf zfwd, zadj, zmm, hw;
     std::vector<std::unique_ptr<DevBuf>> rwx, rwy, pwx, pwy;  // per generation
 };
 
@@ -318,6 +318,7 @@ struct Plan {
     int device = 0;
     int wait_polls = kDefaultWaitPolls;  // mbarrier polls per row before a TMA-fed kernel gives up
     int persistent = 0;  // radial sides as one persistent launch per group: resident blocks per SM (0: off; mgbf_batch_use_persistent)
+    int vpasses = 2;     // vertical filter passes of procs 1/6: 2 as the reference, 1 = M = Bz Bz^T once (mgbf_set_vertical_passes)
 };
 
 int gen_I(const Plan& P, int g) { return P.I >> g; }
@@ -342,6 +343,7 @@ int ensure_tables(Plan& P, Group& G, DType t) {
     if (!G.zs.fwd.empty()) {
         if ((rc = upload_acc(T.zfwd, G.zs.fwd, t))) return rc;
         if ((rc = upload_acc(T.zadj, G.zs.adj, t))) return rc;
+        if (!G.zs.mm.empty() && (rc = upload_acc(T.zmm, G.zs.mm, t))) return rc;
     }
     if ((rc = upload_acc(T.hw, G.hs.w, t))) return rc;
     if (!G.mrow.p && (rc = upload(G.mrow, G.hs.mrow))) return rc;
@@ -524,9 +526,10 @@ struct Exec {
         return slot.second.get();
     }
 
-    // y = Bz (base + P coarse) for the generation 2 -> 1 step; -1 if the
-    // fused kernel does not cover this shape.
-    int prolong_z(View coarse, View base, View y, int nzcol) {
+    // y = Bz (base + P coarse) for the generation 2 -> 1 step (with mm: the
+    // band M = Bz Bz^T instead of Bz); -1 if the fused kernel does not cover
+    // this shape.
+    int prolong_z(View coarse, View base, View y, int nzcol, bool mm = false) {
         ProlongZArgs z;
         ProlongArgs& a = z.p;
         a.coarse = coarse; a.base = base; a.out = y; a.nk = G.nk;
@@ -534,7 +537,8 @@ struct Exec {
         a.ix = static_cast<const int*>(P.pix[0].p); a.iy = static_cast<const int*>(P.piy[0].p);
         a.wxp = G.tab[ai()].pwx[0]->p; a.wyp = G.tab[ai()].pwy[0]->p;
         a.has_base = 1;
-        z.band = G.tab[ai()].zfwd.p; z.lm = G.lm; z.nzk = nzcol * G.lm; z.mz = G.zs.mz;
+        z.band = mm ? G.tab[ai()].zmm.p : G.tab[ai()].zfwd.p;
+        z.lm = G.lm; z.nzk = nzcol * G.lm; z.mz = mm ? G.zs.mmz : G.zs.mz;
         if (z.lm < 2 || z.lm > 256 || z.mz > 8) return -1;  // the fused kernel's limits
         const PzBox pb = prolongz_box(t, z.lm, a.ntap);
         if (pb.lv) {
@@ -882,8 +886,88 @@ struct Exec {
         return zstage(A(0), y, zadj_out, nzcol, 0);
     }
 
+    // The vertical filters commute with everything else (the restrictions,
+    // radial filters, weights and prolongations act on every level alike;
+    // Bz on every column alike), so Bz H Bz^T x = M H x with M = Bz Bz^T,
+    // applied once, in the last prolongation.  Generation 1's first radial
+    // pass then reads the caller's field itself (edge tiles mirrored in
+    // shared memory) and the restriction writes no generation-1 copy: one
+    // write of the field less per call.  -1 (nothing launched) when a
+    // condition fails; forward() then runs the chain as written.
+    int forward_direct(View x, View y, int nzcol) {
+        const bool z = nzcol > 0 && !G.zs.fwd.empty();
+        if (t == DType::F64 || fast || lin2 || lin3 || n3 >= 0 || zadj_out || !moment_path() || P.persistent ||
+            P.gm < 2 || G.nk % 2 || G.hs.R > 16 || P.I < G.hs.R || !P.status.p ||
+            (z && (G.zs.mm.empty() || G.zs.mmz > 8)))
+            return -1;
+        const CUtensorMap* hm = view_map(x, P.I, P.J, 64, hmom_tma_cols(G.hs.R));
+        const CUtensorMap* rm = xmap(x, 1, 0, 0);
+        if (!hm || !rm || ((uintptr_t)B(0).p & 7u)) return -1;
+        // 1. R x into generation 2 (restriction only)
+        ZRestrictArgs zr;
+        RestrictArgs& a = zr.r;
+        a.fine = x; a.coarse = A(1); a.nk = G.nk; a.If = P.I; a.Jf = P.J;
+        a.wx = G.tab[ai()].rwx[0]->p; a.wy = G.tab[ai()].rwy[0]->p;
+        a.mirror_hx = G.hs.R;
+        zr.zout = A(0); zr.mirror_z = 0; zr.write_zout = 0;
+        zr.band = nullptr; zr.lm = 1; zr.nzk = 0; zr.mz = 0;
+        zr.status = static_cast<int*>(P.status.p);
+        zr.max_polls = P.wait_polls;
+        zr.tmap = rm;
+        {
+            StageTimer tm(ST_UPSEND, stream, pts(0));
+            const int r = launch_zrestrict(t, zr, stream);
+            if (r == -1) {
+                tm.cancel();
+                return -1;
+            }
+            LK(r);
+        }
+        int rc;
+        for (int g = 1; g + 1 < P.gm; ++g)
+            if ((rc = restrict_(g, A(g), A(g + 1)))) return rc;
+        // 2. first radial side: generation 1 straight from x
+        {
+            HMomArgs h;
+            h.in = x; h.out = B(0); h.nk = G.nk; h.I = P.I; h.J = P.J;
+            h.mirror_hx = G.hs.R; h.scale = P.a[0] * G.hs.s; h.halo = 0;
+            h.tmap = hm;
+            h.status = static_cast<int*>(P.status.p);
+            h.max_polls = P.wait_polls;
+            h.variant = 1;
+            auto it = G.tune.find((int)t * 1024 + 0);
+            h.rows = it != G.tune.end() ? it->second.second : default_rows(0);
+            h.mirror_in = 1;
+            StageTimer tm(ST_HFILTT, stream, pts(0));
+            LK(launch_hmom(t, G.hs.R, G.hs.p, h, G.hs.mom, stream));
+        }
+        for (int g = 1; g < P.gm; ++g)
+            if ((rc = hpass(g, A(g), B(g), P.a[g], G.hs.R, ST_HFILTT, 0))) return rc;
+        // 3. second radial side, prolongations, M
+        for (int g = 0; g < P.gm; ++g)
+            if ((rc = hpass(g, B(g), A(g), 1.0, 0, ST_HFILT, 1))) return rc;
+        for (int g = P.gm - 1; g >= 2; --g)
+            if ((rc = prolong(g - 1, A(g), A(g - 1), A(g - 1)))) return rc;
+        if (!z) return prolong(0, A(1), A(0), y);
+        const int r = prolong_z(A(1), A(0), y, nzcol, true);
+        if (r != -1) return r;
+        if ((rc = prolong(0, A(1), A(0), A(0)))) return rc;
+        StageTimer tm(ST_VFILT, stream, pts(0));
+        ZArgs za;
+        za.in = A(0); za.out = y; za.nk = G.nk; za.I = P.I; za.J = P.J;
+        za.lm = G.lm; za.nzk = nzcol * G.lm; za.mz = G.zs.mmz;
+        za.band = G.tab[ai()].zmm.p;
+        za.mirror_hx = 0;
+        LK(launch_zfilter(t, za, stream));
+        return 0;
+    }
+
     int forward(View x, View y, int nzcol, bool filt1) {
         int rc;
+        if (filt1 && P.vpasses == 1) {
+            const int r = forward_direct(x, y, nzcol);
+            if (r != -1) return r;
+        }
         auto Bf = [&](int g) { return B(g); };
         if ((rc = half_chain(x, nzcol, filt1, Bf, true, P.a))) return rc;
         return second_half(y, nzcol, filt1, nullptr);
@@ -1893,9 +1977,11 @@ static int autotune_plan(Plan& P, DType t, void* stream) {
         if ((rc = ensure_tables(P, G, t)) || (rc = ensure_bufs(P, G, t, false))) return rc;
         Exec ex{P, G, t, stream};
         if (!ex.moment_path()) continue;
+        // the buffers hold a normal nonzero value in every element (the byte
+        // pattern 0x3f): kernels timed on zeros draw less power than on data
         for (int g = 0; g < P.gm; ++g) {
-            CU(cudaMemsetAsync(G.bufs[(int)t].A[g]->p, 0, G.bufs[(int)t].A[g]->bytes, s));
-            CU(cudaMemsetAsync(G.bufs[(int)t].B[g]->p, 0, G.bufs[(int)t].B[g]->bytes, s));
+            CU(cudaMemsetAsync(G.bufs[(int)t].A[g]->p, 0x3f, G.bufs[(int)t].A[g]->bytes, s));
+            CU(cudaMemsetAsync(G.bufs[(int)t].B[g]->p, 0x3f, G.bufs[(int)t].B[g]->bytes, s));
         }
         for (int g = 0; g < P.gm; ++g)
             for (int pass = 0; pass < 2; ++pass) {
@@ -1907,25 +1993,39 @@ static int autotune_plan(Plan& P, DType t, void* stream) {
                 rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
                 const int nvar = t == DType::F64 ? 1 : kHMomVariants;
                 View in = pass ? ex.B(g) : ex.A(g), out = pass ? ex.A(g) : ex.B(g);
+                // two sweeps over the candidates, each candidate's best of
+                // the two: a single sample is skewed by the clock state of
+                // the moment, and neighbouring variants are close
+                std::vector<float> best_ms(nvar * rows.size(), 1e30f);
+                for (int sweep = 0; sweep < 2; ++sweep)
+                    for (int v = 0; v < nvar; ++v)
+                        for (size_t ri = 0; ri < rows.size(); ++ri) {
+                            const int r = rows[ri];
+                            if ((rc = ex.hmom(g, in, out, 1.0, pass ? 0 : G.hs.R, pass, v, r))) return rc;  // warm
+                            CU(cudaEventRecord(e0, s));
+                            for (int rep = 0; rep < 5; ++rep)
+                                if ((rc = ex.hmom(g, in, out, 1.0, pass ? 0 : G.hs.R, pass, v, r))) return rc;
+                            CU(cudaEventRecord(e1, s));
+                            CU(cudaEventSynchronize(e1));
+                            float ms = 0.f;
+                            CU(cudaEventElapsedTime(&ms, e0, e1));
+                            float& b = best_ms[v * rows.size() + ri];
+                            b = std::min(b, ms);
+                        }
                 float best = 1e30f;
                 std::pair<int, int> choice(0, r0);
                 for (int v = 0; v < nvar; ++v)
-                    for (int r : rows) {
-                        if ((rc = ex.hmom(g, in, out, 1.0, pass ? 0 : G.hs.R, pass, v, r))) return rc;  // warm
-                        CU(cudaEventRecord(e0, s));
-                        for (int rep = 0; rep < 3; ++rep)
-                            if ((rc = ex.hmom(g, in, out, 1.0, pass ? 0 : G.hs.R, pass, v, r))) return rc;
-                        CU(cudaEventRecord(e1, s));
-                        CU(cudaEventSynchronize(e1));
-                        float ms = 0.f;
-                        CU(cudaEventElapsedTime(&ms, e0, e1));
-                        if (ms < best) {
-                            best = ms;
-                            choice = {v, r};
+                    for (size_t ri = 0; ri < rows.size(); ++ri)
+                        if (best_ms[v * rows.size() + ri] < best) {
+                            best = best_ms[v * rows.size() + ri];
+                            choice = {v, rows[ri]};
                         }
-                    }
                 G.tune[(int)t * 1024 + g * 2 + pass] = choice;
             }
+        for (int g = 0; g < P.gm; ++g) {  // leave the buffers as a first call finds them
+            CU(cudaMemsetAsync(G.bufs[(int)t].A[g]->p, 0, G.bufs[(int)t].A[g]->bytes, s));
+            CU(cudaMemsetAsync(G.bufs[(int)t].B[g]->p, 0, G.bufs[(int)t].B[g]->bytes, s));
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1958,6 +2058,23 @@ int mgbf_batch_status(mgbf_batch* b) {
 int mgbf_set_wait_limit(mgbf_handle* h, int polls) {
     if (!h) return fail(MGBF_ERR_ARG, "null handle");
     h->plan.wait_polls = polls < 0 ? kDefaultWaitPolls : polls;
+    return MGBF_OK;
+}
+
+int mgbf_set_vertical_passes(mgbf_handle* h, int passes) {
+    if (!h) return fail(MGBF_ERR_ARG, "null handle");
+    if (passes != 1 && passes != 2) return fail(MGBF_ERR_ARG, "vertical passes must be 1 or 2");
+    h->plan.vpasses = passes;
+    return MGBF_OK;
+}
+
+int mgbf_batch_set_vertical_passes(mgbf_batch* b, int passes) {
+    if (!b) return fail(MGBF_ERR_ARG, "null handle");
+    if (passes != 1 && passes != 2) return fail(MGBF_ERR_ARG, "vertical passes must be 1 or 2");
+    DeviceGuard dg(b->plan.device);
+    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);  // captured with the other chain
+    b->graphs.clear();
+    b->plan.vpasses = passes;
     return MGBF_OK;
 }
 

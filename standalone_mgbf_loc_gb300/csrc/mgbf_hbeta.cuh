@@ -662,7 +662,7 @@ __host__ __device__ constexpr int hmom_tma1_rows(int out_rows) {
     return ((out_rows + 2 * R + kStages - 1) / kStages) * kStages;
 }
 
-template <int R, int P, int TX, typename T>
+template <int R, int P, int TX, typename T, bool MIRROR = false>
 __device__ __forceinline__ bool hmom_tma1_tile(const HMomArgs& a, const CUtensorMap* tmap, const HMomCoefs2& c,
                                                int k0, int ib, int jb, unsigned sbase, unsigned bbase, int rbase) {
     constexpr int U = kStages;
@@ -735,6 +735,32 @@ __device__ __forceinline__ bool hmom_tma1_tile(const HMomArgs& a, const CUtensor
     for (int s2 = 0; s2 < kStages - 1; ++s2) issue(s2);
     bool failed = false;
     int waited = 0;  // rows whose barrier has been waited
+    // MIRROR (input without x halo, a.mirror_in): tile column c holds input
+    // column g0 + c; the copy engine zero-fills columns outside 0..I-1, and
+    // the edge tiles replace those that feed stored outputs (-R..-1 and
+    // I..I+R-1) by their half-sample mirrors, which lie inside the same tile
+    // (I >= R)
+    const bool edge = MIRROR && (ib < R || ib + kStageWarps * TX + R > a.I);  // block-uniform
+    auto mirror_edges = [&](int st) {
+        constexpr int CH = 64 * (int)sizeof(T) / 16;  // 16-byte chunks per tile column
+        constexpr int EPC = 16 / (int)sizeof(T);
+        const int g0 = ib - R;
+        const int nfl = max(0, min(NC, -g0));                      // tile columns left of column 0
+        const int cr0 = a.I - g0;                                  // tile column of input column I
+        const int nfr = max(0, min(NC, a.I + R - g0) - cr0);       // needed columns right of I - 1
+        T* tw = reinterpret_cast<T*>(smem_raw) + st * TILE;
+#pragma unroll 1
+        for (int q = tid; q < (nfl + nfr) * CH; q += kStageWarps * 32) {
+            const int cc = q / CH, ch = q - cc * CH;
+            const int c = cc < nfl ? cc : cr0 + (cc - nfl);
+            const int gc = g0 + c;
+            const int cs = (gc < 0 ? -1 - gc : 2 * a.I - 1 - gc) - g0;  // in-range source column
+            *reinterpret_cast<int4*>(tw + c * 64 + ch * EPC) = *reinterpret_cast<const int4*>(tw + cs * 64 + ch * EPC);
+        }
+        // these generic writes precede the copy engine's next write of the stage
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+    };
     for (int r0 = 0; r0 < nrp && !failed; r0 += U) {
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -745,6 +771,8 @@ __device__ __forceinline__ bool hmom_tma1_tile(const HMomArgs& a, const CUtensor
                 break;
             }
             waited = r + 1;
+            if constexpr (MIRROR)
+                if (edge) mirror_edges(u);
             issue(r + kStages - 1);
             row(u, u);
         }
@@ -791,9 +819,10 @@ __device__ __forceinline__ bool hmom_tma1_tile(const HMomArgs& a, const CUtensor
 
 // Single-row variant of the TMA kernel: one tile per block; fewer registers
 // than the two-row kernel, more blocks per SM; the autotuner picks between
-// them.
-template <int R, int P, int TX, typename T>
-__global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
+// them.  MIRROR: the input has no x halo (HMomArgs::mirror_in).
+template <int R, int P, int TX, typename T, bool MIRROR = false>
+__global__ void __launch_bounds__(128, (MIRROR && R <= 8) ? 4 : 1)
+    k_hmom_tma1(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
                                                   const __grid_constant__ HMomCoefs2 c) {
     __shared__ __align__(8) unsigned long long bars[kStages];
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -805,8 +834,8 @@ __global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_cons
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
-    hmom_tma1_tile<R, P, TX, T>(a, &tmap, c, blockIdx.x * 64, blockIdx.y * (kStageWarps * TX), blockIdx.z * a.rows, sbase,
-                                bbase, 0);
+    hmom_tma1_tile<R, P, TX, T, MIRROR>(a, &tmap, c, blockIdx.x * 64, blockIdx.y * (kStageWarps * TX), blockIdx.z * a.rows,
+                                        sbase, bbase, 0);
 }
 
 // Persistent form of one radial side: every generation's tiles of one
@@ -877,6 +906,33 @@ static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t
     // columns must start on 16-byte boundaries and 16-byte chunks must not
     // straddle the end of a column: nk * sizeof(T) % 16 == 0
     const bool staged = (a.nk * (int)sizeof(T)) % 16 == 0 && (((uintptr_t)a.in.p) & 15u) == 0 && a.halo >= R;
+    if (a.mirror_in) {
+        // input without x halo: only the single-row TMA kernel mirrors edge
+        // tiles itself (the caller checks these conditions first); reaches
+        // up to 16
+        if constexpr (sizeof(A) == 4 && R <= 16) {
+            if (!a.tmap || !a.status || a.nk % 2 || ((uintptr_t)a.out.p & 7u) || a.I < R || a.halo != 0)
+                return (int)cudaErrorInvalidValue;
+            constexpr int TX2 = hmom_p2_tx(R);
+            HMomCoefs2 c2;
+            for (int g = 0; g <= kMaxReach; ++g) c2.coef[g] = make_float2((float)cd.coef[g * (P + 1)], (float)cd.coef[g * (P + 1)]);
+            for (int t = 0; t < (kMaxReach + 1) * (kMaxMomP + 1); ++t)
+                c2.upow[t] = make_float2((float)cd.upow[t], (float)cd.upow[t]);
+            const int nstrip2 = (a.I + TX2 - 1) / TX2;
+            dim3 grid2((a.nk + 63) / 64, (nstrip2 + NW - 1) / NW, (a.J + rows - 1) / rows);
+            constexpr size_t smt = (size_t)kStages * (kStageWarps * TX2 + 2 * R) * 64 * sizeof(T);
+            if (smt + 1024 > 48 * 1024) {
+                static unsigned long long done = 0;  // per instantiation
+                cudaError_t ea = smem_optin(k_hmom_tma1<R, P, TX2, T, true>, smt, done);
+                if (ea != cudaSuccess) return (int)ea;
+            }
+            k_hmom_tma1<R, P, TX2, T, true><<<grid2, block, smt, s>>>(b, *static_cast<const CUtensorMap*>(a.tmap), c2);
+            cudaError_t e = cudaGetLastError();
+            return e == cudaSuccess ? 0 : (int)e;
+        } else {
+            return (int)cudaErrorInvalidValue;
+        }
+    }
     if constexpr (sizeof(A) == 4) {
         // packed pairs: nk even and 16-byte aligned columns
         if (staged && a.nk % 2 == 0 && ((uintptr_t)a.out.p & 7u) == 0) {

@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(kRsWarps * 32, 3)
                 }
                 V4<T>::st(cp, y);
                 const int gc = 2 * cs - 3 + col;
-                if (own_row && col >= 3 && col < 3 + 2 * kRsWarps * CX && gc < a.If) {
+                if (z.write_zout && own_row && col >= 3 && col < 3 + 2 * kRsWarps * CX && gc < a.If) {
                     V4<T>::st(zrow + z.zout.si * gc, y);
                     if (gc < z.mirror_z) V4<T>::st(zrow + z.zout.si * (-1 - gc), y);
                     if (gc >= a.If - z.mirror_z) V4<T>::st(zrow + z.zout.si * (2 * a.If - 1 - gc), y);
@@ -538,10 +538,13 @@ __global__ void __launch_bounds__(kRsWarps * 32, 3)
     };
 
     // pipeline fill: pair 0 filtered before the first restriction
+    // (restriction only -- no z columns, generation 1 not written -- skips
+    // the z pass, which would copy the staged rows onto themselves)
+    const bool zpass = z.nzk > 0 || z.write_zout;
     int waited = 0;                          // pairs whose barrier every thread has passed
     int issued = min(niter, kZrPairs);       // pairs whose loads thread 0 has issued
     bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(bbase, 0u, z.max_polls));
-    if (ok) {
+    if (ok && zpass) {
         zfilter_row(0, 2 * d0 - 3);
         zfilter_row(1, 2 * d0 - 2);
     }
@@ -552,7 +555,7 @@ __global__ void __launch_bounds__(kRsWarps * 32, 3)
         if (it + 1 < niter) {
             const int sl1 = (it + 1) % kZrPairs;
             ok = __all_sync(0xffffffffu, mbar_wait_bounded(bbase + 8 * sl1, (unsigned)(((it + 1) / kZrPairs) & 1), z.max_polls));
-            if (ok) {
+            if (ok && zpass) {
                 zfilter_row(2 * sl1, 2 * d0 - 1 + 2 * it);
                 zfilter_row(2 * sl1 + 1, 2 * d0 + 2 * it);
             }

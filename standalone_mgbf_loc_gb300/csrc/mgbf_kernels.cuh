@@ -174,6 +174,7 @@ struct ZRestrictArgs {
     const void* tmap = nullptr;  // host CUtensorMap of the fine field: levels x If x Jf (box: see zrestrict_box)
     int* status = nullptr;       // device status word: set to 1 when a bounded wait runs out
     int max_polls = kDefaultWaitPolls;
+    int write_zout = 1;          // 0: restriction only (generation 1 is neither filtered nor written)
 };
 
 struct ProlongArgs {
@@ -226,6 +227,10 @@ struct HMomArgs {
     int variant = 0;         // FP32 kernels: 0 TMA two-row, 1 TMA one-row, 2 cp.async staged,
                              // 3 TMA two rows per barrier filtered one after the other
     int max_polls = kDefaultWaitPolls;  // polls of a row's barrier before the block gives up
+    // 1: the input view has no x halo (halo = 0; the TMA map covers columns
+    // 0..I-1, I >= R) and edge tiles take the half-sample mirror of their
+    // out-of-range columns in shared memory.  Single-row TMA kernel only.
+    int mirror_in = 0;
 };
 
 constexpr int kHMomVariants = 4;

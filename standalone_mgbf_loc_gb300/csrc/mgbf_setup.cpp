@@ -186,6 +186,19 @@ int build_zstencil(int p, double ampl01, int hz, int lm, bool need, ZStencil& Z,
             if (r < 0 || r >= lm) continue;
             Z.adj[(size_t)L * bw + d + mz] = Z.fwd[(size_t)r * bw + (-d) + mz];
         }
+    // M = Bz Bz^T: M(L, L+e) = sum_k Bz(L, k) Bz(L+e, k)
+    Z.mmz = std::min(2 * mz, lm - 1);
+    const int mw = 2 * Z.mmz + 1;
+    Z.mm.assign((size_t)lm * mw, 0.0);
+    for (int L = 0; L < lm; ++L)
+        for (int e = -Z.mmz; e <= Z.mmz; ++e) {
+            const int L2 = L + e;
+            if (L2 < 0 || L2 >= lm) continue;
+            double acc = 0.0;
+            for (int k = std::max(0, std::max(L, L2) - mz); k <= std::min(lm - 1, std::min(L, L2) + mz); ++k)
+                acc += Z.fwd[(size_t)L * bw + (k - L) + mz] * Z.fwd[(size_t)L2 * bw + (k - L2) + mz];
+            Z.mm[(size_t)L * mw + e + Z.mmz] = acc;
+        }
     return MGBF_OK;
 }
 

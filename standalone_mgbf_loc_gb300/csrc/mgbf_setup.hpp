@@ -93,6 +93,10 @@ struct ZStencil {
     std::vector<double> wz;     // 2mz+1 tap weights
     std::vector<double> fwd;    // lm x (2mz+1) band of Bz
     std::vector<double> adj;    // lm x (2mz+1) band of Bz^T
+    // M = Bz Bz^T (symmetric, half-width mmz = min(2mz, lm-1)), lm x (2mmz+1):
+    // the whole vertical filtering of a column when it is applied in one pass
+    int mmz = 0;
+    std::vector<double> mm;
 };
 
 struct Interp1D {

@@ -235,6 +235,12 @@ class MGBF:
         reports MGBF_ERR_TIMEOUT (polls < 0: the default)."""
         _abi.check(self._lib.mgbf_set_wait_limit(self._h, int(polls)), "mgbf_set_wait_limit")
 
+    def set_vertical_passes(self, passes: int) -> None:
+        """2 (default): Bz^T first and Bz last, as the reference; 1: M = Bz Bz^T
+        once, in the last prolongation (same operator, one field write less
+        per call where it applies)."""
+        _abi.check(self._lib.mgbf_set_vertical_passes(self._h, int(passes)), "mgbf_set_vertical_passes")
+
     def line_filters(self) -> list:
         """Procedures 2 and 7's three line filters (colors 1..3): dicts with
         the generator d, half-span h, formal half-span hs and weights fil[0..h]."""
@@ -415,6 +421,10 @@ class MGBFBatch:
     def set_wait_limit(self, polls: int) -> None:
         """As MGBF.set_wait_limit, for every group of the batch."""
         _abi.check(self._lib.mgbf_batch_set_wait_limit(self._h, int(polls)), "mgbf_batch_set_wait_limit")
+
+    def set_vertical_passes(self, passes: int) -> None:
+        """As MGBF.set_vertical_passes, for every group of the batch."""
+        _abi.check(self._lib.mgbf_batch_set_vertical_passes(self._h, int(passes)), "mgbf_batch_set_vertical_passes")
 
     def set_procedure(self, mg_filt: int) -> None:
         """6: radial filters (default); 8: the fast 1D+1D line filters."""

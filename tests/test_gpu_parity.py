@@ -337,6 +337,53 @@ def test_fused_vertical_adjoint_and_restriction(lib, cuda, dtype, lm, km3, km2):
 
 
 @pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("layout", ["compact", "halo"])
+@pytest.mark.parametrize("hz,hx,grid", [(2, 4, (4, 4)), (4, 8, (4, 4)), (3, 4, (1, 1))])
+def test_one_vertical_pass_and_direct_first_pass(lib, cuda, dtype, layout, hz, hx, grid):
+    """Vertical reach <= 4 (FP32/BF16, radial moment kernel): the filter runs
+    as M H x with M = Bz Bz^T applied once in the last prolongation;
+    generation 1's first radial pass reads the caller's field itself, its
+    edge tiles mirrored in shared memory (grid (1, 1): a 16 x 12 field whose
+    tiles reach past both edges).  No vertical stage runs before the
+    radial passes; forward against the oracle, adjoint by the dot-product
+    test."""
+    c = small_config(nxPE=grid[0], nyPE=grid[1], lm=8, km3=2, n_ens=1, hz=hz, mg_ampl01=canonical_z(hz), hx=hx, hy=hx,
+                     mg_ampl02=canonical(hx),
+                     layout=_abi.MGBF_LAYOUT_COMPACT if layout == "compact" else _abi.MGBF_LAYOUT_HALO)
+    op = MGBF(c)
+    op.set_vertical_passes(1)
+    rng = np.random.default_rng(500 + hz + hx + grid[0])
+    x, yv = rng.standard_normal(op.field_shape()), rng.standard_normal(op.field_shape())
+    if layout == "compact":
+        ref = O.filter_compact(oracle_cfg(c, 1), x)
+    else:
+        ref = x.copy()
+        O.filtering_procedure(oracle_cfg(c, 1), ref)
+    _abi.timers_enable(True)
+    lx = run_gpu(op, 1, x, dtype, cuda)
+    stages = _abi.timers_read()
+    _abi.timers_enable(False)
+    assert "upsend" in stages and "dnsend+vfilt" in stages
+    assert "vfiltT" not in stages and "vfiltT+upsend" not in stages
+    assert rel_l2(lx, ref) < TOL[dtype]
+    if dtype == torch.float32:
+        lty = run_gpu(op, 1, yv, dtype, cuda, adjoint=True)
+        a, b = (lx * yv).sum(), (x * lty).sum()
+        assert abs(a - b) / (np.linalg.norm(lx) * np.linalg.norm(yv)) < 1e-6
+        # the reference's two passes on the same handle: the same operator
+        op.set_vertical_passes(2)
+        _abi.timers_enable(True)
+        l2 = run_gpu(op, 1, x, dtype, cuda)
+        stages = _abi.timers_read()
+        _abi.timers_enable(False)
+        assert "vfiltT+upsend" in stages
+        assert rel_l2(l2, lx) < 1e-6
+    with pytest.raises(_abi.MGBFError):
+        op.set_vertical_passes(3)
+    op.close()
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
 @pytest.mark.parametrize("lm", [16, 48])
 @pytest.mark.parametrize("hz", [5, 6, 7, 8])
 def test_fused_z_kernels_vertical_reach_above_four(lib, cuda, dtype, lm, hz):
