@@ -913,7 +913,8 @@ struct Exec {
         zr.band = nullptr; zr.lm = 1; zr.nzk = 0; zr.mz = 0;
         zr.status = static_cast<int*>(P.status.p);
         zr.max_polls = P.wait_polls;
-        zr.tmap = rm;
+        zr.tmap = rm = xmap(x, 1, 0, 0);
+        if (!rm) return -1;
         {
             StageTimer tm(ST_UPSEND, stream, pts(0));
             const int r = launch_zrestrict(t, zr, stream);
@@ -928,6 +929,10 @@ struct Exec {
             if ((rc = restrict_(g, A(g), A(g + 1)))) return rc;
         // 2. first radial side: generation 1 straight from x
         {
+            // fetched again: a lookup may clear the map cache, so a pointer
+            // is only used before the next one (the launch copies the map)
+            hm = view_map(x, P.I, P.J, 64, hmom_tma_cols(G.hs.R));
+            if (!hm) return fail(MGBF_ERR_CUDA, "tensor map of the field for the radial pass");
             HMomArgs h;
             h.in = x; h.out = B(0); h.nk = G.nk; h.I = P.I; h.J = P.J;
             h.mirror_hx = G.hs.R; h.scale = P.a[0] * G.hs.s; h.halo = 0;

@@ -222,6 +222,40 @@ def test_batched_groups(lib, cuda):
         assert rel_l2(t.double().cpu().numpy(), O.filter_compact(oc, x)) < 1e-5
 
 
+def test_batch_one_vertical_pass(lib, cuda):
+    """A batch with one vertical pass (M = Bz Bz^T in the last prolongation),
+    replayed as a graph: against the oracle and against the two-pass chain
+    (rounding only)."""
+    I = J = 64
+    groups = [GroupDesc(nk=3 * 8, lm=8, nzcol=3, hx=4, hy=4, hz=3, p=2, mg_ampl01=canonical_z(3),
+                        mg_ampl02=canonical(4)),
+              GroupDesc(nk=6, lm=1, nzcol=0, hx=6, hy=6, hz=2, p=2, mg_ampl01=canonical_z(2),
+                        mg_ampl02=canonical(6))]
+    w = [1.0, 0.5, 0.25]
+    rng = np.random.default_rng(13)
+    xs = [rng.standard_normal((J, I, g.nk)) for g in groups]
+    outs = {}
+    for passes in (2, 1):
+        b = MGBFBatch(I, J, 3, w, groups)
+        b.use_graphs(True)
+        b.set_vertical_passes(passes)
+        ts = [torch.from_numpy(x).to(cuda, torch.float32) for x in xs]
+        for _ in range(3):  # direct, capture, replay: each call starts from x again
+            for t, x in zip(ts, xs):
+                t.copy_(torch.from_numpy(x))
+            b.apply(ts)
+        torch.cuda.synchronize()
+        b.status()
+        outs[passes] = [t.double().cpu().numpy() for t in ts]
+        b.close()
+    for g, x, y1, y2 in zip(groups, xs, outs[1], outs[2]):
+        oc = O.OracleConfig(I=I, J=J, nk=g.nk, hx=g.hx, hy=g.hy, hz=g.hz, p=g.p, ampl01=g.mg_ampl01,
+                            ampl02=g.mg_ampl02, gm=3, weights=w, proc=6, lm=g.lm, nzcol=g.nzcol,
+                            l_vertical_filter=g.nzcol > 0)
+        assert rel_l2(y1, O.filter_compact(oc, x)) < 1e-5
+        assert rel_l2(y1, y2) < 1e-6
+
+
 @pytest.mark.parametrize("mode", [1, 2])
 def test_batch_graph_node_priorities(lib, cuda, mode):
     """Graph-node priorities change only the order in which the SMs take
