@@ -365,6 +365,11 @@ int mgbf_batch_set_priorities(mgbf_batch* b, int mode);
  * Extension for reporting what the autotuner chose; the reference has no
  * counterpart. */
 int mgbf_batch_get_tuning(const mgbf_batch* b, int dtype, int group, int gen, int pass, int* variant, int* rows);
+/* Pins the radial-filter kernel of one group, generation and pass (as
+ * mgbf_batch_get_tuning reports it): variant as in mgbf_set_tuning (-1
+ * returns to the default), rows the output rows per block (0: the
+ * default).  Releases graphs captured before.  No reference counterpart. */
+int mgbf_batch_set_tuning(mgbf_batch* b, int dtype, int group, int gen, int pass, int variant, int rows);
 
 /* ------------------------------------------------------------------------
  * Allocation-free radial filtering (no counterpart in the reference).

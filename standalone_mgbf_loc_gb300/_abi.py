@@ -111,6 +111,7 @@ SIGNATURES = {
     "mgbf_batch_set_wait_limit": (_I, [_HP, _I]),
     "mgbf_set_vertical_passes": (_I, [_HP, _I]),
     "mgbf_batch_set_vertical_passes": (_I, [_HP, _I]),
+    "mgbf_batch_set_tuning": (_I, [_HP, _I, _I, _I, _I, _I, _I]),
     "mgbf_batch_set_weights": (_I, [_HP, ctypes.POINTER(_D), _I]),
     "mgbf_radial_filter_noalloc": (_I, [_VP, _VP, _I, _I, _I, _I, _D, _I, _I, _D, _VP]),
     "mgbf_timers_enable": (_I, [_I]),

@@ -2132,6 +2132,28 @@ int mgbf_batch_get_tuning(const mgbf_batch* b, int dtype, int group, int gen, in
     return MGBF_OK;
 }
 
+int mgbf_batch_set_tuning(mgbf_batch* b, int dtype, int group, int gen, int pass, int variant, int rows) {
+    if (!b) return fail(MGBF_ERR_ARG, "null handle");
+    if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");
+    Plan& P = b->plan;
+    if (group < 0 || group >= (int)P.groups.size() || gen < 0 || gen >= P.gm || pass < 0 || pass > 1)
+        return fail(MGBF_ERR_ARG, "group, generation or pass out of range");
+    if (variant >= kHMomVariants) return fail(MGBF_ERR_ARG, "unknown radial kernel variant");
+    DeviceGuard dg(P.device);
+    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);  // captured with the old choice
+    b->graphs.clear();
+    Group& G = P.groups[group];
+    const int key = dtype * 1024 + gen * 2 + pass;
+    if (variant < 0) {
+        G.tune.erase(key);
+    } else {
+        Exec ex{P, G, (DType)dtype, nullptr};
+        const int J = gen_J(P, gen);
+        G.tune[key] = {variant, rows > 0 ? std::min(rows, J) : ex.default_rows(gen)};
+    }
+    return MGBF_OK;
+}
+
 int mgbf_batch_autotune(mgbf_batch* b, int dtype, void* stream) {
     if (!b) return fail(MGBF_ERR_ARG, "null handle");
     if (!valid_dtype(dtype)) return fail(MGBF_ERR_ARG, "bad dtype");

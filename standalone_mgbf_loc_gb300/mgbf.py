@@ -422,6 +422,13 @@ class MGBFBatch:
         """As MGBF.set_wait_limit, for every group of the batch."""
         _abi.check(self._lib.mgbf_batch_set_wait_limit(self._h, int(polls)), "mgbf_batch_set_wait_limit")
 
+    def set_tuning(self, group: int, gen: int, pass_: int, variant: int, rows: int = 0, dtype=None) -> None:
+        """Pin the radial kernel of one group, generation and pass (variant
+        -1: back to the default; rows 0: the default)."""
+        dt = _dtype_code(dtype if dtype is not None else torch.float32)
+        _abi.check(self._lib.mgbf_batch_set_tuning(self._h, dt, int(group), int(gen), int(pass_), int(variant), int(rows)),
+                   "mgbf_batch_set_tuning")
+
     def set_vertical_passes(self, passes: int) -> None:
         """As MGBF.set_vertical_passes, for every group of the batch."""
         _abi.check(self._lib.mgbf_batch_set_vertical_passes(self._h, int(passes)), "mgbf_batch_set_vertical_passes")

@@ -222,6 +222,36 @@ def test_batched_groups(lib, cuda):
         assert rel_l2(t.double().cpu().numpy(), O.filter_compact(oc, x)) < 1e-5
 
 
+def test_batch_set_tuning_pins_variant(lib, cuda):
+    """mgbf_batch_set_tuning pins one group's kernel for one generation and
+    pass (read back by mgbf_batch_get_tuning; -1 returns to the default);
+    the result still matches the oracle."""
+    I = J = 64
+    groups = [GroupDesc(nk=2 * 8, lm=8, nzcol=2, hx=4, hy=4, hz=2, p=2, mg_ampl01=canonical_z(2),
+                        mg_ampl02=canonical(4))]
+    w = [1.0, 0.5, 0.25]
+    b = MGBFBatch(I, J, 3, w, groups)
+    b.use_graphs(True)
+    x = np.random.default_rng(14).standard_normal((J, I, 16))
+    oc = O.OracleConfig(I=I, J=J, nk=16, hx=4, hy=4, hz=2, p=2, ampl01=canonical_z(2), ampl02=canonical(4), gm=3,
+                        weights=w, proc=6, lm=8, nzcol=2, l_vertical_filter=True)
+    ref = O.filter_compact(oc, x)
+    for variant in (1, 2, 3, 0):
+        b.set_tuning(0, 0, 0, variant, 16)
+        b.set_tuning(0, 0, 1, variant, 32)
+        assert b.tuning()[0][0] == [(variant, 16), (variant, 32)]
+        t = torch.from_numpy(x).to(cuda, torch.float32)
+        b.apply([t])
+        torch.cuda.synchronize()
+        b.status()
+        assert rel_l2(t.double().cpu().numpy(), ref) < 1e-5
+    b.set_tuning(0, 0, 0, -1)
+    assert b.tuning()[0][0][0] == (-1, 0)
+    with pytest.raises(_abi.MGBFError):
+        b.set_tuning(0, 5, 0, 1)
+    b.close()
+
+
 def test_batch_one_vertical_pass(lib, cuda):
     """A batch with one vertical pass (M = Bz Bz^T in the last prolongation),
     replayed as a graph: against the oracle and against the two-pass chain
