@@ -240,11 +240,28 @@ def run_gpu(args):
     for blocks_per_sm in (0, 1, 2, 8):  # 0: per generation; else persistent with up to that many blocks per SM
         batch.use_persistent(blocks_per_sm)
         trials[blocks_per_sm] = trial_ms()
+    # per generation with the single-row TMA kernel everywhere (the rows per
+    # block the autotuner chose), against the autotuner's variants: its
+    # kernels are timed alone, the step runs the groups side by side
+    batch.use_persistent(0)
+    tuned_choice = batch.tuning(torch.float32)
+    for q, per_group in enumerate(tuned_choice):
+        for g, pair in enumerate(per_group):
+            for p, (v, r) in enumerate(pair):
+                if v >= 0:
+                    batch.set_tuning(q, g, p, 1, r)
+    trials["tma1"] = trial_ms()
     best = min(trials, key=trials.get)
-    batch.use_persistent(best)
-    radial_launch = {"ms_per_step": {("per generation" if k == 0 else f"persistent, <= {k} blocks/SM"): v
-                                     for k, v in trials.items()},
-                     "chosen": "per generation" if best == 0 else f"persistent, <= {best} blocks/SM"}
+    if best != "tma1":
+        for q, per_group in enumerate(tuned_choice):  # back to the autotuner's variants
+            for g, pair in enumerate(per_group):
+                for p, (v, r) in enumerate(pair):
+                    if v >= 0:
+                        batch.set_tuning(q, g, p, v, r)
+        batch.use_persistent(best)
+    names = {0: "per generation", "tma1": "per generation, single-row TMA kernel everywhere"}
+    radial_launch = {"ms_per_step": {names.get(k, f"persistent, <= {k} blocks/SM"): v for k, v in trials.items()},
+                     "chosen": names.get(best, f"persistent, <= {best} blocks/SM")}
     # graph-node priorities of the concurrent group branches (0 none, 1
     # memory-bound kernels first, 2 radial kernels first) and the vertical
     # filter passes (2 as the reference: Bz^T first, Bz last; 1: M = Bz Bz^T

@@ -1982,11 +1982,9 @@ static int autotune_plan(Plan& P, DType t, void* stream) {
         if ((rc = ensure_tables(P, G, t)) || (rc = ensure_bufs(P, G, t, false))) return rc;
         Exec ex{P, G, t, stream};
         if (!ex.moment_path()) continue;
-        // the buffers hold a normal nonzero value in every element (the byte
-        // pattern 0x3f): kernels timed on zeros draw less power than on data
         for (int g = 0; g < P.gm; ++g) {
-            CU(cudaMemsetAsync(G.bufs[(int)t].A[g]->p, 0x3f, G.bufs[(int)t].A[g]->bytes, s));
-            CU(cudaMemsetAsync(G.bufs[(int)t].B[g]->p, 0x3f, G.bufs[(int)t].B[g]->bytes, s));
+            CU(cudaMemsetAsync(G.bufs[(int)t].A[g]->p, 0, G.bufs[(int)t].A[g]->bytes, s));
+            CU(cudaMemsetAsync(G.bufs[(int)t].B[g]->p, 0, G.bufs[(int)t].B[g]->bytes, s));
         }
         for (int g = 0; g < P.gm; ++g)
             for (int pass = 0; pass < 2; ++pass) {
@@ -1998,39 +1996,25 @@ static int autotune_plan(Plan& P, DType t, void* stream) {
                 rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
                 const int nvar = t == DType::F64 ? 1 : kHMomVariants;
                 View in = pass ? ex.B(g) : ex.A(g), out = pass ? ex.A(g) : ex.B(g);
-                // two sweeps over the candidates, each candidate's best of
-                // the two: a single sample is skewed by the clock state of
-                // the moment, and neighbouring variants are close
-                std::vector<float> best_ms(nvar * rows.size(), 1e30f);
-                for (int sweep = 0; sweep < 2; ++sweep)
-                    for (int v = 0; v < nvar; ++v)
-                        for (size_t ri = 0; ri < rows.size(); ++ri) {
-                            const int r = rows[ri];
-                            if ((rc = ex.hmom(g, in, out, 1.0, pass ? 0 : G.hs.R, pass, v, r))) return rc;  // warm
-                            CU(cudaEventRecord(e0, s));
-                            for (int rep = 0; rep < 5; ++rep)
-                                if ((rc = ex.hmom(g, in, out, 1.0, pass ? 0 : G.hs.R, pass, v, r))) return rc;
-                            CU(cudaEventRecord(e1, s));
-                            CU(cudaEventSynchronize(e1));
-                            float ms = 0.f;
-                            CU(cudaEventElapsedTime(&ms, e0, e1));
-                            float& b = best_ms[v * rows.size() + ri];
-                            b = std::min(b, ms);
-                        }
                 float best = 1e30f;
                 std::pair<int, int> choice(0, r0);
                 for (int v = 0; v < nvar; ++v)
-                    for (size_t ri = 0; ri < rows.size(); ++ri)
-                        if (best_ms[v * rows.size() + ri] < best) {
-                            best = best_ms[v * rows.size() + ri];
-                            choice = {v, rows[ri]};
+                    for (int r : rows) {
+                        if ((rc = ex.hmom(g, in, out, 1.0, pass ? 0 : G.hs.R, pass, v, r))) return rc;  // warm
+                        CU(cudaEventRecord(e0, s));
+                        for (int rep = 0; rep < 3; ++rep)
+                            if ((rc = ex.hmom(g, in, out, 1.0, pass ? 0 : G.hs.R, pass, v, r))) return rc;
+                        CU(cudaEventRecord(e1, s));
+                        CU(cudaEventSynchronize(e1));
+                        float ms = 0.f;
+                        CU(cudaEventElapsedTime(&ms, e0, e1));
+                        if (ms < best) {
+                            best = ms;
+                            choice = {v, r};
                         }
+                    }
                 G.tune[(int)t * 1024 + g * 2 + pass] = choice;
             }
-        for (int g = 0; g < P.gm; ++g) {  // leave the buffers as a first call finds them
-            CU(cudaMemsetAsync(G.bufs[(int)t].A[g]->p, 0, G.bufs[(int)t].A[g]->bytes, s));
-            CU(cudaMemsetAsync(G.bufs[(int)t].B[g]->p, 0, G.bufs[(int)t].B[g]->bytes, s));
-        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

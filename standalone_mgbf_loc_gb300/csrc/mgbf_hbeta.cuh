@@ -819,10 +819,9 @@ __device__ __forceinline__ bool hmom_tma1_tile(const HMomArgs& a, const CUtensor
 
 // Single-row variant of the TMA kernel: one tile per block; fewer registers
 // than the two-row kernel, more blocks per SM; the autotuner picks between
-// them.  MIRROR: the input has no x halo (HMomArgs::mirror_in).
-template <int R, int P, int TX, typename T, bool MIRROR = false>
-__global__ void __launch_bounds__(128, (MIRROR && R <= 8) ? 4 : 1)
-    k_hmom_tma1(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
+// them.
+template <int R, int P, int TX, typename T>
+__global__ void __launch_bounds__(128) k_hmom_tma1(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
                                                   const __grid_constant__ HMomCoefs2 c) {
     __shared__ __align__(8) unsigned long long bars[kStages];
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -834,8 +833,27 @@ __global__ void __launch_bounds__(128, (MIRROR && R <= 8) ? 4 : 1)
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
-    hmom_tma1_tile<R, P, TX, T, MIRROR>(a, &tmap, c, blockIdx.x * 64, blockIdx.y * (kStageWarps * TX), blockIdx.z * a.rows,
-                                        sbase, bbase, 0);
+    hmom_tma1_tile<R, P, TX, T>(a, &tmap, c, blockIdx.x * 64, blockIdx.y * (kStageWarps * TX), blockIdx.z * a.rows, sbase,
+                                bbase, 0);
+}
+
+// The single-row kernel for an input without x halo (HMomArgs::mirror_in):
+// edge tiles fill their half-sample mirror in shared memory.
+template <int R, int P, int TX, typename T>
+__global__ void __launch_bounds__(128, R <= 8 ? 4 : 1) k_hmom_tma1_mirror(HMomArgs a, const __grid_constant__ CUtensorMap tmap,
+                                                                        const __grid_constant__ HMomCoefs2 c) {
+    __shared__ __align__(8) unsigned long long bars[kStages];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const unsigned bbase = (unsigned)__cvta_generic_to_shared(bars);
+    if (threadIdx.y == 0 && threadIdx.x == 0) {
+#pragma unroll
+        for (int s2 = 0; s2 < kStages; ++s2) mbar_init(bbase + 8 * s2, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    hmom_tma1_tile<R, P, TX, T, true>(a, &tmap, c, blockIdx.x * 64, blockIdx.y * (kStageWarps * TX), blockIdx.z * a.rows,
+                                      sbase, bbase, 0);
 }
 
 // Persistent form of one radial side: every generation's tiles of one
@@ -923,10 +941,10 @@ static int run_hmom(const HMomArgs& a, const HMomCoefs<double>& cd, cudaStream_t
             constexpr size_t smt = (size_t)kStages * (kStageWarps * TX2 + 2 * R) * 64 * sizeof(T);
             if (smt + 1024 > 48 * 1024) {
                 static unsigned long long done = 0;  // per instantiation
-                cudaError_t ea = smem_optin(k_hmom_tma1<R, P, TX2, T, true>, smt, done);
+                cudaError_t ea = smem_optin(k_hmom_tma1_mirror<R, P, TX2, T>, smt, done);
                 if (ea != cudaSuccess) return (int)ea;
             }
-            k_hmom_tma1<R, P, TX2, T, true><<<grid2, block, smt, s>>>(b, *static_cast<const CUtensorMap*>(a.tmap), c2);
+            k_hmom_tma1_mirror<R, P, TX2, T><<<grid2, block, smt, s>>>(b, *static_cast<const CUtensorMap*>(a.tmap), c2);
             cudaError_t e = cudaGetLastError();
             return e == cudaSuccess ? 0 : (int)e;
         } else {

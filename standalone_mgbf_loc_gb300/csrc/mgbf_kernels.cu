@@ -386,7 +386,9 @@ __host__ __device__ constexpr size_t zr_row_bytes() {
 template <typename T, int CX, int LV, int MZ>
 constexpr size_t zr_smem() { return 2 * kZrPairs * zr_row_bytes<T, CX, LV, MZ>(); }
 
-template <typename T, int CX, int LV, int MZ>
+// RONLY: restriction only (no z columns, generation 1 not written); the
+// two-pass chain's form compiles without that branch
+template <typename T, int CX, int LV, int MZ, bool RONLY = false>
 __global__ void __launch_bounds__(kRsWarps * 32, 3)
     k_zrestrict_tma(ZRestrictArgs z, const __grid_constant__ CUtensorMap xmap, int seg_rows) {
     static_assert(sizeof(T) <= 4, "FP32 accumulation: float or bfloat16 storage");
@@ -488,7 +490,7 @@ __global__ void __launch_bounds__(kRsWarps * 32, 3)
                 }
                 V4<T>::st(cp, y);
                 const int gc = 2 * cs - 3 + col;
-                if (z.write_zout && own_row && col >= 3 && col < 3 + 2 * kRsWarps * CX && gc < a.If) {
+                if (own_row && col >= 3 && col < 3 + 2 * kRsWarps * CX && gc < a.If) {
                     V4<T>::st(zrow + z.zout.si * gc, y);
                     if (gc < z.mirror_z) V4<T>::st(zrow + z.zout.si * (-1 - gc), y);
                     if (gc >= a.If - z.mirror_z) V4<T>::st(zrow + z.zout.si * (2 * a.If - 1 - gc), y);
@@ -538,9 +540,9 @@ __global__ void __launch_bounds__(kRsWarps * 32, 3)
     };
 
     // pipeline fill: pair 0 filtered before the first restriction
-    // (restriction only -- no z columns, generation 1 not written -- skips
-    // the z pass, which would copy the staged rows onto themselves)
-    const bool zpass = z.nzk > 0 || z.write_zout;
+    // (restriction only skips the z pass, which would copy the staged rows
+    // onto themselves)
+    constexpr bool zpass = !RONLY;
     int waited = 0;                          // pairs whose barrier every thread has passed
     int issued = min(niter, kZrPairs);       // pairs whose loads thread 0 has issued
     bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(bbase, 0u, z.max_polls));
@@ -1625,7 +1627,7 @@ ZrBox zrestrict_box(DType t, int lm, int nzk, int mz) {
     return b;
 }
 
-template <typename T, int LV, int MZ>
+template <typename T, int LV, int MZ, bool RONLY = false>
 static int zrlaunch(const ZRestrictArgs& z, cudaStream_t s) {
     constexpr int CX = 2;
     const RestrictArgs& a = z.r;
@@ -1635,9 +1637,9 @@ static int zrlaunch(const ZRestrictArgs& z, cudaStream_t s) {
     grid.z = (Jc + rows - 1) / rows;
     constexpr size_t sm = zr_smem<T, CX, LV, MZ>();
     static unsigned long long done = 0;  // per instantiation
-    cudaError_t e = smem_optin(k_zrestrict_tma<T, CX, LV, MZ>, sm, done);
+    cudaError_t e = smem_optin(k_zrestrict_tma<T, CX, LV, MZ, RONLY>, sm, done);
     if (e != cudaSuccess) return (int)e;
-    k_zrestrict_tma<T, CX, LV, MZ><<<grid, block, sm, s>>>(z, *static_cast<const CUtensorMap*>(z.tmap), rows);
+    k_zrestrict_tma<T, CX, LV, MZ, RONLY><<<grid, block, sm, s>>>(z, *static_cast<const CUtensorMap*>(z.tmap), rows);
     return last_err();
 }
 
@@ -1645,6 +1647,7 @@ static int zrlaunch(const ZRestrictArgs& z, cudaStream_t s) {
 // z.mz <= MZ, taps past it have zero weight
 template <typename T, int LV>
 static int zrdispatch(const ZRestrictArgs& z, cudaStream_t s) {
+    if (!z.write_zout && z.nzk == 0) return zrlaunch<T, LV, 4, true>(z, s);
     if (z.mz <= 4) return zrlaunch<T, LV, 4>(z, s);
     if (z.mz == 5) return zrlaunch<T, LV, 5>(z, s);
     if (z.mz == 6) return zrlaunch<T, LV, 6>(z, s);

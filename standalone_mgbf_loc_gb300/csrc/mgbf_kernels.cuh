@@ -174,7 +174,7 @@ struct ZRestrictArgs {
     const void* tmap = nullptr;  // host CUtensorMap of the fine field: levels x If x Jf (box: see zrestrict_box)
     int* status = nullptr;       // device status word: set to 1 when a bounded wait runs out
     int max_polls = kDefaultWaitPolls;
-    int write_zout = 1;          // 0: restriction only (generation 1 is neither filtered nor written)
+    int write_zout = 1;          // 0 with nzk == 0: restriction only (generation 1 neither filtered nor written)
 };
 
 struct ProlongArgs {
