@@ -27,3 +27,30 @@ def test_vertical_filter_commutes_with_the_horizontal_chain(proc, hz, lquart):
     y = O.filter_compact(oc, x)                    # Bz H Bz^T x, as the reference runs it
     assert rel_l2(O.filter_compact(horiz, m(x)), y) < 1e-13
     assert rel_l2(m(O.filter_compact(horiz, x)), y) < 1e-13
+
+
+def test_option_setters_validate_arguments():
+    """The pass-form, priority and tuning setters refuse bad values with
+    MGBF_ERR_ARG and take good ones; none needs a GPU."""
+    from standalone_mgbf_loc_gb300 import MGBF, GroupDesc, MGBFBatch, _abi
+    op = MGBF(small_config())
+    op.set_vertical_passes(1)
+    op.set_vertical_passes(2)
+    for bad in (0, 3):
+        with pytest.raises(_abi.MGBFError) as e:
+            op.set_vertical_passes(bad)
+        assert e.value.code == _abi.MGBF_ERR_ARG
+    op.close()
+    b = MGBFBatch(64, 64, 3, [1.0, 0.5, 0.25],
+                  [GroupDesc(nk=16, lm=8, nzcol=2, hx=4, hy=4, hz=2, p=2, mg_ampl01=canonical_z(2),
+                             mg_ampl02=canonical(4))])
+    b.set_vertical_passes(1)
+    b.set_priorities(2)
+    b.set_tuning(0, 0, 0, 1, 16)
+    b.set_tuning(0, 0, 0, -1)
+    for call in (lambda: b.set_vertical_passes(3), lambda: b.set_priorities(5), lambda: b.set_tuning(0, 9, 0, 1),
+                 lambda: b.set_tuning(1, 0, 0, 1), lambda: b.set_tuning(0, 0, 2, 1), lambda: b.set_tuning(0, 0, 0, 7)):
+        with pytest.raises(_abi.MGBFError) as e:
+            call()
+        assert e.value.code == _abi.MGBF_ERR_ARG
+    b.close()
